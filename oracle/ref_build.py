@@ -1,0 +1,161 @@
+"""Build recipe for the REFERENCE tracer's host code (test infrastructure only).
+
+The reference (meirbon/CudaTracer) is MSVC-only and does not compile unmodified
+with g++: its binary BVH node puts an anonymous struct with glm members inside a
+union (src/BVH/BVHNode.cuh:32-40), which g++ rejects ("member with constructor
+not allowed in anonymous aggregate"). This recipe therefore
+
+  1. copies the few source files the host BVH/camera path needs, plus the
+     vendored header-only glm/assimp/GLFW headers, from the reference checkout
+     into oracle/_ref/src and oracle/_ref/include (git-ignored build output);
+  2. applies one mechanical patch that keeps the 32-byte layout:
+       BVHNode.cuh  union{AABB bounds; struct{vec3 min; int leftFirst; vec3 max; int count;};}
+                    -> AABB bounds;   (Intersect reads bounds.xMin.. / bounds.xMax..)
+       BVHNode.cu   this->min[axis] -> bounds.bmin[axis]   (2 sites)
+  3. compiles oracle/ref_harness.cpp with those sources into oracle/_ref/libctref.so,
+     with -ffp-contract=off so no multiply-add is fused (matching the MSVC
+     x86-64 build the reference targets).
+
+Nothing produced here is committed. When the reference checkout is absent (the
+GPU host), step 1-2 are skipped and an existing oracle/_ref/src (carried over
+with the working tree) is compiled for the local architecture instead.
+"""
+from __future__ import annotations
+
+import os
+import platform
+import shutil
+import subprocess
+import sys
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+REF_OUT = os.path.join(HERE, "_ref")
+LIB = os.path.join(REF_OUT, "libctref.so")
+DEFAULT_REFERENCE = "/root/reference"
+
+SRC_FILES = [
+    "BVH/AABB.h", "BVH/BVHNode.cuh", "BVH/BVHNode.cu", "BVH/BVHTree.h", "BVH/BVHTree.cpp",
+    "BVH/MBVHNode.cuh", "BVH/MBVHNode.cu", "BVH/MBVHTree.h", "BVH/MBVHTree.cpp",
+    "Core/BSDF.h", "Core/Camera.h", "Core/Camera.cpp", "Core/Material.cuh", "Core/Microfacet.cuh",
+    "Core/Random.cuh", "Core/Ray.cuh", "Core/SceneData.cuh", "Core/Tools.h", "Core/Triangle.cuh",
+    "Core/TriangleList.h", "CUDA/CudaAssert.h", "Utils/ctpl.h", "Utils/Timer.h", "Utils/Surface.h",
+]
+INCLUDE_DIRS = ["glm", "assimp", "GLFW"]
+COMPILED = ["BVH/BVHNode.cu", "BVH/BVHTree.cpp", "BVH/MBVHNode.cu", "BVH/MBVHTree.cpp", "Core/Camera.cpp"]
+
+PATCHES = {
+    "BVH/BVHNode.cuh": [
+        (
+            "\tunion {\n\t\tAABB bounds;\n\t\tstruct {\n\t\t\tglm::vec3 min;\n\t\t\tint leftFirst;\n"
+            "\t\t\tglm::vec3 max;\n\t\t\tint count;\n\t\t};\n\t};\n",
+            "\tAABB bounds;\n",
+            1,
+        ),
+        (
+            "const vec3 t1 = (this->min - org) * dirInverse;",
+            "const vec3 t1 = (glm::vec3(bounds.xMin, bounds.yMin, bounds.zMin) - org) * dirInverse;",
+            1,
+        ),
+        (
+            "const vec3 t2 = (this->max - org) * dirInverse;",
+            "const vec3 t2 = (glm::vec3(bounds.xMax, bounds.yMax, bounds.zMax) - org) * dirInverse;",
+            1,
+        ),
+    ],
+    "BVH/BVHNode.cu": [("this->min[axis]", "bounds.bmin[axis]", 2)],
+}
+
+
+def _normalise(text: str) -> str:
+    return text.replace("\r\n", "\n")
+
+
+def stage_sources(reference: str) -> None:
+    src_out = os.path.join(REF_OUT, "src")
+    inc_out = os.path.join(REF_OUT, "include")
+    os.makedirs(src_out, exist_ok=True)
+    for rel in SRC_FILES:
+        with open(os.path.join(reference, "src", rel), "r", encoding="utf-8-sig", errors="replace") as f:
+            text = _normalise(f.read())
+        for old, new, count in PATCHES.get(rel, []):
+            found = text.count(old)
+            if found != count:
+                raise RuntimeError(f"reference patch for {rel}: expected {count} match(es), found {found}")
+            text = text.replace(old, new)
+        dst = os.path.join(src_out, rel)
+        os.makedirs(os.path.dirname(dst), exist_ok=True)
+        with open(dst, "w", encoding="utf-8") as f:
+            f.write(text)
+    for d in INCLUDE_DIRS:
+        dst = os.path.join(inc_out, d)
+        if os.path.isdir(dst):
+            shutil.rmtree(dst)
+        shutil.copytree(os.path.join(reference, "include", d), dst)
+
+
+def _is_x86() -> bool:
+    return platform.machine().lower() in ("x86_64", "amd64", "i686", "i386")
+
+
+def compile_lib(verbose: bool = False) -> str:
+    src_dir = os.path.join(REF_OUT, "src")
+    if not os.path.isdir(src_dir):
+        raise FileNotFoundError("oracle/_ref/src is missing: the reference checkout was never staged")
+    harness = os.path.join(HERE, "ref_harness.cpp")
+    inputs = [harness] + [os.path.join(src_dir, c) for c in COMPILED]
+    newest = max(os.path.getmtime(p) for p in inputs + [os.path.abspath(__file__)])
+    if os.path.exists(LIB) and os.path.getmtime(LIB) >= newest and _lib_matches_arch(LIB):
+        return LIB
+    shim = os.path.join(HERE, "ref_shim")
+    cuda_inc = os.path.join(os.environ.get("CUDA_HOME", "/usr/local/cuda"), "include")
+    flags = [
+        "-std=c++17", "-O2", "-fPIC", "-pthread", "-ffp-contract=off", "-fno-fast-math", "-w",
+        "-DGLM_FORCE_PURE", "-DGLEW_NO_GLU", "-DGLFW_INCLUDE_NONE",
+        "-include", os.path.join(shim, "ct_ref_shim.h"),
+        "-I", os.path.join(shim, "stub"),
+    ]
+    if not _is_x86():
+        flags += ["-I", os.path.join(shim, "portable")]
+    flags += ["-I", src_dir, "-I", os.path.join(REF_OUT, "include"), "-I", cuda_inc]
+    objs = []
+    procs = []
+    for p in inputs:
+        obj = os.path.join(REF_OUT, os.path.basename(p).replace(".", "_") + ".o")
+        cmd = ["g++"] + flags + ["-x", "c++", "-c", p, "-o", obj]
+        if verbose:
+            print(" ".join(cmd))
+        procs.append((subprocess.Popen(cmd, stdout=subprocess.PIPE, stderr=subprocess.STDOUT), p))
+        objs.append(obj)
+    for proc, p in procs:
+        out, _ = proc.communicate()
+        if proc.returncode != 0:
+            raise RuntimeError(f"compiling {p} failed:\n{out.decode(errors='replace')}")
+    tmp = LIB + ".tmp"
+    cmd = ["g++", "-shared", "-pthread", "-o", tmp] + objs
+    subprocess.run(cmd, check=True)
+    os.replace(tmp, LIB)
+    return LIB
+
+
+def _lib_matches_arch(path: str) -> bool:
+    try:
+        with open(path, "rb") as f:
+            head = f.read(20)
+        machine = int.from_bytes(head[18:20], "little")
+        return machine == (62 if _is_x86() else 183)  # EM_X86_64 / EM_AARCH64
+    except OSError:
+        return False
+
+
+def build(reference: str | None = None, verbose: bool = False) -> str | None:
+    """Stage (when the reference checkout exists) and compile; returns the .so path or None."""
+    reference = reference or os.environ.get("CT_REFERENCE_DIR", DEFAULT_REFERENCE)
+    if os.path.isdir(os.path.join(reference, "src", "BVH")):
+        stage_sources(reference)
+    if not os.path.isdir(os.path.join(REF_OUT, "src")):
+        return None
+    return compile_lib(verbose=verbose)
+
+
+if __name__ == "__main__":
+    print(build(verbose="-v" in sys.argv))
