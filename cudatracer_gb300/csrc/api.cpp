@@ -1,0 +1,709 @@
+// C-ABI host runtime: contexts, scenes, BVHs, ray queries and render jobs.
+// Compiled with -ffp-contract=off so the camera basis matches the reference's
+// host arithmetic (src/CUDA/Kernel.cu:274-290, src/Core/Camera.cpp:11-16).
+#include "../../include/cudatracer.h"
+
+#include <cuda_runtime.h>
+
+#include <atomic>
+#include <chrono>
+#include <cmath>
+#include <cstring>
+#include <mutex>
+#include <string>
+#include <thread>
+#include <vector>
+
+#include "bvh_build.h"
+#include "ct_internal.h"
+
+using namespace ct;
+
+struct ct_ctx {
+  int device = 0;
+  mutable std::mutex mu;
+  std::string err;
+  uint64_t budget = 0;
+  std::atomic<uint64_t> bytes{0};
+  uint32_t* d_error = nullptr;
+};
+
+namespace {
+
+struct Allocs {
+  std::vector<std::pair<void*, size_t>> list;
+};
+
+ct_status fail(ct_ctx* ctx, ct_status s, const std::string& msg) {
+  if (ctx) {
+    std::lock_guard<std::mutex> g(ctx->mu);
+    ctx->err = msg;
+  }
+  return s;
+}
+
+ct_status cuda_fail(ct_ctx* ctx, cudaError_t e, const char* what) {
+  return fail(ctx, e == cudaErrorMemoryAllocation ? CT_ERR_OUT_OF_MEMORY : CT_ERR_CUDA,
+              std::string(what) + ": " + cudaGetErrorString(e));
+}
+
+#define CT_CUDA(ctx, call)                                  \
+  do {                                                      \
+    cudaError_t e_ = (call);                                \
+    if (e_ != cudaSuccess) return cuda_fail(ctx, e_, #call); \
+  } while (0)
+
+ct_status dev_alloc(ct_ctx* ctx, Allocs& a, void** p, size_t bytes) {
+  *p = nullptr;
+  if (bytes == 0) bytes = 16;
+  bytes = (bytes + 255) & ~(size_t)255;
+  if (ctx->budget && ctx->bytes.load() + bytes > ctx->budget)
+    return fail(ctx, CT_ERR_OUT_OF_MEMORY,
+                "device memory budget exceeded: " + std::to_string(ctx->bytes.load() + bytes) + " > " +
+                    std::to_string(ctx->budget) + " bytes");
+  cudaError_t e = cudaMalloc(p, bytes);
+  if (e != cudaSuccess) {
+    cudaGetLastError();
+    *p = nullptr;
+    return cuda_fail(ctx, e, "cudaMalloc");
+  }
+  ctx->bytes += bytes;
+  a.list.push_back({*p, bytes});
+  return CT_OK;
+}
+
+void free_all(ct_ctx* ctx, Allocs& a) {
+  for (auto& p : a.list) {
+    cudaFree(p.first);
+    ctx->bytes -= p.second;
+  }
+  a.list.clear();
+}
+
+template <typename T>
+ct_status upload(ct_ctx* ctx, Allocs& a, T** dst, const void* src, size_t bytes) {
+  void* p = nullptr;
+  ct_status s = dev_alloc(ctx, a, &p, bytes);
+  if (s != CT_OK) return s;
+  if (bytes && src) {
+    cudaError_t e = cudaMemcpy(p, src, bytes, cudaMemcpyHostToDevice);
+    if (e != cudaSuccess) return cuda_fail(ctx, e, "cudaMemcpy");
+  } else if (bytes) {
+    cudaError_t e = cudaMemset(p, 0, bytes);
+    if (e != cudaSuccess) return cuda_fail(ctx, e, "cudaMemset");
+  }
+  *dst = (T*)p;
+  return CT_OK;
+}
+
+bool finite3(const float* p) { return std::isfinite(p[0]) && std::isfinite(p[1]) && std::isfinite(p[2]); }
+
+}  // namespace
+
+struct ct_scene {
+  uint32_t nv = 0, nt = 0;
+  std::vector<float> verts;    // 3 per vertex (host copy for BVH builds)
+  std::vector<uint32_t> idx;   // 3 per triangle
+  std::vector<ct_material> mats;
+  DevScene dev{};
+  DevMaterial* d_mats = nullptr;
+  Allocs allocs;
+};
+
+struct ct_bvh {
+  HostBVH host;
+  DeviceLayout layout;
+  DevBVH dev{};
+  ct_bvh_info info{};
+  uint32_t nt = 0;
+  Allocs allocs;
+};
+
+struct ct_render {
+  int32_t w = 0, h = 0;
+  DevQueues q{};
+  Allocs allocs;
+};
+
+namespace {
+
+DevMaterial to_dev(const ct_material& m) {
+  DevMaterial d;
+  d.albedo_ior = make_float4(m.albedo[0], m.albedo[1], m.albedo[2], m.refract_idx);
+  d.tex = make_int4(m.diffuse_tex, m.normal_tex, m.mask_tex, m.displace_tex);
+  float type_bits;
+  std::memcpy(&type_bits, &m.type, 4);
+  d.type_rough = make_float4(type_bits, m.roughness, 0.0f, 0.0f);
+  d.absorption = make_float4(m.absorption[0], m.absorption[1], m.absorption[2], 0.0f);
+  return d;
+}
+
+ct_status set_device(ct_ctx* ctx) {
+  cudaError_t e = cudaSetDevice(ctx->device);
+  if (e != cudaSuccess) return cuda_fail(ctx, e, "cudaSetDevice");
+  return CT_OK;
+}
+
+ct_status finish_bvh(ct_ctx* ctx, const ct_scene* scene, ct_bvh* b) {
+  const auto t0 = std::chrono::high_resolution_clock::now();
+  std::string err = to_device_layout(b->host, scene->verts.data(), scene->idx.data(), scene->nt, b->layout);
+  if (!err.empty()) return fail(ctx, CT_ERR_UNSUPPORTED, err);
+  ct_status s;
+  QNodeDev* nodes = nullptr;
+  float4* tris = nullptr;
+  if ((s = upload(ctx, b->allocs, &nodes, b->layout.nodes.data(), b->layout.nodes.size())) != CT_OK) return s;
+  if ((s = upload(ctx, b->allocs, &tris, b->layout.tris.data(), b->layout.tris.size() * 4)) != CT_OK) return s;
+  b->dev.nodes = nodes;
+  b->dev.tris = tris;
+  b->dev.leaf_shift = b->layout.leaf_shift;
+  b->dev.first_mask = b->layout.first_mask;
+  b->dev.count_mask = b->layout.count_mask;
+  b->dev.prim_count = (uint32_t)b->host.prims.size();
+  b->dev.node_count = (uint32_t)b->host.quad.size();
+  b->dev.stack_entries = b->layout.stack_entries;
+  b->nt = scene->nt;
+  const auto t1 = std::chrono::high_resolution_clock::now();
+  ct_bvh_info& i = b->info;
+  i.binary_node_count = (uint32_t)b->host.bin.size();
+  i.quad_node_count = (uint32_t)b->host.quad.size();
+  i.prim_count = (uint32_t)b->host.prims.size();
+  i.max_leaf_size = b->layout.max_leaf;
+  i.quad_depth = b->layout.depth;
+  i.stack_entries = (uint32_t)b->layout.stack_entries;
+  i.build_ms = b->host.build_ms;
+  i.collapse_ms = b->host.collapse_ms;
+  i.upload_ms = std::chrono::duration<double, std::milli>(t1 - t0).count();
+  uint64_t bytes = 0;
+  for (auto& p : b->allocs.list) bytes += p.second;
+  i.device_bytes = bytes;
+  return CT_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+uint32_t ct_abi_version(void) { return CT_ABI_VERSION; }
+
+void ct_render_params_default(ct_render_params* p) {
+  if (!p) return;
+  std::memset(p, 0, sizeof(*p));
+  p->width = 0;
+  p->height = 0;
+  p->max_depth = 5;  // maxPathLength, src/CUDA/Kernel.cu:320
+  p->frame_index = 0;
+  p->shading_mode = CT_SHADE_COMPAT;
+  p->exact_math = 0;
+  p->shadow = 1;
+  p->indirect = 1;
+  p->sky = 1;
+  p->normal_eps = 1e-5f;  // SceneData defaults, src/Core/SceneData.cuh:43-45
+  p->dist_eps = 1e-5f;
+  p->tri_eps = 1e-3f;
+}
+
+ct_status ct_ctx_create(int32_t device, ct_ctx** out) {
+  if (!out) return CT_ERR_INVALID_ARGUMENT;
+  *out = nullptr;
+  int n = 0;
+  if (cudaGetDeviceCount(&n) != cudaSuccess || n <= 0) {
+    cudaGetLastError();
+    return CT_ERR_NO_DEVICE;
+  }
+  if (device < 0 || device >= n) return CT_ERR_INVALID_ARGUMENT;
+  if (cudaSetDevice(device) != cudaSuccess) return CT_ERR_NO_DEVICE;
+  cudaDeviceProp prop;
+  if (cudaGetDeviceProperties(&prop, device) != cudaSuccess) return CT_ERR_NO_DEVICE;
+  if (prop.major * 10 + prop.minor < 100) return CT_ERR_NO_DEVICE;  // built for sm_103a only
+  auto* c = new ct_ctx();
+  c->device = device;
+  if (cudaMalloc(&c->d_error, 256) != cudaSuccess || cudaMemset(c->d_error, 0, 256) != cudaSuccess) {
+    delete c;
+    return CT_ERR_OUT_OF_MEMORY;
+  }
+  *out = c;
+  return CT_OK;
+}
+
+ct_status ct_ctx_destroy(ct_ctx* ctx) {
+  if (!ctx) return CT_ERR_INVALID_ARGUMENT;
+  cudaSetDevice(ctx->device);
+  cudaFree(ctx->d_error);
+  delete ctx;
+  return CT_OK;
+}
+
+const char* ct_last_error(const ct_ctx* ctx) {
+  if (!ctx) return "null context";
+  std::lock_guard<std::mutex> g(ctx->mu);
+  thread_local std::string copy;
+  copy = ctx->err;
+  return copy.c_str();
+}
+
+ct_status ct_ctx_set_memory_budget(ct_ctx* ctx, uint64_t bytes) {
+  if (!ctx) return CT_ERR_INVALID_ARGUMENT;
+  ctx->budget = bytes;
+  return CT_OK;
+}
+
+uint64_t ct_ctx_device_bytes(const ct_ctx* ctx) { return ctx ? ctx->bytes.load() : 0; }
+
+ct_status ct_ctx_check(ct_ctx* ctx, void* stream) {
+  if (!ctx) return CT_ERR_INVALID_ARGUMENT;
+  ct_status s = set_device(ctx);
+  if (s != CT_OK) return s;
+  CT_CUDA(ctx, cudaStreamSynchronize((cudaStream_t)stream));
+  uint32_t err = 0;
+  CT_CUDA(ctx, cudaMemcpy(&err, ctx->d_error, 4, cudaMemcpyDeviceToHost));
+  if (err) {
+    CT_CUDA(ctx, cudaMemset(ctx->d_error, 0, 4));
+    if (err & kErrStackOverflow)
+      return fail(ctx, CT_ERR_STACK_OVERFLOW, "a traversal stack limit was reached; affected rays report no hit");
+    return fail(ctx, CT_ERR_CUDA, "device error word " + std::to_string(err));
+  }
+  return CT_OK;
+}
+
+ct_status ct_scene_create(ct_ctx* ctx, const ct_scene_desc* d, ct_scene** out) {
+  if (!ctx || !d || !out) return fail(ctx, CT_ERR_INVALID_ARGUMENT, "null argument");
+  *out = nullptr;
+  if (!d->vertices || !d->normals || !d->indices) return fail(ctx, CT_ERR_INVALID_ARGUMENT, "vertices, normals and indices are required");
+  if (d->triangle_count == 0 || d->vertex_count == 0) return fail(ctx, CT_ERR_INVALID_ARGUMENT, "empty scene");
+  if (!d->materials || d->material_count == 0) return fail(ctx, CT_ERR_INVALID_ARGUMENT, "at least one material is required");
+  if (d->triangle_count >= (1u << 30)) return fail(ctx, CT_ERR_INVALID_ARGUMENT, "too many triangles");
+  const uint32_t nv = d->vertex_count, nt = d->triangle_count;
+  for (uint32_t i = 0; i < nv; i++)
+    if (!finite3(d->vertices + 3 * (size_t)i)) return fail(ctx, CT_ERR_INVALID_ARGUMENT, "non-finite vertex " + std::to_string(i));
+  for (uint64_t i = 0; i < 3ull * nt; i++)
+    if (d->indices[i] >= nv) return fail(ctx, CT_ERR_INVALID_ARGUMENT, "vertex index out of range in triangle " + std::to_string(i / 3));
+  if (d->material_indices)
+    for (uint32_t i = 0; i < nt; i++)
+      if (d->material_indices[i] >= d->material_count)
+        return fail(ctx, CT_ERR_INVALID_ARGUMENT, "material index out of range in triangle " + std::to_string(i));
+  if (d->light_count && !d->light_indices) return fail(ctx, CT_ERR_INVALID_ARGUMENT, "light_count without light_indices");
+  if (d->light_count > nt) return fail(ctx, CT_ERR_INVALID_ARGUMENT, "more lights than triangles");
+  for (uint32_t i = 0; i < d->light_count; i++)
+    if (d->light_indices[i] >= nt) return fail(ctx, CT_ERR_INVALID_ARGUMENT, "light index out of range");
+  if (d->texture_count && (!d->texture_dims || !d->texture_offsets || !d->texels))
+    return fail(ctx, CT_ERR_INVALID_ARGUMENT, "texture arrays missing");
+  for (uint32_t i = 0; i < d->texture_count; i++) {
+    const uint64_t w = d->texture_dims[2 * i], h = d->texture_dims[2 * i + 1];
+    if (w == 0 || h == 0 || (uint64_t)d->texture_offsets[i] + w * h > d->texel_count)
+      return fail(ctx, CT_ERR_INVALID_ARGUMENT, "texture " + std::to_string(i) + " exceeds the texel array");
+  }
+  auto tex_ok = [&](int32_t t) { return t < 0 || (uint32_t)t < d->texture_count; };
+  if (!tex_ok(d->skybox_texture)) return fail(ctx, CT_ERR_INVALID_ARGUMENT, "skybox texture out of range");
+  for (uint32_t i = 0; i < d->material_count; i++) {
+    const ct_material& m = d->materials[i];
+    if (!tex_ok(m.diffuse_tex) || !tex_ok(m.normal_tex)) return fail(ctx, CT_ERR_INVALID_ARGUMENT, "material texture out of range");
+    if (m.type < 0 || m.type > CT_MAT_FRESNEL_TROWBRIDGE) return fail(ctx, CT_ERR_INVALID_ARGUMENT, "unknown material type");
+  }
+  ct_status s = set_device(ctx);
+  if (s != CT_OK) return s;
+  auto* sc = new ct_scene();
+  sc->nv = nv;
+  sc->nt = nt;
+  sc->verts.assign(d->vertices, d->vertices + 3 * (size_t)nv);
+  sc->idx.assign(d->indices, d->indices + 3 * (size_t)nt);
+  sc->mats.assign(d->materials, d->materials + d->material_count);
+  std::vector<float4> v4(nv), n4(nv), cn(nt);
+  std::vector<float2> uv(nv, make_float2(0.0f, 0.0f));
+  std::vector<uint4> i4(nt);
+  for (uint32_t i = 0; i < nv; i++) {
+    const float* p = d->vertices + 3 * (size_t)i;
+    const float* n = d->normals + 3 * (size_t)i;
+    v4[i] = make_float4(p[0], p[1], p[2], 0.0f);
+    n4[i] = make_float4(n[0], n[1], n[2], 0.0f);
+    if (d->texcoords) uv[i] = make_float2(d->texcoords[2 * (size_t)i], d->texcoords[2 * (size_t)i + 1]);
+  }
+  for (uint32_t i = 0; i < nt; i++) {
+    const uint32_t* t = d->indices + 3 * (size_t)i;
+    i4[i] = make_uint4(t[0], t[1], t[2], d->material_indices ? d->material_indices[i] : 0u);
+    if (d->center_normals) {
+      const float* c = d->center_normals + 3 * (size_t)i;
+      cn[i] = make_float4(c[0], c[1], c[2], 0.0f);
+    } else {
+      // (n0 + n1 + n2) / 3.0f, TriangleList.cpp:140
+      const float* a = d->normals + 3 * (size_t)t[0];
+      const float* b = d->normals + 3 * (size_t)t[1];
+      const float* c = d->normals + 3 * (size_t)t[2];
+      cn[i] = make_float4(((a[0] + b[0]) + c[0]) / 3.0f, ((a[1] + b[1]) + c[1]) / 3.0f, ((a[2] + b[2]) + c[2]) / 3.0f,
+                          0.0f);
+    }
+  }
+  std::vector<DevMaterial> dm(d->material_count);
+  for (uint32_t i = 0; i < d->material_count; i++) dm[i] = to_dev(d->materials[i]);
+  std::vector<uint2> dims(d->texture_count);
+  for (uint32_t i = 0; i < d->texture_count; i++) dims[i] = make_uint2(d->texture_dims[2 * i], d->texture_dims[2 * i + 1]);
+  DevScene& ds = sc->dev;
+  float4 *dv = nullptr, *dn = nullptr, *dc = nullptr, *dt = nullptr;
+  float2* duv = nullptr;
+  uint4* di = nullptr;
+  uint32_t *dl = nullptr, *doff = nullptr;
+  uint2* ddim = nullptr;
+  if ((s = upload(ctx, sc->allocs, &dv, v4.data(), v4.size() * sizeof(float4))) != CT_OK ||
+      (s = upload(ctx, sc->allocs, &dn, n4.data(), n4.size() * sizeof(float4))) != CT_OK ||
+      (s = upload(ctx, sc->allocs, &duv, uv.data(), uv.size() * sizeof(float2))) != CT_OK ||
+      (s = upload(ctx, sc->allocs, &di, i4.data(), i4.size() * sizeof(uint4))) != CT_OK ||
+      (s = upload(ctx, sc->allocs, &dc, cn.data(), cn.size() * sizeof(float4))) != CT_OK ||
+      (s = upload(ctx, sc->allocs, &sc->d_mats, dm.data(), dm.size() * sizeof(DevMaterial))) != CT_OK ||
+      (s = upload(ctx, sc->allocs, &dl, d->light_indices, (size_t)d->light_count * 4)) != CT_OK ||
+      (s = upload(ctx, sc->allocs, &dt, d->texels, (size_t)d->texel_count * sizeof(float4))) != CT_OK ||
+      (s = upload(ctx, sc->allocs, &ddim, dims.data(), dims.size() * sizeof(uint2))) != CT_OK ||
+      (s = upload(ctx, sc->allocs, &doff, d->texture_offsets, (size_t)d->texture_count * 4)) != CT_OK) {
+    free_all(ctx, sc->allocs);
+    delete sc;
+    return s;
+  }
+  ds.verts = dv;
+  ds.normals = dn;
+  ds.uvs = duv;
+  ds.idx = di;
+  ds.cnormals = dc;
+  ds.mats = sc->d_mats;
+  ds.lights = dl;
+  ds.light_count = d->light_count;
+  ds.tri_count = nt;
+  ds.texels = dt;
+  ds.tex_dims = ddim;
+  ds.tex_offsets = doff;
+  ds.sky_tex = d->skybox_texture;
+  ds.tex_count = d->texture_count;
+  *out = sc;
+  return CT_OK;
+}
+
+ct_status ct_scene_destroy(ct_ctx* ctx, ct_scene* scene) {
+  if (!ctx || !scene) return CT_ERR_INVALID_ARGUMENT;
+  set_device(ctx);
+  free_all(ctx, scene->allocs);
+  delete scene;
+  return CT_OK;
+}
+
+ct_status ct_scene_set_material(ct_ctx* ctx, ct_scene* scene, uint32_t index, const ct_material* m) {
+  if (!ctx || !scene || !m) return fail(ctx, CT_ERR_INVALID_ARGUMENT, "null argument");
+  if (index >= scene->mats.size()) return fail(ctx, CT_ERR_INVALID_ARGUMENT, "material index out of range");
+  if (m->type < 0 || m->type > CT_MAT_FRESNEL_TROWBRIDGE) return fail(ctx, CT_ERR_INVALID_ARGUMENT, "unknown material type");
+  auto tex_ok = [&](int32_t t) { return t < 0 || (uint32_t)t < scene->dev.tex_count; };
+  if (!tex_ok(m->diffuse_tex) || !tex_ok(m->normal_tex)) return fail(ctx, CT_ERR_INVALID_ARGUMENT, "material texture out of range");
+  ct_status s = set_device(ctx);
+  if (s != CT_OK) return s;
+  scene->mats[index] = *m;
+  const DevMaterial dm = to_dev(*m);
+  CT_CUDA(ctx, cudaMemcpy(scene->d_mats + index, &dm, sizeof(dm), cudaMemcpyHostToDevice));
+  return CT_OK;
+}
+
+ct_status ct_bvh_build(ct_ctx* ctx, const ct_scene* scene, int32_t nthreads, ct_bvh** out) {
+  if (!ctx || !scene || !out) return fail(ctx, CT_ERR_INVALID_ARGUMENT, "null argument");
+  *out = nullptr;
+  ct_status s = set_device(ctx);
+  if (s != CT_OK) return s;
+  auto* b = new ct_bvh();
+  build_binary(scene->verts.data(), scene->idx.data(), scene->nt, nthreads, b->host);
+  collapse_quad(b->host);
+  if ((s = finish_bvh(ctx, scene, b)) != CT_OK) {
+    free_all(ctx, b->allocs);
+    delete b;
+    return s;
+  }
+  *out = b;
+  return CT_OK;
+}
+
+ct_status ct_bvh_import_quad(ct_ctx* ctx, const ct_scene* scene, const void* nodes, uint32_t node_count,
+                             const uint32_t* prim_indices, uint32_t prim_count, ct_bvh** out) {
+  if (!ctx || !scene || !nodes || !prim_indices || !out) return fail(ctx, CT_ERR_INVALID_ARGUMENT, "null argument");
+  *out = nullptr;
+  if (prim_count != scene->nt) return fail(ctx, CT_ERR_INVALID_ARGUMENT, "prim_count differs from the scene's triangle count");
+  for (uint32_t i = 0; i < prim_count; i++)
+    if (prim_indices[i] >= scene->nt) return fail(ctx, CT_ERR_INVALID_ARGUMENT, "primitive index out of range");
+  auto* b = new ct_bvh();
+  b->host.quad.resize(node_count);
+  std::memcpy(b->host.quad.data(), nodes, (size_t)node_count * sizeof(QuadNode));
+  b->host.prims.assign(prim_indices, prim_indices + prim_count);
+  std::string err = validate_quad(b->host.quad, prim_count);
+  ct_status s = err.empty() ? set_device(ctx) : fail(ctx, CT_ERR_INVALID_ARGUMENT, err);
+  if (s == CT_OK) s = finish_bvh(ctx, scene, b);
+  if (s != CT_OK) {
+    free_all(ctx, b->allocs);
+    delete b;
+    return s;
+  }
+  *out = b;
+  return CT_OK;
+}
+
+ct_status ct_bvh_import_binary(ct_ctx* ctx, const ct_scene* scene, const void* nodes, uint32_t node_count,
+                               const uint32_t* prim_indices, uint32_t prim_count, ct_bvh** out) {
+  if (!ctx || !scene || !nodes || !prim_indices || !out) return fail(ctx, CT_ERR_INVALID_ARGUMENT, "null argument");
+  *out = nullptr;
+  if (prim_count != scene->nt) return fail(ctx, CT_ERR_INVALID_ARGUMENT, "prim_count differs from the scene's triangle count");
+  for (uint32_t i = 0; i < prim_count; i++)
+    if (prim_indices[i] >= scene->nt) return fail(ctx, CT_ERR_INVALID_ARGUMENT, "primitive index out of range");
+  auto* b = new ct_bvh();
+  b->host.bin.resize(node_count);
+  std::memcpy(b->host.bin.data(), nodes, (size_t)node_count * sizeof(BinNode));
+  b->host.prims.assign(prim_indices, prim_indices + prim_count);
+  std::string err = validate_binary(b->host.bin, prim_count);
+  ct_status s = err.empty() ? set_device(ctx) : fail(ctx, CT_ERR_INVALID_ARGUMENT, err);
+  if (s == CT_OK) {
+    collapse_quad(b->host);
+    s = finish_bvh(ctx, scene, b);
+  }
+  if (s != CT_OK) {
+    free_all(ctx, b->allocs);
+    delete b;
+    return s;
+  }
+  *out = b;
+  return CT_OK;
+}
+
+ct_status ct_bvh_info_get(const ct_bvh* bvh, ct_bvh_info* info) {
+  if (!bvh || !info) return CT_ERR_INVALID_ARGUMENT;
+  *info = bvh->info;
+  return CT_OK;
+}
+
+ct_status ct_bvh_export(const ct_bvh* bvh, ct_bvh_layout layout, void* nodes, uint32_t* prim_indices) {
+  if (!bvh) return CT_ERR_INVALID_ARGUMENT;
+  if (layout == CT_BVH_BINARY) {
+    if (bvh->host.bin.empty() && nodes) return CT_ERR_UNSUPPORTED;
+    if (nodes) std::memcpy(nodes, bvh->host.bin.data(), bvh->host.bin.size() * sizeof(BinNode));
+  } else if (layout == CT_BVH_QUAD) {
+    if (nodes) std::memcpy(nodes, bvh->host.quad.data(), bvh->host.quad.size() * sizeof(QuadNode));
+  } else {
+    return CT_ERR_INVALID_ARGUMENT;
+  }
+  if (prim_indices) std::memcpy(prim_indices, bvh->host.prims.data(), bvh->host.prims.size() * 4);
+  return CT_OK;
+}
+
+ct_status ct_bvh_destroy(ct_ctx* ctx, ct_bvh* bvh) {
+  if (!ctx || !bvh) return CT_ERR_INVALID_ARGUMENT;
+  set_device(ctx);
+  free_all(ctx, bvh->allocs);
+  delete bvh;
+  return CT_OK;
+}
+
+struct ct_host_bvh {
+  HostBVH host;
+};
+
+ct_status ct_host_bvh_build(const float* vertices, uint32_t vertex_count, const uint32_t* indices,
+                            uint32_t triangle_count, int32_t nthreads, ct_host_bvh** out) {
+  if (!vertices || !indices || !out || triangle_count == 0 || vertex_count == 0) return CT_ERR_INVALID_ARGUMENT;
+  *out = nullptr;
+  for (uint32_t i = 0; i < vertex_count; i++)
+    if (!finite3(vertices + 3 * (size_t)i)) return CT_ERR_INVALID_ARGUMENT;
+  for (uint64_t i = 0; i < 3ull * triangle_count; i++)
+    if (indices[i] >= vertex_count) return CT_ERR_INVALID_ARGUMENT;
+  auto* h = new ct_host_bvh();
+  build_binary(vertices, indices, triangle_count, nthreads, h->host);
+  collapse_quad(h->host);
+  *out = h;
+  return CT_OK;
+}
+
+ct_status ct_host_bvh_counts(const ct_host_bvh* h, uint32_t* binary_nodes, uint32_t* quad_nodes, uint32_t* prims,
+                             double* build_ms, double* collapse_ms) {
+  if (!h) return CT_ERR_INVALID_ARGUMENT;
+  if (binary_nodes) *binary_nodes = (uint32_t)h->host.bin.size();
+  if (quad_nodes) *quad_nodes = (uint32_t)h->host.quad.size();
+  if (prims) *prims = (uint32_t)h->host.prims.size();
+  if (build_ms) *build_ms = h->host.build_ms;
+  if (collapse_ms) *collapse_ms = h->host.collapse_ms;
+  return CT_OK;
+}
+
+ct_status ct_host_bvh_export(const ct_host_bvh* h, ct_bvh_layout layout, void* nodes, uint32_t* prim_indices) {
+  if (!h) return CT_ERR_INVALID_ARGUMENT;
+  if (layout == CT_BVH_BINARY) {
+    if (nodes) std::memcpy(nodes, h->host.bin.data(), h->host.bin.size() * sizeof(BinNode));
+  } else if (layout == CT_BVH_QUAD) {
+    if (nodes) std::memcpy(nodes, h->host.quad.data(), h->host.quad.size() * sizeof(QuadNode));
+  } else {
+    return CT_ERR_INVALID_ARGUMENT;
+  }
+  if (prim_indices) std::memcpy(prim_indices, h->host.prims.data(), h->host.prims.size() * 4);
+  return CT_OK;
+}
+
+ct_status ct_host_bvh_destroy(ct_host_bvh* h) {
+  if (!h) return CT_ERR_INVALID_ARGUMENT;
+  delete h;
+  return CT_OK;
+}
+
+static ct_status check_rays(ct_ctx* ctx, const ct_bvh* bvh, const float* org, const float* dir, uint32_t n) {
+  if (!ctx || !bvh) return fail(ctx, CT_ERR_INVALID_ARGUMENT, "null argument");
+  if (n && (!org || !dir)) return fail(ctx, CT_ERR_INVALID_ARGUMENT, "null ray buffer");
+  if (((uintptr_t)org | (uintptr_t)dir) & 15) return fail(ctx, CT_ERR_INVALID_ARGUMENT, "ray buffers must be 16-byte aligned");
+  return set_device(ctx);
+}
+
+ct_status ct_trace_closest(ct_ctx* ctx, const ct_bvh* bvh, const float* org, const float* dir, int32_t* hit, float* t,
+                           uint32_t n, float tri_eps, void* stream) {
+  ct_status s = check_rays(ctx, bvh, org, dir, n);
+  if (s != CT_OK) return s;
+  if (n && (!hit || !t)) return fail(ctx, CT_ERR_INVALID_ARGUMENT, "null output buffer");
+  CT_CUDA(ctx, launch_trace_closest(bvh->dev, (const float4*)org, (const float4*)dir, hit, t, n, tri_eps, ctx->d_error,
+                                    (cudaStream_t)stream));
+  return CT_OK;
+}
+
+ct_status ct_trace_any(ct_ctx* ctx, const ct_bvh* bvh, const float* org, const float* dir, uint8_t* occluded,
+                       uint32_t n, float tri_eps, void* stream) {
+  ct_status s = check_rays(ctx, bvh, org, dir, n);
+  if (s != CT_OK) return s;
+  if (n && !occluded) return fail(ctx, CT_ERR_INVALID_ARGUMENT, "null output buffer");
+  CT_CUDA(ctx, launch_trace_any(bvh->dev, (const float4*)org, (const float4*)dir, occluded, n, tri_eps, ctx->d_error,
+                                (cudaStream_t)stream));
+  return CT_OK;
+}
+
+ct_status ct_render_create(ct_ctx* ctx, int32_t width, int32_t height, ct_render** out) {
+  if (!ctx || !out) return fail(ctx, CT_ERR_INVALID_ARGUMENT, "null argument");
+  *out = nullptr;
+  if (width <= 0 || height <= 0 || (int64_t)width * height > (1ll << 28))
+    return fail(ctx, CT_ERR_INVALID_ARGUMENT, "bad render size");
+  ct_status s = set_device(ctx);
+  if (s != CT_OK) return s;
+  auto* r = new ct_render();
+  r->w = width;
+  r->h = height;
+  const size_t n = (size_t)width * height;
+  DevQueues& q = r->q;
+  q.capacity = (int32_t)n;
+  auto alloc4 = [&](float4** p) { return upload(ctx, r->allocs, p, nullptr, n * sizeof(float4)); };
+  if ((s = alloc4(&q.org[0])) != CT_OK || (s = alloc4(&q.org[1])) != CT_OK || (s = alloc4(&q.dir[0])) != CT_OK ||
+      (s = alloc4(&q.dir[1])) != CT_OK || (s = alloc4(&q.thr[0])) != CT_OK || (s = alloc4(&q.thr[1])) != CT_OK ||
+      (s = alloc4(&q.sorg)) != CT_OK || (s = alloc4(&q.sdir)) != CT_OK || (s = alloc4(&q.scol)) != CT_OK ||
+      (s = alloc4(&q.accum)) != CT_OK || (s = upload(ctx, r->allocs, &q.hit, nullptr, n * sizeof(int2))) != CT_OK ||
+      (s = upload(ctx, r->allocs, &q.counts, nullptr, 16 * sizeof(int32_t))) != CT_OK ||
+      (s = upload(ctx, r->allocs, &q.stats, nullptr, 8 * sizeof(unsigned long long))) != CT_OK) {
+    free_all(ctx, r->allocs);
+    delete r;
+    return s;
+  }
+  q.error = ctx->d_error;
+  *out = r;
+  return CT_OK;
+}
+
+ct_status ct_render_destroy(ct_ctx* ctx, ct_render* r) {
+  if (!ctx || !r) return CT_ERR_INVALID_ARGUMENT;
+  set_device(ctx);
+  free_all(ctx, r->allocs);
+  delete r;
+  return CT_OK;
+}
+
+ct_status ct_render_reset(ct_ctx* ctx, ct_render* r, void* stream) {
+  if (!ctx || !r) return fail(ctx, CT_ERR_INVALID_ARGUMENT, "null argument");
+  ct_status s = set_device(ctx);
+  if (s != CT_OK) return s;
+  CT_CUDA(ctx, cudaMemsetAsync(r->q.accum, 0, (size_t)r->w * r->h * sizeof(float4), (cudaStream_t)stream));
+  return CT_OK;
+}
+
+ct_status ct_render_accumulate(ct_ctx* ctx, const ct_scene* scene, const ct_bvh* bvh, const ct_camera* cam,
+                               const ct_render_params* p, ct_render* r, void* stream) {
+  if (!ctx || !scene || !bvh || !cam || !p || !r) return fail(ctx, CT_ERR_INVALID_ARGUMENT, "null argument");
+  if (p->width != r->w || p->height != r->h) return fail(ctx, CT_ERR_INVALID_ARGUMENT, "params size differs from the render job's");
+  if (p->max_depth < 1 || p->max_depth > 64) return fail(ctx, CT_ERR_INVALID_ARGUMENT, "max_depth must be in [1, 64]");
+  if (bvh->nt != scene->nt) return fail(ctx, CT_ERR_INVALID_ARGUMENT, "BVH was built for another scene");
+  if (p->shading_mode != CT_SHADE_COMPAT) return fail(ctx, CT_ERR_UNSUPPORTED, "shading mode not available");
+  if (!finite3(cam->position) || !finite3(cam->forward) || !finite3(cam->up) || !std::isfinite(cam->fov_deg))
+    return fail(ctx, CT_ERR_INVALID_ARGUMENT, "non-finite camera");
+  ct_status s = set_device(ctx);
+  if (s != CT_OK) return s;
+  cudaStream_t st = (cudaStream_t)stream;
+  // Camera constructor: m_PlaneDistance = tanf(radians(fov * 0.5f)) (Camera.cpp:16);
+  // sample(): u = normalize(cross(w, up)), v = normalize(cross(u, w)), aspect on the longer axis.
+  const float dist = tanf((cam->fov_deg * 0.5f) * 0.01745329251994329576923690768489f);
+  const float w[3] = {cam->forward[0], cam->forward[1], cam->forward[2]};
+  const float* up = cam->up;
+  auto cross = [](const float* a, const float* b, float* o) {
+    o[0] = a[1] * b[2] - b[1] * a[2];
+    o[1] = a[2] * b[0] - b[2] * a[0];
+    o[2] = a[0] * b[1] - b[0] * a[1];
+  };
+  auto normalize = [](float* v) {
+    const float d = (v[0] * v[0] + v[1] * v[1]) + v[2] * v[2];
+    const float inv = 1.0f / std::sqrt(d);
+    v[0] *= inv, v[1] *= inv, v[2] *= inv;
+  };
+  float u[3], v[3];
+  cross(w, up, u);
+  normalize(u);
+  cross(u, w, v);
+  normalize(v);
+  float hor[3] = {u[0] * dist, u[1] * dist, u[2] * dist};
+  float ver[3] = {v[0] * dist, v[1] * dist, v[2] * dist};
+  const float aspect = (float)p->width / (float)p->height;
+  if (p->width > p->height)
+    hor[0] *= aspect, hor[1] *= aspect, hor[2] *= aspect;
+  else
+    ver[0] *= aspect, ver[1] *= aspect, ver[2] *= aspect;
+  FrameConst f;
+  f.cam_pos = make_float3(cam->position[0], cam->position[1], cam->position[2]);
+  f.cam_w = make_float3(w[0], w[1], w[2]);
+  f.hor = make_float3(hor[0], hor[1], hor[2]);
+  f.ver = make_float3(ver[0], ver[1], ver[2]);
+  f.width = p->width;
+  f.height = p->height;
+  f.frame = p->frame_index;
+  f.normal_eps = p->normal_eps;
+  f.dist_eps = p->dist_eps;
+  f.tri_eps = p->tri_eps;
+  f.shadow = p->shadow;
+  f.indirect = p->indirect;
+  f.sky = p->sky;
+  f.shading_mode = p->shading_mode;
+  CT_CUDA(ctx, launch_raygen(r->q, f, p->exact_math, st));
+  for (int pass = 0; pass < p->max_depth; pass++) {
+    const int cur = pass & 1;
+    const int path_length = pass == 0 ? 0 : pass + 1;  // Kernel.cu:306, 330
+    CT_CUDA(ctx, launch_extend(bvh->dev, r->q, cur, p->tri_eps, st));
+    CT_CUDA(ctx, launch_shade(scene->dev, r->q, f, cur, path_length, p->exact_math, st));
+    if (p->shadow) CT_CUDA(ctx, launch_connect(bvh->dev, r->q, p->tri_eps, st));
+  }
+  return CT_OK;
+}
+
+ct_status ct_render_accum(const ct_render* r, float** accum_device) {
+  if (!r || !accum_device) return CT_ERR_INVALID_ARGUMENT;
+  *accum_device = (float*)r->q.accum;
+  return CT_OK;
+}
+
+ct_status ct_present(ct_ctx* ctx, const ct_render* r, float samples, float* rgba_device, void* stream) {
+  if (!ctx || !r || !rgba_device) return fail(ctx, CT_ERR_INVALID_ARGUMENT, "null argument");
+  if (((uintptr_t)rgba_device) & 15) return fail(ctx, CT_ERR_INVALID_ARGUMENT, "output must be 16-byte aligned");
+  ct_status s = set_device(ctx);
+  if (s != CT_OK) return s;
+  CT_CUDA(ctx, launch_present(r->q.accum, (float4*)rgba_device, r->w * r->h, samples, (cudaStream_t)stream));
+  return CT_OK;
+}
+
+ct_status ct_render_stats(ct_ctx* ctx, ct_render* r, ct_frame_stats* stats, int32_t reset, void* stream) {
+  if (!ctx || !r || !stats) return fail(ctx, CT_ERR_INVALID_ARGUMENT, "null argument");
+  ct_status s = set_device(ctx);
+  if (s != CT_OK) return s;
+  unsigned long long h[4] = {0, 0, 0, 0};
+  CT_CUDA(ctx, cudaStreamSynchronize((cudaStream_t)stream));
+  CT_CUDA(ctx, cudaMemcpy(h, r->q.stats, sizeof(h), cudaMemcpyDeviceToHost));
+  stats->extension_rays = h[0];
+  stats->shadow_rays = h[1];
+  stats->samples = h[2];
+  stats->frames = (uint32_t)h[3];
+  if (reset) CT_CUDA(ctx, cudaMemset(r->q.stats, 0, sizeof(h)));
+  return CT_OK;
+}
+
+}  // extern "C"

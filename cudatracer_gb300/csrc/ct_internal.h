@@ -1,0 +1,121 @@
+// Internal declarations shared by the host runtime (.cpp) and the kernels (.cu).
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include <cstddef>
+
+namespace ct {
+
+// ---------------------------------------------------------------------------
+// Device data layout (all arrays in HBM, 16-byte vector loads)
+// ---------------------------------------------------------------------------
+
+// Quad-BVH node: 128 bytes, 128-byte aligned, read as eight LDG.128. Bounds are
+// the reference MBVHNode planes bit for bit (src/BVH/MBVHNode.cuh:35-60) so the
+// slab test and its child order reproduce the reference; children are packed
+// 32-bit references:
+//   >= 0          inner node index
+//   kEmptyChild   unused slot (the reference keeps count 0 there)
+//   bit 31 set    leaf: first = ref & first_mask, count = (ref >> leaf_shift) & count_mask
+struct __align__(128) QNodeDev {
+  float4 bminx, bmaxx, bminy, bmaxy, bminz, bmaxz;
+  int4 child;
+  int4 meta;  // reserved, zero
+};
+static_assert(sizeof(QNodeDev) == 128, "QNodeDev is 128 bytes");
+constexpr int32_t kEmptyChild = -1;
+
+// Triangle in leaf order, 48 bytes: {p0.xyz, prim id}, {p1-p0, 0}, {p2-p0, 0}.
+// The edges are the exact float differences the reference forms per test
+// (src/Core/Triangle.cuh:15-16), precomputed once.
+
+struct DevBVH {
+  const QNodeDev* nodes;
+  const float4* tris;  // 3 float4 per leaf slot
+  uint32_t leaf_shift;
+  uint32_t first_mask;
+  uint32_t count_mask;
+  uint32_t prim_count;
+  uint32_t node_count;
+  int32_t stack_entries;
+};
+
+// 64-byte material (reference Material fields, padded to 4 x float4).
+struct __align__(16) DevMaterial {
+  float4 albedo_ior;      // albedo/emission xyz, refractIdx
+  int4 tex;               // diffuse, normal, mask, displace texture ids
+  float4 type_rough;      // type (as int bits), roughness, 0, 0
+  float4 absorption;      // xyz, 0
+};
+
+struct DevScene {
+  const float4* verts;     // per vertex, w = 0
+  const float4* normals;   // per vertex
+  const float2* uvs;       // per vertex
+  const uint4* idx;        // per triangle, w = material index
+  const float4* cnormals;  // per triangle centre normal
+  const DevMaterial* mats;
+  const uint32_t* lights;
+  uint32_t light_count;
+  uint32_t tri_count;
+  const float4* texels;
+  const uint2* tex_dims;
+  const uint32_t* tex_offsets;
+  int32_t sky_tex;
+  uint32_t tex_count;
+};
+
+// Per-job wavefront state (SoA queues, 16-byte records).
+struct DevQueues {
+  float4* org[2];    // origin xyz, w = pixel index (int bits)
+  float4* dir[2];    // direction xyz, w = last bounce type (int bits: 0 specular, 1 diffuse)
+  float4* thr[2];    // throughput xyz, w = last BSDF pdf
+  int2* hit;         // closest hit: x = primitive id, y = t (float bits)
+  float4* sorg;      // shadow origin xyz, w = pixel
+  float4* sdir;      // shadow direction xyz, w = max distance
+  float4* scol;      // shadow contribution xyz, w unused
+  float4* accum;     // FP32 RGBA accumulation, one per pixel
+  // device counters
+  int32_t* counts;   // [0],[1] ray queue sizes, [2] shadow queue size
+  unsigned long long* stats;  // [0] extension rays, [1] shadow rays, [2] samples, [3] frames
+  uint32_t* error;   // error bits (1 = stack overflow)
+  int32_t capacity;
+  // queue selection without dynamic indexing into the (by-value) parameter struct
+  __host__ __device__ float4* org_q(int i) const { return i ? org[1] : org[0]; }
+  __host__ __device__ float4* dir_q(int i) const { return i ? dir[1] : dir[0]; }
+  __host__ __device__ float4* thr_q(int i) const { return i ? thr[1] : thr[0]; }
+};
+
+struct FrameConst {
+  float3 cam_pos, cam_w, hor, ver;
+  int32_t width, height;
+  uint32_t frame;
+  float normal_eps, dist_eps, tri_eps;
+  int32_t shadow, indirect, sky;
+  int32_t shading_mode;
+};
+
+enum : uint32_t { kErrStackOverflow = 1u };
+
+// ---------------------------------------------------------------------------
+// Kernel launchers (defined in the .cu files)
+// ---------------------------------------------------------------------------
+int sm_count();
+
+cudaError_t launch_trace_closest(const DevBVH& b, const float4* org, const float4* dir, int32_t* hit, float* t,
+                                 uint32_t n, float eps, uint32_t* err, cudaStream_t s);
+cudaError_t launch_trace_any(const DevBVH& b, const float4* org, const float4* dir, uint8_t* occ, uint32_t n,
+                             float eps, uint32_t* err, cudaStream_t s);
+
+// wavefront stages; the active count lives at counts[queue] on the device
+cudaError_t launch_extend(const DevBVH& b, const DevQueues& q, int queue, float eps, cudaStream_t s);
+cudaError_t launch_connect(const DevBVH& b, const DevQueues& q, float eps, cudaStream_t s);
+cudaError_t launch_raygen(const DevQueues& q, const FrameConst& f, int exact, cudaStream_t s);
+cudaError_t launch_shade(const DevScene& sc, const DevQueues& q, const FrameConst& f, int queue, int path_length,
+                         int exact, cudaStream_t s);
+cudaError_t launch_reset_counts(const DevQueues& q, int next_queue, cudaStream_t s);
+cudaError_t launch_present(const float4* accum, float4* out, int n, float samples, cudaStream_t s);
+
+}  // namespace ct

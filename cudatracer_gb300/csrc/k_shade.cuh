@@ -1,0 +1,335 @@
+// Ray generation, shading and presentation kernels of the wavefront loop.
+//
+// This file is compiled twice: k_shade_exact.cu (-fmad=false, sin/cos/atan2/
+// acos evaluated in double and rounded once: reproducible bit for bit by the
+// CPU oracle) and k_shade_fast.cu (FMA contraction and CUDA's float
+// transcendentals). CT_SHADE_NS names the namespace, CT_EXACT selects the math.
+//
+// Compat shading restates the reference's `shade` kernel
+// (src/CUDA/Kernel.cu:88-206) with its BSDF (src/Core/BSDF.h:26-63): every
+// non-emitter is shaded by roughness (mirror below 0.1, cosine-weighted
+// Lambert otherwise) and next-event estimation samples one light triangle
+// with the balance heuristic. Surviving paths and shadow rays are appended to
+// their queues with one atomic per warp (ballot + popcount prefix) instead of
+// the reference's per-thread atomicAdd.
+#pragma once
+
+#include "ct_internal.h"
+#include "vmath.cuh"
+
+#ifndef CT_SHADE_NS
+#error "define CT_SHADE_NS"
+#endif
+
+namespace ct {
+namespace CT_SHADE_NS {
+
+constexpr float kMaxDistance = 1e34f;
+constexpr float kOneOverPi = 0.318309886183790671537767526745028724f;
+constexpr float kTwoPi = 6.28318530717958647692528676655900576f;
+constexpr int kBlock = 128;
+
+#if CT_EXACT
+__device__ __forceinline__ float xsin(float x) { return (float)sin((double)x); }
+__device__ __forceinline__ float xcos(float x) { return (float)cos((double)x); }
+__device__ __forceinline__ float xatan2(float y, float x) { return (float)atan2((double)y, (double)x); }
+__device__ __forceinline__ float xacos(float x) { return (float)acos((double)x); }
+#else
+__device__ __forceinline__ float xsin(float x) { return sinf(x); }
+__device__ __forceinline__ float xcos(float x) { return cosf(x); }
+__device__ __forceinline__ float xatan2(float y, float x) { return atan2f(y, x); }
+__device__ __forceinline__ float xacos(float x) { return acosf(x); }
+#endif
+
+// ---- RNG: src/Core/Random.cuh:10-34 ----
+__device__ __forceinline__ uint32_t wang_hash(uint32_t s) {
+  s = (s ^ 61u) ^ (s >> 16);
+  s *= 9u;
+  s = s ^ (s >> 4);
+  s *= 0x27d4eb2du;
+  s = s ^ (s >> 15);
+  return s;
+}
+__device__ __forceinline__ uint32_t rnd_int(uint32_t& s) {
+  s ^= s << 13;
+  s ^= s << 17;
+  s ^= s << 5;
+  return s;
+}
+__device__ __forceinline__ float rnd_float(uint32_t& s) { return (float)rnd_int(s) * 2.3283064365387e-10f; }
+__device__ __forceinline__ int rnd_int_max(uint32_t& s, int maxv) {
+  return (int)(rnd_float(s) * ((float)maxv + 0.99999f));
+}
+
+// Texel index of SceneData::getTextureColor (src/Core/SceneData.cuh:81-97).
+// For finite uv this is the reference's index; NaN or out-of-range values are
+// clamped to the texture instead of reading past it.
+__device__ __forceinline__ uint32_t texel_index(const DevScene& sc, int tex, float x, float y) {
+  const uint2 dim = __ldg(sc.tex_dims + tex);
+  const float fx = x * (float)(dim.x - 1), fy = y * (float)(dim.y - 1);
+  uint32_t ix = fx >= 0.0f ? (uint32_t)fminf(fx, (float)(dim.x - 1)) : 0u;
+  uint32_t iy = fy >= 0.0f ? (uint32_t)fminf(fy, (float)(dim.y - 1)) : 0u;
+  return __ldg(sc.tex_offsets + tex) + (ix + iy * dim.x);
+}
+__device__ __forceinline__ float4 tex_color(const DevScene& sc, int tex, float u, float v) {
+  float x = fmodf(u, 1.0f), y = fmodf(v, 1.0f);
+  if (x < 0) x += 1.0f;
+  if (y < 0) y += 1.0f;
+  return __ldg(sc.texels + texel_index(sc, tex, x, y));
+}
+// SceneData::getTextureNormal (src/Core/SceneData.cuh:99-116): no wrap, only +1 for negatives
+__device__ __forceinline__ V3 tex_normal(const DevScene& sc, int tex, float u, float v) {
+  float x = u, y = v;
+  if (x < 0) x += 1.0f;
+  if (y < 0) y += 1.0f;
+  return normalize(v3(__ldg(sc.texels + texel_index(sc, tex, x, y))));
+}
+// convertToLocalSpace (src/Core/Random.cuh:37-42) + localToWorld
+__device__ __forceinline__ V3 sample_to_world(V3 s, V3 n) {
+  const V3 W = fabsf(n.x) > 0.99f ? v3(0.0f, 1.0f, 0.0f) : v3(1.0f, 0.0f, 0.0f);
+  const V3 T = normalize(cross(n, W));
+  const V3 B = cross(n, T);
+  return (T * s.x + B * s.y) + n * s.z;
+}
+
+__device__ __forceinline__ void accum_add(float4* accum, int pix, V3 c) {
+  float4 a = accum[pix];
+  a.x += c.x;
+  a.y += c.y;
+  a.z += c.z;
+  a.w += 1.0f;
+  accum[pix] = a;
+}
+
+// Heron's formula, triangle::getArea (src/Core/Triangle.cuh:89-95)
+__device__ __forceinline__ float tri_area(V3 p0, V3 p1, V3 p2) {
+  const float a = length(p0 - p1), b = length(p1 - p2), c = length(p2 - p0);
+  const float s = ((a + b) + c) / 2.f;
+  return sqrtf(((s * (s - a)) * (s - b)) * (s - c));
+}
+
+struct Emit {
+  bool cont, shadow;
+  float4 no, nd, nt;  // continuation ray
+  float4 so, sd, sc;  // shadow ray
+};
+
+// One ray of the compat shade stage.
+__device__ __forceinline__ void shade_compat(const DevScene& sc, const DevQueues& q, const FrameConst& f, int cur,
+                                             int i, uint32_t path_length, Emit& e) {
+  const float4 o4 = q.org_q(cur)[i], d4 = q.dir_q(cur)[i], t4 = q.thr_q(cur)[i];
+  const int2 h = q.hit[i];
+  const int pix = __float_as_int(o4.w);
+  V3 org = v3(o4), dir = v3(d4), T = v3(t4);
+  const float last_pdf = t4.w;
+  const bool last_specular = __float_as_int(d4.w) == 0;
+  const float t = __int_as_float(h.y);
+  if (!(t < kMaxDistance)) {
+    if (f.sky && sc.sky_tex >= 0) {
+      const float u = 1.0f + (xatan2(dir.x, -dir.z) * kOneOverPi) * 0.5f;
+      const float v = 1.0f - xacos(dir.y) * kOneOverPi;
+      const float4 tc = tex_color(sc, sc.sky_tex, u, v);
+      accum_add(q.accum, pix, (T / last_pdf) * v3(tc));
+    }
+    return;
+  }
+  const int prim = h.x;
+  const uint4 ti = __ldg(sc.idx + prim);
+  V3 N = v3(__ldg(sc.cnormals + prim));
+  const V3 p0 = v3(__ldg(sc.verts + ti.x)), p1 = v3(__ldg(sc.verts + ti.y)), p2 = v3(__ldg(sc.verts + ti.z));
+  // triangle::getBaryCoords at the ray ORIGIN, before it moves (Kernel.cu:107)
+  const float aABC = dot(N, cross(p1 - p0, p2 - p0));
+  const float aPBC = dot(N, cross(p1 - org, p2 - org));
+  const float aPCA = dot(N, cross(p2 - org, p0 - org));
+  const float ba = aPBC / aABC, bb = aPCA / aABC, bc = (1.f - ba) - bb;
+  V3 iN = (v3(__ldg(sc.normals + ti.x)) * ba + v3(__ldg(sc.normals + ti.y)) * bb) + v3(__ldg(sc.normals + ti.z)) * bc;
+  const float2 uv0 = __ldg(sc.uvs + ti.x), uv1 = __ldg(sc.uvs + ti.y), uv2 = __ldg(sc.uvs + ti.z);
+  const float tu = (uv0.x * ba + uv1.x * bb) + uv2.x * bc;
+  const float tv = (uv0.y * ba + uv1.y * bb) + uv2.y * bc;
+  const DevMaterial* mp = sc.mats + ti.w;
+  const float4 alb = __ldg(&mp->albedo_ior);
+  const int4 mtex = __ldg(&mp->tex);
+  const float4 tr = __ldg(&mp->type_rough);
+  const int mtype = __float_as_int(tr.x);
+  if (mtex.y >= 0) iN = sample_to_world(tex_normal(sc, mtex.y, tu, tv), iN);
+  if (mtype == 0) {  // emitter (Kernel.cu:114-136)
+    if (!f.indirect) return;
+    const float DdotNL = -dot(dir, iN);
+    V3 c;
+    if (last_specular) {
+      c = T * v3(alb);
+    } else {
+      const float lightPDF = ((t * t) / (DdotNL * tri_area(p0, p1, p2))) * (float)sc.light_count;
+      c = (T * v3(alb)) * (1.0f / (last_pdf + lightPDF));
+    }
+    accum_add(q.accum, pix, vmax0(c));
+    return;
+  }
+  org = org + dir * t;  // getHitpoint
+  T = vmax0(T / last_pdf);
+  const float flip = dot(dir, N) > 0 ? -1.0f : 1.0f;
+  N = N * flip;
+  iN = iN * flip;
+  uint32_t seed = wang_hash((uint32_t)pix * 16789u + f.frame * 1791u + path_length * 720898027u);
+  V3 color = v3(alb);
+  if (mtex.x >= 0) color = v3(tex_color(sc, mtex.x, tu, tv));
+  // SampleBSDF (BSDF.h:33-63); its two random numbers are drawn left to right
+  const float r3 = rnd_float(seed), r4 = rnd_float(seed);
+  V3 wo, fval;
+  float pdf;
+  bool diffuse;  // the reference leaves the type unset when pdf = 0; NEE still runs then
+  if (tr.y < 0.1f) {
+    wo = dir - (iN * dot(iN, dir)) * 2.0f;  // reflect(-wi, iN)
+    if (dot(N, wo) <= 0.0f) {
+      pdf = 0.0f;
+      fval = v3(0, 0, 0);
+      diffuse = true;
+    } else {
+      pdf = 1.0f;
+      diffuse = false;
+      fval = color * (1.0f / fabsf(dot(iN, wo)));
+    }
+  } else {
+    // DiffuseReflectionCosWeighted (Tools.h:162-169): sqrt(1.0 - r1) in double
+    const float term1 = kTwoPi * r3;
+    const float term2 = (float)sqrt(1.0 - (double)r4);
+    const float sn = xsin(term1), cs = xcos(term1);
+    const V3 vl = v3(cs * term2, sn * term2, sqrtf(r4));
+    // Tangent2World (Tools.h:110-137)
+    V3 B, Tt;
+    const V3 n = iN;
+    if (n.z < 0.) {
+      const float a = 1.0f / (1.0f - n.z);
+      const float b = (n.x * n.y) * a;
+      B = v3(1.0f - (n.x * n.x) * a, -b, n.x);
+      Tt = v3(b, (n.y * n.y) * a - 1.0f, -n.y);
+    } else {
+      const float a = 1.0f / (1.0f + n.z);
+      const float b = (-n.x * n.y) * a;
+      B = v3(1.0f - (n.x * n.x) * a, b, -n.x);
+      Tt = v3(b, 1.0f - (n.y * n.y) * a, -n.y);
+    }
+    wo = normalize((Tt * vl.x + B * vl.y) + n * vl.z);
+    if (dot(N, wo) <= 0.0f) {
+      pdf = 0.0f;
+      fval = v3(0, 0, 0);
+    } else {
+      pdf = gmax(0.0f, dot(wo, iN)) * kOneOverPi;
+      fval = color * kOneOverPi;
+    }
+    diffuse = true;
+  }
+  bool specular_next = !diffuse;
+  dir = wo;
+  if (diffuse && f.shadow && sc.light_count > 0) {
+    // RandomIntMax; clamped because float rounding can reach light_count above 2^24 lights
+    const int light = min(rnd_int_max(seed, (int)sc.light_count - 1), (int)sc.light_count - 1);
+    const uint32_t lprim = __ldg(sc.lights + light);
+    const uint4 li = __ldg(sc.idx + lprim);
+    const V3 l0 = v3(__ldg(sc.verts + li.x)), l1 = v3(__ldg(sc.verts + li.y)), l2 = v3(__ldg(sc.verts + li.z));
+    float q1 = rnd_float(seed), q2 = rnd_float(seed);
+    if (q1 + q2 > 1.0f) q1 = 1.0f - q1, q2 = 1.0f - q2;  // getRandomPointOnSurface
+    const float qa = (1.0f - q1) - q2;
+    const V3 lp = (l0 * qa + l1 * q1) + l2 * q2;
+    V3 L = lp - org;
+    const float sq = dot(L, L);
+    const float dist = sqrtf(sq);
+    L = L / dist;
+    const V3 lN = v3(__ldg(sc.cnormals + lprim));
+    const float NdotL = dot(iN, L);
+    const float LNdotL = -dot(lN, L);
+    if (NdotL > 0 && LNdotL > 0) {
+      const float area = tri_area(l0, l1, l2);
+      // emission of material m_MaterialIdxs[light]: the light-LIST index (Kernel.cu:178)
+      const uint32_t em_mat = __ldg(&sc.idx[light].w);
+      const V3 em = v3(__ldg(&sc.mats[em_mat].albedo_ior));
+      const float shadowPDF = fabsf(dot(L, iN)) * kOneOverPi;  // EvaluateBSDF (BSDF.h:26-31)
+      const V3 sb = color * kOneOverPi;
+      if (shadowPDF > 0) {
+        const float lightPDF = (sq / (LNdotL * area)) * (float)sc.light_count;
+        const V3 scol = ((T * em) * sb) * (NdotL / (shadowPDF + lightPDF));
+        e.shadow = true;
+        e.so = f4(org + L * f.normal_eps, __int_as_float(pix));
+        e.sd = f4(L, dist - 2.0f * f.dist_eps);
+        e.sc = f4(scol, 0.0f);
+      }
+    }
+    specular_next = false;
+  }
+  if (pdf < 1e-6f || isnan(pdf) || isnan(T.x) || isnan(T.y) || isnan(T.z) ||
+      (T.x <= 0.0f && T.y <= 0.0f && T.z <= 0.0f))
+    return;
+  T = vmax0((T * fval) * fabsf(dot(iN, dir)));
+  org = org + N * f.normal_eps;
+  e.cont = true;
+  e.no = f4(org, __int_as_float(pix));
+  e.nd = f4(dir, __int_as_float(specular_next ? 0 : 1));
+  e.nt = f4(T, pdf);
+}
+
+// Warp-aggregated append: one atomicAdd per warp, lanes take popc-prefix slots.
+__device__ __forceinline__ int warp_append(bool want, int* counter) {
+  const unsigned m = __ballot_sync(0xffffffffu, want);
+  if (m == 0) return -1;
+  const int lane = threadIdx.x & 31;
+  int base = 0;
+  if (lane == __ffs(m) - 1) base = atomicAdd(counter, __popc(m));
+  base = __shfl_sync(0xffffffffu, base, __ffs(m) - 1);
+  return want ? base + __popc(m & ((1u << lane) - 1u)) : -1;
+}
+
+__global__ void __launch_bounds__(kBlock) k_shade(DevScene sc, DevQueues q, FrameConst f, int cur,
+                                                   uint32_t path_length) {
+  const int n = q.counts[cur];
+  const int nxt = cur ^ 1;
+  const int lane = threadIdx.x & 31;
+  const int stride = gridDim.x * kBlock;
+  for (int base = blockIdx.x * kBlock + (threadIdx.x & ~31); base < n; base += stride) {
+    const int i = base + lane;
+    Emit e;
+    e.cont = false;
+    e.shadow = false;
+    if (i < n) shade_compat(sc, q, f, cur, i, path_length, e);
+    const int si = warp_append(e.shadow, &q.counts[2]);
+    if (si >= 0) {
+      q.sorg[si] = e.so;
+      q.sdir[si] = e.sd;
+      q.scol[si] = e.sc;
+    }
+    const int ci = warp_append(e.cont, &q.counts[nxt]);
+    if (ci >= 0) {
+      q.org_q(nxt)[ci] = e.no;
+      q.dir_q(nxt)[ci] = e.nd;
+      q.thr_q(nxt)[ci] = e.nt;
+    }
+  }
+}
+
+// generatePrimaryRays + Ray::generate (Kernel.cu:208-234, Ray.cuh:85-95) with
+// start_position = 0: buffer index == pixel.
+__global__ void __launch_bounds__(kBlock) k_raygen(DevQueues q, FrameConst f) {
+  const int npix = f.width * f.height;
+  if (blockIdx.x == 0 && threadIdx.x == 0) {
+    q.counts[0] = npix;
+    atomicAdd(&q.stats[2], (unsigned long long)npix);
+    atomicAdd(&q.stats[3], 1ull);
+  }
+  const float invw = 1.0f / (float)f.width, invh = 1.0f / (float)f.height;
+  const V3 w = v3(f.cam_w.x, f.cam_w.y, f.cam_w.z), hor = v3(f.hor.x, f.hor.y, f.hor.z),
+           ver = v3(f.ver.x, f.ver.y, f.ver.z);
+  for (int i = blockIdx.x * kBlock + threadIdx.x; i < npix; i += gridDim.x * kBlock) {
+    uint32_t seed = ((uint32_t)i + f.frame * 147565741u) * 720898027u;
+    const int x = i % f.width, y = (i / f.width) % f.height;
+    const float px = ((float)x + rnd_float(seed)) - 0.5f;
+    const float py = ((float)y + rnd_float(seed)) - 0.5f;
+    const float sx = 2.0f * (px * invw) - 1.0f;
+    const float sy = 1.0f - 2.0f * (py * invh);
+    const V3 p = (w + hor * sx) + ver * sy;
+    q.org_q(0)[i] = make_float4(f.cam_pos.x, f.cam_pos.y, f.cam_pos.z, __int_as_float(i));
+    q.dir_q(0)[i] = f4(normalize(p), __int_as_float(0));  // lastBounceType = SPECULAR
+    q.thr_q(0)[i] = make_float4(1.0f, 1.0f, 1.0f, 1.0f);  // throughput 1, lastBsdfPDF 1
+  }
+}
+
+}  // namespace CT_SHADE_NS
+}  // namespace ct

@@ -1,0 +1,62 @@
+// Fast build of the shading kernels (FMA contraction, CUDA float
+// transcendentals), plus the launchers that pick a build and the present pass.
+#define CT_SHADE_NS fast
+#define CT_EXACT 0
+#include "k_shade.cuh"
+
+namespace ct {
+namespace exact {
+__global__ void __launch_bounds__(128) k_shade(DevScene sc, DevQueues q, FrameConst f, int cur, uint32_t path_length);
+__global__ void __launch_bounds__(128) k_raygen(DevQueues q, FrameConst f);
+}  // namespace exact
+
+namespace {
+constexpr int kBlock = 128;
+
+template <typename K>
+int fill_grid(K kernel, int work) {
+  int per_sm = 0;
+  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kernel, kBlock, 0);
+  if (per_sm <= 0) per_sm = 1;
+  const int blocks = (work + kBlock - 1) / kBlock;
+  return blocks < per_sm * sm_count() ? (blocks > 0 ? blocks : 1) : per_sm * sm_count();
+}
+
+// draw_framebuffer (src/CUDA/Kernel.cu:258-270) into a device buffer.
+__global__ void k_present(const float4* __restrict__ accum, float4* __restrict__ out, int n, float samples) {
+  const float e = 1.0f / 2.2f;
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+    const float4 a = accum[i];
+    out[i] = make_float4(powf(a.x / samples, e), powf(a.y / samples, e), powf(a.z / samples, e), 1.0f);
+  }
+}
+}  // namespace
+
+cudaError_t launch_raygen(const DevQueues& q, const FrameConst& f, int exact_math, cudaStream_t s) {
+  const int npix = f.width * f.height;
+  if (exact_math) {
+    exact::k_raygen<<<fill_grid(exact::k_raygen, npix), kBlock, 0, s>>>(q, f);
+  } else {
+    fast::k_raygen<<<fill_grid(fast::k_raygen, npix), kBlock, 0, s>>>(q, f);
+  }
+  return cudaGetLastError();
+}
+
+cudaError_t launch_shade(const DevScene& sc, const DevQueues& q, const FrameConst& f, int queue, int path_length,
+                         int exact_math, cudaStream_t s) {
+  if (exact_math) {
+    exact::k_shade<<<fill_grid(exact::k_shade, q.capacity), kBlock, 0, s>>>(sc, q, f, queue, (uint32_t)path_length);
+  } else {
+    fast::k_shade<<<fill_grid(fast::k_shade, q.capacity), kBlock, 0, s>>>(sc, q, f, queue, (uint32_t)path_length);
+  }
+  return cudaGetLastError();
+}
+
+cudaError_t launch_present(const float4* accum, float4* out, int n, float samples, cudaStream_t s) {
+  if (n <= 0) return cudaSuccess;
+  const int grid = (n + 255) / 256 < 4096 ? (n + 255) / 256 : 4096;
+  k_present<<<grid, 256, 0, s>>>(accum, out, n, samples);
+  return cudaGetLastError();
+}
+
+}  // namespace ct

@@ -1,0 +1,236 @@
+/*
+ * cudatracer.h - C ABI of the GB300 (sm_103a) wavefront path tracer.
+ *
+ * Plain C: opaque handles, plain pointers and sizes, status codes. No CUDA or
+ * C++ types cross this boundary; `stream` arguments are a cudaStream_t passed
+ * as void* (NULL = the legacy default stream). Every call returns a ct_status
+ * and never aborts the process; ct_last_error() gives the message of the most
+ * recent failure on a context.
+ *
+ * Each entry point names the reference interface it replaces
+ * (meirbon/CudaTracer, paths relative to that project).
+ */
+#ifndef CUDATRACER_H_
+#define CUDATRACER_H_
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define CT_ABI_VERSION 1
+
+typedef enum ct_status {
+  CT_OK = 0,
+  CT_ERR_INVALID_ARGUMENT = 1, /* NULL pointer, bad size, index out of range, non-finite vertex */
+  CT_ERR_OUT_OF_MEMORY = 2,    /* device allocation refused (or the context's HBM budget exceeded) */
+  CT_ERR_CUDA = 3,             /* a CUDA runtime call failed; see ct_last_error */
+  CT_ERR_UNSUPPORTED = 4,      /* e.g. a BVH whose leaves cannot be encoded */
+  CT_ERR_TIMEOUT = 5,          /* a bounded device-side wait ran out */
+  CT_ERR_STACK_OVERFLOW = 6,   /* a traversal stack limit was reached; affected rays report no hit */
+  CT_ERR_NO_DEVICE = 7         /* no CUDA device, or the library was not built for it */
+} ct_status;
+
+typedef struct ct_ctx ct_ctx;
+typedef struct ct_scene ct_scene;
+typedef struct ct_bvh ct_bvh;
+typedef struct ct_render ct_render;
+
+/* Material record, byte-compatible with the reference `Material`
+ * (src/Core/Material.cuh:29-41, 52 bytes). `albedo` doubles as the emission of
+ * CT_MAT_LIGHT materials, exactly as the reference's union does. */
+typedef struct ct_material {
+  float albedo[3];
+  float refract_idx;
+  int32_t diffuse_tex;
+  int32_t normal_tex;
+  int32_t mask_tex;
+  int32_t displace_tex;
+  int32_t type; /* CT_MAT_* */
+  float roughness;
+  float absorption[3];
+} ct_material;
+
+/* Material types: the reference MaterialType values (src/Core/Material.cuh:13-27). */
+enum {
+  CT_MAT_LIGHT = 0,
+  CT_MAT_SPECULAR = 1,
+  CT_MAT_FRESNEL = 2,
+  CT_MAT_LAMBERTIAN = 3,
+  CT_MAT_BECKMANN = 4,
+  CT_MAT_GGX = 5,
+  CT_MAT_TROWBRIDGE = 6,
+  CT_MAT_FRESNEL_BECKMANN = 7,
+  CT_MAT_FRESNEL_GGX = 8,
+  CT_MAT_FRESNEL_TROWBRIDGE = 9
+};
+
+/* Scene arrays: the contents of the reference's device `SceneData`
+ * (src/Core/SceneData.cuh:18-45) as uploaded by Application::allocateTriangles
+ * (src/Application.cpp:156-193) and allocateTextures (:195-212). All arrays
+ * are HOST memory; ct_scene_create copies them and the caller keeps ownership. */
+typedef struct ct_scene_desc {
+  const float* vertices;          /* float3 per vertex (TriangleList::m_Vertices) */
+  const float* normals;           /* float3 per vertex (m_Normals), used as given */
+  const float* texcoords;         /* float2 per vertex (m_TexCoords), NULL = all zero */
+  uint32_t vertex_count;
+  const uint32_t* indices;        /* uint3 per triangle (m_Indices) */
+  const float* center_normals;    /* float3 per triangle (m_CenterNormals); NULL = (n0+n1+n2)/3 */
+  const uint32_t* material_indices; /* per triangle (m_MaterialIdxs), NULL = all 0 */
+  uint32_t triangle_count;
+  const ct_material* materials;   /* m_Materials */
+  uint32_t material_count;
+  const uint32_t* light_indices;  /* triangle ids of emitters (m_LightIndices); NULL = none */
+  uint32_t light_count;
+  const float* texels;            /* RGBA float4 texels of all textures, concatenated */
+  uint64_t texel_count;
+  const uint32_t* texture_dims;   /* (width, height) per texture */
+  const uint32_t* texture_offsets;/* first texel of each texture */
+  uint32_t texture_count;
+  int32_t skybox_texture;         /* texture index of the equirect sky, -1 = none */
+} ct_scene_desc;
+
+/* BVH layouts. BINARY and QUAD are the reference's BVHNode (32 B) and
+ * MBVHNode (128 B) trees (src/BVH/BVHNode.cuh:29-46, src/BVH/MBVHNode.cuh:35-63). */
+typedef enum ct_bvh_layout { CT_BVH_BINARY = 0, CT_BVH_QUAD = 1 } ct_bvh_layout;
+
+typedef struct ct_bvh_info {
+  uint32_t binary_node_count; /* 0 when the BVH was imported as a quad tree */
+  uint32_t quad_node_count;
+  uint32_t prim_count;
+  uint32_t max_leaf_size;
+  uint32_t quad_depth;        /* levels of the quad tree */
+  uint32_t stack_entries;     /* traversal stack entries per ray the kernels reserve */
+  double build_ms;            /* host binary SAH build */
+  double collapse_ms;         /* host quad collapse */
+  double upload_ms;
+  uint64_t device_bytes;
+} ct_bvh_info;
+
+/* Pinhole camera (core::Camera, src/Core/Camera.h:12-93): the basis and the
+ * plane distance tan(fov/2) are derived exactly as Camera's constructor and
+ * sample() do (src/Core/Camera.cpp:11-16, src/CUDA/Kernel.cu:274-290). */
+typedef struct ct_camera {
+  float position[3];
+  float forward[3];
+  float up[3];
+  float fov_deg;
+} ct_camera;
+
+enum { CT_SHADE_COMPAT = 0, CT_SHADE_FULL = 1 };
+
+/* Per-frame parameters: the reference `Params` (src/CUDA/Kernel.cuh:23-72) and
+ * SceneData flags/epsilons (src/Core/SceneData.cuh:19-45). Defaults from
+ * ct_render_params_default() match the reference: depth 5, shadow, indirect,
+ * sky on, epsilons 1e-5 / 1e-5 / 1e-3. */
+typedef struct ct_render_params {
+  int32_t width;
+  int32_t height;
+  int32_t max_depth;     /* extend+shade+connect passes per path (reference: 5) */
+  uint32_t frame_index;  /* RNG frame; the reference's launchKernels advances it by 2 per frame */
+  int32_t shading_mode;  /* CT_SHADE_COMPAT (reference shade) or CT_SHADE_FULL (all materials, MIS) */
+  int32_t exact_math;    /* 1: sin/cos/atan2/acos evaluated in double and rounded once (bit-reproducible) */
+  int32_t shadow;        /* SceneData::shadow */
+  int32_t indirect;      /* SceneData::indirect */
+  int32_t sky;           /* SceneData::skyboxEnabled (needs a skybox texture) */
+  float normal_eps;      /* SceneData::normalEpsilon */
+  float dist_eps;        /* SceneData::distEpsilon */
+  float tri_eps;         /* SceneData::triangleEpsilon */
+} ct_render_params;
+
+typedef struct ct_frame_stats {
+  uint64_t extension_rays; /* closest-hit rays traced since the last reset of the counters */
+  uint64_t shadow_rays;    /* any-hit rays traced */
+  uint64_t samples;        /* camera paths started */
+  uint32_t frames;
+} ct_frame_stats;
+
+/* ---- context ---- */
+uint32_t ct_abi_version(void);
+void ct_render_params_default(ct_render_params* p);
+ct_status ct_ctx_create(int32_t device, ct_ctx** out);
+ct_status ct_ctx_destroy(ct_ctx* ctx);
+const char* ct_last_error(const ct_ctx* ctx);
+/* Cap on device bytes this context may hold (0 = unlimited); creations beyond it fail with CT_ERR_OUT_OF_MEMORY. */
+ct_status ct_ctx_set_memory_budget(ct_ctx* ctx, uint64_t bytes);
+uint64_t ct_ctx_device_bytes(const ct_ctx* ctx);
+/* Synchronises `stream` and reports device-side errors raised since the last
+ * call (stack overflow, bounded-wait timeouts), then clears them. */
+ct_status ct_ctx_check(ct_ctx* ctx, void* stream);
+
+/* ---- scene: replaces TriangleList + Application::allocateTriangles/allocateTextures ---- */
+ct_status ct_scene_create(ct_ctx* ctx, const ct_scene_desc* desc, ct_scene** out);
+ct_status ct_scene_destroy(ct_ctx* ctx, ct_scene* scene);
+/* Overwrite one material (the ImGui material editor's path, Application.cpp:259-283). */
+ct_status ct_scene_set_material(ct_ctx* ctx, ct_scene* scene, uint32_t index, const ct_material* m);
+
+/* ---- BVH: replaces BVHTree/MBVHTree::constructBVH (src/BVH/BVHTree.cpp:13,
+ * src/BVH/MBVHTree.cpp:15) and the node uploads (Application.cpp:158-165).
+ * ct_bvh_build runs the reference's SAH (ten planes per axis, axis-outer, leaf
+ * below 4 primitives or at depth 64) and quad collapse on the host with all
+ * cores, producing the same trees, then uploads the device layout.
+ * nthreads <= 0 uses every hardware thread. */
+ct_status ct_bvh_build(ct_ctx* ctx, const ct_scene* scene, int32_t nthreads, ct_bvh** out);
+/* Import trees built by the reference itself so its exact trees can be traced:
+ * `nodes` are MBVHNode (128 B) / BVHNode (32 B) records and `prim_indices` the
+ * builder's m_PrimitiveIndices. */
+ct_status ct_bvh_import_quad(ct_ctx* ctx, const ct_scene* scene, const void* nodes, uint32_t node_count,
+                             const uint32_t* prim_indices, uint32_t prim_count, ct_bvh** out);
+ct_status ct_bvh_import_binary(ct_ctx* ctx, const ct_scene* scene, const void* nodes, uint32_t node_count,
+                               const uint32_t* prim_indices, uint32_t prim_count, ct_bvh** out);
+ct_status ct_bvh_info_get(const ct_bvh* bvh, ct_bvh_info* info);
+/* Copy the host-side trees out in the reference layouts (NULL skips an array). */
+ct_status ct_bvh_export(const ct_bvh* bvh, ct_bvh_layout layout, void* nodes, uint32_t* prim_indices);
+ct_status ct_bvh_destroy(ct_ctx* ctx, ct_bvh* bvh);
+
+/* Host-only build, no device needed: BVHTree(list, pool)::constructBVH followed
+ * by MBVHTree(tree)::constructBVH (src/BVH/BVHTree.cpp:13, src/BVH/MBVHTree.cpp:15).
+ * vertices: float3 array, indices: uint3 array. */
+typedef struct ct_host_bvh ct_host_bvh;
+ct_status ct_host_bvh_build(const float* vertices, uint32_t vertex_count, const uint32_t* indices,
+                            uint32_t triangle_count, int32_t nthreads, ct_host_bvh** out);
+ct_status ct_host_bvh_counts(const ct_host_bvh* h, uint32_t* binary_nodes, uint32_t* quad_nodes, uint32_t* prims,
+                             double* build_ms, double* collapse_ms);
+ct_status ct_host_bvh_export(const ct_host_bvh* h, ct_bvh_layout layout, void* nodes, uint32_t* prim_indices);
+ct_status ct_host_bvh_destroy(ct_host_bvh* h);
+
+/* ---- ray queries: replace the host MBVHNode::traverseMBVH (src/BVH/MBVHNode.cuh:207)
+ * and the device traverseMBVH/traverseMBVHShadow (:126, :165).
+ * DEVICE buffers, SoA, 16-byte aligned:
+ *   org  float4 per ray: origin xyz, w ignored
+ *   dir  float4 per ray: direction xyz, w = initial t (closest: the reference uses 1e34;
+ *                        any-hit: the maximum distance)
+ * Outputs: hit (int32, primitive id or -1), t (float; stays at dir.w on a miss),
+ * occluded (uint8, 1 when any triangle is hit before dir.w). `tri_eps` is the
+ * triangle epsilon (reference default 1e-3). Asynchronous on `stream`. */
+ct_status ct_trace_closest(ct_ctx* ctx, const ct_bvh* bvh, const float* org, const float* dir, int32_t* hit, float* t,
+                           uint32_t n, float tri_eps, void* stream);
+ct_status ct_trace_any(ct_ctx* ctx, const ct_bvh* bvh, const float* org, const float* dir, uint8_t* occluded,
+                       uint32_t n, float tri_eps, void* stream);
+
+/* ---- rendering: replaces launchKernels (src/CUDA/Kernel.cu:355) and its
+ * buffers (Application::allocateBuffers, src/Application.cpp:141-154).
+ * A ct_render holds one job's resident state: ray queues, shadow queue,
+ * hit buffer and the FP32 RGBA accumulation buffer. */
+ct_status ct_render_create(ct_ctx* ctx, int32_t width, int32_t height, ct_render** out);
+ct_status ct_render_destroy(ct_ctx* ctx, ct_render* r);
+/* Zero the accumulation buffer (Params::reset, src/CUDA/Kernel.cuh:66-71). */
+ct_status ct_render_reset(ct_ctx* ctx, ct_render* r, void* stream);
+/* One 1-spp frame: ray generation, then max_depth x (closest hit, shade with
+ * compaction, shadow any-hit), adding into the accumulation buffer. Async. */
+ct_status ct_render_accumulate(ct_ctx* ctx, const ct_scene* scene, const ct_bvh* bvh, const ct_camera* cam,
+                               const ct_render_params* params, ct_render* r, void* stream);
+/* Device pointer to the float4 accumulation buffer (width*height entries). */
+ct_status ct_render_accum(const ct_render* r, float** accum_device);
+/* draw_framebuffer (src/CUDA/Kernel.cu:258-270) without the GL surface: writes
+ * pow(sum.rgb / samples, 1/2.2), alpha 1, to a DEVICE float4 buffer. */
+ct_status ct_present(ct_ctx* ctx, const ct_render* r, float samples, float* rgba_device, void* stream);
+/* Counters accumulated on the device (synchronises `stream`). */
+ct_status ct_render_stats(ct_ctx* ctx, ct_render* r, ct_frame_stats* stats, int32_t reset, void* stream);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* CUDATRACER_H_ */

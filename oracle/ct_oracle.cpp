@@ -565,16 +565,36 @@ inline float xcos(float x, int exact) { return exact ? (float)std::cos((double)x
 inline float xatan2(float y, float x, int exact) { return exact ? (float)std::atan2((double)y, (double)x) : atan2f(y, x); }
 inline float xacos(float x, int exact) { return exact ? (float)std::acos((double)x) : acosf(x); }
 
-// SceneData::getTextureColor (src/Core/SceneData.cuh:81-97)
-inline const float* tex_color(const SceneView& s, int idx, float u, float v) {
+// Texel addressing of SceneData::getTextureColor/getTextureNormal
+// (src/Core/SceneData.cuh:81-116); NaN or out-of-range coordinates are clamped
+// to the texture (the reference would read outside it).
+inline const float* texel(const SceneView& s, int idx, float x, float y) {
   const uint32_t w = s.tex_dims[idx * 2], h = s.tex_dims[idx * 2 + 1];
+  const float fx = x * (float)(w - 1), fy = y * (float)(h - 1);
+  const uint32_t ix = fx >= 0.0f ? (uint32_t)std::fmin(fx, (float)(w - 1)) : 0u;
+  const uint32_t iy = fy >= 0.0f ? (uint32_t)std::fmin(fy, (float)(h - 1)) : 0u;
+  const uint32_t off = s.tex_offsets[idx] + (ix + iy * w);
+  return s.tex + 4 * (size_t)off;
+}
+inline const float* tex_color(const SceneView& s, int idx, float u, float v) {
   float x = std::fmod(u, 1.0f), y = std::fmod(v, 1.0f);
   if (x < 0) x += 1.0f;
   if (y < 0) y += 1.0f;
-  const uint32_t ix = (uint32_t)(x * (float)(w - 1));
-  const uint32_t iy = (uint32_t)(y * (float)(h - 1));
-  const uint32_t off = s.tex_offsets[idx] + (ix + iy * w);
-  return s.tex + 4 * (size_t)off;
+  return texel(s, idx, x, y);
+}
+inline V3 tex_normal(const SceneView& s, int idx, float u, float v) {
+  float x = u, y = v;
+  if (x < 0) x += 1.0f;
+  if (y < 0) y += 1.0f;
+  const float* t = texel(s, idx, x, y);
+  return normalize(v3(t[0], t[1], t[2]));
+}
+// sampleToWorld = convertToLocalSpace + localToWorld (src/Core/Random.cuh:37-52)
+inline V3 sample_to_world(V3 sm, V3 n) {
+  const V3 W = std::fabs(n.x) > 0.99f ? v3(0.0f, 1.0f, 0.0f) : v3(1.0f, 0.0f, 0.0f);
+  const V3 T = normalize(cross(n, W));
+  const V3 B = cross(n, T);
+  return add(add(muls(T, sm.x), muls(B, sm.y)), muls(n, sm.z));
 }
 
 struct PathState {
@@ -638,7 +658,7 @@ void render_path(const SceneView& s, const Geo& g, int pixel, int px, int py, in
     const float tu = (ba * uv0[0] + bb * uv1[0]) + bc * uv2[0];
     const float tv = (ba * uv0[1] + bb * uv1[1]) + bc * uv2[1];
     const Material& mat = s.mats[s.mat_idx[hit]];
-    // normal maps (mat.normalTex >= 0) are not part of the tested scenes
+    if (mat.normalTex >= 0) iN = sample_to_world(tex_normal(s, mat.normalTex, tu, tv), iN);
     if (mat.type == 0) {  // Light
       if (!s.indirect) return;
       const float DdotNL = -dot(r.dir, iN);
@@ -719,7 +739,7 @@ void render_path(const SceneView& s, const Geo& g, int pixel, int px, int py, in
     r.specular = (type == 1 || type == -1) ? 0 : 1;
     r.dir = wo;
     if ((type == 1 || type == -1) && s.shadow && s.light_count > 0) {
-      const int light = rnd_int_max(sd, (int)s.light_count - 1);
+      const int light = std::min(rnd_int_max(sd, (int)s.light_count - 1), (int)s.light_count - 1);
       const uint32_t lprim = s.lights[light];
       const uint32_t* li = s.idx + 3 * (size_t)lprim;
       const V3 l0 = load3(s.verts, li[0]), l1 = load3(s.verts, li[1]), l2 = load3(s.verts, li[2]);
@@ -767,6 +787,9 @@ void render_path(const SceneView& s, const Geo& g, int pixel, int px, int py, in
 extern "C" {
 
 int or_abi_version() { return 1; }
+
+/* Camera constructor: m_PlaneDistance = tanf(radians(fov * 0.5f)) (src/Core/Camera.cpp:16). */
+float or_plane_distance(float fov_deg) { return tanf((fov_deg * 0.5f) * 0.01745329251994329576923690768489f); }
 
 void or_triangle_bounds(const float* verts, const uint32_t* idx, int ntri, float* out_min, float* out_max) {
   for (int i = 0; i < ntri; i++) {
