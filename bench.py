@@ -1,0 +1,493 @@
+#!/usr/bin/env python
+"""Benchmark: path-traced Msamples/s of the wavefront tracer on one GB300.
+
+Workload (one step = one 1-spp frame, the reference's launchKernels):
+  1920x1080, max depth 8, quad BVH, FP32 RGBA accumulation, over a seeded
+  fBm-displaced 1024x1024-vertex terrain (2,093,058 triangles) + 200
+  icospheres of 5,120 triangles (radii U[0.5,3]) + 4 emissive quads, with a
+  2048x1024 FP32 equirect sky (3,117,066 triangles). Synthetic, seeded data.
+  Reference shading (compat mode), CUDA float transcendentals.
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl reference]
+
+Prints one JSON line (rank 0). `value` is device-resident throughput; `e2e`
+is the same through the C ABI with the presented frame read back to pinned
+host memory every step. Under torchrun each rank renders its own replica
+(the tracer does not shard), and value sums all ranks' samples over the
+slowest rank's time.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import re
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+sys.path.insert(0, os.path.join(ROOT, "oracle"))
+
+W, H, DEPTH = 1920, 1080, 8
+METRIC = "Msamples/s path-traced"
+UNIT = "Msamples/s"
+WORKLOAD = "wavefront path tracing 1920x1080 1spp/frame depth 8, 3.12M-tri fBm terrain + 200 spheres, quad BVH"
+
+
+def parse_args():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=64)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
+    ap.add_argument("--cpu-seconds", type=float, default=12.0, help="CPU-baseline sample budget")
+    ap.add_argument("--exact-math", action="store_true")
+    ap.add_argument("--width", type=int, default=1920, help="smaller frames for profiler captures")
+    ap.add_argument("--height", type=int, default=1080)
+    ap.add_argument("--skip-extras", action="store_true",
+                    help="only the timed frames: no e2e pass, roofline model, CPU baseline or sphere query")
+    args = ap.parse_args()
+    global W, H
+    W, H = args.width, args.height
+    return args
+
+
+# ------------------------------------------------------------------ common --
+def dist_setup(args):
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    if world > 1:
+        import torch
+        import torch.distributed as dist
+
+        backend = "nccl" if torch.cuda.is_available() else "gloo"
+        if backend == "nccl":
+            torch.cuda.set_device(local)
+        dist.init_process_group(backend)
+    return world, rank, local
+
+
+def barrier(world):
+    if world > 1:
+        import torch.distributed as dist
+
+        dist.barrier()
+
+
+def max_over_ranks(x: float, world: int) -> float:
+    if world == 1:
+        return x
+    import torch
+    import torch.distributed as dist
+
+    t = torch.tensor([x], dtype=torch.float64, device="cuda" if torch.cuda.is_available() else "cpu")
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+class Clocks:
+    """nvidia-smi sampling of SM clock and throttle reasons during a region."""
+
+    FIELDS = ("clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,clocks_event_reasons.hw_slowdown,"
+              "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+              "clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index: int):
+        self.index = index
+        self.lines = []
+        self.proc = None
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.index), f"--query-gpu={self.FIELDS}", "--format=csv,noheader,nounits",
+                 "-lms", "50"], stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.thread = threading.Thread(target=self._read, daemon=True)
+            self.thread.start()
+        except OSError:
+            self.proc = None
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def stop(self) -> dict:
+        if self.proc is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        time.sleep(0.12)
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.proc.kill()
+        sm, mx, reasons = [], [], set()
+        names = ("hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap")
+        for ln in self.lines:
+            parts = [p.strip() for p in ln.split(",")]
+            if len(parts) < 8:
+                continue
+            try:
+                sm.append(float(parts[0]))
+                mx.append(float(parts[1]))
+            except ValueError:
+                continue
+            for nm, v in zip(names, parts[4:8]):
+                if v.lower().startswith("active"):
+                    reasons.add(nm)
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(mx) if mx else None,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def measured_peaks():
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            p = json.load(f)
+        return float(p["hbm_gbs"]), "measured"
+    except (OSError, KeyError, ValueError):
+        return 6800.0, "fallback"
+
+
+def profiled_traffic():
+    """DRAM bytes per extension ray of the extend kernel, from the committed ncu
+    summary (profiles/extend_terrain_1080p.md), or None."""
+    path = os.path.join(ROOT, "profiles", "extend_terrain_1080p.md")
+    try:
+        txt = open(path).read()
+    except OSError:
+        return None
+    m = re.search(r"dram_bytes_per_extension_ray:\s*([0-9.eE+]+)", txt)
+    return float(m.group(1)) if m else None
+
+
+def build_scene():
+    from cudatracer_gb300 import scenes
+
+    ts, cam = scenes.terrain_scene()
+    return ts, cam, scenes.scene_arrays(ts)
+
+
+# ---------------------------------------------------------------- our arm --
+def cpu_baseline_port(arrays, textures, materials_packed, quad, prims, cam, seconds: float) -> dict:
+    """The oracle's restatement of the reference wavefront path (port), all host
+    threads, on whole rows of the same frame until `seconds` of CPU time pass."""
+    import numpy as np
+
+    import oracle
+
+    threads = os.cpu_count() or 1
+    acc = np.zeros((W * H, 4), np.float32)
+    rows, samples, t0 = 0, 0, time.perf_counter()
+    row_step = 8
+    r = 0
+    while time.perf_counter() - t0 < seconds and rows < H:
+        oracle.render_frames(arrays, materials_packed, quad, prims, cam, W, H, [0], DEPTH, accum=acc,
+                             exact_math=False, textures=textures, sky_tex=0,
+                             pixels=(r * W, (r + row_step) * W), nthreads=threads)
+        samples += row_step * W
+        rows += row_step
+        r = (r + 97 * row_step) % (H - row_step)
+    dt = time.perf_counter() - t0
+    return {"value": samples / dt / 1e6, "unit": UNIT, "cores": threads, "kind": "port",
+            "sample": f"{samples} paths ({rows} rows of frame 0, depth {DEPTH}) in {dt:.1f} s; oracle restatement "
+                      f"of the reference shade/extend/connect kernels on the host"}
+
+
+def reference_traversal_baseline() -> dict | None:
+    """The reference's own host BVH build + MBVH closest-hit traversal on the
+    81,920-triangle sphere and 256x256 pinhole rays (oracle/_ref)."""
+    import ctypes
+
+    import numpy as np
+
+    import oracle
+    from cudatracer_gb300 import scenes
+
+    if not oracle.ref_available():
+        return None
+    R = oracle.ref()
+    s = scenes.sphere_scene(6)
+    v, ix = np.ascontiguousarray(s.vertices), np.ascontiguousarray(s.indices)
+    P = ctypes.c_void_p
+    threads = os.cpu_count() or 1
+    h = R.ctref_build(v.ctypes.data_as(P), v.shape[0], ix.ctypes.data_as(P), ix.shape[0], threads)
+    o, d = scenes.pinhole_rays(256, 256, 60.0)
+    reps = 20
+    O = np.ascontiguousarray(np.tile(o, (reps, 1)))
+    D = np.ascontiguousarray(np.tile(d, (reps, 1)))
+    hit = np.zeros(O.shape[0], np.int32)
+    t = np.zeros(O.shape[0], np.float32)
+    t0 = time.perf_counter()
+    R.ctref_trace_mbvh(h, O.ctypes.data_as(P), D.ctypes.data_as(P), O.shape[0], hit.ctypes.data_as(P),
+                       t.ctypes.data_as(P), threads)
+    dt = time.perf_counter() - t0
+    out = {"kind": "reference", "cores": threads, "build_ms": R.ctref_build_ms(h), "collapse_ms": R.ctref_mbvh_ms(h),
+           "traverse_mrays_per_s": O.shape[0] / dt / 1e6,
+           "sample": f"81,920-triangle sphere, {O.shape[0]} primary rays (256x256 x {reps})"}
+    R.ctref_free(h)
+    return out
+
+
+def gpu_closest_hit_c1(ctx):
+    """Mrays/s of ct_trace_closest on the 81,920-triangle sphere, 256x256 rays x 64."""
+    import numpy as np
+    import torch
+
+    from cudatracer_gb300 import api, scenes
+
+    s = scenes.sphere_scene(6)
+    sc = ctx.scene(scenes.scene_arrays(s), [api.Material()])
+    bvh = sc.build_bvh()
+    o, d = scenes.pinhole_rays(256, 256, 60.0)
+    O = np.zeros((o.shape[0], 4), np.float32)
+    O[:, :3] = o
+    D = np.zeros_like(O)
+    D[:, :3] = d
+    D[:, 3] = 1e34
+    O = torch.from_numpy(np.tile(O, (64, 1))).cuda()
+    D = torch.from_numpy(np.tile(D, (64, 1))).cuda()
+    hit = torch.empty(O.shape[0], dtype=torch.int32, device="cuda")
+    t = torch.empty(O.shape[0], device="cuda")
+    for _ in range(3):
+        bvh.trace_closest(O, D, hit, t)
+    torch.cuda.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record()
+    for _ in range(10):
+        bvh.trace_closest(O, D, hit, t)
+    e1.record()
+    torch.cuda.synchronize()
+    ms = e0.elapsed_time(e1) / 10
+    sc.close()
+    bvh.close()
+    return {"mrays_per_s": O.shape[0] / ms / 1e3, "rays": int(O.shape[0]),
+            "workload": "81,920-tri sphere, 256x256 pinhole rays x64, ct_trace_closest"}
+
+
+def run_ours(args, world, rank, local):
+    import numpy as np
+    import torch
+
+    from cudatracer_gb300 import _build, api
+
+    _build.build()
+    torch.cuda.set_device(local)
+    ctx = api.Context(local)
+    t_setup = time.perf_counter()
+    ts, cam, arrays = build_scene()
+    sc = ctx.scene(arrays, [api.Material(**m) for m in ts.materials], ts.textures, ts.skybox_texture)
+    bvh = sc.build_bvh(0)
+    info = bvh.info()
+    setup_s = time.perf_counter() - t_setup
+    job = api.RenderJob(ctx, W, H)
+    camera = api.Camera(W, H, cam["fov"], cam["position"], cam["forward"], cam["up"])
+    params = api.Params(W, H, camera=camera, max_depth=DEPTH, exact_math=args.exact_math)
+    stream = torch.cuda.Stream()
+    params.reset(job, stream)
+    for _ in range(args.warmup):
+        api.launch_kernels(job, sc, bvh, params, stream=stream)
+    stream.synchronize()
+    job.stats(reset=True, stream=stream)
+    job.profile(True)
+    job.profile_read(reset=True)
+    clocks = Clocks(local)
+    barrier(world)
+    torch.cuda.synchronize()
+    clocks.start()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    for _ in range(args.steps):
+        api.launch_kernels(job, sc, bvh, params, stream=stream)
+    e1.record(stream)
+    stream.synchronize()
+    torch.cuda.synchronize()
+    barrier(world)
+    clk = clocks.stop()
+    ms = e0.elapsed_time(e1)
+    ctx.check(stream)
+    prof = job.profile_read(reset=True)
+    job.profile(False)
+    st = job.stats(reset=True, stream=stream)
+    ms_max = max_over_ranks(ms, world)
+    samples = W * H * args.steps
+    value = world * samples / (ms_max / 1e3) / 1e6
+    mrays = world * (st["extension_rays"] + st["shadow_rays"]) / (ms_max / 1e3) / 1e6
+
+    if args.skip_extras:
+        if rank == 0:
+            print(json.dumps({"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+                              "ms_per_step": ms_max / args.steps, "mrays_per_s": mrays,
+                              "stage_ms": {k: v["ms"] for k, v in prof.items()},
+                              "config": {"width": W, "height": H, "max_depth": DEPTH}}), flush=True)
+        return
+
+    # ---- e2e: C ABI with the presented frame copied to pinned host memory each step
+    out_dev = torch.empty((W * H, 4), device="cuda")
+    out_host = torch.empty((W * H, 4), pin_memory=True)
+    params_e2e = api.Params(W, H, camera=camera, max_depth=DEPTH, exact_math=args.exact_math)
+    params_e2e.reset(job, stream)
+    for _ in range(args.warmup):
+        api.launch_kernels(job, sc, bvh, params_e2e, present_out=out_dev, stream=stream)
+        with torch.cuda.stream(stream):
+            out_host.copy_(out_dev, non_blocking=True)
+    stream.synchronize()
+    barrier(world)
+    w0 = time.perf_counter()
+    e0.record(stream)
+    for _ in range(args.steps):
+        api.launch_kernels(job, sc, bvh, params_e2e, present_out=out_dev, stream=stream)
+        with torch.cuda.stream(stream):
+            out_host.copy_(out_dev, non_blocking=True)
+    e1.record(stream)
+    stream.synchronize()
+    wall_ms = (time.perf_counter() - w0) * 1e3
+    e2e_ms = max_over_ranks(max(e0.elapsed_time(e1), wall_ms), world)
+    e2e_value = world * samples / (e2e_ms / 1e3) / 1e6
+    h2d_bytes = 40 + 48  # ct_camera + ct_render_params passed from host memory per frame
+    d2h_bytes = W * H * 16
+
+    # ---- roofline of the dominant kernel (extend: closest-hit traversal)
+    peak, peak_kind = measured_peaks()
+    ext = prof["extend"]
+    roofline = None
+    cpu_base = None
+    work = None
+    if rank == 0:
+        import oracle
+
+        oracle.build_oracle()
+        quad, prims = bvh.export()
+        omats = oracle.pack_materials(ts.materials)
+        # traversal work per extension ray on sampled rows (the reference's traverseMBVH counts)
+        oracle.work_read(reset=True)
+        acc = np.zeros((W * H, 4), np.float32)
+        for r0 in range(0, H, 135):
+            oracle.render_frames(arrays, omats, quad, prims, cam, W, H, [0], DEPTH, accum=acc, exact_math=False,
+                                 textures=ts.textures, sky_tex=0, pixels=(r0 * W, (r0 + 2) * W),
+                                 nthreads=os.cpu_count() or 1)
+        work = oracle.work_read(reset=True)
+        v_node = work["ext_nodes"] / max(1, work["ext_rays"])
+        v_tri = work["ext_tris"] / max(1, work["ext_rays"])
+        b_ray = 32 + v_node * 128 + v_tri * 52
+        ext_rays = st["extension_rays"]
+        achieved = ext_rays * b_ray / (ext["ms"] / 1e3) / 1e9 if ext["ms"] > 0 else None
+        tpr = profiled_traffic()
+        roofline = {
+            "kernel": "k_extend (closest-hit quad-BVH traversal)", "bound": "hbm",
+            "achieved": achieved, "peak": peak, "unit": "GB/s",
+            "frac": achieved / peak if achieved else None, "peak_source": peak_kind,
+            "traffic": (tpr * ext_rays / max(1, ext["launches"])) if tpr else None,
+            "algorithmic_bytes_per_ray": b_ray, "mean_node_visits": v_node, "mean_tri_tests": v_tri,
+            "rays_per_launch": ext_rays / max(1, ext["launches"]),
+            "avg_launch_ms": ext["ms"] / max(1, ext["launches"]),
+        }
+        if world == 1 and args.cpu_seconds > 0:
+            cpu_base = cpu_baseline_port(arrays, ts.textures, omats, quad, prims, cam, args.cpu_seconds)
+            ref_tr = reference_traversal_baseline()
+            if ref_tr:
+                cpu_base["reference_host_traversal"] = ref_tr
+    c1 = gpu_closest_hit_c1(ctx) if rank == 0 else None
+    launches = sum(v["launches"] for v in prof.values())
+    line = {
+        "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": ms_max / args.steps, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded procedural scene)",
+        "config": {"workload": WORKLOAD, "width": W, "height": H, "max_depth": DEPTH, "triangles": int(ts.ntri),
+                   "frames_per_step": 1, "shading": "compat (reference shade)",
+                   "math": "exact" if args.exact_math else "fast",
+                   "l2": "inputs larger than L2: 94 MB nodes + 150 MB triangles + 150 MB scene arrays + 300 MB queues",
+                   "parallelism": f"replicas x{world}"},
+        "mrays_per_s": mrays, "rays_per_step": (st["extension_rays"] + st["shadow_rays"]) / args.steps,
+        "stage_ms": {k: v["ms"] for k, v in prof.items()},
+        "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": h2d_bytes, "d2h_bytes_per_step": d2h_bytes},
+        "gpu_launches": launches,
+        "roofline": roofline, "cpu_baseline": cpu_base, "closest_hit": c1, "clocks": clk,
+        "setup": {"scene_and_bvh_s": setup_s, "bvh_build_ms": info["build_ms"], "bvh_collapse_ms": info["collapse_ms"],
+                  "quad_nodes": info["quad_node_count"]},
+    }
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+
+
+# ---------------------------------------------------------- reference arm --
+def run_reference(args, world, rank):
+    """The reference's path on the host cores: its own host BVH build
+    (oracle/_ref) when available, and the oracle's restatement of its
+    wavefront kernels for shading (the reference has no CPU shading path)."""
+    if rank != 0:
+        return
+    import ctypes
+
+    import numpy as np
+
+    import oracle
+
+    oracle.build_oracle()
+    ts, cam, arrays = build_scene()
+    threads = os.cpu_count() or 1
+    kind = "port"
+    if oracle.ref_available():
+        R = oracle.ref()
+        P = ctypes.c_void_p
+        v, ix = np.ascontiguousarray(ts.vertices), np.ascontiguousarray(ts.indices)
+        h = R.ctref_build(v.ctypes.data_as(P), v.shape[0], ix.ctypes.data_as(P), ix.shape[0], threads)
+        quad = np.zeros((R.ctref_mbvh_count(h), 32), np.int32)
+        prims = np.zeros(ix.shape[0], np.uint32)
+        R.ctref_export(h, None, prims.ctypes.data_as(P), quad.ctypes.data_as(P))
+        build_ms = R.ctref_build_ms(h) + R.ctref_mbvh_ms(h)
+        R.ctref_free(h)
+        bvh_src = "reference host BVHTree+MBVHTree build"
+    else:
+        t0 = time.perf_counter()
+        b = oracle.bvh_build(ts.vertices, ts.indices, threads)
+        quad, prims = b["quad"], b["prims"]
+        build_ms = (time.perf_counter() - t0) * 1e3
+        bvh_src = "oracle restatement of the reference SAH build"
+    omats = oracle.pack_materials(ts.materials)
+    acc = np.zeros((W * H, 4), np.float32)
+    rows_per_step = 16
+    for s in range(args.warmup):
+        oracle.render_frames(arrays, omats, quad, prims, cam, W, H, [0], DEPTH, accum=acc, exact_math=False,
+                             textures=ts.textures, sky_tex=0, pixels=(0, rows_per_step * W), nthreads=threads)
+    t0 = time.perf_counter()
+    for s in range(args.steps):
+        r0 = (s * rows_per_step * 7) % (H - rows_per_step)
+        oracle.render_frames(arrays, omats, quad, prims, cam, W, H, [2 * s], DEPTH, accum=acc, exact_math=False,
+                             textures=ts.textures, sky_tex=0, pixels=(r0 * W, (r0 + rows_per_step) * W),
+                             nthreads=threads)
+    dt = time.perf_counter() - t0
+    samples = args.steps * rows_per_step * W
+    value = samples / dt / 1e6
+    line = {
+        "impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": dt * 1e3 / args.steps, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded procedural scene)",
+        "config": {"workload": WORKLOAD, "width": W, "height": H, "max_depth": DEPTH, "triangles": int(ts.ntri),
+                   "step_sample": f"{rows_per_step} rows x {W} px of one frame per step"},
+        "cpu_baseline": {"value": value, "unit": UNIT, "cores": threads, "kind": kind,
+                         "sample": f"{rows_per_step * W} paths per step; BVH from the {bvh_src} "
+                                   f"({build_ms:.0f} ms)"},
+        "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+
+
+def main():
+    args = parse_args()
+    world, rank, local = dist_setup(args)
+    if args.impl == "reference":
+        run_reference(args, world, rank)
+    else:
+        run_ours(args, world, rank, local)
+    if world > 1:
+        import torch.distributed as dist
+
+        dist.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

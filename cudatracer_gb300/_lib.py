@@ -71,6 +71,10 @@ class ct_frame_stats(Structure):
     _fields_ = [("extension_rays", c_uint64), ("shadow_rays", c_uint64), ("samples", c_uint64), ("frames", c_uint32)]
 
 
+class ct_stage_times(Structure):
+    _fields_ = [("ms", c_double * 4), ("launches", c_uint32 * 4)]
+
+
 P = c_void_p
 PP = POINTER(c_void_p)
 # name -> (restype, argtypes)
@@ -106,6 +110,8 @@ SIGNATURES = {
     "ct_render_accum": (c_int32, [P, PP]),
     "ct_present": (c_int32, [P, P, c_float, P, P]),
     "ct_render_stats": (c_int32, [P, P, POINTER(ct_frame_stats), c_int32, P]),
+    "ct_render_profile": (c_int32, [P, P, c_int32]),
+    "ct_render_profile_read": (c_int32, [P, P, POINTER(ct_stage_times), c_int32]),
 }
 
 _lib = None

@@ -428,6 +428,18 @@ class RenderJob:
         return {k: getattr(s, k) for k, _ in s._fields_}
 
 
+    STAGES = ("raygen", "extend", "shade", "connect")
+
+    def profile(self, enable: bool = True):
+        """Bracket every stage launch with CUDA events (see profile_read)."""
+        check(self.ctx.lib.ct_render_profile(self.ctx.h, self.h, int(enable)), self.ctx.h)
+
+    def profile_read(self, reset: bool = True) -> dict:
+        s = _lib.ct_stage_times()
+        check(self.ctx.lib.ct_render_profile_read(self.ctx.h, self.h, ctypes.byref(s), int(reset)), self.ctx.h)
+        return {name: {"ms": s.ms[i], "launches": s.launches[i]} for i, name in enumerate(self.STAGES)}
+
+
 def _device_view(addr: int, numel: int, dtype):
     """Wrap device memory owned by the library as a torch tensor (no copy)."""
     import torch

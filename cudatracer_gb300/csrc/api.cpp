@@ -25,7 +25,7 @@ struct ct_ctx {
   std::string err;
   uint64_t budget = 0;
   std::atomic<uint64_t> bytes{0};
-  uint32_t* d_error = nullptr;
+  uint32_t* d_error = nullptr;  // device error word
 };
 
 namespace {
@@ -123,7 +123,44 @@ struct ct_render {
   int32_t w = 0, h = 0;
   DevQueues q{};
   Allocs allocs;
+  // stage profiling: event pairs per stage, recycled through a pool
+  bool profile = false;
+  std::vector<std::pair<cudaEvent_t, cudaEvent_t>> marks[4];
+  std::vector<cudaEvent_t> pool;
+  cudaEvent_t take() {
+    if (!pool.empty()) {
+      cudaEvent_t e = pool.back();
+      pool.pop_back();
+      return e;
+    }
+    cudaEvent_t e = nullptr;
+    cudaEventCreate(&e);
+    return e;
+  }
+  void recycle() {
+    for (auto& m : marks)
+      for (auto& p : m) pool.push_back(p.first), pool.push_back(p.second);
+    for (auto& m : marks) m.clear();
+  }
+  ~ct_render() {
+    recycle();
+    for (cudaEvent_t e : pool) cudaEventDestroy(e);
+  }
 };
+
+namespace {
+// Bracket one stage launch with events when profiling is on.
+template <typename F>
+cudaError_t staged(ct_render* r, int stage, cudaStream_t st, F&& launch) {
+  if (!r->profile) return launch();
+  cudaEvent_t a = r->take(), b = r->take();
+  cudaEventRecord(a, st);
+  cudaError_t e = launch();
+  cudaEventRecord(b, st);
+  r->marks[stage].push_back({a, b});
+  return e;
+}
+}  // namespace
 
 namespace {
 
@@ -220,8 +257,7 @@ ct_status ct_ctx_create(int32_t device, ct_ctx** out) {
   if (cudaMalloc(&c->d_error, 256) != cudaSuccess || cudaMemset(c->d_error, 0, 256) != cudaSuccess) {
     delete c;
     return CT_ERR_OUT_OF_MEMORY;
-  }
-  *out = c;
+  }  *out = c;
   return CT_OK;
 }
 
@@ -665,13 +701,15 @@ ct_status ct_render_accumulate(ct_ctx* ctx, const ct_scene* scene, const ct_bvh*
   f.indirect = p->indirect;
   f.sky = p->sky;
   f.shading_mode = p->shading_mode;
-  CT_CUDA(ctx, launch_raygen(r->q, f, p->exact_math, st));
+  CT_CUDA(ctx, staged(r, 0, st, [&] { return launch_raygen(r->q, f, p->exact_math, st); }));
   for (int pass = 0; pass < p->max_depth; pass++) {
     const int cur = pass & 1;
     const int path_length = pass == 0 ? 0 : pass + 1;  // Kernel.cu:306, 330
-    CT_CUDA(ctx, launch_extend(bvh->dev, r->q, cur, p->tri_eps, st));
-    CT_CUDA(ctx, launch_shade(scene->dev, r->q, f, cur, path_length, p->exact_math, st));
-    if (p->shadow) CT_CUDA(ctx, launch_connect(bvh->dev, r->q, p->tri_eps, st));
+    CT_CUDA(ctx, staged(r, 1, st, [&] { return launch_extend(bvh->dev, r->q, cur, p->tri_eps, st); }));
+    CT_CUDA(ctx, staged(r, 2, st, [&] {
+              return launch_shade(scene->dev, r->q, f, cur, path_length, p->exact_math, st);
+            }));
+    if (p->shadow) CT_CUDA(ctx, staged(r, 3, st, [&] { return launch_connect(bvh->dev, r->q, p->tri_eps, st); }));
   }
   return CT_OK;
 }
@@ -703,6 +741,31 @@ ct_status ct_render_stats(ct_ctx* ctx, ct_render* r, ct_frame_stats* stats, int3
   stats->samples = h[2];
   stats->frames = (uint32_t)h[3];
   if (reset) CT_CUDA(ctx, cudaMemset(r->q.stats, 0, sizeof(h)));
+  return CT_OK;
+}
+
+ct_status ct_render_profile(ct_ctx* ctx, ct_render* r, int32_t enable) {
+  if (!ctx || !r) return fail(ctx, CT_ERR_INVALID_ARGUMENT, "null argument");
+  r->profile = enable != 0;
+  return CT_OK;
+}
+
+ct_status ct_render_profile_read(ct_ctx* ctx, ct_render* r, ct_stage_times* out, int32_t reset) {
+  if (!ctx || !r || !out) return fail(ctx, CT_ERR_INVALID_ARGUMENT, "null argument");
+  ct_status s = set_device(ctx);
+  if (s != CT_OK) return s;
+  for (int k = 0; k < 4; k++) {
+    double ms = 0.0;
+    for (auto& p : r->marks[k]) {
+      CT_CUDA(ctx, cudaEventSynchronize(p.second));
+      float e = 0.0f;
+      CT_CUDA(ctx, cudaEventElapsedTime(&e, p.first, p.second));
+      ms += e;
+    }
+    out->ms[k] = ms;
+    out->launches[k] = (uint32_t)r->marks[k].size();
+  }
+  if (reset) r->recycle();
   return CT_OK;
 }
 

@@ -115,7 +115,6 @@ cudaError_t launch_connect(const DevBVH& b, const DevQueues& q, float eps, cudaS
 cudaError_t launch_raygen(const DevQueues& q, const FrameConst& f, int exact, cudaStream_t s);
 cudaError_t launch_shade(const DevScene& sc, const DevQueues& q, const FrameConst& f, int queue, int path_length,
                          int exact, cudaStream_t s);
-cudaError_t launch_reset_counts(const DevQueues& q, int next_queue, cudaStream_t s);
 cudaError_t launch_present(const float4* accum, float4* out, int n, float samples, cudaStream_t s);
 
 }  // namespace ct

@@ -230,6 +230,18 @@ ct_status ct_present(ct_ctx* ctx, const ct_render* r, float samples, float* rgba
 /* Counters accumulated on the device (synchronises `stream`). */
 ct_status ct_render_stats(ct_ctx* ctx, ct_render* r, ct_frame_stats* stats, int32_t reset, void* stream);
 
+/* Per-stage GPU timing (no reference counterpart; the reference prints host
+ * build times only, src/BVH/BVHTree.cpp:53): when enabled, every stage launch
+ * of ct_render_accumulate is bracketed by CUDA events on its stream. Reading
+ * synchronises on the recorded events. Stage index: 0 raygen, 1 extend
+ * (closest hit), 2 shade, 3 connect (shadow any hit). */
+typedef struct ct_stage_times {
+  double ms[4];
+  uint32_t launches[4];
+} ct_stage_times;
+ct_status ct_render_profile(ct_ctx* ctx, ct_render* r, int32_t enable);
+ct_status ct_render_profile_read(ct_ctx* ctx, ct_render* r, ct_stage_times* out, int32_t reset);
+
 #ifdef __cplusplus
 }
 #endif

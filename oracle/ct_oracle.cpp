@@ -367,9 +367,15 @@ struct Geo {
 // MBVHNode::traverseMBVH (src/BVH/MBVHNode.cuh:126-163). The stack is 128
 // deep (the reference's 32 has no overflow check); overflow_out counts rays
 // whose stack would have exceeded 32 entries.
-void trace_closest(const Geo& g, V3 org, V3 dir, float* t, int* hit, int* deep) {
+// Work counters (node visits, triangle tests) for the algorithmic-bytes model.
+struct Work {
+  uint64_t rays = 0, nodes = 0, tris = 0;
+};
+
+void trace_closest(const Geo& g, V3 org, V3 dir, float* t, int* hit, int* deep, Work* w = nullptr) {
   int stk_first[256], stk_count[256];
   int sp = 0, maxsp = 0;
+  if (w) w->rays++;
   stk_first[0] = 0;
   stk_count[0] = -1;
   const V3 inv = v3(1.0f / dir.x, 1.0f / dir.y, 1.0f / dir.z);
@@ -377,6 +383,7 @@ void trace_closest(const Geo& g, V3 org, V3 dir, float* t, int* hit, int* deep) 
     const int lf = stk_first[sp], cnt = stk_count[sp];
     sp--;
     if (cnt > -1) {
+      if (w) w->tris += (uint64_t)cnt;
       for (int i = 0; i < cnt; i++) {
         const uint32_t prim = g.prims[lf + i];
         const uint32_t* ix = g.idx + 3 * (size_t)prim;
@@ -388,6 +395,7 @@ void trace_closest(const Geo& g, V3 org, V3 dir, float* t, int* hit, int* deep) 
     float tmin[4];
     bool res[4];
     const QNode& n = g.qnodes[lf];
+    if (w) w->nodes++;
     quad_intersect(n, org, inv, *t, tmin, res);
     for (int i = 3; i >= 0; i--) {
       const int c = (int)(fbits(tmin[i]) & 3u);
@@ -404,9 +412,10 @@ void trace_closest(const Geo& g, V3 org, V3 dir, float* t, int* hit, int* deep) 
 }
 
 // MBVHNode::traverseMBVHShadow (src/BVH/MBVHNode.cuh:165-205)
-bool trace_any(const Geo& g, V3 org, V3 dir, float maxDist) {
+bool trace_any(const Geo& g, V3 org, V3 dir, float maxDist, Work* w = nullptr) {
   int stk_first[256], stk_count[256];
   int sp = 0;
+  if (w) w->rays++;
   stk_first[0] = 0;
   stk_count[0] = -1;
   const V3 inv = v3(1.0f / dir.x, 1.0f / dir.y, 1.0f / dir.z);
@@ -415,6 +424,7 @@ bool trace_any(const Geo& g, V3 org, V3 dir, float maxDist) {
     sp--;
     if (cnt > -1) {
       for (int i = 0; i < cnt; i++) {
+        if (w) w->tris++;
         const uint32_t prim = g.prims[lf + i];
         const uint32_t* ix = g.idx + 3 * (size_t)prim;
         if (tri_intersect(org, dir, &maxDist, load3(g.verts, ix[0]), load3(g.verts, ix[1]), load3(g.verts, ix[2]),
@@ -426,6 +436,7 @@ bool trace_any(const Geo& g, V3 org, V3 dir, float maxDist) {
     float tmin[4];
     bool res[4];
     const QNode& n = g.qnodes[lf];
+    if (w) w->nodes++;
     quad_intersect(n, org, inv, maxDist, tmin, res);
     for (int i = 3; i >= 0; i--) {
       const int c = (int)(fbits(tmin[i]) & 3u);
@@ -597,6 +608,54 @@ inline V3 sample_to_world(V3 sm, V3 n) {
   return add(add(muls(T, sm.x), muls(B, sm.y)), muls(n, sm.z));
 }
 
+/* SampleBSDF (src/Core/BSDF.h:33-63) with DiffuseReflectionCosWeighted and
+ * Tangent2World (src/Core/Tools.h:110-137, 162-169). dir is the incoming ray
+ * direction (wi = -dir). type: 0 mirror, 1 diffuse, -1 where the reference
+ * leaves it unset (pdf = 0). */
+void sample_bsdf(V3 color, float roughness, V3 iN, V3 N, V3 dir, float r3, float r4, int exact, V3& wo, V3& f,
+                 float& pdf, int& type) {
+  if (roughness < 0.1f) {
+    wo = sub(dir, muls(muls(iN, dot(iN, dir)), 2.0f));  // reflect(-wi, iN)
+    if (dot(N, wo) <= 0.0f) {
+      pdf = 0.0f;
+      f = v3(0, 0, 0);
+      type = -1;
+    } else {
+      pdf = 1.0f;
+      type = 0;
+      f = muls(color, 1.0f / std::fabs(dot(iN, wo)));
+    }
+    return;
+  }
+  const float term1 = kTwoPi * r3;
+  const float term2 = (float)std::sqrt(1.0 - (double)r4);  // sqrt(1.0 - r1) in double
+  const float sn = xsin(term1, exact), cs = xcos(term1, exact);
+  const V3 Vl = v3(cs * term2, sn * term2, std::sqrt(r4));
+  V3 B, Tt;
+  const V3 n = iN;
+  if (n.z < 0.) {
+    const float a = 1.0f / (1.0f - n.z);
+    const float b = (n.x * n.y) * a;
+    B = v3(1.0f - (n.x * n.x) * a, -b, n.x);
+    Tt = v3(b, (n.y * n.y) * a - 1.0f, -n.y);
+  } else {
+    const float a = 1.0f / (1.0f + n.z);
+    const float b = (-n.x * n.y) * a;
+    B = v3(1.0f - (n.x * n.x) * a, b, -n.x);
+    Tt = v3(b, 1.0f - (n.y * n.y) * a, -n.y);
+  }
+  wo = normalize(add(add(muls(Tt, Vl.x), muls(B, Vl.y)), muls(n, Vl.z)));
+  if (dot(N, wo) <= 0.0f) {
+    pdf = 0.0f;
+    f = v3(0, 0, 0);
+    type = -1;
+  } else {
+    type = 1;
+    pdf = gmax(0.0f, dot(wo, iN)) * kOneOverPi;
+    f = muls(color, kOneOverPi);
+  }
+}
+
 struct PathState {
   V3 org, dir, T;
   float pdf;
@@ -613,7 +672,8 @@ inline void accum_add(float* acc, V3 c) {
 /* One path through `depth` extend/shade/connect passes, adding into acc[4]
  * in the order the wavefront kernels do. */
 void render_path(const SceneView& s, const Geo& g, int pixel, int px, int py, int W, int H, uint32_t frame, int depth,
-                 V3 cam_o, V3 cam_w, V3 hor, V3 ver, int exact, float* acc) {
+                 V3 cam_o, V3 cam_w, V3 hor, V3 ver, int exact, float* acc, Work* wext = nullptr,
+                 Work* wshd = nullptr) {
   // generatePrimaryRays (Kernel.cu:208-234) with start_position = 0.
   uint32_t seed = ((uint32_t)pixel + frame * 147565741u) * 720898027u;
   const float fx = ((float)px + rnd_float(seed)) - 0.5f;
@@ -629,7 +689,7 @@ void render_path(const SceneView& s, const Geo& g, int pixel, int px, int py, in
     const int pathLength = pass == 0 ? 0 : pass + 1;  // Kernel.cu:306,330
     float t = kMaxDistance;
     int hit = -1;
-    trace_closest(g, r.org, r.dir, &t, &hit, nullptr);
+    trace_closest(g, r.org, r.dir, &t, &hit, nullptr, wext);
     // ---- shade (Kernel.cu:88-206) ----
     if (!(t < kMaxDistance)) {
       if (s.sky_enabled) {
@@ -690,52 +750,10 @@ void render_path(const SceneView& s, const Geo& g, int pixel, int px, int py, in
     // convertToLocalSpace (Random.cuh:37-42): T only feeds EvaluateBSDF's unused arg
     // SampleBSDF (BSDF.h:33-63); arguments taken left to right.
     const float r3 = rnd_float(sd), r4 = rnd_float(sd);
-    V3 wo;
+    V3 wo, f;
     float pdf;
     int type;  // 0 specular, 1 diffuse, -1 unset by the reference (treated as diffuse)
-    V3 f;
-    if (mat.roughness < 0.1f) {
-      wo = sub(r.dir, muls(muls(iN, dot(iN, r.dir)), 2.0f));  // reflect(-wi, iN)
-      if (dot(N, wo) <= 0.0f) {
-        pdf = 0.0f;
-        f = v3(0, 0, 0);
-        type = -1;
-      } else {
-        pdf = 1.0f;
-        type = 0;
-        f = muls(color, 1.0f / std::fabs(dot(iN, wo)));
-      }
-    } else {
-      // DiffuseReflectionCosWeighted (Tools.h:162-169), sqrt(1.0 - r1) in double
-      const float term1 = kTwoPi * r3;
-      const float term2 = (float)std::sqrt(1.0 - (double)r4);
-      const float sn = xsin(term1, exact), cs = xcos(term1, exact);
-      const V3 Vl = v3(cs * term2, sn * term2, std::sqrt(r4));
-      // Tangent2World (Tools.h:110-137)
-      V3 B, Tt;
-      const V3 n = iN;
-      if (n.z < 0.) {
-        const float a = 1.0f / (1.0f - n.z);
-        const float b = (n.x * n.y) * a;
-        B = v3(1.0f - (n.x * n.x) * a, -b, n.x);
-        Tt = v3(b, (n.y * n.y) * a - 1.0f, -n.y);
-      } else {
-        const float a = 1.0f / (1.0f + n.z);
-        const float b = (-n.x * n.y) * a;
-        B = v3(1.0f - (n.x * n.x) * a, b, -n.x);
-        Tt = v3(b, 1.0f - (n.y * n.y) * a, -n.y);
-      }
-      wo = normalize(add(add(muls(Tt, Vl.x), muls(B, Vl.y)), muls(n, Vl.z)));
-      if (dot(N, wo) <= 0.0f) {
-        pdf = 0.0f;
-        f = v3(0, 0, 0);
-        type = -1;
-      } else {
-        type = 1;
-        pdf = gmax(0.0f, dot(wo, iN)) * kOneOverPi;
-        f = muls(color, kOneOverPi);
-      }
-    }
+    sample_bsdf(color, mat.roughness, iN, N, r.dir, r3, r4, exact, wo, f, pdf, type);
     r.specular = (type == 1 || type == -1) ? 0 : 1;
     r.dir = wo;
     if ((type == 1 || type == -1) && s.shadow && s.light_count > 0) {
@@ -768,7 +786,7 @@ void render_path(const SceneView& s, const Geo& g, int pixel, int px, int py, in
           // ---- connect (Kernel.cu:247-256) ----
           const V3 so = add(r.org, muls(L, s.normal_eps));
           const float smax = dist - 2.0f * s.dist_eps;
-          if (!trace_any(g, so, L, smax)) accum_add(acc, sc);
+          if (!trace_any(g, so, L, smax, wshd)) accum_add(acc, sc);
         }
       }
       r.specular = 0;
@@ -783,6 +801,8 @@ void render_path(const SceneView& s, const Geo& g, int pixel, int px, int py, in
 }
 
 }  // namespace
+
+static std::atomic<uint64_t> g_work[6];
 
 extern "C" {
 
@@ -939,12 +959,105 @@ void or_render_frame(const OrSceneDesc* sd, const float* cam_pos, const float* c
   const V3 co = load3(cam_pos, 0), cw = load3(cam_w, 0), h = load3(hor, 0), v = load3(ver, 0);
   const int n = p_end - p_begin;
   parallel_range(n, nthreads, [&](int b, int e) {
+    Work we, ws;
     for (int i = b; i < e; i++) {
       const int pix = p_begin + i;
       render_path(s, g, pix, pix % W, (pix / W) % H, W, H, frame, depth, co, cw, h, v, exact_math,
-                  accum + 4 * (size_t)pix);
+                  accum + 4 * (size_t)pix, &we, &ws);
     }
+    g_work[0] += we.rays, g_work[1] += we.nodes, g_work[2] += we.tris;
+    g_work[3] += ws.rays, g_work[4] += ws.nodes, g_work[5] += ws.tris;
   });
+}
+
+/* Traversal work of the frames rendered since the last reset:
+ * [ext rays, ext quad-node visits, ext triangle tests, shadow rays, shadow
+ * node visits, shadow triangle tests]. */
+void or_work_read(uint64_t* out, int reset) {
+  for (int k = 0; k < 6; k++) {
+    out[k] = g_work[k].load();
+    if (reset) g_work[k] = 0;
+  }
+}
+
+/* ---- per-function entry points for the known-answer tests ---- */
+void or_sample_bsdf(const float* color, float roughness, const float* iN, const float* N, const float* wi, float r3,
+                    float r4, int exact, float* f_out, float* wo_out, float* pdf_out, int* type_out) {
+  V3 wo, f;
+  float pdf;
+  int type;
+  const V3 w = load3(wi, 0);
+  sample_bsdf(load3(color, 0), roughness, load3(iN, 0), load3(N, 0), v3(-w.x, -w.y, -w.z), r3, r4, exact, wo, f, pdf,
+              type);
+  f_out[0] = f.x, f_out[1] = f.y, f_out[2] = f.z;
+  wo_out[0] = wo.x, wo_out[1] = wo.y, wo_out[2] = wo.z;
+  *pdf_out = pdf;
+  *type_out = type;
+}
+uint32_t or_wang_hash(uint32_t s) { return wang_hash(s); }
+void or_random_stream(uint32_t seed, int n, uint32_t* ints, float* floats) {
+  uint32_t a = seed, b = seed;
+  for (int i = 0; i < n; i++) {
+    ints[i] = rnd_int(a);
+    floats[i] = rnd_float(b);
+  }
+}
+int or_tri_intersect(const float* o, const float* d, float* t, const float* p0, const float* p1, const float* p2,
+                     float eps) {
+  return tri_intersect(load3(o, 0), load3(d, 0), t, load3(p0, 0), load3(p1, 0), load3(p2, 0), eps) ? 1 : 0;
+}
+void or_quad_intersect(const void* node, const float* o, const float* inv, float t, int32_t* tmini, int32_t* res) {
+  float tm[4];
+  bool r[4];
+  quad_intersect(*(const QNode*)node, load3(o, 0), load3(inv, 0), t, tm, r);
+  for (int k = 0; k < 4; k++) tmini[k] = (int32_t)fbits(tm[k]), res[k] = r[k] ? 1 : 0;
+}
+void or_bary(const float* p, const float* n, const float* a, const float* b, const float* c, float* out) {
+  const V3 P = load3(p, 0), N = load3(n, 0), p0 = load3(a, 0), p1 = load3(b, 0), p2 = load3(c, 0);
+  const float aABC = dot(N, cross(sub(p1, p0), sub(p2, p0)));
+  const float aPBC = dot(N, cross(sub(p1, P), sub(p2, P)));
+  const float aPCA = dot(N, cross(sub(p2, P), sub(p0, P)));
+  out[0] = aPBC / aABC, out[1] = aPCA / aABC, out[2] = (1.f - out[0]) - out[1];
+}
+float or_area(const float* a, const float* b, const float* c) {
+  const V3 p0 = load3(a, 0), p1 = load3(b, 0), p2 = load3(c, 0);
+  const float x = length(sub(p0, p1)), y = length(sub(p1, p2)), z = length(sub(p2, p0));
+  const float s = ((x + y) + z) / 2.f;
+  return std::sqrt(((s * (s - x)) * (s - y)) * (s - z));
+}
+void or_random_point(const float* a, const float* b, const float* c, float r1, float r2, float* out) {
+  if (r1 + r2 > 1.0f) r1 = 1.0f - r1, r2 = 1.0f - r2;
+  const float qa = (1.0f - r1) - r2;
+  const V3 q = add(add(muls(load3(a, 0), qa), muls(load3(b, 0), r1)), muls(load3(c, 0), r2));
+  out[0] = q.x, out[1] = q.y, out[2] = q.z;
+}
+void or_tangent2world(const float* v, const float* nn, float* out) {
+  const V3 V = load3(v, 0), n = load3(nn, 0);
+  V3 B, T;
+  if (n.z < 0.) {
+    const float a = 1.0f / (1.0f - n.z);
+    const float b = (n.x * n.y) * a;
+    B = v3(1.0f - (n.x * n.x) * a, -b, n.x);
+    T = v3(b, (n.y * n.y) * a - 1.0f, -n.y);
+  } else {
+    const float a = 1.0f / (1.0f + n.z);
+    const float b = (-n.x * n.y) * a;
+    B = v3(1.0f - (n.x * n.x) * a, b, -n.x);
+    T = v3(b, 1.0f - (n.y * n.y) * a, -n.y);
+  }
+  const V3 r = add(add(muls(T, V.x), muls(B, V.y)), muls(n, V.z));
+  out[0] = r.x, out[1] = r.y, out[2] = r.z;
+}
+void or_local_space(const float* nn, float* T, float* B) {
+  const V3 n = load3(nn, 0);
+  const V3 W = std::fabs(n.x) > 0.99f ? v3(0.0f, 1.0f, 0.0f) : v3(1.0f, 0.0f, 0.0f);
+  const V3 t = normalize(cross(n, W)), b = cross(n, t);
+  T[0] = t.x, T[1] = t.y, T[2] = t.z, B[0] = b.x, B[1] = b.y, B[2] = b.z;
+}
+void or_cos_weighted(float r3, float r4, int exact, float* out) {
+  const float term1 = kTwoPi * r3;
+  const float term2 = (float)std::sqrt(1.0 - (double)r4);
+  out[0] = xcos(term1, exact) * term2, out[1] = xsin(term1, exact) * term2, out[2] = std::sqrt(r4);
 }
 
 /* draw_framebuffer (Kernel.cu:258-270): pow(sum.rgb / samples, 1/2.2), alpha 1. */

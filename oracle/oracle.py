@@ -228,6 +228,16 @@ def pack_materials(mats) -> np.ndarray:
     return out
 
 
+def work_read(reset: bool = True) -> dict:
+    """Traversal work counted by render_frames since the last reset."""
+    L = lib()
+    L.or_work_read.argtypes = [P, ctypes.c_int]
+    w = np.zeros(6, np.uint64)
+    L.or_work_read(_p(w), int(reset))
+    keys = ("ext_rays", "ext_nodes", "ext_tris", "shadow_rays", "shadow_nodes", "shadow_tris")
+    return {k: int(v) for k, v in zip(keys, w)}
+
+
 def camera_basis(forward, up, fov_deg, width, height):
     L = lib()
     fw = np.asarray(forward, np.float32)

@@ -1,0 +1,178 @@
+"""GPU wavefront frames against the CPU oracle's restatement of the reference
+kernels (generatePrimaryRays/extend/shade/connect, src/CUDA/Kernel.cu).
+
+Tolerance: 1e-4 relative per pixel channel. With exact_math the GPU and the
+oracle evaluate every operation identically and the accumulation buffers are
+expected to be bit-identical."""
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+RTOL = 1e-4
+
+
+@pytest.fixture(scope="module")
+def small(gpu_ctx, orc):
+    from cudatracer_gb300 import api, scenes
+
+    ts, cam = scenes.terrain_scene(grid=128, spheres=12, sky_size=(256, 128))
+    arr = scenes.scene_arrays(ts)
+    mats = [api.Material(**m) for m in ts.materials]
+    sc = gpu_ctx.scene(arr, mats, ts.textures, ts.skybox_texture)
+    bvh = sc.build_bvh()
+    ob = orc.bvh_build(ts.vertices, ts.indices)
+    return dict(ts=ts, cam=cam, arr=arr, sc=sc, bvh=bvh, ob=ob, omats=orc.pack_materials(ts.materials))
+
+
+def _render(gpu_ctx, S, W, H, frames, depth, exact, **kw):
+    from cudatracer_gb300 import api
+
+    job = api.RenderJob(gpu_ctx, W, H)
+    cam = S["cam"]
+    p = api.Params(W, H, camera=api.Camera(W, H, cam["fov"], cam["position"], cam["forward"], cam["up"]),
+                   max_depth=depth, exact_math=exact, **kw)
+    p.reset(job)
+    for _ in range(frames):
+        api.launch_kernels(job, S["sc"], S["bvh"], p)
+    gpu_ctx.check()
+    acc = job.accum_tensor().cpu().numpy().copy()
+    return job, p, acc
+
+
+def _oracle(orc, S, W, H, frames, depth, exact, **kw):
+    return orc.render_frames(S["arr"], S["omats"], S["ob"]["quad"], S["ob"]["prims"], S["cam"], W, H,
+                             [2 * f for f in range(frames)], depth, exact_math=exact, textures=S["ts"].textures,
+                             sky_tex=0, **kw)
+
+
+def _bad(a, b):
+    rel = np.abs(a - b) / np.maximum(np.abs(b), 1e-6)
+    return (rel > RTOL).any(axis=1)
+
+
+def test_exact_frames_match_oracle(gpu_ctx, orc, small):
+    W, H = 96, 64
+    _, p, acc = _render(gpu_ctx, small, W, H, 3, 5, True)
+    assert p.samples == 6  # launchKernels advances the counter by 2 per frame
+    oacc = _oracle(orc, small, W, H, 3, 5, True)
+    assert _bad(acc, oacc).sum() == 0
+    bit = (acc.view(np.int32) == oacc.view(np.int32)).all(axis=1).mean()
+    assert bit >= 0.999
+    assert acc[:, 3].max() > 0
+
+
+@pytest.mark.parametrize("flags", [dict(shadow=False), dict(indirect=False), dict(sky=False)])
+def test_exact_frames_flags(gpu_ctx, orc, small, flags):
+    W, H = 64, 48
+    _, _, acc = _render(gpu_ctx, small, W, H, 1, 8, True, **flags)
+    oacc = _oracle(orc, small, W, H, 1, 8, True, **flags)
+    assert _bad(acc, oacc).sum() == 0
+
+
+def test_fast_math_frames_close_to_oracle(gpu_ctx, orc, small):
+    W, H = 96, 64
+    _, _, acc = _render(gpu_ctx, small, W, H, 4, 5, False)
+    oacc = _oracle(orc, small, W, H, 4, 5, True)
+    # CUDA's float sin/cos/atan2/acos differ from the double-rounded ones by an
+    # ulp; a path that grazes an edge then diverges. Most pixels stay within
+    # tolerance and the image total stays close.
+    assert _bad(acc, oacc).mean() < 0.10
+    assert abs(acc[:, :3].sum() - oacc[:, :3].sum()) / oacc[:, :3].sum() < 0.02
+
+
+def test_present_matches_draw_framebuffer(gpu_ctx, orc, small):
+    import torch
+
+    W, H = 64, 48
+    job, p, acc = _render(gpu_ctx, small, W, H, 2, 5, True)
+    out = torch.zeros((W * H, 4), device="cuda")
+    job.present(p.samples, out)
+    rgba = np.zeros((W * H, 4), np.float32)
+    L = orc.lib()
+    L.or_present(acc.ctypes.data_as(orc.P), W * H, float(p.samples), rgba.ctypes.data_as(orc.P))
+    g = out.cpu().numpy()
+    assert np.allclose(g, rgba, rtol=2e-6, atol=1e-7)
+    assert (g[:, 3] == 1.0).all()
+
+
+def test_stats_and_validation(gpu_ctx, small):
+    from cudatracer_gb300 import _lib, api
+
+    W, H = 32, 16
+    job, p, _ = _render(gpu_ctx, small, W, H, 2, 5, False)
+    st = job.stats(reset=True)
+    assert st["samples"] == 2 * W * H and st["frames"] == 2
+    assert W * H * 2 <= st["extension_rays"] <= W * H * 2 * 5
+    bad = p.to_ct()
+    bad.width = W + 1
+    with pytest.raises(_lib.CTError) as e:
+        job.accumulate(small["sc"], small["bvh"], p.camera, bad)
+    assert e.value.status == 1
+    bad = p.to_ct()
+    bad.max_depth = 0
+    with pytest.raises(_lib.CTError):
+        job.accumulate(small["sc"], small["bvh"], p.camera, bad)
+    with pytest.raises(_lib.CTError):
+        api.RenderJob(gpu_ctx, 0, 10)
+
+
+def test_scene_validation(gpu_ctx):
+    from cudatracer_gb300 import _lib, api
+
+    v = np.array([[0, 0, 0], [1, 0, 0], [0, 1, 0]], np.float32)
+    n = np.tile(np.array([[0, 0, 1]], np.float32), (3, 1))
+    with pytest.raises(_lib.CTError):
+        gpu_ctx.scene({"vertices": v, "normals": n, "indices": np.array([[0, 1, 5]], np.uint32)}, [api.Material()])
+    with pytest.raises(_lib.CTError):
+        gpu_ctx.scene({"vertices": v, "normals": n, "indices": np.array([[0, 1, 2]], np.uint32),
+                       "material_idxs": np.array([3], np.uint32)}, [api.Material()])
+    bad = v.copy()
+    bad[1, 0] = np.inf
+    with pytest.raises(_lib.CTError):
+        gpu_ctx.scene({"vertices": bad, "normals": n, "indices": np.array([[0, 1, 2]], np.uint32)}, [api.Material()])
+    with pytest.raises(_lib.CTError):
+        gpu_ctx.scene({"vertices": v, "normals": n, "indices": np.array([[0, 1, 2]], np.uint32)},
+                      [api.Material(diffuse_tex=0)])
+
+
+def test_memory_budget_refuses_allocation(gpu_ctx):
+    from cudatracer_gb300 import _lib, api
+
+    used = gpu_ctx.device_bytes
+    gpu_ctx.set_memory_budget(used + (1 << 20))
+    try:
+        with pytest.raises(_lib.CTError) as e:
+            api.RenderJob(gpu_ctx, 1024, 1024)
+        assert e.value.status == 2
+        assert gpu_ctx.device_bytes == used  # nothing leaked by the failed creation
+    finally:
+        gpu_ctx.set_memory_budget(0)
+
+
+def test_full_size_frame_properties(gpu_ctx, orc):
+    """The 1920x1080, depth-8 workload on the 3.1M-triangle terrain scene:
+    two runs give bit-identical accumulation (compaction order does not leak
+    into results), the exact build matches the oracle on sampled rows, and
+    the image is finite and non-negative."""
+    from cudatracer_gb300 import api, scenes
+
+    ts, cam = scenes.terrain_scene()
+    arr = scenes.scene_arrays(ts)
+    sc = gpu_ctx.scene(arr, [api.Material(**m) for m in ts.materials], ts.textures, ts.skybox_texture)
+    bvh = sc.build_bvh()
+    S = dict(ts=ts, cam=cam, arr=arr, sc=sc, bvh=bvh)
+    W, H = 1920, 1080
+    _, _, a1 = _render(gpu_ctx, S, W, H, 1, 8, True)
+    _, _, a2 = _render(gpu_ctx, S, W, H, 1, 8, True)
+    assert np.array_equal(a1.view(np.int32), a2.view(np.int32))
+    assert np.isfinite(a1).all() and (a1 >= 0).all()
+    _, _, f1 = _render(gpu_ctx, S, W, H, 1, 8, False)
+    assert np.isfinite(f1).all() and (f1 >= 0).all()
+    ob = orc.bvh_build(ts.vertices, ts.indices)
+    S.update(ob=ob, omats=orc.pack_materials(ts.materials))
+    rows = [(0, 1), (400, 401), (700, 701), (1079, 1080)]
+    for r0, r1 in rows:
+        oacc = orc.render_frames(arr, S["omats"], ob["quad"], ob["prims"], cam, W, H, [0], 8, exact_math=True,
+                                 textures=ts.textures, sky_tex=0, pixels=(r0 * W, r1 * W))
+        sl = slice(r0 * W, r1 * W)
+        assert _bad(a1[sl], oacc[sl]).sum() == 0
