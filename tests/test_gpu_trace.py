@@ -81,20 +81,25 @@ def test_soup_closest_and_any_vs_oracle(gpu_ctx, orc, ntri, nray, seed):
     sc = _scene(gpu_ctx, s.vertices, s.indices)
     bvh = sc.build_bvh()
     o, d = scenes.incoherent_rays(nray, seed=seed + 10)
-    hit, t = bvh.trace_closest(_t4(o), _t4(d))
     ob = orc.bvh_build(s.vertices, s.indices)
-    oh, ot = orc.trace_closest(ob["quad"], ob["prims"], s.vertices, s.indices, o, d)
-    gpu_ctx.check()
-    assert np.array_equal(hit.cpu().numpy(), oh)
-    assert np.array_equal(t.cpu().numpy().view(np.int32), ot.view(np.int32))
-    rng = np.random.default_rng(seed)
-    tmax = np.where(ot < 1e30, ot * rng.uniform(0.5, 1.5, size=nray), rng.uniform(0.01, 2.0, size=nray))
-    occ = bvh.trace_any(_t4(o), _t4(d, tmax.astype(np.float32)))
-    oocc = orc.trace_any(ob["quad"], ob["prims"], s.vertices, s.indices, o, d, tmax.astype(np.float32))
-    assert np.array_equal(occ.cpu().numpy(), oocc)
-    assert oocc.sum() < nray
-    if (ot < 1e30).sum() > 100:  # tmax below the closest hit for about half of the hitting rays
-        assert oocc.sum() > 0
+    # The reference's absolute epsilon (1e-3 on the determinant) rejects every
+    # triangle with edges below ~0.03, i.e. the whole soup: check both that
+    # behaviour and a small epsilon under which the soup is visible.
+    for eps in (1e-3, 1e-12):
+        hit, t = bvh.trace_closest(_t4(o), _t4(d), tri_eps=eps)
+        oh, ot = orc.trace_closest(ob["quad"], ob["prims"], s.vertices, s.indices, o, d, eps=eps)
+        gpu_ctx.check()
+        assert np.array_equal(hit.cpu().numpy(), oh)
+        assert np.array_equal(t.cpu().numpy().view(np.int32), ot.view(np.int32))
+        rng = np.random.default_rng(seed)
+        tmax = np.where(ot < 1e30, ot * rng.uniform(0.5, 1.5, size=nray), rng.uniform(0.01, 2.0, size=nray))
+        occ = bvh.trace_any(_t4(o), _t4(d, tmax.astype(np.float32)), tri_eps=eps)
+        oocc = orc.trace_any(ob["quad"], ob["prims"], s.vertices, s.indices, o, d, tmax.astype(np.float32), eps=eps)
+        assert np.array_equal(occ.cpu().numpy(), oocc)
+        if eps == 1e-3:
+            assert (oh < 0).all() and oocc.sum() == 0
+        else:
+            assert (oh >= 0).sum() > 100 and 0 < oocc.sum() < nray
 
 
 def test_edge_rays_and_zero_count(gpu_ctx, orc):
@@ -185,14 +190,15 @@ def test_full_size_properties(gpu_ctx):
     bvh = sc.build_bvh()
     o, d = scenes.incoherent_rays(4_000_000, seed=21)
     O, D = _t4(o), _t4(d)
-    hit, t = bvh.trace_closest(O, D)
-    hit2, t2 = bvh.trace_closest(O, D)
+    eps = 1e-12  # the soup's triangles are far below the reference's 1e-3 determinant epsilon
+    hit, t = bvh.trace_closest(O, D, tri_eps=eps)
+    hit2, t2 = bvh.trace_closest(O, D, tri_eps=eps)
     perm = torch.randperm(O.shape[0], device="cuda")
-    hit3, t3 = bvh.trace_closest(O[perm].contiguous(), D[perm].contiguous())
+    hit3, t3 = bvh.trace_closest(O[perm].contiguous(), D[perm].contiguous(), tri_eps=eps)
     gpu_ctx.check()
     h, tt = hit.cpu().numpy(), t.cpu().numpy()
     assert ((h >= -1) & (h < s.ntri)).all()
-    assert (tt[h >= 0] > 1e-3).all() and (tt[h < 0] == np.float32(1e34)).all()
+    assert (tt[h >= 0] > eps).all() and (tt[h < 0] == np.float32(1e34)).all()
     assert torch.equal(hit, hit2) and torch.equal(t, t2)
     assert torch.equal(hit3, hit[perm]) and torch.equal(t3, t[perm])
     assert 0.05 < (h >= 0).mean() < 0.999
