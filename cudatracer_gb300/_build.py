@@ -28,6 +28,7 @@ SOURCES = {
     "k_trace.cu": [],
     "k_shade_exact.cu": ["-fmad=false"],
     "k_shade_fast.cu": [],
+    "noalloc.cu": [],
 }
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 

@@ -112,6 +112,7 @@ SIGNATURES = {
     "ct_render_stats": (c_int32, [P, P, POINTER(ct_frame_stats), c_int32, P]),
     "ct_render_profile": (c_int32, [P, P, c_int32]),
     "ct_render_profile_read": (c_int32, [P, P, POINTER(ct_stage_times), c_int32]),
+    "ct_render_accumulate_noalloc": (c_int32, [P, P, P, POINTER(ct_camera), POINTER(ct_render_params), P, P]),
 }
 
 _lib = None

@@ -714,6 +714,59 @@ ct_status ct_render_accumulate(ct_ctx* ctx, const ct_scene* scene, const ct_bvh*
   return CT_OK;
 }
 
+ct_status ct_render_accumulate_noalloc(ct_ctx* ctx, const ct_scene* scene, const ct_bvh* bvh, const ct_camera* cam,
+                                       const ct_render_params* p, float* accum_device, void* stream) {
+  if (!ctx || !scene || !bvh || !cam || !p || !accum_device) return fail(ctx, CT_ERR_INVALID_ARGUMENT, "null argument");
+  if (((uintptr_t)accum_device) & 15) return fail(ctx, CT_ERR_INVALID_ARGUMENT, "accumulation buffer must be 16-byte aligned");
+  if (p->width <= 0 || p->height <= 0) return fail(ctx, CT_ERR_INVALID_ARGUMENT, "bad frame size");
+  if ((int64_t)p->width * p->height > (int64_t)noalloc_max_pixels())
+    return fail(ctx, CT_ERR_INVALID_ARGUMENT,
+                "frame of " + std::to_string((int64_t)p->width * p->height) + " pixels exceeds the allocation-free limit of " +
+                    std::to_string(noalloc_max_pixels()) + " (CT_NOALLOC_MAX_PIXELS)");
+  if (p->max_depth < 1 || p->max_depth > 64) return fail(ctx, CT_ERR_INVALID_ARGUMENT, "max_depth must be in [1, 64]");
+  if (bvh->nt != scene->nt) return fail(ctx, CT_ERR_INVALID_ARGUMENT, "BVH was built for another scene");
+  if (p->shading_mode != CT_SHADE_COMPAT) return fail(ctx, CT_ERR_UNSUPPORTED, "shading mode not available");
+  if (!finite3(cam->position) || !finite3(cam->forward) || !finite3(cam->up) || !std::isfinite(cam->fov_deg))
+    return fail(ctx, CT_ERR_INVALID_ARGUMENT, "non-finite camera");
+  ct_status s = set_device(ctx);
+  if (s != CT_OK) return s;
+  // camera basis exactly as ct_render_accumulate derives it
+  const float dist = tanf((cam->fov_deg * 0.5f) * 0.01745329251994329576923690768489f);
+  const float* w = cam->forward;
+  const float* up = cam->up;
+  float u[3] = {w[1] * up[2] - up[1] * w[2], w[2] * up[0] - up[2] * w[0], w[0] * up[1] - up[0] * w[1]};
+  float inv = 1.0f / std::sqrt((u[0] * u[0] + u[1] * u[1]) + u[2] * u[2]);
+  u[0] *= inv, u[1] *= inv, u[2] *= inv;
+  float v[3] = {u[1] * w[2] - w[1] * u[2], u[2] * w[0] - w[2] * u[0], u[0] * w[1] - w[0] * u[1]};
+  inv = 1.0f / std::sqrt((v[0] * v[0] + v[1] * v[1]) + v[2] * v[2]);
+  v[0] *= inv, v[1] *= inv, v[2] *= inv;
+  float hor[3] = {u[0] * dist, u[1] * dist, u[2] * dist};
+  float ver[3] = {v[0] * dist, v[1] * dist, v[2] * dist};
+  const float aspect = (float)p->width / (float)p->height;
+  if (p->width > p->height)
+    hor[0] *= aspect, hor[1] *= aspect, hor[2] *= aspect;
+  else
+    ver[0] *= aspect, ver[1] *= aspect, ver[2] *= aspect;
+  FrameConst f;
+  f.cam_pos = make_float3(cam->position[0], cam->position[1], cam->position[2]);
+  f.cam_w = make_float3(w[0], w[1], w[2]);
+  f.hor = make_float3(hor[0], hor[1], hor[2]);
+  f.ver = make_float3(ver[0], ver[1], ver[2]);
+  f.width = p->width;
+  f.height = p->height;
+  f.frame = p->frame_index;
+  f.normal_eps = p->normal_eps;
+  f.dist_eps = p->dist_eps;
+  f.tri_eps = p->tri_eps;
+  f.shadow = p->shadow;
+  f.indirect = p->indirect;
+  f.sky = p->sky;
+  f.shading_mode = p->shading_mode;
+  CT_CUDA(ctx, noalloc_render(ctx->device, scene->dev, bvh->dev, f, p->max_depth, p->exact_math,
+                              (float4*)accum_device, ctx->d_error, (cudaStream_t)stream));
+  return CT_OK;
+}
+
 ct_status ct_render_accum(const ct_render* r, float** accum_device) {
   if (!r || !accum_device) return CT_ERR_INVALID_ARGUMENT;
   *accum_device = (float*)r->q.accum;

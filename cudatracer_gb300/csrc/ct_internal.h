@@ -117,4 +117,9 @@ cudaError_t launch_shade(const DevScene& sc, const DevQueues& q, const FrameCons
                          int exact, cudaStream_t s);
 cudaError_t launch_present(const float4* accum, float4* out, int n, float samples, cudaStream_t s);
 
+// allocation-free frame (noalloc.cu): queues in a static device array
+uint32_t noalloc_max_pixels();
+cudaError_t noalloc_render(int device, const DevScene& sc, const DevBVH& bvh, const FrameConst& f, int max_depth,
+                           int exact_math, float4* accum, uint32_t* err, cudaStream_t s);
+
 }  // namespace ct

@@ -242,6 +242,30 @@ typedef struct ct_stage_times {
 ct_status ct_render_profile(ct_ctx* ctx, ct_render* r, int32_t enable);
 ct_status ct_render_profile_read(ct_ctx* ctx, ct_render* r, ct_stage_times* out, int32_t reset);
 
+/* Allocation-free frame. No counterpart in the reference: its launchKernels
+ * always works in buffers that Application::allocateBuffers obtained with
+ * cudaMalloc. This entry point allocates no device memory at all. It is for
+ * hosts that must not let the library allocate while they render: an
+ * application that accounts for every byte of device memory itself, or a
+ * render thread that must never enter the CUDA allocator, since cudaMalloc
+ * and cudaFree can synchronise the device and stall a frame. The scene and
+ * BVH are made once beforehand; per frame the caller passes the camera,
+ * the parameters and its own accumulation buffer (DEVICE float4 per pixel,
+ * 16-byte aligned, added to exactly as ct_render_accumulate adds to a
+ * ct_render's buffer). The ray and shadow queues live in one static device
+ * array inside the library (about 9.5 MiB, held by every GPU that loads the
+ * library until the process exits), so:
+ *   - width * height must not exceed CT_NOALLOC_MAX_PIXELS, or the call fails
+ *     with CT_ERR_INVALID_ARGUMENT;
+ *   - every call shares that array: calls whose work overlaps on the GPU
+ *     (other streams, threads or contexts on the same device) race and must
+ *     be serialised by the caller;
+ *   - the first call on each device looks up the array's device address
+ *     (cudaGetSymbolAddress); make that first call before any stream capture. */
+#define CT_NOALLOC_MAX_PIXELS 65536
+ct_status ct_render_accumulate_noalloc(ct_ctx* ctx, const ct_scene* scene, const ct_bvh* bvh, const ct_camera* cam,
+                                       const ct_render_params* params, float* accum_device, void* stream);
+
 #ifdef __cplusplus
 }
 #endif
