@@ -26,6 +26,7 @@ struct ct_ctx {
   uint64_t budget = 0;
   std::atomic<uint64_t> bytes{0};
   uint32_t* d_error = nullptr;  // device error word
+  int* d_cursor = nullptr;      // ray-query fetch cursor (inside the same allocation)
 };
 
 namespace {
@@ -257,7 +258,8 @@ ct_status ct_ctx_create(int32_t device, ct_ctx** out) {
   if (cudaMalloc(&c->d_error, 256) != cudaSuccess || cudaMemset(c->d_error, 0, 256) != cudaSuccess) {
     delete c;
     return CT_ERR_OUT_OF_MEMORY;
-  }  *out = c;
+  }
+  c->d_cursor = (int*)(c->d_error + 32);  *out = c;
   return CT_OK;
 }
 
@@ -588,7 +590,7 @@ ct_status ct_trace_closest(ct_ctx* ctx, const ct_bvh* bvh, const float* org, con
   if (s != CT_OK) return s;
   if (n && (!hit || !t)) return fail(ctx, CT_ERR_INVALID_ARGUMENT, "null output buffer");
   CT_CUDA(ctx, launch_trace_closest(bvh->dev, (const float4*)org, (const float4*)dir, hit, t, n, tri_eps, ctx->d_error,
-                                    (cudaStream_t)stream));
+                                    ctx->d_cursor, (cudaStream_t)stream));
   return CT_OK;
 }
 
@@ -598,7 +600,7 @@ ct_status ct_trace_any(ct_ctx* ctx, const ct_bvh* bvh, const float* org, const f
   if (s != CT_OK) return s;
   if (n && !occluded) return fail(ctx, CT_ERR_INVALID_ARGUMENT, "null output buffer");
   CT_CUDA(ctx, launch_trace_any(bvh->dev, (const float4*)org, (const float4*)dir, occluded, n, tri_eps, ctx->d_error,
-                                (cudaStream_t)stream));
+                                ctx->d_cursor, (cudaStream_t)stream));
   return CT_OK;
 }
 
@@ -705,11 +707,11 @@ ct_status ct_render_accumulate(ct_ctx* ctx, const ct_scene* scene, const ct_bvh*
   for (int pass = 0; pass < p->max_depth; pass++) {
     const int cur = pass & 1;
     const int path_length = pass == 0 ? 0 : pass + 1;  // Kernel.cu:306, 330
-    CT_CUDA(ctx, staged(r, 1, st, [&] { return launch_extend(bvh->dev, r->q, cur, p->tri_eps, st); }));
+    CT_CUDA(ctx, staged(r, 1, st, [&] { return launch_extend(bvh->dev, r->q, cur, p->tri_eps, !p->exact_math, st); }));
     CT_CUDA(ctx, staged(r, 2, st, [&] {
               return launch_shade(scene->dev, r->q, f, cur, path_length, p->exact_math, st);
             }));
-    if (p->shadow) CT_CUDA(ctx, staged(r, 3, st, [&] { return launch_connect(bvh->dev, r->q, p->tri_eps, st); }));
+    if (p->shadow) CT_CUDA(ctx, staged(r, 3, st, [&] { return launch_connect(bvh->dev, r->q, p->tri_eps, !p->exact_math, st); }));
   }
   return CT_OK;
 }

@@ -78,7 +78,7 @@ struct DevQueues {
   float4* scol;      // shadow contribution xyz, w unused
   float4* accum;     // FP32 RGBA accumulation, one per pixel
   // device counters
-  int32_t* counts;   // [0],[1] ray queue sizes, [2] shadow queue size
+  int32_t* counts;   // [0],[1] ray queue sizes, [2] shadow queue size, [4] extend fetch cursor
   unsigned long long* stats;  // [0] extension rays, [1] shadow rays, [2] samples, [3] frames
   uint32_t* error;   // error bits (1 = stack overflow)
   int32_t capacity;
@@ -104,14 +104,17 @@ enum : uint32_t { kErrStackOverflow = 1u };
 // ---------------------------------------------------------------------------
 int sm_count();
 
+// `cursor`: a device int the launch resets; the kernel's warps take ray indices from it
 cudaError_t launch_trace_closest(const DevBVH& b, const float4* org, const float4* dir, int32_t* hit, float* t,
-                                 uint32_t n, float eps, uint32_t* err, cudaStream_t s);
+                                 uint32_t n, float eps, uint32_t* err, int* cursor, cudaStream_t s);
 cudaError_t launch_trace_any(const DevBVH& b, const float4* org, const float4* dir, uint8_t* occ, uint32_t n,
-                             float eps, uint32_t* err, cudaStream_t s);
+                             float eps, uint32_t* err, int* cursor, cudaStream_t s);
 
-// wavefront stages; the active count lives at counts[queue] on the device
-cudaError_t launch_extend(const DevBVH& b, const DevQueues& q, int queue, float eps, cudaStream_t s);
-cudaError_t launch_connect(const DevBVH& b, const DevQueues& q, float eps, cudaStream_t s);
+// wavefront stages; the active count lives at counts[queue] on the device and
+// extend's fetch cursor at counts[4] (zeroed by raygen and by every shade).
+// `fast` selects hardware min/max in the slab test (fast-math frames only).
+cudaError_t launch_extend(const DevBVH& b, const DevQueues& q, int queue, float eps, bool fast, cudaStream_t s);
+cudaError_t launch_connect(const DevBVH& b, const DevQueues& q, float eps, bool fast, cudaStream_t s);
 cudaError_t launch_raygen(const DevQueues& q, const FrameConst& f, int exact, cudaStream_t s);
 cudaError_t launch_shade(const DevScene& sc, const DevQueues& q, const FrameConst& f, int queue, int path_length,
                          int exact, cudaStream_t s);

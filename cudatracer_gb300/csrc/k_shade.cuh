@@ -282,6 +282,7 @@ __global__ void __launch_bounds__(kBlock) k_shade(DevScene sc, DevQueues q, Fram
                                                    uint32_t path_length) {
   const int n = q.counts[cur];
   const int nxt = cur ^ 1;
+  if (blockIdx.x == 0 && threadIdx.x == 0) q.counts[4] = 0;  // fetch cursor of the next extend
   const int lane = threadIdx.x & 31;
   const int stride = gridDim.x * kBlock;
   for (int base = blockIdx.x * kBlock + (threadIdx.x & ~31); base < n; base += stride) {
@@ -311,6 +312,7 @@ __global__ void __launch_bounds__(kBlock) k_raygen(DevQueues q, FrameConst f) {
   const int npix = f.width * f.height;
   if (blockIdx.x == 0 && threadIdx.x == 0) {
     q.counts[0] = npix;
+    q.counts[4] = 0;  // fetch cursor of the first extend
     atomicAdd(&q.stats[2], (unsigned long long)npix);
     atomicAdd(&q.stats[3], 1ull);
   }

@@ -1,11 +1,13 @@
 // Traversal kernels: public closest/any-hit queries and the wavefront's
 // extend (closest hit) and connect (shadow any hit + accumulate) stages.
 //
-// Launch shape: 128-thread blocks, each thread owns one ray at a time; the
-// traversal stack lives in dynamic shared memory laid out [entry][thread] so
-// that a warp's pushes and pops hit 32 distinct banks. Queue-driven stages
-// read their active count from device memory (no host round trip) and walk
-// the queue with a grid-stride loop over a grid sized to fill every SM.
+// Launch shape: 128-thread blocks, as many as are resident on all SMs. Ray
+// queries and extend use persistent warps that pull rays from a device
+// cursor (trace_persistent); connect walks its queue with a grid-stride loop
+// (shadow rays finish early, so refilling costs more than it saves there).
+// Queue-driven stages read their active count on the device: no host round
+// trip between stages. The traversal stack lives in dynamic shared memory laid
+// out [entry][thread], so a warp's pushes and pops hit 32 distinct banks.
 #include "trace.cuh"
 
 namespace ct {
@@ -42,37 +44,66 @@ cudaError_t prepare(K kernel, size_t smem) {
   return cudaSuccess;
 }
 
-// ---- public ray queries (ct_trace_closest / ct_trace_any) ----
-template <bool ANY>
-__global__ void __launch_bounds__(kBlock) k_query(DevBVH b, const float4* __restrict__ org,
-                                                   const float4* __restrict__ dir, int32_t* __restrict__ hit_out,
-                                                   float* __restrict__ t_out, uint8_t* __restrict__ occ_out,
-                                                   uint32_t n, float eps, uint32_t* err) {
-  extern __shared__ int s_stack[];
-  int* stack = s_stack + threadIdx.x;
-  for (uint32_t i = blockIdx.x * kBlock + threadIdx.x; i < n; i += gridDim.x * kBlock) {
-    const float4 o = __ldg(org + i), d = __ldg(dir + i);
-    float t = d.w;
-    int hit = -1;
-    if (!traverse<ANY>(b, o.x, o.y, o.z, d.x, d.y, d.z, eps, t, hit, stack, kBlock)) {
+// ---- ray sources and result sinks ----
+struct QueryIO {
+  const float4* __restrict__ org;
+  const float4* __restrict__ dir;
+  int32_t* hit_out;
+  float* t_out;
+  uint8_t* occ_out;
+  uint32_t* err;
+  __device__ void load(int i, float4& o, float4& d, float& t0) {
+    o = __ldg(org + i);
+    d = __ldg(dir + i);
+    t0 = d.w;
+  }
+  __device__ void store(int i, const RayState& r, bool overflow) {
+    int hit = r.hit;
+    float t = r.t;
+    if (overflow) {
       atomicOr(err, kErrStackOverflow);
       hit = -1;
-      t = d.w;
+      t = __ldg(&dir[i].w);
     }
-    if (ANY) {
+    if (occ_out) {
       occ_out[i] = hit >= 0 ? 1 : 0;
     } else {
       hit_out[i] = hit;
       t_out[i] = t;
     }
   }
+};
+
+// extend (src/CUDA/Kernel.cu:236-245): t restarts at MAX_DISTANCE every pass
+struct ExtendIO {
+  const float4* __restrict__ org;
+  const float4* __restrict__ dir;
+  int2* hit;
+  uint32_t* err;
+  __device__ void load(int i, float4& o, float4& d, float& t0) {
+    o = __ldg(org + i);
+    d = __ldg(dir + i);
+    t0 = kMaxDistance;
+  }
+  __device__ void store(int i, const RayState& r, bool overflow) {
+    if (overflow) {
+      atomicOr(err, kErrStackOverflow);
+      hit[i] = make_int2(-1, __float_as_int(kMaxDistance));
+      return;
+    }
+    hit[i] = make_int2(r.hit, __float_as_int(r.t));
+  }
+};
+
+template <bool ANY>
+__global__ void __launch_bounds__(kBlock) k_query(DevBVH b, QueryIO io, int n, int* cursor, float eps) {
+  extern __shared__ int s_stack[];
+  trace_persistent<ANY, false>(b, n, cursor, eps, io, s_stack + threadIdx.x, kBlock);
 }
 
-// ---- wavefront extend: closest hit for every ray of queue `qi` ----
-// (the reference's extend, src/CUDA/Kernel.cu:236-245: t reset to MAX_DISTANCE)
+template <bool FASTMM>
 __global__ void __launch_bounds__(kBlock) k_extend(DevBVH b, DevQueues q, int qi, float eps) {
   extern __shared__ int s_stack[];
-  int* stack = s_stack + threadIdx.x;
   const int n = q.counts[qi];
   if (blockIdx.x == 0 && threadIdx.x == 0) {
     // the shade stage that follows appends to these (setGlobals, Kernel.cu:75-86)
@@ -80,23 +111,13 @@ __global__ void __launch_bounds__(kBlock) k_extend(DevBVH b, DevQueues q, int qi
     q.counts[2] = 0;
     atomicAdd(&q.stats[0], (unsigned long long)n);
   }
-  const float4* __restrict__ org = q.org_q(qi);
-  const float4* __restrict__ dir = q.dir_q(qi);
-  for (int i = blockIdx.x * kBlock + threadIdx.x; i < n; i += gridDim.x * kBlock) {
-    const float4 o = __ldg(org + i), d = __ldg(dir + i);
-    float t = kMaxDistance;
-    int hit = -1;
-    if (!traverse<false>(b, o.x, o.y, o.z, d.x, d.y, d.z, eps, t, hit, stack, kBlock)) {
-      atomicOr(q.error, kErrStackOverflow);
-      hit = -1;
-      t = kMaxDistance;
-    }
-    q.hit[i] = make_int2(hit, __float_as_int(t));
-  }
+  ExtendIO io{q.org_q(qi), q.dir_q(qi), q.hit, q.error};
+  trace_persistent<false, FASTMM>(b, n, q.counts + 4, eps, io, s_stack + threadIdx.x, kBlock);
 }
 
-// ---- wavefront connect: shadow any hit, add unoccluded contributions ----
-// (src/CUDA/Kernel.cu:247-256)
+// connect (src/CUDA/Kernel.cu:247-256): unoccluded shadow rays add their
+// contribution to their pixel (one shadow ray per pixel per pass: no race)
+template <bool FASTMM>
 __global__ void __launch_bounds__(kBlock) k_connect(DevBVH b, DevQueues q, float eps) {
   extern __shared__ int s_stack[];
   int* stack = s_stack + threadIdx.x;
@@ -104,16 +125,16 @@ __global__ void __launch_bounds__(kBlock) k_connect(DevBVH b, DevQueues q, float
   if (blockIdx.x == 0 && threadIdx.x == 0) atomicAdd(&q.stats[1], (unsigned long long)n);
   for (int i = blockIdx.x * kBlock + threadIdx.x; i < n; i += gridDim.x * kBlock) {
     const float4 o = __ldg(q.sorg + i), d = __ldg(q.sdir + i);
-    float t = d.w;
-    int hit = -1;
-    if (!traverse<true>(b, o.x, o.y, o.z, d.x, d.y, d.z, eps, t, hit, stack, kBlock)) {
+    RayState r;
+    ray_begin(r, o, d, d.w);
+    if (!traverse<true, FASTMM>(b, r, eps, stack, kBlock)) {
       atomicOr(q.error, kErrStackOverflow);
       continue;
     }
-    if (hit < 0) {
+    if (r.hit < 0) {
       const float4 c = __ldg(q.scol + i);
       const int pix = __float_as_int(o.w);
-      float4 a = q.accum[pix];  // one shadow ray per pixel per pass: no race
+      float4 a = q.accum[pix];
       a.x = __fadd_rn(a.x, c.x);
       a.y = __fadd_rn(a.y, c.y);
       a.z = __fadd_rn(a.z, c.z);
@@ -123,49 +144,50 @@ __global__ void __launch_bounds__(kBlock) k_connect(DevBVH b, DevQueues q, float
   }
 }
 
+template <bool ANY>
+cudaError_t launch_query(const DevBVH& b, const QueryIO& io, uint32_t n, int* cursor, float eps, cudaStream_t s) {
+  if (n == 0) return cudaSuccess;
+  const size_t smem = stack_bytes(b);
+  cudaError_t e = prepare(k_query<ANY>, smem);
+  if (e != cudaSuccess) return e;
+  if ((e = cudaMemsetAsync(cursor, 0, sizeof(int), s)) != cudaSuccess) return e;
+  const uint32_t blocks = (n + kBlock - 1) / kBlock;
+  const uint32_t grid = std::min<uint32_t>(blocks, (uint32_t)resident_grid(k_query<ANY>, smem));
+  k_query<ANY><<<grid, kBlock, smem, s>>>(b, io, (int)n, cursor, eps);
+  return cudaGetLastError();
+}
+
 }  // namespace
 
 cudaError_t launch_trace_closest(const DevBVH& b, const float4* org, const float4* dir, int32_t* hit, float* t,
-                                 uint32_t n, float eps, uint32_t* err, cudaStream_t s) {
-  if (n == 0) return cudaSuccess;
-  const size_t smem = stack_bytes(b);
-  cudaError_t e = prepare(k_query<false>, smem);
-  if (e != cudaSuccess) return e;
-  const uint32_t blocks = (n + kBlock - 1) / kBlock;
-  const uint32_t grid = std::min<uint32_t>(blocks, (uint32_t)resident_grid(k_query<false>, smem) * 8u);
-  k_query<false><<<grid, kBlock, smem, s>>>(b, org, dir, hit, t, nullptr, n, eps, err);
-  return cudaGetLastError();
+                                 uint32_t n, float eps, uint32_t* err, int* cursor, cudaStream_t s) {
+  return launch_query<false>(b, QueryIO{org, dir, hit, t, nullptr, err}, n, cursor, eps, s);
 }
 
 cudaError_t launch_trace_any(const DevBVH& b, const float4* org, const float4* dir, uint8_t* occ, uint32_t n,
-                             float eps, uint32_t* err, cudaStream_t s) {
-  if (n == 0) return cudaSuccess;
+                             float eps, uint32_t* err, int* cursor, cudaStream_t s) {
+  return launch_query<true>(b, QueryIO{org, dir, nullptr, nullptr, occ, err}, n, cursor, eps, s);
+}
+
+cudaError_t launch_extend(const DevBVH& b, const DevQueues& q, int queue, float eps, bool fast, cudaStream_t s) {
   const size_t smem = stack_bytes(b);
-  cudaError_t e = prepare(k_query<true>, smem);
+  auto kernel = fast ? k_extend<true> : k_extend<false>;
+  cudaError_t e = prepare(kernel, smem);
   if (e != cudaSuccess) return e;
-  const uint32_t blocks = (n + kBlock - 1) / kBlock;
-  const uint32_t grid = std::min<uint32_t>(blocks, (uint32_t)resident_grid(k_query<true>, smem) * 8u);
-  k_query<true><<<grid, kBlock, smem, s>>>(b, org, dir, nullptr, nullptr, occ, n, eps, err);
+  const int cap_blocks = (q.capacity + kBlock - 1) / kBlock;
+  const int grid = std::max(1, std::min(cap_blocks, resident_grid(kernel, smem)));
+  kernel<<<grid, kBlock, smem, s>>>(b, q, queue, eps);
   return cudaGetLastError();
 }
 
-cudaError_t launch_extend(const DevBVH& b, const DevQueues& q, int queue, float eps, cudaStream_t s) {
+cudaError_t launch_connect(const DevBVH& b, const DevQueues& q, float eps, bool fast, cudaStream_t s) {
   const size_t smem = stack_bytes(b);
-  cudaError_t e = prepare(k_extend, smem);
+  auto kernel = fast ? k_connect<true> : k_connect<false>;
+  cudaError_t e = prepare(kernel, smem);
   if (e != cudaSuccess) return e;
   const int cap_blocks = (q.capacity + kBlock - 1) / kBlock;
-  const int grid = std::max(1, std::min(cap_blocks, resident_grid(k_extend, smem)));
-  k_extend<<<grid, kBlock, smem, s>>>(b, q, queue, eps);
-  return cudaGetLastError();
-}
-
-cudaError_t launch_connect(const DevBVH& b, const DevQueues& q, float eps, cudaStream_t s) {
-  const size_t smem = stack_bytes(b);
-  cudaError_t e = prepare(k_connect, smem);
-  if (e != cudaSuccess) return e;
-  const int cap_blocks = (q.capacity + kBlock - 1) / kBlock;
-  const int grid = std::max(1, std::min(cap_blocks, resident_grid(k_connect, smem)));
-  k_connect<<<grid, kBlock, smem, s>>>(b, q, eps);
+  const int grid = std::max(1, std::min(cap_blocks, resident_grid(kernel, smem)));
+  kernel<<<grid, kBlock, smem, s>>>(b, q, eps);
   return cudaGetLastError();
 }
 

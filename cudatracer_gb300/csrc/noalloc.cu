@@ -84,9 +84,9 @@ cudaError_t noalloc_render(int device, const DevScene& sc, const DevBVH& bvh, co
   for (int pass = 0; pass < max_depth; pass++) {
     const int cur = pass & 1;
     const int path_length = pass == 0 ? 0 : pass + 1;
-    if ((e = launch_extend(bvh, q, cur, f.tri_eps, s)) != cudaSuccess) return e;
+    if ((e = launch_extend(bvh, q, cur, f.tri_eps, !exact_math, s)) != cudaSuccess) return e;
     if ((e = launch_shade(sc, q, f, cur, path_length, exact_math, s)) != cudaSuccess) return e;
-    if (f.shadow && (e = launch_connect(bvh, q, f.tri_eps, s)) != cudaSuccess) return e;
+    if (f.shadow && (e = launch_connect(bvh, q, f.tri_eps, !exact_math, s)) != cudaSuccess) return e;
   }
   return cudaSuccess;
 }

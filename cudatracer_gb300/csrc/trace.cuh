@@ -6,6 +6,12 @@
 // operations, in the same order, as the reference's glm code
 // (src/BVH/MBVHNode.cuh:69-110, src/Core/Triangle.cuh:13-44), which is what
 // makes closest-hit primitive ids and t bit-exact against it.
+//
+// Min/max: glm::min(x,y) = y < x ? y : x and glm::max(x,y) = x < y ? y : x.
+// With FASTMM the hardware min/max is used instead; the two agree except when
+// a slab term is NaN (a zero direction component with the origin exactly on a
+// bounding plane) or when two zeros of opposite sign meet (an origin on two
+// planes). The fast-math render path uses FASTMM; exact paths never do.
 #pragma once
 
 #include "ct_internal.h"
@@ -16,7 +22,15 @@ namespace ct {
 __device__ __forceinline__ float fsub(float a, float b) { return __fsub_rn(a, b); }
 __device__ __forceinline__ float fadd(float a, float b) { return __fadd_rn(a, b); }
 __device__ __forceinline__ float fmul(float a, float b) { return __fmul_rn(a, b); }
-// gmin / gmax (vmath.cuh) are glm::min / glm::max: (y < x) ? y : x and (x < y) ? y : x.
+
+template <bool FASTMM>
+__device__ __forceinline__ float mn(float x, float y) {
+  return FASTMM ? fminf(x, y) : gmin(x, y);
+}
+template <bool FASTMM>
+__device__ __forceinline__ float mx(float x, float y) {
+  return FASTMM ? fmaxf(x, y) : gmax(x, y);
+}
 
 template <typename T>
 __device__ __forceinline__ T sel4(T a, T b, T c, T d, int i) {
@@ -24,20 +38,21 @@ __device__ __forceinline__ T sel4(T a, T b, T c, T d, int i) {
 }
 
 // One child's slab interval, reference order: x, then y, then z.
+template <bool FASTMM>
 __device__ __forceinline__ void slab(float bminx, float bmaxx, float bminy, float bmaxy, float bminz, float bmaxz,
                                      float ox, float oy, float oz, float ix, float iy, float iz, float& tmin,
                                      float& tmax) {
   float t1 = fmul(fsub(bminx, ox), ix), t2 = fmul(fsub(bmaxx, ox), ix);
-  tmin = gmin(t1, t2);
-  tmax = gmax(t1, t2);
+  tmin = mn<FASTMM>(t1, t2);
+  tmax = mx<FASTMM>(t1, t2);
   t1 = fmul(fsub(bminy, oy), iy);
   t2 = fmul(fsub(bmaxy, oy), iy);
-  tmin = gmax(tmin, gmin(t1, t2));
-  tmax = gmin(tmax, gmax(t1, t2));
+  tmin = mx<FASTMM>(tmin, mn<FASTMM>(t1, t2));
+  tmax = mn<FASTMM>(tmax, mx<FASTMM>(t1, t2));
   t1 = fmul(fsub(bminz, oz), iz);
   t2 = fmul(fsub(bmaxz, oz), iz);
-  tmin = gmax(tmin, gmin(t1, t2));
-  tmax = gmin(tmax, gmax(t1, t2));
+  tmin = mx<FASTMM>(tmin, mn<FASTMM>(t1, t2));
+  tmax = mn<FASTMM>(tmax, mx<FASTMM>(t1, t2));
 }
 
 // Moller-Trumbore with the reference's absolute epsilon. Returns the new t
@@ -70,86 +85,168 @@ __device__ __forceinline__ bool tri_test(const float4 a, const float4 e1v, const
   return false;
 }
 
-// Traverse one ray. ANY = stop at the first hit (traverseMBVHShadow semantics:
-// nodes culled against maxDist, triangles accepted below it).
-// `stack` points at this thread's column of a [entries][stride] shared array.
-// Returns false if the stack limit was reached (the ray's result is dropped).
-template <bool ANY>
-__device__ __forceinline__ bool traverse(const DevBVH& b, float ox, float oy, float oz, float dx, float dy, float dz,
-                                         float eps, float& t, int& hit, int* stack, int stride) {
-  const float ix = __frcp_rn(dx), iy = __frcp_rn(dy), iz = __frcp_rn(dz);
-  const int limit = b.stack_entries;
-  int sp = 0;
-  int ref = 0;  // root: inner node 0 (the reference's todo[0] = {0, -1})
-  while (true) {
-    if (ref >= 0) {
-      const QNodeDev* n = b.nodes + ref;
-      const float4 nx0 = __ldg(&n->bminx), nx1 = __ldg(&n->bmaxx);
-      const float4 ny0 = __ldg(&n->bminy), ny1 = __ldg(&n->bmaxy);
-      const float4 nz0 = __ldg(&n->bminz), nz1 = __ldg(&n->bmaxz);
-      const int4 ch = __ldg(&n->child);
-      float tn0, tn1, tn2, tn3, tf0, tf1, tf2, tf3;
-      slab(nx0.x, nx1.x, ny0.x, ny1.x, nz0.x, nz1.x, ox, oy, oz, ix, iy, iz, tn0, tf0);
-      slab(nx0.y, nx1.y, ny0.y, ny1.y, nz0.y, nz1.y, ox, oy, oz, ix, iy, iz, tn1, tf1);
-      slab(nx0.z, nx1.z, ny0.z, ny1.z, nz0.z, nz1.z, ox, oy, oz, ix, iy, iz, tn2, tf2);
-      slab(nx0.w, nx1.w, ny0.w, ny1.w, nz0.w, nz1.w, ox, oy, oz, ix, iy, iz, tn3, tf3);
-      // child id in the low two bits of tmin (MBVHNode.cuh:91-94)
-      float p0 = __int_as_float((__float_as_int(tn0) & ~3) | 0);
-      float p1 = __int_as_float((__float_as_int(tn1) & ~3) | 1);
-      float p2 = __int_as_float((__float_as_int(tn2) & ~3) | 2);
-      float p3 = __int_as_float((__float_as_int(tn3) & ~3) | 3);
-      const bool r0 = tf0 > 0.0f && p0 <= tf0 && p0 < t;
-      const bool r1 = tf1 > 0.0f && p1 <= tf1 && p1 < t;
-      const bool r2 = tf2 > 0.0f && p2 <= tf2 && p2 < t;
-      const bool r3 = tf3 > 0.0f && p3 <= tf3 && p3 < t;
-      // the reference's 5-exchange network, last pair (2,3) (MBVHNode.cuh:98-107)
-      float s;
-      if (p0 > p1) s = p0, p0 = p1, p1 = s;
-      if (p2 > p3) s = p2, p2 = p3, p3 = s;
-      if (p0 > p2) s = p0, p0 = p2, p2 = s;
-      if (p1 > p3) s = p1, p1 = p3, p3 = s;
-      if (p2 > p3) s = p2, p2 = p3, p3 = s;
-      // push far to near (i = 3..0); the nearest stays in a register
-      int held = kEmptyChild;
-      bool have = false;
+// Per-ray traversal state.
+struct RayState {
+  float ox, oy, oz, dx, dy, dz, ix, iy, iz, t;
+  int hit, sp, ref;
+};
+
+__device__ __forceinline__ void ray_begin(RayState& r, float4 o, float4 d, float t0) {
+  r.ox = o.x, r.oy = o.y, r.oz = o.z, r.dx = d.x, r.dy = d.y, r.dz = d.z;
+  r.ix = __frcp_rn(d.x), r.iy = __frcp_rn(d.y), r.iz = __frcp_rn(d.z);
+  r.t = t0;
+  r.hit = -1;
+  r.sp = 0;
+  r.ref = 0;  // root: inner node 0 (the reference's todo[0] = {0, -1})
+}
+
+enum StepResult { kContinue = 0, kDone = 1, kOverflow = 2 };
+
+// Visit the inner node r.ref: slab-test the four children (MBVHNode.cuh:69-110),
+// then continue with the nearest hit child and push the others far to near
+// (:153-161). With zero or one child hit the order network cannot matter, so
+// it is skipped; with two or more it runs over all four packed tmin values,
+// exactly as the reference's does.
+template <bool FASTMM>
+__device__ __forceinline__ StepResult inner_step(const DevBVH& b, RayState& r, int* stack, int stride, int limit) {
+  const QNodeDev* n = b.nodes + r.ref;
+  const float4 nx0 = __ldg(&n->bminx), nx1 = __ldg(&n->bmaxx);
+  const float4 ny0 = __ldg(&n->bminy), ny1 = __ldg(&n->bmaxy);
+  const float4 nz0 = __ldg(&n->bminz), nz1 = __ldg(&n->bmaxz);
+  const int4 ch = __ldg(&n->child);
+  float tn0, tn1, tn2, tn3, tf0, tf1, tf2, tf3;
+  slab<FASTMM>(nx0.x, nx1.x, ny0.x, ny1.x, nz0.x, nz1.x, r.ox, r.oy, r.oz, r.ix, r.iy, r.iz, tn0, tf0);
+  slab<FASTMM>(nx0.y, nx1.y, ny0.y, ny1.y, nz0.y, nz1.y, r.ox, r.oy, r.oz, r.ix, r.iy, r.iz, tn1, tf1);
+  slab<FASTMM>(nx0.z, nx1.z, ny0.z, ny1.z, nz0.z, nz1.z, r.ox, r.oy, r.oz, r.ix, r.iy, r.iz, tn2, tf2);
+  slab<FASTMM>(nx0.w, nx1.w, ny0.w, ny1.w, nz0.w, nz1.w, r.ox, r.oy, r.oz, r.ix, r.iy, r.iz, tn3, tf3);
+  // child id in the low two bits of tmin (MBVHNode.cuh:91-94)
+  float p0 = __int_as_float((__float_as_int(tn0) & ~3) | 0);
+  float p1 = __int_as_float((__float_as_int(tn1) & ~3) | 1);
+  float p2 = __int_as_float((__float_as_int(tn2) & ~3) | 2);
+  float p3 = __int_as_float((__float_as_int(tn3) & ~3) | 3);
+  const float t = r.t;
+  // hit mask by child slot (MBVHNode.cuh:96); empty slots are never pushed
+  const unsigned vm = ((tf0 > 0.0f && p0 <= tf0 && p0 < t && ch.x != kEmptyChild) ? 1u : 0u) |
+                      ((tf1 > 0.0f && p1 <= tf1 && p1 < t && ch.y != kEmptyChild) ? 2u : 0u) |
+                      ((tf2 > 0.0f && p2 <= tf2 && p2 < t && ch.z != kEmptyChild) ? 4u : 0u) |
+                      ((tf3 > 0.0f && p3 <= tf3 && p3 < t && ch.w != kEmptyChild) ? 8u : 0u);
+  if (vm == 0) {
+    if (r.sp == 0) return kDone;
+    r.ref = stack[--r.sp * stride];
+    return kContinue;
+  }
+  if ((vm & (vm - 1)) == 0) {
+    r.ref = vm == 1 ? ch.x : (vm == 2 ? ch.y : (vm == 4 ? ch.z : ch.w));
+    return kContinue;
+  }
+  // the reference's 5-exchange network, last pair (2,3) (MBVHNode.cuh:98-107)
+  float s;
+  if (p0 > p1) s = p0, p0 = p1, p1 = s;
+  if (p2 > p3) s = p2, p2 = p3, p3 = s;
+  if (p0 > p2) s = p0, p0 = p2, p2 = s;
+  if (p1 > p3) s = p1, p1 = p3, p3 = s;
+  if (p2 > p3) s = p2, p2 = p3, p3 = s;
+  int held = kEmptyChild;
+  bool have = false;
 #pragma unroll
-      for (int i = 3; i >= 0; i--) {
-        const float pi = sel4(p0, p1, p2, p3, i);
-        const int c = __float_as_int(pi) & 3;
-        const bool ri = sel4(r0, r1, r2, r3, c);
-        const int cr = sel4(ch.x, ch.y, ch.z, ch.w, c);
-        if (ri && cr != kEmptyChild) {
-          if (have) {
-            if (sp >= limit) return false;
-            stack[sp * stride] = held;
-            sp++;
-          }
-          held = cr;
-          have = true;
-        }
-      }
+  for (int i = 3; i >= 0; i--) {
+    const int c = __float_as_int(sel4(p0, p1, p2, p3, i)) & 3;
+    if ((vm >> c) & 1u) {
+      const int cr = sel4(ch.x, ch.y, ch.z, ch.w, c);
       if (have) {
-        ref = held;
-        continue;
+        if (r.sp >= limit) return kOverflow;
+        stack[r.sp * stride] = held;
+        r.sp++;
       }
-    } else {
-      const uint32_t u = (uint32_t)ref;
-      const uint32_t first = u & b.first_mask;
-      const uint32_t cnt = (u >> b.leaf_shift) & b.count_mask;
-      const float4* tp = b.tris + 3 * (size_t)first;
-      for (uint32_t i = 0; i < cnt; i++) {
-        const float4 a = __ldg(tp + 3 * i), e1 = __ldg(tp + 3 * i + 1), e2 = __ldg(tp + 3 * i + 2);
-        if (tri_test(a, e1, e2, ox, oy, oz, dx, dy, dz, eps, t)) {
-          hit = __float_as_int(a.w);
-          if (ANY) return true;
+      held = cr;
+      have = true;
+    }
+  }
+  r.ref = held;
+  return kContinue;
+}
+
+// Test the leaf r.ref's triangles in primitive order, then pop.
+template <bool ANY>
+__device__ __forceinline__ StepResult leaf_step(const DevBVH& b, RayState& r, float eps, int* stack, int stride) {
+  const uint32_t u = (uint32_t)r.ref;
+  const uint32_t first = u & b.first_mask;
+  const uint32_t cnt = (u >> b.leaf_shift) & b.count_mask;
+  const float4* tp = b.tris + 3 * (size_t)first;
+  for (uint32_t k = 0; k < cnt; k++) {
+    const float4 a = __ldg(tp + 3 * k), e1 = __ldg(tp + 3 * k + 1), e2 = __ldg(tp + 3 * k + 2);
+    if (tri_test(a, e1, e2, r.ox, r.oy, r.oz, r.dx, r.dy, r.dz, eps, r.t)) {
+      r.hit = __float_as_int(a.w);
+      if (ANY) return kDone;
+    }
+  }
+  if (r.sp == 0) return kDone;
+  r.ref = stack[--r.sp * stride];
+  return kContinue;
+}
+
+// Whole traversal of one ray by one thread. ANY = stop at the first hit
+// (traverseMBVHShadow: nodes culled against maxDist, triangles accepted below
+// it). `stack` is this thread's column of a [entries][stride] shared array.
+// Returns false when the stack limit was reached (the ray's result is dropped).
+template <bool ANY, bool FASTMM>
+__device__ __forceinline__ bool traverse(const DevBVH& b, RayState& r, float eps, int* stack, int stride) {
+  const int limit = b.stack_entries;
+  while (true) {
+    const StepResult s = r.ref >= 0 ? inner_step<FASTMM>(b, r, stack, stride, limit) : leaf_step<ANY>(b, r, eps, stack, stride);
+    if (s == kDone) return true;
+    if (s == kOverflow) return false;
+  }
+}
+
+// Persistent traversal with per-warp dynamic ray fetch. Each lane owns a ray
+// and performs one step (an inner node or a leaf) per round; lanes whose ray
+// finished take the next rays from a device cursor (one atomicAdd per warp),
+// so a warp is not held back by its longest ray. Every ray still performs the
+// reference's exact sequence of node tests, pushes, pops and triangle tests:
+// only the interleaving across lanes changes.
+//   IO::load(int i, float4& org, float4& dir, float& t0)
+//   IO::store(int i, const RayState& r, bool overflow)
+template <bool ANY, bool FASTMM, class IO>
+__device__ __forceinline__ void trace_persistent(const DevBVH& b, int n, int* cursor, float eps, IO& io, int* stack,
+                                                 int stride) {
+  const unsigned FULL = 0xffffffffu;
+  const int lane = threadIdx.x & 31;
+  const unsigned below = (1u << lane) - 1u;
+  const int limit = b.stack_entries;
+  int rid = -1;
+  bool exhausted = false;
+  RayState r;
+  r.ref = kEmptyChild;
+  while (true) {
+    if (!exhausted) {
+      const unsigned m = __ballot_sync(FULL, rid < 0);
+      if (m) {
+        const int leader = __ffs(m) - 1;
+        int base = 0;
+        if (lane == leader) base = atomicAdd(cursor, __popc(m));
+        base = __shfl_sync(FULL, base, leader);
+        if (base + __popc(m) >= n) exhausted = true;
+        if (rid < 0) {
+          const int my = base + __popc(m & below);
+          if (my < n) {
+            float4 o, d;
+            float t0;
+            io.load(my, o, d, t0);
+            ray_begin(r, o, d, t0);
+            rid = my;
+          }
         }
       }
     }
-    if (sp == 0) break;
-    sp--;
-    ref = stack[sp * stride];
+    if (__ballot_sync(FULL, rid >= 0) == 0) break;
+    if (rid < 0) continue;
+    const StepResult s = r.ref >= 0 ? inner_step<FASTMM>(b, r, stack, stride, limit) : leaf_step<ANY>(b, r, eps, stack, stride);
+    if (s != kContinue) {
+      io.store(rid, r, s == kOverflow);
+      rid = -1;
+    }
   }
-  return true;
 }
 
 }  // namespace ct
