@@ -655,7 +655,8 @@ ct_status ct_render_accumulate(ct_ctx* ctx, const ct_scene* scene, const ct_bvh*
   if (p->width != r->w || p->height != r->h) return fail(ctx, CT_ERR_INVALID_ARGUMENT, "params size differs from the render job's");
   if (p->max_depth < 1 || p->max_depth > 64) return fail(ctx, CT_ERR_INVALID_ARGUMENT, "max_depth must be in [1, 64]");
   if (bvh->nt != scene->nt) return fail(ctx, CT_ERR_INVALID_ARGUMENT, "BVH was built for another scene");
-  if (p->shading_mode != CT_SHADE_COMPAT) return fail(ctx, CT_ERR_UNSUPPORTED, "shading mode not available");
+  if (p->shading_mode != CT_SHADE_COMPAT && p->shading_mode != CT_SHADE_FULL)
+    return fail(ctx, CT_ERR_INVALID_ARGUMENT, "unknown shading mode");
   if (!finite3(cam->position) || !finite3(cam->forward) || !finite3(cam->up) || !std::isfinite(cam->fov_deg))
     return fail(ctx, CT_ERR_INVALID_ARGUMENT, "non-finite camera");
   ct_status s = set_device(ctx);
@@ -727,7 +728,8 @@ ct_status ct_render_accumulate_noalloc(ct_ctx* ctx, const ct_scene* scene, const
                     std::to_string(noalloc_max_pixels()) + " (CT_NOALLOC_MAX_PIXELS)");
   if (p->max_depth < 1 || p->max_depth > 64) return fail(ctx, CT_ERR_INVALID_ARGUMENT, "max_depth must be in [1, 64]");
   if (bvh->nt != scene->nt) return fail(ctx, CT_ERR_INVALID_ARGUMENT, "BVH was built for another scene");
-  if (p->shading_mode != CT_SHADE_COMPAT) return fail(ctx, CT_ERR_UNSUPPORTED, "shading mode not available");
+  if (p->shading_mode != CT_SHADE_COMPAT && p->shading_mode != CT_SHADE_FULL)
+    return fail(ctx, CT_ERR_INVALID_ARGUMENT, "unknown shading mode");
   if (!finite3(cam->position) || !finite3(cam->forward) || !finite3(cam->up) || !std::isfinite(cam->fov_deg))
     return fail(ctx, CT_ERR_INVALID_ARGUMENT, "non-finite camera");
   ct_status s = set_device(ctx);

@@ -14,8 +14,13 @@
 // the reference's per-thread atomicAdd.
 #pragma once
 
+#include "bsdf_full.cuh"
 #include "ct_internal.h"
 #include "vmath.cuh"
+
+#ifndef CT_MODE_FULL
+#define CT_MODE_FULL 1  // CT_SHADE_FULL in include/cudatracer.h
+#endif
 
 #ifndef CT_SHADE_NS
 #error "define CT_SHADE_NS"
@@ -267,6 +272,147 @@ __device__ __forceinline__ void shade_compat(const DevScene& sc, const DevQueues
   e.nt = f4(T, pdf);
 }
 
+// ---------------------------------------------------------------------------
+// CT_SHADE_FULL: every material type of the reference's Material record
+// (bsdf_full.cuh), next-event estimation for the non-delta reflective lobes,
+// power-heuristic MIS between light sampling and BSDF sampling. Unlike compat
+// mode the geometry is taken at the hit point: barycentrics of the hit, a
+// normalised interpolated normal, the face normal for ray offsets, and the
+// emitter's own material for NEE.
+//   ray flags (dir.w bits): 2 = the previous vertex sampled a light, so an
+//   emitter hit is weighted against the light-sampling density
+//   throughput.w: solid-angle density of the sampled direction
+// ---------------------------------------------------------------------------
+constexpr int kFlagMis = 2;
+constexpr float kShadowRel = 1e-4f;  // shadow rays end at dist * (1 - kShadowRel) - 2 * dist_eps
+
+// orthonormal basis around n (Duff et al. 2017)
+__device__ __forceinline__ void onb(V3 n, V3& t, V3& b) {
+  const float sign = copysignf(1.0f, n.z);
+  const float a = -1.0f / (sign + n.z);
+  const float bb = n.x * n.y * a;
+  t = v3(1.0f + sign * n.x * n.x * a, sign * bb, -sign * n.x);
+  b = v3(bb, sign + n.y * n.y * a, -n.y);
+}
+
+__device__ __forceinline__ void shade_full(const DevScene& sc, const DevQueues& q, const FrameConst& f, int cur, int i,
+                                           uint32_t path_length, Emit& e) {
+  const float4 o4 = q.org_q(cur)[i], d4 = q.dir_q(cur)[i], t4 = q.thr_q(cur)[i];
+  const int2 h = q.hit[i];
+  const int pix = __float_as_int(o4.w);
+  const V3 dir = v3(d4);
+  V3 T = v3(t4);
+  const float last_pdf = t4.w;
+  const int flags = __float_as_int(d4.w);
+  const float t = __int_as_float(h.y);
+  if (!(t < kMaxDistance)) {
+    if (f.sky && sc.sky_tex >= 0) {
+      const float u = 1.0f + (xatan2(dir.x, -dir.z) * kOneOverPi) * 0.5f;
+      const float v = 1.0f - xacos(fminf(fmaxf(dir.y, -1.0f), 1.0f)) * kOneOverPi;
+      accum_add(q.accum, pix, T * v3(tex_color(sc, sc.sky_tex, u, v)));
+    }
+    return;
+  }
+  const int prim = h.x;
+  const uint4 ti = __ldg(sc.idx + prim);
+  const V3 p0 = v3(__ldg(sc.verts + ti.x)), p1 = v3(__ldg(sc.verts + ti.y)), p2 = v3(__ldg(sc.verts + ti.z));
+  const V3 p = v3(o4) + dir * t;
+  V3 Ngf = cross(p1 - p0, p2 - p0);
+  const float area2 = sqrtf(dot(Ngf, Ngf));
+  Ngf = Ngf * (1.0f / area2);
+  // barycentrics of the hit point
+  const float b1 = dot(Ngf, cross(p2 - p, p0 - p)) / area2, b2 = dot(Ngf, cross(p0 - p, p1 - p)) / area2;
+  const float b0 = 1.0f - b1 - b2;
+  V3 Ns = v3(__ldg(sc.normals + ti.x)) * b0 + v3(__ldg(sc.normals + ti.y)) * b1 + v3(__ldg(sc.normals + ti.z)) * b2;
+  const float nl = dot(Ns, Ns);
+  Ns = nl > 0.0f ? Ns * (1.0f / sqrtf(nl)) : Ngf;
+  const float2 uv0 = __ldg(sc.uvs + ti.x), uv1 = __ldg(sc.uvs + ti.y), uv2 = __ldg(sc.uvs + ti.z);
+  const float tu = uv0.x * b0 + uv1.x * b1 + uv2.x * b2, tv = uv0.y * b0 + uv1.y * b1 + uv2.y * b2;
+  const DevMaterial* mp = sc.mats + ti.w;
+  const float4 alb = __ldg(&mp->albedo_ior);
+  const int4 mtex = __ldg(&mp->tex);
+  const float4 tr = __ldg(&mp->type_rough);
+  const int mtype = __float_as_int(tr.x);
+  if (mtex.y >= 0) Ns = normalize(sample_to_world(tex_normal(sc, mtex.y, tu, tv), Ns));
+  if (mtype == full::kLight) {
+    if (!f.indirect) return;
+    // emitters radiate on the side their centre normal faces (as the reference's NEE assumes)
+    const V3 cn = normalize(v3(__ldg(sc.cnormals + prim)));
+    const float cos_l = -dot(cn, dir);
+    if (cos_l <= 0.0f) return;
+    float w = 1.0f;
+    if ((flags & kFlagMis) && sc.light_count > 0) {
+      const float light_pdf = (t * t) / (cos_l * 0.5f * area2 * (float)sc.light_count);
+      w = (last_pdf * last_pdf) / (last_pdf * last_pdf + light_pdf * light_pdf);
+    }
+    accum_add(q.accum, pix, vmax0(T * v3(alb) * w));
+    return;
+  }
+  const bool dielectric = full::is_dielectric(mtype);
+  const bool front = dot(dir, Ngf) < 0.0f;
+  const V3 Ng = front ? Ngf : -Ngf;  // faces the incoming ray
+  // shading frame: towards the incoming ray for reflectors, outward for dielectrics
+  V3 N = dielectric ? (dot(Ns, Ngf) < 0.0f ? -Ns : Ns) : (dot(Ns, Ng) < 0.0f ? -Ns : Ns);
+  V3 Tt, Bt;
+  onb(N, Tt, Bt);
+  const V3 wo = -dir;
+  const V3 wo_l = v3(dot(wo, Tt), dot(wo, Bt), dot(wo, N));
+  V3 color = v3(alb);
+  if (mtex.x >= 0) color = v3(tex_color(sc, mtex.x, tu, tv));
+  uint32_t seed = wang_hash((uint32_t)pix * 16789u + f.frame * 1791u + path_length * 720898027u);
+  const float u1 = rnd_float(seed), u2 = rnd_float(seed), u3 = rnd_float(seed);
+  const float rough = tr.y;
+  const float alpha = full::roughness_to_alpha(rough);
+  bool nee = false;
+  if (full::has_nee(mtype) && f.shadow && sc.light_count > 0 && wo_l.z > 0.0f) {
+    nee = true;
+    const int light = min(rnd_int_max(seed, (int)sc.light_count - 1), (int)sc.light_count - 1);
+    const uint32_t lprim = __ldg(sc.lights + light);
+    const uint4 li = __ldg(sc.idx + lprim);
+    const V3 l0 = v3(__ldg(sc.verts + li.x)), l1 = v3(__ldg(sc.verts + li.y)), l2 = v3(__ldg(sc.verts + li.z));
+    float q1 = rnd_float(seed), q2 = rnd_float(seed);
+    if (q1 + q2 > 1.0f) q1 = 1.0f - q1, q2 = 1.0f - q2;
+    const V3 lp = l0 * (1.0f - q1 - q2) + l1 * q1 + l2 * q2;
+    V3 L = lp - p;
+    const float sq = dot(L, L);
+    const float dist = sqrtf(sq);
+    L = L * (1.0f / dist);
+    const V3 lcn = normalize(v3(__ldg(sc.cnormals + lprim)));
+    const float cos_l = -dot(lcn, L);
+    const V3 lc = cross(l1 - l0, l2 - l0);
+    const float larea = 0.5f * sqrtf(dot(lc, lc));
+    if (cos_l > 0.0f && dot(Ng, L) > 0.0f && larea > 0.0f) {
+      const V3 wi_l = v3(dot(L, Tt), dot(L, Bt), dot(L, N));
+      float pb;
+      const V3 fv = full::eval(mtype, color, alpha, wo_l, wi_l, pb);
+      if (pb > 0.0f) {
+        const float light_pdf = sq / (cos_l * larea * (float)sc.light_count);
+        const float w = (light_pdf * light_pdf) / (light_pdf * light_pdf + pb * pb);
+        const V3 le = v3(__ldg(&sc.mats[__ldg(&sc.idx[lprim].w)].albedo_ior));
+        const V3 contrib = T * fv * le * (wi_l.z * w / light_pdf);
+        if (contrib.x > 0.0f || contrib.y > 0.0f || contrib.z > 0.0f) {
+          e.shadow = true;
+          e.so = f4(p + Ng * f.normal_eps, __int_as_float(pix));
+          // stop short of the light by a relative margin as well: at distances of tens of
+          // units the light's own FP32 hit distance can fall inside an absolute 2 * dist_eps
+          e.sd = f4(L, dist * (1.0f - kShadowRel) - 2.0f * f.dist_eps);
+          e.sc = f4(contrib, 0.0f);
+        }
+      }
+    }
+  }
+  const full::Sample s = full::sample(mtype, color, rough, alb.w, wo_l, u1, u2, u3);
+  if (!s.valid) return;
+  const V3 wi = Tt * s.wi.x + Bt * s.wi.y + N * s.wi.z;
+  T = T * s.weight;
+  if (isnan(T.x) || isnan(T.y) || isnan(T.z) || (T.x <= 0.0f && T.y <= 0.0f && T.z <= 0.0f)) return;
+  const float side = dot(wi, Ngf) > 0.0f ? 1.0f : -1.0f;
+  e.cont = true;
+  e.no = f4(p + Ngf * (side * f.normal_eps), __int_as_float(pix));
+  e.nd = f4(wi, __int_as_float((nee && !s.delta) ? kFlagMis : 0));
+  e.nt = f4(T, s.pdf);
+}
+
 // Warp-aggregated append: one atomicAdd per warp, lanes take popc-prefix slots.
 __device__ __forceinline__ int warp_append(bool want, int* counter) {
   const unsigned m = __ballot_sync(0xffffffffu, want);
@@ -290,7 +436,12 @@ __global__ void __launch_bounds__(kBlock) k_shade(DevScene sc, DevQueues q, Fram
     Emit e;
     e.cont = false;
     e.shadow = false;
-    if (i < n) shade_compat(sc, q, f, cur, i, path_length, e);
+    if (i < n) {
+      if (f.shading_mode == CT_MODE_FULL)
+        shade_full(sc, q, f, cur, i, path_length, e);
+      else
+        shade_compat(sc, q, f, cur, i, path_length, e);
+    }
     const int si = warp_append(e.shadow, &q.counts[2]);
     if (si >= 0) {
       q.sorg[si] = e.so;

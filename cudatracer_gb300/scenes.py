@@ -214,6 +214,24 @@ def terrain_scene(grid: int = 1024, spheres: int = 200, seed: int = 7, extent: f
     return sc, cam
 
 
+def material_zoo_scene(grid: int = 48, spheres: int = 27, seed: int = 11) -> tuple[Scene, dict]:
+    """A small terrain scene whose spheres cycle through every non-emitter
+    material type (Lambertian, specular, Fresnel, Beckmann, GGX, Trowbridge and
+    the three rough dielectrics), for checking the full-material mode."""
+    sc, cam = terrain_scene(grid=grid, spheres=spheres, seed=seed, extent=60.0, sky_size=(256, 128))
+    kinds = [MAT_LAMBERTIAN, MAT_SPECULAR, MAT_FRESNEL, MAT_BECKMANN, MAT_GGX, MAT_TROWBRIDGE,
+             MAT_FRESNEL_BECKMANN, MAT_FRESNEL_GGX, MAT_FRESNEL_TROWBRIDGE]
+    rng = np.random.default_rng(seed + 1)
+    for k in range(spheres):
+        m = sc.materials[1 + k]
+        m["type"] = kinds[k % len(kinds)]
+        m["roughness"] = float(rng.uniform(0.15, 0.6))
+        m["refract_idx"] = 1.5
+        m["albedo"] = tuple(float(c) for c in rng.uniform(0.4, 0.95, 3))
+    cam = dict(position=(0.0, 14.0, 34.0), forward=_unit((0.0, -0.35, -1.0)), up=(0.0, 1.0, 0.0), fov=60.0)
+    return sc, cam
+
+
 def _unit(v):
     v = np.asarray(v, np.float64)
     v = v / np.linalg.norm(v)

@@ -53,9 +53,83 @@ def build_oracle(force: bool = False) -> str:
     return ORACLE_LIB
 
 
+FP64_SRC = os.path.join(HERE, "ct_fp64.cpp")
+FP64_LIB = os.path.join(HERE, "libfp64.so")
+
+
+def build_fp64(force: bool = False) -> str:
+    fresh = (os.path.exists(FP64_LIB) and os.path.getmtime(FP64_LIB) >= os.path.getmtime(FP64_SRC)
+             and _elf_machine(FP64_LIB) == _native_machine())
+    if fresh and not force:
+        return FP64_LIB
+    tmp = FP64_LIB + ".tmp"
+    subprocess.run(["g++", "-std=c++17", "-O2", "-fPIC", "-shared", "-pthread", "-ffp-contract=off",
+                    "-fno-fast-math", "-o", tmp, FP64_SRC], check=True)
+    os.replace(tmp, FP64_LIB)
+    return FP64_LIB
+
+
+_fp64 = None
+
+
+def fp64() -> ctypes.CDLL:
+    global _fp64
+    if _fp64 is None:
+        build_fp64()
+        L = ctypes.CDLL(FP64_LIB)
+        L.fp64_render.argtypes = [P, P, P, P, P, ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_int,
+                                  ctypes.c_uint64, P, P, ctypes.c_int]
+        L.fp64_microfacet.argtypes = [ctypes.c_int, ctypes.c_double, P, ctypes.c_double, ctypes.c_double, P, P, P]
+        L.fp64_roughness_to_alpha.restype = ctypes.c_double
+        L.fp64_roughness_to_alpha.argtypes = [ctypes.c_double]
+        _fp64 = L
+    return _fp64
+
+
+def render_fp64(arrays: dict, materials: np.ndarray, quad, prims, camera: dict, width: int, height: int, spp: int,
+                depth: int, textures=(), sky_tex: int = -1, sky: bool = True, shadow: bool = True,
+                indirect: bool = True, eps=(1e-5, 1e-5, 1e-3), seed: int = 1, nthreads: int = 8):
+    """FP64 Monte Carlo estimate of the full-material image: per-pixel (mean, standard error), (h*w, 3) each."""
+    L = fp64()
+    a = {k: np.ascontiguousarray(v) for k, v in arrays.items()}
+    texels = dims = offs = None
+    if textures:
+        flat, dl, ol, o = [], [], [], 0
+        for tx in textures:
+            tx = np.ascontiguousarray(tx, np.float32)
+            h, w = tx.shape[:2]
+            flat.append(tx.reshape(-1, 4))
+            dl += [w, h]
+            ol.append(o)
+            o += w * h
+        texels = np.ascontiguousarray(np.concatenate(flat))
+        dims = np.asarray(dl, np.uint32)
+        offs = np.asarray(ol, np.uint32)
+    li = a.get("light_indices")
+    mats = np.ascontiguousarray(materials)
+    q = np.ascontiguousarray(quad)
+    pr = np.ascontiguousarray(prims, np.uint32)
+    d = OrSceneDesc(
+        _p(a["vertices"]), _p(a["normals"]), _p(a["center_normals"]), _p(a["texcoords"]), _p(a["indices"]),
+        _p(a["material_idxs"]), _p(mats), _p(li) if li is not None and li.size else None,
+        0 if li is None else int(li.size), _p(texels), _p(dims), _p(offs), sky_tex,
+        int(sky and sky_tex >= 0), int(shadow), int(indirect), eps[0], eps[1], eps[2], _p(q), _p(pr))
+    hor, ver = camera_basis(camera["forward"], camera["up"], camera["fov"], width, height)
+    pos = np.asarray(camera["position"], np.float32)
+    fw = np.asarray(camera["forward"], np.float32)
+    s = np.zeros((width * height, 3), np.float64)
+    s2 = np.zeros((width * height, 3), np.float64)
+    L.fp64_render(ctypes.byref(d), _p(pos), _p(fw), _p(hor), _p(ver), width, height, spp, depth, seed, _p(s), _p(s2),
+                  nthreads)
+    mean = s / spp
+    var = np.maximum(s2 / spp - mean * mean, 0.0)
+    return mean, np.sqrt(var / spp)
+
+
 def build(force: bool = False) -> None:
     """Compile the oracle restatement and, where its sources exist, the reference."""
     build_oracle(force)
+    build_fp64(force)
     try:
         from . import ref_build  # type: ignore
     except ImportError:

@@ -169,6 +169,33 @@ def test_traversal_matches_reference(orc, c1):
     assert (hb != g["hit"]).sum() <= 8
 
 
+def test_fp64_microfacet_matches_reference(orc, kat):
+    """The FP64 oracle's microfacet sampling and Smith G1 against the reference's
+    Material::sample / Material::evaluate (src/Core/Material.cuh:175-215) for
+    isotropic alphas: visible-normal sampling for Beckmann/GGX, full-distribution
+    sampling for Trowbridge-Reitz, and G1(Lambda(wo)) as the visible-mode pdf."""
+    L = orc.fp64()
+    tv, al, inp, out, pdf = (kat["mf_type_vis"], kat["mf_alpha"], kat["mf_in"], kat["mf_out"], kat["mf_pdf"])
+    m = np.zeros(3, np.float64)
+    g1 = np.zeros(1, np.float64)
+    checked_m = checked_g = 0
+    for (typ, vis), (ax, ay), row, ref_m, ref_pdf in zip(tv, al, inp, out, pdf):
+        if ax != ay:
+            continue
+        wi = np.ascontiguousarray(row[0:3], np.float32)
+        wo = np.ascontiguousarray(row[5:8], np.float32)
+        L.fp64_microfacet(int(typ), float(ax), _p(wi), float(row[3]), float(row[4]), _p(wo), _p(m), _p(g1))
+        if vis == 1 or typ in (6, 9):
+            assert np.allclose(m, ref_m, rtol=2e-3, atol=2e-3), (typ, vis, m, ref_m)
+            checked_m += 1
+        if vis == 1:
+            assert abs(g1[0] - ref_pdf) <= 1e-5 * max(1.0, abs(ref_pdf)), (typ, g1[0], ref_pdf)
+            checked_g += 1
+    assert checked_m >= 100 and checked_g >= 60
+    for r, a in zip(kat["r2a_in"], kat["r2a_out"]):
+        assert abs(L.fp64_roughness_to_alpha(float(r)) - a) <= 1e-5
+
+
 @pytest.mark.parametrize("w,h", [(16, 12)])
 def test_frame_oracle_runs_and_is_deterministic(orc, w, h):
     from cudatracer_gb300 import scenes
