@@ -93,6 +93,11 @@ ct_status upload(ct_ctx* ctx, Allocs& a, T** dst, const void* src, size_t bytes)
     cudaError_t e = cudaMemset(p, 0, bytes);
     if (e != cudaSuccess) return cuda_fail(ctx, e, "cudaMemset");
   }
+  // Both calls can return before the device has finished, and they are ordered
+  // only on the legacy stream: wait, so that work the caller (or a frame slot)
+  // issues on a non-blocking stream never sees the buffer before it is filled.
+  cudaError_t e = cudaStreamSynchronize(0);
+  if (e != cudaSuccess) return cuda_fail(ctx, e, "cudaStreamSynchronize");
   *dst = (T*)p;
   return CT_OK;
 }
@@ -124,6 +129,14 @@ struct ct_render {
   int32_t w = 0, h = 0;
   DevQueues q{};
   Allocs allocs;
+  // overlapped fast-math frames: two private queue sets + accumulation buffers
+  struct Slot {
+    DevQueues q{};
+    cudaStream_t stream = nullptr;
+    cudaEvent_t free_ev = nullptr;  // recorded after the slot's buffer was folded
+    cudaEvent_t done_ev = nullptr;  // recorded after the slot's frame finished
+  } slots[2];
+  int next_slot = 0;
   // stage profiling: event pairs per stage, recycled through a pool
   bool profile = false;
   std::vector<std::pair<cudaEvent_t, cudaEvent_t>> marks[4];
@@ -255,7 +268,8 @@ ct_status ct_ctx_create(int32_t device, ct_ctx** out) {
   if (prop.major * 10 + prop.minor < 100) return CT_ERR_NO_DEVICE;  // built for sm_103a only
   auto* c = new ct_ctx();
   c->device = device;
-  if (cudaMalloc(&c->d_error, 256) != cudaSuccess || cudaMemset(c->d_error, 0, 256) != cudaSuccess) {
+  if (cudaMalloc(&c->d_error, 256) != cudaSuccess || cudaMemset(c->d_error, 0, 256) != cudaSuccess ||
+      cudaStreamSynchronize(0) != cudaSuccess) {
     delete c;
     return CT_ERR_OUT_OF_MEMORY;
   }
@@ -296,6 +310,7 @@ ct_status ct_ctx_check(ct_ctx* ctx, void* stream) {
   CT_CUDA(ctx, cudaMemcpy(&err, ctx->d_error, 4, cudaMemcpyDeviceToHost));
   if (err) {
     CT_CUDA(ctx, cudaMemset(ctx->d_error, 0, 4));
+    CT_CUDA(ctx, cudaStreamSynchronize(0));
     if (err & kErrStackOverflow)
       return fail(ctx, CT_ERR_STACK_OVERFLOW, "a traversal stack limit was reached; affected rays report no hit");
     return fail(ctx, CT_ERR_CUDA, "device error word " + std::to_string(err));
@@ -431,6 +446,7 @@ ct_status ct_scene_set_material(ct_ctx* ctx, ct_scene* scene, uint32_t index, co
   scene->mats[index] = *m;
   const DevMaterial dm = to_dev(*m);
   CT_CUDA(ctx, cudaMemcpy(scene->d_mats + index, &dm, sizeof(dm), cudaMemcpyHostToDevice));
+  CT_CUDA(ctx, cudaStreamSynchronize(0));  // the copy may still be in flight when cudaMemcpy returns
   return CT_OK;
 }
 
@@ -604,6 +620,21 @@ ct_status ct_trace_any(ct_ctx* ctx, const ct_bvh* bvh, const float* org, const f
   return CT_OK;
 }
 
+static ct_status alloc_queues(ct_ctx* ctx, Allocs& a, size_t n, DevQueues& q) {
+  ct_status s;
+  q.capacity = (int32_t)n;
+  auto alloc4 = [&](float4** p) { return upload(ctx, a, p, nullptr, n * sizeof(float4)); };
+  if ((s = alloc4(&q.org[0])) != CT_OK || (s = alloc4(&q.org[1])) != CT_OK || (s = alloc4(&q.dir[0])) != CT_OK ||
+      (s = alloc4(&q.dir[1])) != CT_OK || (s = alloc4(&q.thr[0])) != CT_OK || (s = alloc4(&q.thr[1])) != CT_OK ||
+      (s = alloc4(&q.sorg)) != CT_OK || (s = alloc4(&q.sdir)) != CT_OK || (s = alloc4(&q.scol)) != CT_OK ||
+      (s = alloc4(&q.accum)) != CT_OK || (s = upload(ctx, a, &q.hit, nullptr, n * sizeof(int2))) != CT_OK ||
+      (s = upload(ctx, a, &q.counts, nullptr, 16 * sizeof(int32_t))) != CT_OK ||
+      (s = upload(ctx, a, &q.stats, nullptr, 8 * sizeof(unsigned long long))) != CT_OK)
+    return s;
+  q.error = ctx->d_error;
+  return CT_OK;
+}
+
 ct_status ct_render_create(ct_ctx* ctx, int32_t width, int32_t height, ct_render** out) {
   if (!ctx || !out) return fail(ctx, CT_ERR_INVALID_ARGUMENT, "null argument");
   *out = nullptr;
@@ -614,21 +645,11 @@ ct_status ct_render_create(ct_ctx* ctx, int32_t width, int32_t height, ct_render
   auto* r = new ct_render();
   r->w = width;
   r->h = height;
-  const size_t n = (size_t)width * height;
-  DevQueues& q = r->q;
-  q.capacity = (int32_t)n;
-  auto alloc4 = [&](float4** p) { return upload(ctx, r->allocs, p, nullptr, n * sizeof(float4)); };
-  if ((s = alloc4(&q.org[0])) != CT_OK || (s = alloc4(&q.org[1])) != CT_OK || (s = alloc4(&q.dir[0])) != CT_OK ||
-      (s = alloc4(&q.dir[1])) != CT_OK || (s = alloc4(&q.thr[0])) != CT_OK || (s = alloc4(&q.thr[1])) != CT_OK ||
-      (s = alloc4(&q.sorg)) != CT_OK || (s = alloc4(&q.sdir)) != CT_OK || (s = alloc4(&q.scol)) != CT_OK ||
-      (s = alloc4(&q.accum)) != CT_OK || (s = upload(ctx, r->allocs, &q.hit, nullptr, n * sizeof(int2))) != CT_OK ||
-      (s = upload(ctx, r->allocs, &q.counts, nullptr, 16 * sizeof(int32_t))) != CT_OK ||
-      (s = upload(ctx, r->allocs, &q.stats, nullptr, 8 * sizeof(unsigned long long))) != CT_OK) {
+  if ((s = alloc_queues(ctx, r->allocs, (size_t)width * height, r->q)) != CT_OK) {
     free_all(ctx, r->allocs);
     delete r;
     return s;
   }
-  q.error = ctx->d_error;
   *out = r;
   return CT_OK;
 }
@@ -636,8 +657,45 @@ ct_status ct_render_create(ct_ctx* ctx, int32_t width, int32_t height, ct_render
 ct_status ct_render_destroy(ct_ctx* ctx, ct_render* r) {
   if (!ctx || !r) return CT_ERR_INVALID_ARGUMENT;
   set_device(ctx);
+  for (auto& sl : r->slots) {
+    if (sl.stream) {
+      cudaStreamSynchronize(sl.stream);
+      cudaStreamDestroy(sl.stream);
+      cudaEventDestroy(sl.free_ev);
+      cudaEventDestroy(sl.done_ev);
+    }
+  }
   free_all(ctx, r->allocs);
   delete r;
+  return CT_OK;
+}
+
+// Frame slots for overlapped fast-math frames, created on first use.
+static ct_status ensure_slots(ct_ctx* ctx, ct_render* r) {
+  if (r->slots[0].stream) return CT_OK;
+  const size_t n = (size_t)r->w * r->h;
+  for (auto& sl : r->slots) {
+    ct_status s = alloc_queues(ctx, r->allocs, n, sl.q);
+    if (s != CT_OK) return s;
+    CT_CUDA(ctx, cudaStreamCreateWithFlags(&sl.stream, cudaStreamNonBlocking));
+    CT_CUDA(ctx, cudaEventCreateWithFlags(&sl.free_ev, cudaEventDisableTiming));
+    CT_CUDA(ctx, cudaEventCreateWithFlags(&sl.done_ev, cudaEventDisableTiming));
+  }
+  return CT_OK;
+}
+
+// Issue one frame's stages on stream st into queues q.
+static ct_status emit_frame(ct_ctx* ctx, ct_render* r, const DevQueues& q, const ct_scene* scene, const ct_bvh* bvh,
+                            const FrameConst& f, const ct_render_params* p, cudaStream_t st) {
+  const bool fast = !p->exact_math;
+  CT_CUDA(ctx, staged(r, 0, st, [&] { return launch_raygen(q, f, p->exact_math, st); }));
+  for (int pass = 0; pass < p->max_depth; pass++) {
+    const int cur = pass & 1;
+    const int path_length = pass == 0 ? 0 : pass + 1;  // Kernel.cu:306, 330
+    CT_CUDA(ctx, staged(r, 1, st, [&] { return launch_extend(bvh->dev, q, cur, p->tri_eps, fast, st); }));
+    CT_CUDA(ctx, staged(r, 2, st, [&] { return launch_shade(scene->dev, q, f, cur, path_length, p->exact_math, st); }));
+    if (p->shadow) CT_CUDA(ctx, staged(r, 3, st, [&] { return launch_connect(bvh->dev, q, p->tri_eps, fast, st); }));
+  }
   return CT_OK;
 }
 
@@ -704,16 +762,20 @@ ct_status ct_render_accumulate(ct_ctx* ctx, const ct_scene* scene, const ct_bvh*
   f.indirect = p->indirect;
   f.sky = p->sky;
   f.shading_mode = p->shading_mode;
-  CT_CUDA(ctx, staged(r, 0, st, [&] { return launch_raygen(r->q, f, p->exact_math, st); }));
-  for (int pass = 0; pass < p->max_depth; pass++) {
-    const int cur = pass & 1;
-    const int path_length = pass == 0 ? 0 : pass + 1;  // Kernel.cu:306, 330
-    CT_CUDA(ctx, staged(r, 1, st, [&] { return launch_extend(bvh->dev, r->q, cur, p->tri_eps, !p->exact_math, st); }));
-    CT_CUDA(ctx, staged(r, 2, st, [&] {
-              return launch_shade(scene->dev, r->q, f, cur, path_length, p->exact_math, st);
-            }));
-    if (p->shadow) CT_CUDA(ctx, staged(r, 3, st, [&] { return launch_connect(bvh->dev, r->q, p->tri_eps, !p->exact_math, st); }));
-  }
+  if (p->exact_math) return emit_frame(ctx, r, r->q, scene, bvh, f, p, st);  // strictly sequential accumulation
+  // Fast-math frames overlap: the frame renders into one of two private slots
+  // (queues + accumulation) on the slot's own stream, so its first passes can
+  // run while the previous frame's last bounces are still draining; the slot
+  // is then added to the job's buffer on the caller's stream, in frame order.
+  if ((s = ensure_slots(ctx, r)) != CT_OK) return s;
+  ct_render::Slot& sl = r->slots[r->next_slot];
+  r->next_slot ^= 1;
+  CT_CUDA(ctx, cudaStreamWaitEvent(sl.stream, sl.free_ev, 0));
+  if ((s = emit_frame(ctx, r, sl.q, scene, bvh, f, p, sl.stream)) != CT_OK) return s;
+  CT_CUDA(ctx, cudaEventRecord(sl.done_ev, sl.stream));
+  CT_CUDA(ctx, cudaStreamWaitEvent(st, sl.done_ev, 0));
+  CT_CUDA(ctx, launch_fold(r->q.accum, sl.q.accum, r->w * r->h, st));
+  CT_CUDA(ctx, cudaEventRecord(sl.free_ev, st));
   return CT_OK;
 }
 
@@ -790,14 +852,21 @@ ct_status ct_render_stats(ct_ctx* ctx, ct_render* r, ct_frame_stats* stats, int3
   if (!ctx || !r || !stats) return fail(ctx, CT_ERR_INVALID_ARGUMENT, "null argument");
   ct_status s = set_device(ctx);
   if (s != CT_OK) return s;
-  unsigned long long h[4] = {0, 0, 0, 0};
+  unsigned long long tot[4] = {0, 0, 0, 0};
   CT_CUDA(ctx, cudaStreamSynchronize((cudaStream_t)stream));
-  CT_CUDA(ctx, cudaMemcpy(h, r->q.stats, sizeof(h), cudaMemcpyDeviceToHost));
-  stats->extension_rays = h[0];
-  stats->shadow_rays = h[1];
-  stats->samples = h[2];
-  stats->frames = (uint32_t)h[3];
-  if (reset) CT_CUDA(ctx, cudaMemset(r->q.stats, 0, sizeof(h)));
+  const DevQueues* qs[3] = {&r->q, &r->slots[0].q, &r->slots[1].q};
+  for (const DevQueues* q : qs) {
+    if (!q->stats) continue;
+    unsigned long long h[4] = {0, 0, 0, 0};
+    CT_CUDA(ctx, cudaMemcpy(h, q->stats, sizeof(h), cudaMemcpyDeviceToHost));
+    for (int k = 0; k < 4; k++) tot[k] += h[k];
+    if (reset) CT_CUDA(ctx, cudaMemset(q->stats, 0, sizeof(h)));
+  }
+  if (reset) CT_CUDA(ctx, cudaStreamSynchronize(0));
+  stats->extension_rays = tot[0];
+  stats->shadow_rays = tot[1];
+  stats->samples = tot[2];
+  stats->frames = (uint32_t)tot[3];
   return CT_OK;
 }
 

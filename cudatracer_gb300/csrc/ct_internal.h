@@ -119,6 +119,8 @@ cudaError_t launch_raygen(const DevQueues& q, const FrameConst& f, int exact, cu
 cudaError_t launch_shade(const DevScene& sc, const DevQueues& q, const FrameConst& f, int queue, int path_length,
                          int exact, cudaStream_t s);
 cudaError_t launch_present(const float4* accum, float4* out, int n, float samples, cudaStream_t s);
+// accum[i] += frame[i]; frame[i] = 0 (folds an overlapped frame's private buffer)
+cudaError_t launch_fold(float4* accum, float4* frame, int n, cudaStream_t s);
 
 // allocation-free frame (noalloc.cu): queues in a static device array
 uint32_t noalloc_max_pixels();

@@ -30,7 +30,26 @@ __global__ void k_present(const float4* __restrict__ accum, float4* __restrict__
     out[i] = make_float4(powf(a.x / samples, e), powf(a.y / samples, e), powf(a.z / samples, e), 1.0f);
   }
 }
+__global__ void k_fold(float4* __restrict__ accum, float4* __restrict__ frame, int n) {
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+    const float4 f = frame[i];
+    float4 a = accum[i];
+    a.x += f.x;
+    a.y += f.y;
+    a.z += f.z;
+    a.w += f.w;
+    accum[i] = a;
+    frame[i] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+  }
+}
 }  // namespace
+
+cudaError_t launch_fold(float4* accum, float4* frame, int n, cudaStream_t s) {
+  if (n <= 0) return cudaSuccess;
+  const int grid = (n + 255) / 256 < 8 * sm_count() ? (n + 255) / 256 : 8 * sm_count();
+  k_fold<<<grid, 256, 0, s>>>(accum, frame, n);
+  return cudaGetLastError();
+}
 
 cudaError_t launch_raygen(const DevQueues& q, const FrameConst& f, int exact_math, cudaStream_t s) {
   const int npix = f.width * f.height;
