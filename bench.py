@@ -181,20 +181,22 @@ def cpu_baseline_port(arrays, textures, materials_packed, quad, prims, cam, seco
 
     threads = os.cpu_count() or 1
     acc = np.zeros((W * H, 4), np.float32)
-    rows, samples, t0 = 0, 0, time.perf_counter()
-    row_step = 8
+    rows, samples, frame, t0 = 0, 0, 0, time.perf_counter()
+    row_step = 30
     r = 0
-    while time.perf_counter() - t0 < seconds and rows < H:
-        oracle.render_frames(arrays, materials_packed, quad, prims, cam, W, H, [0], DEPTH, accum=acc,
+    while time.perf_counter() - t0 < seconds:
+        oracle.render_frames(arrays, materials_packed, quad, prims, cam, W, H, [2 * frame], DEPTH, accum=acc,
                              exact_math=False, textures=textures, sky_tex=0,
                              pixels=(r * W, (r + row_step) * W), nthreads=threads)
         samples += row_step * W
         rows += row_step
-        r = (r + 97 * row_step) % (H - row_step)
+        r += row_step
+        if r + row_step > H:
+            r, frame = 0, frame + 1
     dt = time.perf_counter() - t0
     return {"value": samples / dt / 1e6, "unit": UNIT, "cores": threads, "kind": "port",
-            "sample": f"{samples} paths ({rows} rows of frame 0, depth {DEPTH}) in {dt:.1f} s; oracle restatement "
-                      f"of the reference shade/extend/connect kernels on the host"}
+            "sample": f"{samples} paths ({rows} rows, {frame} whole frames, depth {DEPTH}) in {dt:.1f} s; oracle "
+                      f"restatement of the reference shade/extend/connect kernels on the host"}
 
 
 def reference_traversal_baseline() -> dict | None:
@@ -390,6 +392,30 @@ def run_ours(args, world, rank, local):
             ref_tr = reference_traversal_baseline()
             if ref_tr:
                 cpu_base["reference_host_traversal"] = ref_tr
+    # ---- the same workload with every material shaded (CT_SHADE_FULL), for context
+    from cudatracer_gb300 import _lib
+
+    pf = api.Params(W, H, camera=camera, max_depth=DEPTH, exact_math=False)
+    pf.reset(job, stream)
+    full_frames = max(8, args.steps // 4)
+
+    def full_frame():
+        c = pf.to_ct()
+        c.shading_mode = _lib.CT_SHADE_FULL
+        job.accumulate(sc, bvh, camera, c, stream)
+        pf.samples += 2
+
+    for _ in range(args.warmup):
+        full_frame()
+    stream.synchronize()
+    e0.record(stream)
+    for _ in range(full_frames):
+        full_frame()
+    e1.record(stream)
+    stream.synchronize()
+    full_ms = e0.elapsed_time(e1) / full_frames
+    full = {"msamples_per_s": W * H / full_ms / 1e3, "ms_per_frame": full_ms, "frames": full_frames,
+            "shading": "full materials (Lambert, mirror, dielectric IOR 1.5, GGX) with MIS"}
     c1 = gpu_closest_hit_c1(ctx) if rank == 0 else None
     launches = sum(v["launches"] for v in prof.values())
     line = {
@@ -405,7 +431,7 @@ def run_ours(args, world, rank, local):
         "stage_ms": {k: v["ms"] for k, v in prof.items()},
         "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": h2d_bytes, "d2h_bytes_per_step": d2h_bytes},
         "gpu_launches": launches,
-        "roofline": roofline, "cpu_baseline": cpu_base, "closest_hit": c1, "clocks": clk,
+        "roofline": roofline, "cpu_baseline": cpu_base, "closest_hit": c1, "full_materials": full, "clocks": clk,
         "setup": {"scene_and_bvh_s": setup_s, "bvh_build_ms": info["build_ms"], "bvh_collapse_ms": info["collapse_ms"],
                   "quad_nodes": info["quad_node_count"]},
     }

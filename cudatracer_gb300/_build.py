@@ -25,6 +25,7 @@ LIB = os.path.join(PKG, "libcudatracer.so")
 SOURCES = {
     "api.cpp": [],
     "bvh_build.cpp": [],
+    "mesh_io.cpp": [],
     "k_trace.cu": [],
     "k_shade_exact.cu": ["-fmad=false"],
     "k_shade_fast.cu": [],

@@ -18,6 +18,7 @@ STATUS_NAMES = {
     0: "CT_OK", 1: "CT_ERR_INVALID_ARGUMENT", 2: "CT_ERR_OUT_OF_MEMORY", 3: "CT_ERR_CUDA",
     4: "CT_ERR_UNSUPPORTED", 5: "CT_ERR_TIMEOUT", 6: "CT_ERR_STACK_OVERFLOW", 7: "CT_ERR_NO_DEVICE",
 }
+globals().update({name: code for code, name in STATUS_NAMES.items()})
 CT_BVH_BINARY, CT_BVH_QUAD = 0, 1
 CT_SHADE_COMPAT, CT_SHADE_FULL = 0, 1
 
@@ -101,6 +102,13 @@ SIGNATURES = {
                                      POINTER(c_double), POINTER(c_double)]),
     "ct_host_bvh_export": (c_int32, [P, c_int32, P, P]),
     "ct_host_bvh_destroy": (c_int32, [P]),
+    "ct_mesh_load_obj": (c_int32, [c_char_p, c_int32, PP]),
+    "ct_mesh_info": (c_int32, [P, POINTER(c_uint32), POINTER(c_uint32), POINTER(c_uint32)]),
+    "ct_mesh_arrays": (c_int32, [P, P, P, P, P, P]),
+    "ct_mesh_material": (c_int32, [P, c_uint32, POINTER(ct_material), P, P, c_uint32]),
+    "ct_mesh_destroy": (c_int32, [P]),
+    "ct_image_load": (c_int32, [c_char_p, POINTER(c_uint32), POINTER(c_uint32), P]),
+    "ct_mesh_last_error": (c_char_p, []),
     "ct_trace_closest": (c_int32, [P, P, P, P, P, P, c_uint32, c_float, P]),
     "ct_trace_any": (c_int32, [P, P, P, P, P, c_uint32, c_float, P]),
     "ct_render_create": (c_int32, [P, c_int32, c_int32, PP]),

@@ -75,6 +75,63 @@ class Material:
         m.absorption[:] = [float(c) for c in self.absorption]
         return m
 
+    @staticmethod
+    def from_ct(m: _lib.ct_material) -> "Material":
+        return Material(tuple(float(c) for c in m.albedo), float(m.refract_idx), int(m.diffuse_tex),
+                        int(m.normal_tex), int(m.mask_tex), int(m.displace_tex), int(m.type), float(m.roughness),
+                        tuple(float(c) for c in m.absorption))
+
+
+def _mesh_check(status: int) -> None:
+    if status != _lib.CT_OK:
+        raw = _lib.load().ct_mesh_last_error()
+        raise _lib.CTError(status, raw.decode(errors="replace") if raw else "")
+
+
+def load_obj(path: str, normalize: bool = True) -> dict:
+    """Import a Wavefront OBJ (+ MTL) through libcudatracer (ct_mesh_load_obj):
+    what assimp hands processMesh in TriangleList::loadModel
+    (src/Core/TriangleList.cpp:63-91, 203-348). Returns float32/uint32 arrays
+    `vertices` (V,3), `normals` (V,3), `texcoords` (V,2), `indices` (T,3),
+    `material_idxs` (T,) into `materials`, and per material the `diffuse_maps`
+    and `normal_maps` paths ("" for none)."""
+    L = _lib.load()
+    h = ctypes.c_void_p()
+    _mesh_check(L.ct_mesh_load_obj(str(path).encode(), int(bool(normalize)), ctypes.byref(h)))
+    try:
+        nv, nt, nm = ctypes.c_uint32(), ctypes.c_uint32(), ctypes.c_uint32()
+        _mesh_check(L.ct_mesh_info(h, ctypes.byref(nv), ctypes.byref(nt), ctypes.byref(nm)))
+        out = {"vertices": np.empty((nv.value, 3), np.float32), "normals": np.empty((nv.value, 3), np.float32),
+               "texcoords": np.empty((nv.value, 2), np.float32), "indices": np.empty((nt.value, 3), np.uint32),
+               "material_idxs": np.empty(nt.value, np.uint32)}
+        _mesh_check(L.ct_mesh_arrays(h, *(ptr(out[k]) for k in ("vertices", "normals", "texcoords", "indices",
+                                                                 "material_idxs"))))
+        mats, dmaps, nmaps = [], [], []
+        cap = 4096
+        for i in range(nm.value):
+            m = _lib.ct_material()
+            dbuf, nbuf = ctypes.create_string_buffer(cap), ctypes.create_string_buffer(cap)
+            _mesh_check(L.ct_mesh_material(h, i, ctypes.byref(m), ctypes.addressof(dbuf), ctypes.addressof(nbuf),
+                                           cap))
+            mats.append(Material.from_ct(m))
+            dmaps.append(dbuf.value.decode())
+            nmaps.append(nbuf.value.decode())
+        out.update(materials=mats, diffuse_maps=dmaps, normal_maps=nmaps)
+        return out
+    finally:
+        L.ct_mesh_destroy(h)
+
+
+def load_image(path: str) -> np.ndarray:
+    """An 8-bit TGA as the reference's Surface stores it (src/Utils/Surface.cpp:71-97):
+    (height, width, 4) float32, channel/255, alpha 1, row 0 at the bottom."""
+    L = _lib.load()
+    w, h = ctypes.c_uint32(), ctypes.c_uint32()
+    _mesh_check(L.ct_image_load(str(path).encode(), ctypes.byref(w), ctypes.byref(h), None))
+    img = np.empty((h.value, w.value, 4), np.float32)
+    _mesh_check(L.ct_image_load(str(path).encode(), ctypes.byref(w), ctypes.byref(h), ptr(img)))
+    return img
+
 
 @dataclass
 class TriangleList:
@@ -94,6 +151,7 @@ class TriangleList:
     materials: list = field(default_factory=list)
     textures: list = field(default_factory=list)  # (h, w, 4) float32 arrays
     _arrays: dict = field(default_factory=dict)
+    _loaded_textures: dict = field(default_factory=dict)  # m_LoadedTextures: path -> index
 
     def __post_init__(self):
         # "Have at least 1 material" (TriangleList.cpp:13-15)
@@ -163,6 +221,65 @@ class TriangleList:
     def arrays(self) -> dict:
         self._flush()
         return self._arrays
+
+    def load_texture(self, path: str) -> int:
+        """TriangleList::loadTexture (TriangleList.cpp:369-387): one texture per
+        distinct path; an unreadable file gives -1."""
+        loaded = self._loaded_textures
+        if path in loaded:
+            return loaded[path]
+        try:
+            img = load_image(path)
+        except _lib.CTError:
+            return -1
+        self.textures.append(img)
+        loaded[path] = len(self.textures) - 1
+        return loaded[path]
+
+    def load_model(self, path: str, scale: float = 1.0, mat=None, material: int = -1, normalize: bool = True):
+        """TriangleList::loadModel (TriangleList.cpp:63-146): import the OBJ,
+        add one material per used MTL entry (with its diffuse and normal maps
+        loaded) unless `material` >= 0 overrides them, then append
+        pos = mat * vec4(p * scale, 1) and norm = mat * vec4(n, 0) in glm's
+        float32 evaluation order, texcoords as imported."""
+        m = load_obj(path, normalize)
+        ids = []
+        for i, mt in enumerate(m["materials"]):
+            mt = Material(**mt.__dict__)
+            if m["diffuse_maps"][i]:
+                mt.diffuse_tex = self.load_texture(m["diffuse_maps"][i])
+            if m["normal_maps"][i]:
+                mt.normal_tex = self.load_texture(m["normal_maps"][i])
+            ids.append(self.add_material(mt))
+        f = np.float32
+        M = np.eye(4, dtype=f) if mat is None else np.asarray(mat, f).reshape(4, 4)
+
+        def xform(v, w):
+            # glm mat4 * vec4 (column-major columns M[:, c]): (c0*x + c1*y) + (c2*z + c3*w)
+            c = [M[:, k][None, :3] for k in range(4)]
+            return ((c[0] * v[:, 0:1] + c[1] * v[:, 1:2]) + (c[2] * v[:, 2:3] + c[3] * f(w))).astype(f)
+
+        pos = xform(m["vertices"] * f(scale), 1.0)
+        nrm = xform(m["normals"], 0.0)
+        tri_mat = np.asarray(ids, np.uint32)[m["material_idxs"]] if material < 0 else \
+            np.full(m["indices"].shape[0], material, np.uint32)
+        # one add_mesh per material so emitters land in the light list
+        base = len(self.arrays()["vertices"])
+        a = self._arrays
+        ix = m["indices"] + np.uint32(base)
+        cn = ((nrm[m["indices"][:, 0]] + nrm[m["indices"][:, 1]]) + nrm[m["indices"][:, 2]]) / f(3.0)
+        t0 = a["indices"].shape[0]
+        a["vertices"] = np.concatenate([a["vertices"], pos])
+        a["normals"] = np.concatenate([a["normals"], nrm])
+        a["texcoords"] = np.concatenate([a["texcoords"], m["texcoords"]])
+        a["indices"] = np.concatenate([a["indices"], ix])
+        a["center_normals"] = np.concatenate([a["center_normals"], cn.astype(f)])
+        a["material_idxs"] = np.concatenate([a["material_idxs"], tri_mat])
+        is_light = np.asarray([mm.type == MAT_LIGHT for mm in self.materials], bool)
+        lights = np.nonzero(is_light[tri_mat])[0]
+        if lights.size:
+            a["light_indices"] = np.concatenate([a["light_indices"], (lights + t0).astype(np.uint32)])
+        return m
 
     def get_prim_count(self) -> int:
         return int(self.arrays()["indices"].shape[0])

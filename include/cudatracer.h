@@ -196,6 +196,40 @@ ct_status ct_host_bvh_counts(const ct_host_bvh* h, uint32_t* binary_nodes, uint3
 ct_status ct_host_bvh_export(const ct_host_bvh* h, ct_bvh_layout layout, void* nodes, uint32_t* prim_indices);
 ct_status ct_host_bvh_destroy(ct_host_bvh* h);
 
+/* ---- model and texture ingest (host only, no device needed): replace the
+ * assimp import in TriangleList::loadModel (src/Core/TriangleList.cpp:63-91)
+ * with processMesh's material choice (:203-348), and FreeImage's 8-bit load in
+ * core::Surface::LoadImage (src/Utils/Surface.cpp:33-98).
+ *
+ * ct_mesh_load_obj reads a Wavefront OBJ and the MTL libraries it names:
+ * polygons with their winding reversed and split into triangles, identical
+ * (position, texcoord, normal) corners joined, smooth normals generated where
+ * the file has none, one group of vertices per material, and with `normalize`
+ * the model centred and scaled so its largest half-extent is 1. Materials come
+ * out as processMesh chooses them (roughness as read; the scene container sets
+ * it to 1 as addMaterial does), with the paths of their diffuse and normal
+ * maps relative to the OBJ's folder ("" when none). Texture indices in the
+ * returned materials are -1: the caller numbers the textures it loads. */
+typedef struct ct_mesh ct_mesh;
+ct_status ct_mesh_load_obj(const char* path, int32_t normalize, ct_mesh** out);
+ct_status ct_mesh_info(const ct_mesh* mesh, uint32_t* vertex_count, uint32_t* triangle_count,
+                       uint32_t* material_count);
+/* vertices/normals: 3 floats per vertex, texcoords: 2, indices: 3 per triangle,
+ * material_idxs: one per triangle (into the mesh's materials); NULL skips an array. */
+ct_status ct_mesh_arrays(const ct_mesh* mesh, float* vertices, float* normals, float* texcoords, uint32_t* indices,
+                         uint32_t* material_idxs);
+/* diffuse_map / normal_map: NUL-terminated paths written into buffers of
+ * path_capacity bytes (NULL skips one); a path that does not fit fails. */
+ct_status ct_mesh_material(const ct_mesh* mesh, uint32_t index, ct_material* out, char* diffuse_map, char* normal_map,
+                           uint32_t path_capacity);
+ct_status ct_mesh_destroy(ct_mesh* mesh);
+/* Truevision TGA (types 1-3 and 9-11). With rgba NULL only the size is
+ * returned; otherwise rgba receives width*height float4 texels, channel/255,
+ * alpha 1, row 0 at the bottom of the picture, as Surface stores them. */
+ct_status ct_image_load(const char* path, uint32_t* width, uint32_t* height, float* rgba);
+/* Message of the last failed ct_mesh_* or ct_image_load call on this thread. */
+const char* ct_mesh_last_error(void);
+
 /* ---- ray queries: replace the host MBVHNode::traverseMBVH (src/BVH/MBVHNode.cuh:207)
  * and the device traverseMBVH/traverseMBVHShadow (:126, :165).
  * DEVICE buffers, SoA, 16-byte aligned:
