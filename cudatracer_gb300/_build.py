@@ -27,6 +27,7 @@ SOURCES = {
     "bvh_build.cpp": [],
     "mesh_io.cpp": [],
     "k_trace.cu": [],
+    "bvh_gpu.cu": [],
     "k_shade_exact.cu": ["-fmad=false"],
     "k_shade_fast.cu": [],
     "noalloc.cu": [],

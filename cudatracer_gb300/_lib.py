@@ -102,6 +102,7 @@ SIGNATURES = {
                                      POINTER(c_double), POINTER(c_double)]),
     "ct_host_bvh_export": (c_int32, [P, c_int32, P, P]),
     "ct_host_bvh_destroy": (c_int32, [P]),
+    "ct_bvh_build_device": (c_int32, [P, P, P, PP]),
     "ct_mesh_load_obj": (c_int32, [c_char_p, c_int32, PP]),
     "ct_mesh_info": (c_int32, [P, POINTER(c_uint32), POINTER(c_uint32), POINTER(c_uint32)]),
     "ct_mesh_arrays": (c_int32, [P, P, P, P, P, P]),

@@ -391,6 +391,14 @@ class Scene:
         check(self.ctx.lib.ct_bvh_build(self.ctx.h, self.h, nthreads, ctypes.byref(h)), self.ctx.h)
         return BVH(self, h)
 
+    def build_bvh_device(self, stream=None) -> "BVH":
+        """The same SAH tree built on the GPU (ct_bvh_build_device): quad nodes
+        equal build_bvh's bit for bit, primitives within a leaf may be reordered."""
+        h = ctypes.c_void_p()
+        s = None if stream is None else getattr(stream, "cuda_stream", stream)
+        check(self.ctx.lib.ct_bvh_build_device(self.ctx.h, self.h, s, ctypes.byref(h)), self.ctx.h)
+        return BVH(self, h)
+
     def import_quad(self, nodes: np.ndarray, prims: np.ndarray) -> "BVH":
         nodes = np.ascontiguousarray(nodes)
         prims = np.ascontiguousarray(prims, np.uint32)

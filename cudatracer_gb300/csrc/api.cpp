@@ -123,6 +123,12 @@ struct ct_bvh {
   ct_bvh_info info{};
   uint32_t nt = 0;
   Allocs allocs;
+  // device-built trees keep the reference-layout quad nodes and the primitive
+  // order on the device only (exported on request)
+  bool device_built = false;
+  int device = 0;
+  void* d_quad = nullptr;
+  uint32_t* d_prims = nullptr;
 };
 
 struct ct_render {
@@ -467,6 +473,89 @@ ct_status ct_bvh_build(ct_ctx* ctx, const ct_scene* scene, int32_t nthreads, ct_
   return CT_OK;
 }
 
+ct_status ct_bvh_build_device(ct_ctx* ctx, const ct_scene* scene, void* stream, ct_bvh** out) {
+  if (!ctx || !scene || !out) return fail(ctx, CT_ERR_INVALID_ARGUMENT, "null argument");
+  *out = nullptr;
+  const uint32_t n = scene->nt;
+  if (n == 0 || n > (1u << 30)) return fail(ctx, CT_ERR_INVALID_ARGUMENT, "triangle count out of range for the device builder");
+  ct_status s = set_device(ctx);
+  if (s != CT_OK) return s;
+  cudaStream_t st = (cudaStream_t)stream;
+  const auto t0 = std::chrono::high_resolution_clock::now();
+  Allocs scratch_allocs;
+  void* scratch = nullptr;
+  uint32_t* hc = nullptr;
+  auto* b = new ct_bvh();
+  auto cleanup = [&](ct_status r) {
+    if (st) cudaStreamSynchronize(st);
+    else cudaDeviceSynchronize();
+    free_all(ctx, scratch_allocs);
+    if (hc) cudaFreeHost(hc);
+    if (r != CT_OK) {
+      free_all(ctx, b->allocs);
+      delete b;
+    }
+    return r;
+  };
+  if ((s = dev_alloc(ctx, scratch_allocs, &scratch, gpu_bvh_scratch_bytes(n))) != CT_OK) return cleanup(s);
+  cudaError_t e = cudaMallocHost((void**)&hc, 64);
+  if (e != cudaSuccess) return cleanup(cuda_fail(ctx, e, "cudaMallocHost"));
+  GpuBvhResult r;
+  e = gpu_bvh_build(scene->dev, scratch, hc, st, r);
+  if (e != cudaSuccess) return cleanup(cuda_fail(ctx, e, "device BVH build"));
+  if (r.error & 1u)
+    return cleanup(fail(ctx, CT_ERR_UNSUPPORTED,
+                        "device BVH build: scene extent too large for the SAH cost (area x count >= 1e34); "
+                        "use ct_bvh_build"));
+  if (r.error) return cleanup(fail(ctx, CT_ERR_CUDA, "device BVH build: internal check failed (code " +
+                                                         std::to_string(r.error) + ")"));
+  const auto t1 = std::chrono::high_resolution_clock::now();
+  uint32_t shift = 0, fm = 0, cm = 0;
+  const std::string enc = leaf_encoding(n, r.max_leaf, shift, fm, cm);
+  if (!enc.empty()) return cleanup(fail(ctx, CT_ERR_UNSUPPORTED, enc));
+  void* quad = nullptr;
+  void* nodes = nullptr;
+  void* tris = nullptr;
+  void* prims = nullptr;
+  if ((s = dev_alloc(ctx, b->allocs, &quad, (size_t)r.quad_nodes * sizeof(QuadNode))) != CT_OK) return cleanup(s);
+  if ((s = dev_alloc(ctx, b->allocs, &nodes, (size_t)r.quad_nodes * sizeof(QNodeDev))) != CT_OK) return cleanup(s);
+  if ((s = dev_alloc(ctx, b->allocs, &tris, (size_t)n * 3 * sizeof(float4))) != CT_OK) return cleanup(s);
+  if ((s = dev_alloc(ctx, b->allocs, &prims, (size_t)n * 4)) != CT_OK) return cleanup(s);
+  e = gpu_bvh_emit(scene->dev, scratch, r, shift, quad, (QNodeDev*)nodes, (float4*)tris, (uint32_t*)prims, st);
+  if (e != cudaSuccess) return cleanup(cuda_fail(ctx, e, "device BVH emit"));
+  e = st ? cudaStreamSynchronize(st) : cudaDeviceSynchronize();
+  if (e != cudaSuccess) return cleanup(cuda_fail(ctx, e, "device BVH build"));
+  const auto t2 = std::chrono::high_resolution_clock::now();
+  b->device_built = true;
+  b->device = ctx->device;
+  b->d_quad = quad;
+  b->d_prims = (uint32_t*)prims;
+  b->dev.nodes = (const QNodeDev*)nodes;
+  b->dev.tris = (const float4*)tris;
+  b->dev.leaf_shift = shift;
+  b->dev.first_mask = fm;
+  b->dev.count_mask = cm;
+  b->dev.prim_count = n;
+  b->dev.node_count = r.quad_nodes;
+  b->dev.stack_entries = (int32_t)std::min<uint32_t>(3 * r.depth + 1, 256);
+  b->nt = n;
+  ct_bvh_info& i = b->info;
+  i.binary_node_count = r.binary_nodes;
+  i.quad_node_count = r.quad_nodes;
+  i.prim_count = n;
+  i.max_leaf_size = r.max_leaf;
+  i.quad_depth = r.depth;
+  i.stack_entries = (uint32_t)b->dev.stack_entries;
+  i.build_ms = std::chrono::duration<double, std::milli>(t1 - t0).count();
+  i.collapse_ms = std::chrono::duration<double, std::milli>(t2 - t1).count();
+  i.upload_ms = 0.0;
+  uint64_t bytes = 0;
+  for (auto& p : b->allocs.list) bytes += p.second;
+  i.device_bytes = bytes;
+  *out = b;
+  return cleanup(CT_OK);
+}
+
 ct_status ct_bvh_import_quad(ct_ctx* ctx, const ct_scene* scene, const void* nodes, uint32_t node_count,
                              const uint32_t* prim_indices, uint32_t prim_count, ct_bvh** out) {
   if (!ctx || !scene || !nodes || !prim_indices || !out) return fail(ctx, CT_ERR_INVALID_ARGUMENT, "null argument");
@@ -524,6 +613,18 @@ ct_status ct_bvh_info_get(const ct_bvh* bvh, ct_bvh_info* info) {
 
 ct_status ct_bvh_export(const ct_bvh* bvh, ct_bvh_layout layout, void* nodes, uint32_t* prim_indices) {
   if (!bvh) return CT_ERR_INVALID_ARGUMENT;
+  if (bvh->device_built) {
+    if (layout == CT_BVH_BINARY) return nodes ? CT_ERR_UNSUPPORTED : CT_OK;
+    if (layout != CT_BVH_QUAD) return CT_ERR_INVALID_ARGUMENT;
+    if (cudaSetDevice(bvh->device) != cudaSuccess) return CT_ERR_CUDA;
+    if (nodes && cudaMemcpy(nodes, bvh->d_quad, (size_t)bvh->info.quad_node_count * sizeof(QuadNode),
+                            cudaMemcpyDeviceToHost) != cudaSuccess)
+      return CT_ERR_CUDA;
+    if (prim_indices &&
+        cudaMemcpy(prim_indices, bvh->d_prims, (size_t)bvh->nt * 4, cudaMemcpyDeviceToHost) != cudaSuccess)
+      return CT_ERR_CUDA;
+    return CT_OK;
+  }
   if (layout == CT_BVH_BINARY) {
     if (bvh->host.bin.empty() && nodes) return CT_ERR_UNSUPPORTED;
     if (nodes) std::memcpy(nodes, bvh->host.bin.data(), bvh->host.bin.size() * sizeof(BinNode));

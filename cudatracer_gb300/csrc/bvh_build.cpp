@@ -437,24 +437,31 @@ std::string validate_quad(const std::vector<QuadNode>& q, uint32_t prim_count) {
   return "";
 }
 
+std::string leaf_encoding(uint32_t np, uint32_t max_leaf, uint32_t& shift, uint32_t& first_mask, uint32_t& count_mask) {
+  // first in the low `shift` bits, count above, bit 31 flag
+  shift = 1;
+  while (shift < 31 && (1ull << shift) <= (uint64_t)np) shift++;
+  const uint32_t count_bits = 31 - shift;
+  if (count_bits == 0 || max_leaf >= (1u << count_bits))
+    return "BVH leaf of " + std::to_string(max_leaf) + " primitives cannot be encoded with " + std::to_string(np) +
+           " primitives";
+  first_mask = (1u << shift) - 1u;
+  count_mask = (1u << count_bits) - 1u;
+  return "";
+}
+
 std::string to_device_layout(const HostBVH& h, const float* verts, const uint32_t* idx, uint32_t ntri,
                              DeviceLayout& out) {
   const uint32_t np = (uint32_t)h.prims.size();
   if (np != ntri) return "primitive index count does not match the scene's triangle count";
-  // leaf encoding: first in the low leaf_shift bits, count above, bit 31 flag
-  uint32_t shift = 1;
-  while (shift < 31 && (1ull << shift) <= (uint64_t)np) shift++;
   uint32_t max_leaf = 0;
   for (const QuadNode& n : h.quad)
     for (int c = 0; c < 4; c++)
       if (n.counts[c] > 0) max_leaf = std::max<uint32_t>(max_leaf, (uint32_t)n.counts[c]);
-  const uint32_t count_bits = 31 - shift;
-  if (count_bits == 0 || max_leaf >= (1u << count_bits))
-    return "BVH leaf of " + std::to_string(max_leaf) + " primitives cannot be encoded with " +
-           std::to_string(np) + " primitives";
+  uint32_t shift = 0;
+  const std::string enc = leaf_encoding(np, max_leaf, shift, out.first_mask, out.count_mask);
+  if (!enc.empty()) return enc;
   out.leaf_shift = shift;
-  out.first_mask = (1u << shift) - 1u;
-  out.count_mask = (1u << count_bits) - 1u;
   out.max_leaf = max_leaf;
   const size_t nn = h.quad.size();
   out.nodes.assign(nn * sizeof(QNodeDev), 0);

@@ -46,6 +46,10 @@ struct DeviceLayout {
   uint32_t depth = 0, max_leaf = 0;
   int32_t stack_entries = 0;
 };
+// Leaf reference encoding for np primitives: first in the low `shift` bits,
+// count above, bit 31 set. Returns "" or why a leaf of max_leaf primitives
+// cannot be encoded.
+std::string leaf_encoding(uint32_t np, uint32_t max_leaf, uint32_t& shift, uint32_t& first_mask, uint32_t& count_mask);
 // Convert to the device layout; returns "" or an error message.
 std::string to_device_layout(const HostBVH& h, const float* verts, const uint32_t* idx, uint32_t ntri,
                              DeviceLayout& out);

@@ -120,6 +120,23 @@ cudaError_t launch_shade(const DevScene& sc, const DevQueues& q, const FrameCons
                          int exact, cudaStream_t s);
 cudaError_t launch_present(const float4* accum, float4* out, int n, float samples, cudaStream_t s);
 // accum[i] += frame[i]; frame[i] = 0 (folds an overlapped frame's private buffer)
+// Device SAH build (bvh_gpu.cu). gpu_bvh_build runs the binary build and the
+// collapse bookkeeping in `scratch` (gpu_bvh_scratch_bytes) and returns the
+// sizes; gpu_bvh_emit then writes the reference-layout quad nodes (QuadNode,
+// pre-order), the traversal nodes, the leaf-ordered triangles and the
+// primitive order into buffers of those sizes. host_counters: 16 words of
+// pinned host memory. Both return after their work is queued on `s`; build
+// synchronises with `s` once per level to read the level's node count.
+struct GpuBvhResult {
+  uint32_t binary_nodes = 0, quad_nodes = 0, max_leaf = 0, depth = 0;
+  uint32_t error = 0;  // 1 degenerate extent, 2 arena, 4 stack, 8 partition mismatch
+  uint32_t levels = 0, small_roots = 0;
+};
+size_t gpu_bvh_scratch_bytes(uint32_t n);
+cudaError_t gpu_bvh_build(const DevScene& sc, void* scratch, uint32_t* host_counters, cudaStream_t s, GpuBvhResult& r);
+cudaError_t gpu_bvh_emit(const DevScene& sc, void* scratch, const GpuBvhResult& r, uint32_t leaf_shift, void* quad,
+                         QNodeDev* nodes, float4* tris, uint32_t* prims, cudaStream_t s);
+
 cudaError_t launch_fold(float4* accum, float4* frame, int n, cudaStream_t s);
 
 // allocation-free frame (noalloc.cu): queues in a static device array

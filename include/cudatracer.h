@@ -103,8 +103,8 @@ typedef struct ct_bvh_info {
   uint32_t max_leaf_size;
   uint32_t quad_depth;        /* levels of the quad tree */
   uint32_t stack_entries;     /* traversal stack entries per ray the kernels reserve */
-  double build_ms;            /* host binary SAH build */
-  double collapse_ms;         /* host quad collapse */
+  double build_ms;            /* binary SAH build (host, or device incl. its readbacks) */
+  double collapse_ms;         /* quad collapse (device builds: collapse + output) */
   double upload_ms;
   uint64_t device_bytes;
 } ct_bvh_info;
@@ -180,6 +180,16 @@ ct_status ct_bvh_import_quad(ct_ctx* ctx, const ct_scene* scene, const void* nod
                              const uint32_t* prim_indices, uint32_t prim_count, ct_bvh** out);
 ct_status ct_bvh_import_binary(ct_ctx* ctx, const ct_scene* scene, const void* nodes, uint32_t node_count,
                                const uint32_t* prim_indices, uint32_t prim_count, ct_bvh** out);
+/* Device build of the same tree: the binned SAH and the MergeNodes collapse
+ * run on the GPU (replaces BVHTree::constructBVH + MBVHTree::constructBVH,
+ * src/BVH/BVHTree.cpp:13, src/BVH/MBVHTree.cpp:15, for large scenes). The quad
+ * nodes equal ct_bvh_build's bit for bit; only the order of the primitives
+ * inside each leaf may differ. Runs on `stream` (a cudaStream_t, NULL = legacy)
+ * and returns when the tree is ready; the build reads one counter back per
+ * tree level. Fails with CT_ERR_UNSUPPORTED when the scene's extent makes
+ * the SAH cost reach 1e34 (coordinates beyond ~1e14). Exports the QUAD layout
+ * only (ct_bvh_export with CT_BVH_BINARY and non-NULL nodes fails). */
+ct_status ct_bvh_build_device(ct_ctx* ctx, const ct_scene* scene, void* stream, ct_bvh** out);
 ct_status ct_bvh_info_get(const ct_bvh* bvh, ct_bvh_info* info);
 /* Copy the host-side trees out in the reference layouts (NULL skips an array). */
 ct_status ct_bvh_export(const ct_bvh* bvh, ct_bvh_layout layout, void* nodes, uint32_t* prim_indices);
