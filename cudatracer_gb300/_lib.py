@@ -21,6 +21,7 @@ STATUS_NAMES = {
 globals().update({name: code for code, name in STATUS_NAMES.items()})
 CT_BVH_BINARY, CT_BVH_QUAD = 0, 1
 CT_SHADE_COMPAT, CT_SHADE_FULL = 0, 1
+CT_TEX_NEAREST, CT_TEX_BILINEAR = 0, 1
 
 
 class CTError(RuntimeError):
@@ -65,6 +66,7 @@ class ct_render_params(Structure):
         ("width", c_int32), ("height", c_int32), ("max_depth", c_int32), ("frame_index", c_uint32),
         ("shading_mode", c_int32), ("exact_math", c_int32), ("shadow", c_int32), ("indirect", c_int32),
         ("sky", c_int32), ("normal_eps", c_float), ("dist_eps", c_float), ("tri_eps", c_float),
+        ("texture_filter", c_int32),
     ]
 
 

@@ -598,6 +598,8 @@ class Params:
     normal_eps: float = 1e-5
     dist_eps: float = 1e-5
     tri_eps: float = 1e-3
+    shading_mode: int = _lib.CT_SHADE_COMPAT
+    texture_filter: int = _lib.CT_TEX_NEAREST
 
     def reset(self, job: RenderJob, stream=None):
         """Params::reset: clear the accumulation buffer and the sample count."""
@@ -611,6 +613,7 @@ class Params:
         p.exact_math = int(self.exact_math)
         p.shadow, p.indirect, p.sky = int(self.shadow), int(self.indirect), int(self.sky)
         p.normal_eps, p.dist_eps, p.tri_eps = self.normal_eps, self.dist_eps, self.tri_eps
+        p.shading_mode, p.texture_filter = int(self.shading_mode), int(self.texture_filter)
         return p
 
 

@@ -816,6 +816,8 @@ ct_status ct_render_accumulate(ct_ctx* ctx, const ct_scene* scene, const ct_bvh*
   if (bvh->nt != scene->nt) return fail(ctx, CT_ERR_INVALID_ARGUMENT, "BVH was built for another scene");
   if (p->shading_mode != CT_SHADE_COMPAT && p->shading_mode != CT_SHADE_FULL)
     return fail(ctx, CT_ERR_INVALID_ARGUMENT, "unknown shading mode");
+  if (p->texture_filter != CT_TEX_NEAREST && p->texture_filter != CT_TEX_BILINEAR)
+    return fail(ctx, CT_ERR_INVALID_ARGUMENT, "unknown texture filter");
   if (!finite3(cam->position) || !finite3(cam->forward) || !finite3(cam->up) || !std::isfinite(cam->fov_deg))
     return fail(ctx, CT_ERR_INVALID_ARGUMENT, "non-finite camera");
   ct_status s = set_device(ctx);
@@ -863,6 +865,7 @@ ct_status ct_render_accumulate(ct_ctx* ctx, const ct_scene* scene, const ct_bvh*
   f.indirect = p->indirect;
   f.sky = p->sky;
   f.shading_mode = p->shading_mode;
+  f.tex_filter = p->texture_filter;
   if (p->exact_math) return emit_frame(ctx, r, r->q, scene, bvh, f, p, st);  // strictly sequential accumulation
   // Fast-math frames overlap: the frame renders into one of two private slots
   // (queues + accumulation) on the slot's own stream, so its first passes can
@@ -893,6 +896,8 @@ ct_status ct_render_accumulate_noalloc(ct_ctx* ctx, const ct_scene* scene, const
   if (bvh->nt != scene->nt) return fail(ctx, CT_ERR_INVALID_ARGUMENT, "BVH was built for another scene");
   if (p->shading_mode != CT_SHADE_COMPAT && p->shading_mode != CT_SHADE_FULL)
     return fail(ctx, CT_ERR_INVALID_ARGUMENT, "unknown shading mode");
+  if (p->texture_filter != CT_TEX_NEAREST && p->texture_filter != CT_TEX_BILINEAR)
+    return fail(ctx, CT_ERR_INVALID_ARGUMENT, "unknown texture filter");
   if (!finite3(cam->position) || !finite3(cam->forward) || !finite3(cam->up) || !std::isfinite(cam->fov_deg))
     return fail(ctx, CT_ERR_INVALID_ARGUMENT, "non-finite camera");
   ct_status s = set_device(ctx);
@@ -929,6 +934,7 @@ ct_status ct_render_accumulate_noalloc(ct_ctx* ctx, const ct_scene* scene, const
   f.indirect = p->indirect;
   f.sky = p->sky;
   f.shading_mode = p->shading_mode;
+  f.tex_filter = p->texture_filter;
   CT_CUDA(ctx, noalloc_render(ctx->device, scene->dev, bvh->dev, f, p->max_depth, p->exact_math,
                               (float4*)accum_device, ctx->d_error, (cudaStream_t)stream));
   return CT_OK;

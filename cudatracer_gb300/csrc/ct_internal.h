@@ -95,6 +95,7 @@ struct FrameConst {
   float normal_eps, dist_eps, tri_eps;
   int32_t shadow, indirect, sky;
   int32_t shading_mode;
+  int32_t tex_filter;  // CT_TEX_NEAREST / CT_TEX_BILINEAR
 };
 
 enum : uint32_t { kErrStackOverflow = 1u };

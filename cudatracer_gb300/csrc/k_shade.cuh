@@ -19,7 +19,8 @@
 #include "vmath.cuh"
 
 #ifndef CT_MODE_FULL
-#define CT_MODE_FULL 1  // CT_SHADE_FULL in include/cudatracer.h
+#define CT_MODE_FULL 1     // CT_SHADE_FULL in include/cudatracer.h
+#define CT_TEX_BILINEAR_ 1  // CT_TEX_BILINEAR in include/cudatracer.h
 #endif
 
 #ifndef CT_SHADE_NS
@@ -66,28 +67,42 @@ __device__ __forceinline__ int rnd_int_max(uint32_t& s, int maxv) {
   return (int)(rnd_float(s) * ((float)maxv + 0.99999f));
 }
 
-// Texel index of SceneData::getTextureColor (src/Core/SceneData.cuh:81-97).
-// For finite uv this is the reference's index; NaN or out-of-range values are
-// clamped to the texture instead of reading past it.
-__device__ __forceinline__ uint32_t texel_index(const DevScene& sc, int tex, float x, float y) {
-  const uint2 dim = __ldg(sc.tex_dims + tex);
-  const float fx = x * (float)(dim.x - 1), fy = y * (float)(dim.y - 1);
-  uint32_t ix = fx >= 0.0f ? (uint32_t)fminf(fx, (float)(dim.x - 1)) : 0u;
-  uint32_t iy = fy >= 0.0f ? (uint32_t)fminf(fy, (float)(dim.y - 1)) : 0u;
-  return __ldg(sc.tex_offsets + tex) + (ix + iy * dim.x);
+// Texel grid of SceneData::getTextureColor (src/Core/SceneData.cuh:81-97):
+// coordinate u*(width-1). For finite uv the nearest texel is the reference's
+// index; NaN or out-of-range values are clamped to the texture instead of
+// reading past it. CT_TEX_BILINEAR blends the four texels around the same
+// grid point, clamped at the last row and column: a + (b - a) * t per axis.
+__device__ __forceinline__ float grid_coord(float x, uint32_t n) {
+  const float g = x * (float)(n - 1);
+  return g >= 0.0f ? fminf(g, (float)(n - 1)) : 0.0f;
 }
-__device__ __forceinline__ float4 tex_color(const DevScene& sc, int tex, float u, float v) {
+__device__ __forceinline__ float4 lerp4(const float4& a, const float4& b, float t) {
+  return make_float4(a.x + (b.x - a.x) * t, a.y + (b.y - a.y) * t, a.z + (b.z - a.z) * t, a.w + (b.w - a.w) * t);
+}
+__device__ __forceinline__ float4 texel_at(const DevScene& sc, int tex, float x, float y, int filter) {
+  const uint2 dim = __ldg(sc.tex_dims + tex);
+  const float4* t = sc.texels + __ldg(sc.tex_offsets + tex);
+  const float gx = grid_coord(x, dim.x), gy = grid_coord(y, dim.y);
+  const uint32_t ix = (uint32_t)gx, iy = (uint32_t)gy;
+  if (filter != CT_TEX_BILINEAR_) return __ldg(t + (ix + iy * dim.x));
+  const uint32_t ix1 = min(ix + 1, dim.x - 1), iy1 = min(iy + 1, dim.y - 1);
+  const float tx = gx - (float)ix, ty = gy - (float)iy;
+  const float4 c00 = __ldg(t + (ix + iy * dim.x)), c10 = __ldg(t + (ix1 + iy * dim.x));
+  const float4 c01 = __ldg(t + (ix + iy1 * dim.x)), c11 = __ldg(t + (ix1 + iy1 * dim.x));
+  return lerp4(lerp4(c00, c10, tx), lerp4(c01, c11, tx), ty);
+}
+__device__ __forceinline__ float4 tex_color(const DevScene& sc, int tex, float u, float v, int filter) {
   float x = fmodf(u, 1.0f), y = fmodf(v, 1.0f);
   if (x < 0) x += 1.0f;
   if (y < 0) y += 1.0f;
-  return __ldg(sc.texels + texel_index(sc, tex, x, y));
+  return texel_at(sc, tex, x, y, filter);
 }
 // SceneData::getTextureNormal (src/Core/SceneData.cuh:99-116): no wrap, only +1 for negatives
-__device__ __forceinline__ V3 tex_normal(const DevScene& sc, int tex, float u, float v) {
+__device__ __forceinline__ V3 tex_normal(const DevScene& sc, int tex, float u, float v, int filter) {
   float x = u, y = v;
   if (x < 0) x += 1.0f;
   if (y < 0) y += 1.0f;
-  return normalize(v3(__ldg(sc.texels + texel_index(sc, tex, x, y))));
+  return normalize(v3(texel_at(sc, tex, x, y, filter)));
 }
 // convertToLocalSpace (src/Core/Random.cuh:37-42) + localToWorld
 __device__ __forceinline__ V3 sample_to_world(V3 s, V3 n) {
@@ -133,7 +148,7 @@ __device__ __forceinline__ void shade_compat(const DevScene& sc, const DevQueues
     if (f.sky && sc.sky_tex >= 0) {
       const float u = 1.0f + (xatan2(dir.x, -dir.z) * kOneOverPi) * 0.5f;
       const float v = 1.0f - xacos(dir.y) * kOneOverPi;
-      const float4 tc = tex_color(sc, sc.sky_tex, u, v);
+      const float4 tc = tex_color(sc, sc.sky_tex, u, v, f.tex_filter);
       accum_add(q.accum, pix, (T / last_pdf) * v3(tc));
     }
     return;
@@ -156,7 +171,7 @@ __device__ __forceinline__ void shade_compat(const DevScene& sc, const DevQueues
   const int4 mtex = __ldg(&mp->tex);
   const float4 tr = __ldg(&mp->type_rough);
   const int mtype = __float_as_int(tr.x);
-  if (mtex.y >= 0) iN = sample_to_world(tex_normal(sc, mtex.y, tu, tv), iN);
+  if (mtex.y >= 0) iN = sample_to_world(tex_normal(sc, mtex.y, tu, tv, f.tex_filter), iN);
   if (mtype == 0) {  // emitter (Kernel.cu:114-136)
     if (!f.indirect) return;
     const float DdotNL = -dot(dir, iN);
@@ -177,7 +192,7 @@ __device__ __forceinline__ void shade_compat(const DevScene& sc, const DevQueues
   iN = iN * flip;
   uint32_t seed = wang_hash((uint32_t)pix * 16789u + f.frame * 1791u + path_length * 720898027u);
   V3 color = v3(alb);
-  if (mtex.x >= 0) color = v3(tex_color(sc, mtex.x, tu, tv));
+  if (mtex.x >= 0) color = v3(tex_color(sc, mtex.x, tu, tv, f.tex_filter));
   // SampleBSDF (BSDF.h:33-63); its two random numbers are drawn left to right
   const float r3 = rnd_float(seed), r4 = rnd_float(seed);
   V3 wo, fval;
@@ -309,7 +324,7 @@ __device__ __forceinline__ void shade_full(const DevScene& sc, const DevQueues& 
     if (f.sky && sc.sky_tex >= 0) {
       const float u = 1.0f + (xatan2(dir.x, -dir.z) * kOneOverPi) * 0.5f;
       const float v = 1.0f - xacos(fminf(fmaxf(dir.y, -1.0f), 1.0f)) * kOneOverPi;
-      accum_add(q.accum, pix, T * v3(tex_color(sc, sc.sky_tex, u, v)));
+      accum_add(q.accum, pix, T * v3(tex_color(sc, sc.sky_tex, u, v, f.tex_filter)));
     }
     return;
   }
@@ -333,7 +348,7 @@ __device__ __forceinline__ void shade_full(const DevScene& sc, const DevQueues& 
   const int4 mtex = __ldg(&mp->tex);
   const float4 tr = __ldg(&mp->type_rough);
   const int mtype = __float_as_int(tr.x);
-  if (mtex.y >= 0) Ns = normalize(sample_to_world(tex_normal(sc, mtex.y, tu, tv), Ns));
+  if (mtex.y >= 0) Ns = normalize(sample_to_world(tex_normal(sc, mtex.y, tu, tv, f.tex_filter), Ns));
   if (mtype == full::kLight) {
     if (!f.indirect) return;
     // emitters radiate on the side their centre normal faces (as the reference's NEE assumes)
@@ -358,7 +373,7 @@ __device__ __forceinline__ void shade_full(const DevScene& sc, const DevQueues& 
   const V3 wo = -dir;
   const V3 wo_l = v3(dot(wo, Tt), dot(wo, Bt), dot(wo, N));
   V3 color = v3(alb);
-  if (mtex.x >= 0) color = v3(tex_color(sc, mtex.x, tu, tv));
+  if (mtex.x >= 0) color = v3(tex_color(sc, mtex.x, tu, tv, f.tex_filter));
   uint32_t seed = wang_hash((uint32_t)pix * 16789u + f.frame * 1791u + path_length * 720898027u);
   const float u1 = rnd_float(seed), u2 = rnd_float(seed), u3 = rnd_float(seed);
   const float rough = tr.y;

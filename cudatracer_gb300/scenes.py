@@ -137,10 +137,13 @@ def sky_gradient(width: int = 2048, height: int = 1024) -> np.ndarray:
 
 
 def terrain_scene(grid: int = 1024, spheres: int = 200, seed: int = 7, extent: float = 200.0,
-                  sky_size=(2048, 1024)) -> tuple[Scene, dict]:
+                  sky_size=(2048, 1024), ground_textures: tuple | None = None) -> tuple[Scene, dict]:
     """fBm terrain + icospheres + four emissive quads + sky.
 
-    Returns (scene, camera) where camera = dict(position, forward, up, fov)."""
+    ground_textures=(w, h) also gives the ground a seeded diffuse texture and a
+    tangent-space normal map of that size (textures 1 and 2; the uv span is
+    tiled 4x so the wrap is exercised). Returns (scene, camera) where camera =
+    dict(position, forward, up, fov)."""
     rng = np.random.default_rng(seed)
     h = _value_noise_fbm(grid, rng) * 12.0
     xs = np.linspace(-extent / 2, extent / 2, grid)
@@ -205,20 +208,38 @@ def terrain_scene(grid: int = 1024, spheres: int = 200, seed: int = 7, extent: f
         d.update(m)
         d["albedo"] = tuple(float(c) for c in d["albedo"])
         full.append(d)
+    textures = [sky_gradient(*sky_size)]
+    if ground_textures is not None:
+        tw, th = ground_textures
+        trng = np.random.default_rng(seed + 100)
+        yy, xx = np.mgrid[0:th, 0:tw]
+        check = ((xx // max(1, tw // 8) + yy // max(1, th // 8)) % 2).astype(np.float32)
+        diff = np.empty((th, tw, 4), np.float32)
+        diff[..., 0] = 0.35 + 0.4 * check + 0.1 * trng.uniform(size=(th, tw))
+        diff[..., 1] = 0.3 + 0.3 * check + 0.1 * trng.uniform(size=(th, tw))
+        diff[..., 2] = 0.25 + 0.2 * (1 - check) + 0.1 * trng.uniform(size=(th, tw))
+        diff[..., 3] = 1.0
+        nrm = np.empty((th, tw, 4), np.float32)
+        bump = trng.normal(scale=0.25, size=(th, tw, 2))
+        nrm[..., 0], nrm[..., 1], nrm[..., 2], nrm[..., 3] = bump[..., 0], bump[..., 1], 1.0, 1.0
+        textures += [diff, nrm]
+        full[0]["diffuse_tex"], full[0]["normal_tex"] = 1, 2
+        uvs[0] = uvs[0] * 4.0
     sc = Scene(
         np.concatenate(verts).astype(np.float32), np.concatenate(norms).astype(np.float32),
         np.concatenate(uvs).astype(np.float32), np.concatenate(faces).astype(np.uint32),
-        np.concatenate(mat_idx).astype(np.uint32), full, np.asarray(light_tris, np.uint32),
-        [sky_gradient(*sky_size)], 0)
+        np.concatenate(mat_idx).astype(np.uint32), full, np.asarray(light_tris, np.uint32), textures, 0)
     cam = dict(position=(0.0, 35.0, 95.0), forward=_unit((0.0, -0.32, -1.0)), up=(0.0, 1.0, 0.0), fov=60.0)
     return sc, cam
 
 
-def material_zoo_scene(grid: int = 48, spheres: int = 27, seed: int = 11) -> tuple[Scene, dict]:
+def material_zoo_scene(grid: int = 48, spheres: int = 27, seed: int = 11,
+                       ground_textures: tuple | None = None) -> tuple[Scene, dict]:
     """A small terrain scene whose spheres cycle through every non-emitter
     material type (Lambertian, specular, Fresnel, Beckmann, GGX, Trowbridge and
     the three rough dielectrics), for checking the full-material mode."""
-    sc, cam = terrain_scene(grid=grid, spheres=spheres, seed=seed, extent=60.0, sky_size=(256, 128))
+    sc, cam = terrain_scene(grid=grid, spheres=spheres, seed=seed, extent=60.0, sky_size=(256, 128),
+                            ground_textures=ground_textures)
     kinds = [MAT_LAMBERTIAN, MAT_SPECULAR, MAT_FRESNEL, MAT_BECKMANN, MAT_GGX, MAT_TROWBRIDGE,
              MAT_FRESNEL_BECKMANN, MAT_FRESNEL_GGX, MAT_FRESNEL_TROWBRIDGE]
     rng = np.random.default_rng(seed + 1)

@@ -120,6 +120,10 @@ typedef struct ct_camera {
 } ct_camera;
 
 enum { CT_SHADE_COMPAT = 0, CT_SHADE_FULL = 1 };
+/* Texture filtering: the reference's nearest texel (SceneData::getTextureColor,
+ * src/Core/SceneData.cuh:81-116), or bilinear over the same texel grid
+ * (texel centres at u*(width-1), v*(height-1), clamped at the edges). */
+enum { CT_TEX_NEAREST = 0, CT_TEX_BILINEAR = 1 };
 
 /* Per-frame parameters: the reference `Params` (src/CUDA/Kernel.cuh:23-72) and
  * SceneData flags/epsilons (src/Core/SceneData.cuh:19-45). Defaults from
@@ -138,6 +142,7 @@ typedef struct ct_render_params {
   float normal_eps;      /* SceneData::normalEpsilon */
   float dist_eps;        /* SceneData::distEpsilon */
   float tri_eps;         /* SceneData::triangleEpsilon */
+  int32_t texture_filter; /* CT_TEX_NEAREST (reference) or CT_TEX_BILINEAR */
 } ct_render_params;
 
 typedef struct ct_frame_stats {

@@ -82,6 +82,7 @@ extern "C" struct Fp64Scene {
   float normal_eps, dist_eps, tri_eps;
   const void* qnodes;
   const uint32_t* prims;
+  int32_t tex_filter;  // 0 nearest, 1 bilinear
 };
 
 namespace {
@@ -159,11 +160,21 @@ D3 texel(const Fp64Scene* s, int idx, double u, double v, bool wrap) {
   if (x < 0) x += 1.0;
   if (y < 0) y += 1.0;
   const uint32_t w = s->tex_dims[2 * idx], h = s->tex_dims[2 * idx + 1];
-  const double fx = x * (double)(w - 1), fy = y * (double)(h - 1);
-  const uint32_t ixx = fx >= 0 ? (uint32_t)std::min(fx, (double)(w - 1)) : 0u;
-  const uint32_t iyy = fy >= 0 ? (uint32_t)std::min(fy, (double)(h - 1)) : 0u;
-  const float* t = s->tex + 4 * (size_t)(s->tex_offsets[idx] + ixx + iyy * w);
-  return d3(t[0], t[1], t[2]);
+  double fx = x * (double)(w - 1), fy = y * (double)(h - 1);
+  fx = fx >= 0 ? std::min(fx, (double)(w - 1)) : 0.0;
+  fy = fy >= 0 ? std::min(fy, (double)(h - 1)) : 0.0;
+  const uint32_t ixx = (uint32_t)fx, iyy = (uint32_t)fy;
+  const float* base = s->tex + 4 * (size_t)s->tex_offsets[idx];
+  auto at = [&](uint32_t i, uint32_t j) {
+    const float* t = base + 4 * (size_t)(i + j * w);
+    return d3(t[0], t[1], t[2]);
+  };
+  if (s->tex_filter != 1) return at(ixx, iyy);
+  const uint32_t ix1 = std::min(ixx + 1, w - 1), iy1 = std::min(iyy + 1, h - 1);
+  const double tx = fx - ixx, ty = fy - iyy;
+  const D3 a = at(ixx, iyy) * (1.0 - tx) + at(ix1, iyy) * tx;
+  const D3 b = at(ixx, iy1) * (1.0 - tx) + at(ix1, iy1) * tx;
+  return a * (1.0 - ty) + b * ty;
 }
 
 // ---- material model (double restatement of bsdf_full.cuh) ----
@@ -429,6 +440,17 @@ D3 radiance(const Scene& S, D3 o, D3 d, int depth, Rng& rng) {
     D3 Ns = ld3(s->normals, ix[0]) * b0 + ld3(s->normals, ix[1]) * b1 + ld3(s->normals, ix[2]) * b2;
     Ns = dot(Ns, Ns) > 0 ? normalize(Ns) : Ngf;
     const Material& mat = S.m[s->mat_idx[hit]];
+    const float* uv0 = s->uvs + 2 * (size_t)ix[0];
+    const float* uv1 = s->uvs + 2 * (size_t)ix[1];
+    const float* uv2 = s->uvs + 2 * (size_t)ix[2];
+    const double tu = uv0[0] * b0 + uv1[0] * b1 + uv2[0] * b2, tv = uv0[1] * b0 + uv1[1] * b1 + uv2[1] * b2;
+    if (mat.normalTex >= 0) {
+      // tangent-space normal map: the texel (normalised) expressed in a frame around Ns
+      const D3 sm = normalize(texel(s, mat.normalTex, tu, tv, false));
+      const D3 W = std::fabs(Ns.x) > 0.99 ? d3(0, 1, 0) : d3(1, 0, 0);
+      const D3 Tn = normalize(cross(Ns, W)), Bn = cross(Ns, Tn);
+      Ns = normalize(Tn * sm.x + Bn * sm.y + Ns * sm.z);
+    }
     const D3 alb = d3(mat.albedo[0], mat.albedo[1], mat.albedo[2]);
     if (mat.type == 0) {
       if (!s->indirect) break;
@@ -451,12 +473,7 @@ D3 radiance(const Scene& S, D3 o, D3 d, int depth, Rng& rng) {
     onb(N, Tt, Bt);
     const D3 wo = -d, wo_l = d3(dot(wo, Tt), dot(wo, Bt), dot(wo, N));
     D3 col = alb;
-    if (mat.diffuseTex >= 0) {
-      const float* uv0 = s->uvs + 2 * (size_t)ix[0];
-      const float* uv1 = s->uvs + 2 * (size_t)ix[1];
-      const float* uv2 = s->uvs + 2 * (size_t)ix[2];
-      col = texel(s, mat.diffuseTex, uv0[0] * b0 + uv1[0] * b1 + uv2[0] * b2, uv0[1] * b0 + uv1[1] * b1 + uv2[1] * b2, true);
-    }
+    if (mat.diffuseTex >= 0) col = texel(s, mat.diffuseTex, tu, tv, true);
     const double a = r2a(mat.roughness);
     const double u1 = rng.next(), u2 = rng.next(), u3 = rng.next();
     bool nee = false;

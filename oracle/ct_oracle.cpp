@@ -569,6 +569,7 @@ struct SceneView {
   float normal_eps, dist_eps, tri_eps;
   const QNode* qnodes;
   const uint32_t* prims;
+  int tex_filter;
 };
 
 inline float xsin(float x, int exact) { return exact ? (float)std::sin((double)x) : sinf(x); }
@@ -577,17 +578,42 @@ inline float xatan2(float y, float x, int exact) { return exact ? (float)std::at
 inline float xacos(float x, int exact) { return exact ? (float)std::acos((double)x) : acosf(x); }
 
 // Texel addressing of SceneData::getTextureColor/getTextureNormal
-// (src/Core/SceneData.cuh:81-116); NaN or out-of-range coordinates are clamped
-// to the texture (the reference would read outside it).
-inline const float* texel(const SceneView& s, int idx, float x, float y) {
-  const uint32_t w = s.tex_dims[idx * 2], h = s.tex_dims[idx * 2 + 1];
-  const float fx = x * (float)(w - 1), fy = y * (float)(h - 1);
-  const uint32_t ix = fx >= 0.0f ? (uint32_t)std::fmin(fx, (float)(w - 1)) : 0u;
-  const uint32_t iy = fy >= 0.0f ? (uint32_t)std::fmin(fy, (float)(h - 1)) : 0u;
-  const uint32_t off = s.tex_offsets[idx] + (ix + iy * w);
-  return s.tex + 4 * (size_t)off;
+// (src/Core/SceneData.cuh:81-116): grid coordinate u*(width-1); NaN or
+// out-of-range coordinates are clamped to the texture (the reference would
+// read outside it). tex_filter 1 (bilinear, not in the reference) blends the
+// four texels around the grid point, clamped at the last row/column, as
+// a + (b - a) * t per axis.
+struct T4 {
+  float v[4];
+};
+inline float grid_coord(float x, uint32_t n) {
+  const float g = x * (float)(n - 1);
+  return g >= 0.0f ? std::fmin(g, (float)(n - 1)) : 0.0f;
 }
-inline const float* tex_color(const SceneView& s, int idx, float u, float v) {
+inline T4 texel(const SceneView& s, int idx, float x, float y) {
+  const uint32_t w = s.tex_dims[idx * 2], h = s.tex_dims[idx * 2 + 1];
+  const float* base = s.tex + 4 * (size_t)s.tex_offsets[idx];
+  const float gx = grid_coord(x, w), gy = grid_coord(y, h);
+  const uint32_t ix = (uint32_t)gx, iy = (uint32_t)gy;
+  T4 o;
+  if (s.tex_filter != 1) {
+    std::memcpy(o.v, base + 4 * (size_t)(ix + iy * w), sizeof(o.v));
+    return o;
+  }
+  const uint32_t ix1 = std::min(ix + 1, w - 1), iy1 = std::min(iy + 1, h - 1);
+  const float tx = gx - (float)ix, ty = gy - (float)iy;
+  const float* c00 = base + 4 * (size_t)(ix + iy * w);
+  const float* c10 = base + 4 * (size_t)(ix1 + iy * w);
+  const float* c01 = base + 4 * (size_t)(ix + iy1 * w);
+  const float* c11 = base + 4 * (size_t)(ix1 + iy1 * w);
+  for (int k = 0; k < 4; k++) {
+    const float a = c00[k] + (c10[k] - c00[k]) * tx;
+    const float b = c01[k] + (c11[k] - c01[k]) * tx;
+    o.v[k] = a + (b - a) * ty;
+  }
+  return o;
+}
+inline T4 tex_color(const SceneView& s, int idx, float u, float v) {
   float x = std::fmod(u, 1.0f), y = std::fmod(v, 1.0f);
   if (x < 0) x += 1.0f;
   if (y < 0) y += 1.0f;
@@ -597,8 +623,8 @@ inline V3 tex_normal(const SceneView& s, int idx, float u, float v) {
   float x = u, y = v;
   if (x < 0) x += 1.0f;
   if (y < 0) y += 1.0f;
-  const float* t = texel(s, idx, x, y);
-  return normalize(v3(t[0], t[1], t[2]));
+  const T4 t = texel(s, idx, x, y);
+  return normalize(v3(t.v[0], t.v[1], t.v[2]));
 }
 // sampleToWorld = convertToLocalSpace + localToWorld (src/Core/Random.cuh:37-52)
 inline V3 sample_to_world(V3 sm, V3 n) {
@@ -695,8 +721,8 @@ void render_path(const SceneView& s, const Geo& g, int pixel, int px, int py, in
       if (s.sky_enabled) {
         const float u = 1.0f + (xatan2(r.dir.x, -r.dir.z, exact) * kOneOverPi) * 0.5f;
         const float v = 1.0f - xacos(r.dir.y, exact) * kOneOverPi;
-        const float* tc = tex_color(s, s.sky_tex, u, v);
-        const V3 c = mul(divs(r.T, r.pdf), v3(tc[0], tc[1], tc[2]));
+        const T4 tc = tex_color(s, s.sky_tex, u, v);
+        const V3 c = mul(divs(r.T, r.pdf), v3(tc.v[0], tc.v[1], tc.v[2]));
         accum_add(acc, c);
       }
       return;
@@ -744,8 +770,8 @@ void render_path(const SceneView& s, const Geo& g, int pixel, int px, int py, in
     uint32_t sd = wang_hash((uint32_t)pixel * 16789u + frame * 1791u + (uint32_t)pathLength * 720898027u);
     V3 color = v3(mat.albedo[0], mat.albedo[1], mat.albedo[2]);
     if (mat.diffuseTex >= 0) {
-      const float* tc = tex_color(s, mat.diffuseTex, tu, tv);
-      color = v3(tc[0], tc[1], tc[2]);
+      const T4 tc = tex_color(s, mat.diffuseTex, tu, tv);
+      color = v3(tc.v[0], tc.v[1], tc.v[2]);
     }
     // convertToLocalSpace (Random.cuh:37-42): T only feeds EvaluateBSDF's unused arg
     // SampleBSDF (BSDF.h:33-63); arguments taken left to right.
@@ -929,6 +955,7 @@ struct OrSceneDesc {
   float normal_eps, dist_eps, tri_eps;
   const void* qnodes;
   const uint32_t* prims;
+  int32_t tex_filter;  // 0 nearest (reference), 1 bilinear
 };
 
 /* Camera basis for a frame, as sample() builds it (Kernel.cu:272-290). */
@@ -954,7 +981,7 @@ void or_render_frame(const OrSceneDesc* sd, const float* cam_pos, const float* c
   SceneView s{sd->verts, sd->normals, sd->center_normals, sd->uvs, sd->idx, sd->mat_idx, (const Material*)sd->materials,
               sd->lights, sd->light_count, sd->tex, sd->tex_dims, sd->tex_offsets, sd->sky_tex, sd->sky_enabled,
               sd->shadow, sd->indirect, sd->normal_eps, sd->dist_eps, sd->tri_eps, (const QNode*)sd->qnodes,
-              sd->prims};
+              sd->prims, sd->tex_filter};
   Geo g{sd->verts, sd->idx, sd->prims, (const QNode*)sd->qnodes, nullptr, sd->tri_eps};
   const V3 co = load3(cam_pos, 0), cw = load3(cam_w, 0), h = load3(hor, 0), v = load3(ver, 0);
   const int n = p_end - p_begin;

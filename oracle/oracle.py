@@ -88,7 +88,8 @@ def fp64() -> ctypes.CDLL:
 
 def render_fp64(arrays: dict, materials: np.ndarray, quad, prims, camera: dict, width: int, height: int, spp: int,
                 depth: int, textures=(), sky_tex: int = -1, sky: bool = True, shadow: bool = True,
-                indirect: bool = True, eps=(1e-5, 1e-5, 1e-3), seed: int = 1, nthreads: int = 8):
+                indirect: bool = True, eps=(1e-5, 1e-5, 1e-3), seed: int = 1, nthreads: int = 8,
+                tex_filter: int = 0):
     """FP64 Monte Carlo estimate of the full-material image: per-pixel (mean, standard error), (h*w, 3) each."""
     L = fp64()
     a = {k: np.ascontiguousarray(v) for k, v in arrays.items()}
@@ -113,7 +114,7 @@ def render_fp64(arrays: dict, materials: np.ndarray, quad, prims, camera: dict, 
         _p(a["vertices"]), _p(a["normals"]), _p(a["center_normals"]), _p(a["texcoords"]), _p(a["indices"]),
         _p(a["material_idxs"]), _p(mats), _p(li) if li is not None and li.size else None,
         0 if li is None else int(li.size), _p(texels), _p(dims), _p(offs), sky_tex,
-        int(sky and sky_tex >= 0), int(shadow), int(indirect), eps[0], eps[1], eps[2], _p(q), _p(pr))
+        int(sky and sky_tex >= 0), int(shadow), int(indirect), eps[0], eps[1], eps[2], _p(q), _p(pr), int(tex_filter))
     hor, ver = camera_basis(camera["forward"], camera["up"], camera["fov"], width, height)
     pos = np.asarray(camera["position"], np.float32)
     fw = np.asarray(camera["forward"], np.float32)
@@ -281,7 +282,7 @@ class OrSceneDesc(ctypes.Structure):
         ("materials", P), ("lights", P), ("light_count", ctypes.c_uint32), ("tex", P), ("tex_dims", P),
         ("tex_offsets", P), ("sky_tex", ctypes.c_int32), ("sky_enabled", ctypes.c_int32), ("shadow", ctypes.c_int32),
         ("indirect", ctypes.c_int32), ("normal_eps", ctypes.c_float), ("dist_eps", ctypes.c_float),
-        ("tri_eps", ctypes.c_float), ("qnodes", P), ("prims", P),
+        ("tri_eps", ctypes.c_float), ("qnodes", P), ("prims", P), ("tex_filter", ctypes.c_int32),
     ]
 
 
@@ -326,7 +327,7 @@ def camera_basis(forward, up, fov_deg, width, height):
 def render_frames(arrays: dict, materials: np.ndarray, quad, prims, camera: dict, width: int, height: int,
                   frames, depth: int, accum: np.ndarray | None = None, exact_math: bool = True,
                   textures=(), sky_tex: int = -1, sky: bool = True, shadow: bool = True, indirect: bool = True,
-                  eps=(1e-5, 1e-5, 1e-3), pixels=None, nthreads: int = 8) -> np.ndarray:
+                  eps=(1e-5, 1e-5, 1e-3), pixels=None, nthreads: int = 8, tex_filter: int = 0) -> np.ndarray:
     """Accumulate 1-spp frames (seed frame indices `frames`) into accum (h*w,4)."""
     L = lib()
     a = {k: np.ascontiguousarray(v) for k, v in arrays.items()}
@@ -353,7 +354,7 @@ def render_frames(arrays: dict, materials: np.ndarray, quad, prims, camera: dict
         _p(a["vertices"]), _p(a["normals"]), _p(a["center_normals"]), _p(a["texcoords"]), _p(a["indices"]),
         _p(a["material_idxs"]), _p(mats), _p(li) if li is not None and li.size else None,
         0 if li is None else int(li.size), _p(texels), _p(dims), _p(offs), sky_tex,
-        int(sky and sky_tex >= 0), int(shadow), int(indirect), eps[0], eps[1], eps[2], _p(q), _p(pr))
+        int(sky and sky_tex >= 0), int(shadow), int(indirect), eps[0], eps[1], eps[2], _p(q), _p(pr), int(tex_filter))
     hor, ver = camera_basis(camera["forward"], camera["up"], camera["fov"], width, height)
     pos = np.asarray(camera["position"], np.float32)
     fw = np.asarray(camera["forward"], np.float32)

@@ -25,7 +25,7 @@ def zoo(gpu_ctx, orc):
     return dict(sc=sc, cam=cam, arr=arr, scene=s, bvh=bvh)
 
 
-def _gpu_batches(gpu_ctx, z, W, H, depth, batches, frames, exact=False):
+def _gpu_batches(gpu_ctx, z, W, H, depth, batches, frames, exact=False, texture_filter=0):
     import torch
 
     from cudatracer_gb300 import _lib, api
@@ -42,6 +42,7 @@ def _gpu_batches(gpu_ctx, z, W, H, depth, batches, frames, exact=False):
             p.frame_index = 2 * (b * frames + f)
             p.shading_mode = _lib.CT_SHADE_FULL
             p.exact_math = int(exact)
+            p.texture_filter = texture_filter
             job.accumulate(z["scene"], z["bvh"], camera, p)
         torch.cuda.synchronize()
         means.append(job.accum_tensor().cpu().numpy()[:, :3].astype(np.float64) / frames)
@@ -73,3 +74,31 @@ def test_full_mode_flags_and_determinism(gpu_ctx, zoo):
     g1, _ = _gpu_batches(gpu_ctx, zoo, W, H, 4, batches=2, frames=2, exact=True)
     g2, _ = _gpu_batches(gpu_ctx, zoo, W, H, 4, batches=2, frames=2, exact=True)
     assert np.array_equal(g1, g2)
+
+
+@pytest.fixture(scope="module")
+def zoo_tex(gpu_ctx):
+    from cudatracer_gb300 import api, scenes
+
+    sc, cam = scenes.material_zoo_scene(ground_textures=(48, 40))
+    arr = scenes.scene_arrays(sc)
+    s = gpu_ctx.scene(arr, [api.Material(**m) for m in sc.materials], sc.textures, sc.skybox_texture)
+    return dict(sc=sc, cam=cam, arr=arr, scene=s, bvh=s.build_bvh_device())
+
+
+def test_full_mode_textured_bilinear_converges(gpu_ctx, orc, zoo_tex):
+    """The same 3-sigma bar with a bilinear-filtered diffuse texture and a
+    normal map on the ground (FP64 oracle filters in double)."""
+    z = zoo_tex
+    W, H, depth = 40, 30, 5
+    g, g_se = _gpu_batches(gpu_ctx, z, W, H, depth, batches=32, frames=32, texture_filter=1)
+    q, p = z["bvh"].export()
+    o, o_se = orc.render_fp64(z["arr"], orc.pack_materials(z["sc"].materials), q, p, z["cam"], W, H, 1024, depth,
+                              textures=z["sc"].textures, sky_tex=0, seed=11, tex_filter=1)
+    se = np.sqrt(g_se ** 2 + o_se ** 2)
+    live = se > 1e-7
+    zz = (g - o)[live] / se[live]
+    assert np.isfinite(g).all() and (g >= 0).all()
+    assert (np.abs(zz) > 3).mean() < 0.01
+    assert abs(zz.mean()) < 0.1
+    assert abs(g.sum() / o.sum() - 1) < 0.005

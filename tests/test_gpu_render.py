@@ -256,3 +256,35 @@ def test_loaded_model_frames_match_oracle(gpu_ctx, orc, tmp_path):
                              textures=tl.textures, sky_tex=-1, sky=False)
     assert _bad(acc, oacc).sum() == 0
     assert acc[:, :3].sum() > 0
+
+
+@pytest.fixture(scope="module")
+def textured(gpu_ctx, orc):
+    from cudatracer_gb300 import api, scenes
+
+    ts, cam = scenes.terrain_scene(grid=128, spheres=12, sky_size=(256, 128), ground_textures=(37, 29))
+    arr = scenes.scene_arrays(ts)
+    sc = gpu_ctx.scene(arr, [api.Material(**m) for m in ts.materials], ts.textures, ts.skybox_texture)
+    bvh = sc.build_bvh()
+    ob = orc.bvh_build(ts.vertices, ts.indices)
+    return dict(ts=ts, cam=cam, arr=arr, sc=sc, bvh=bvh, ob=ob, omats=orc.pack_materials(ts.materials))
+
+
+@pytest.mark.parametrize("filt", [0, 1])
+def test_textured_frames_match_oracle(gpu_ctx, orc, textured, filt):
+    """Diffuse texture + normal map on the ground, nearest (the reference's
+    lookup) and bilinear: exact frames agree with the oracle within 1e-4."""
+    W, H = 96, 64
+    _, _, acc = _render(gpu_ctx, textured, W, H, 2, 5, True, texture_filter=filt)
+    oacc = _oracle(orc, textured, W, H, 2, 5, True, tex_filter=filt)
+    assert _bad(acc, oacc).sum() == 0
+    assert (acc.view(np.int32) == oacc.view(np.int32)).all(axis=1).mean() >= 0.999
+
+
+def test_bilinear_differs_from_nearest(gpu_ctx, textured):
+    W, H = 96, 64
+    _, _, a = _render(gpu_ctx, textured, W, H, 1, 3, True, texture_filter=0)
+    _, _, b = _render(gpu_ctx, textured, W, H, 1, 3, True, texture_filter=1)
+    assert not np.array_equal(a, b)
+    with pytest.raises(Exception):
+        _render(gpu_ctx, textured, W, H, 1, 3, True, texture_filter=7)
