@@ -28,6 +28,7 @@ SOURCES = {
     "mesh_io.cpp": [],
     "k_trace.cu": [],
     "bvh_gpu.cu": [],
+    "k_trace_wide.cu": [],
     "k_shade_exact.cu": ["-fmad=false"],
     "k_shade_fast.cu": [],
     "noalloc.cu": [],

@@ -19,7 +19,7 @@ STATUS_NAMES = {
     4: "CT_ERR_UNSUPPORTED", 5: "CT_ERR_TIMEOUT", 6: "CT_ERR_STACK_OVERFLOW", 7: "CT_ERR_NO_DEVICE",
 }
 globals().update({name: code for code, name in STATUS_NAMES.items()})
-CT_BVH_BINARY, CT_BVH_QUAD = 0, 1
+CT_BVH_BINARY, CT_BVH_QUAD, CT_BVH_WIDE8_Q8 = 0, 1, 2
 CT_SHADE_COMPAT, CT_SHADE_FULL = 0, 1
 CT_TEX_NEAREST, CT_TEX_BILINEAR = 0, 1
 
@@ -105,6 +105,8 @@ SIGNATURES = {
     "ct_host_bvh_export": (c_int32, [P, c_int32, P, P]),
     "ct_host_bvh_destroy": (c_int32, [P]),
     "ct_bvh_build_device": (c_int32, [P, P, P, PP]),
+    "ct_bvh_build_wide": (c_int32, [P, P, P, PP]),
+    "ct_bvh_wide_stats": (c_int32, [P, P, POINTER(c_uint64), POINTER(c_uint64), POINTER(c_uint64), c_int32]),
     "ct_mesh_load_obj": (c_int32, [c_char_p, c_int32, PP]),
     "ct_mesh_info": (c_int32, [P, POINTER(c_uint32), POINTER(c_uint32), POINTER(c_uint32)]),
     "ct_mesh_arrays": (c_int32, [P, P, P, P, P, P]),

@@ -399,6 +399,15 @@ class Scene:
         check(self.ctx.lib.ct_bvh_build_device(self.ctx.h, self.h, s, ctypes.byref(h)), self.ctx.h)
         return BVH(self, h)
 
+    def build_bvh_wide(self, stream=None) -> "BVH":
+        """8-wide BVH with 8-bit quantised child bounds for ray queries
+        (ct_bvh_build_wide): FP32 watertight tests settled in FP64 where FP32
+        cannot decide, so queries return the FP64 closest hit."""
+        h = ctypes.c_void_p()
+        s = None if stream is None else getattr(stream, "cuda_stream", stream)
+        check(self.ctx.lib.ct_bvh_build_wide(self.ctx.h, self.h, s, ctypes.byref(h)), self.ctx.h)
+        return BVH(self, h)
+
     def import_quad(self, nodes: np.ndarray, prims: np.ndarray) -> "BVH":
         nodes = np.ascontiguousarray(nodes)
         prims = np.ascontiguousarray(prims, np.uint32)
@@ -432,12 +441,19 @@ class BVH:
 
     def export(self, layout=_lib.CT_BVH_QUAD):
         inf = self.info()
-        n = inf["quad_node_count"] if layout == _lib.CT_BVH_QUAD else inf["binary_node_count"]
-        rec = 128 if layout == _lib.CT_BVH_QUAD else 32
+        n = inf["binary_node_count"] if layout == _lib.CT_BVH_BINARY else inf["quad_node_count"]
+        rec = {_lib.CT_BVH_BINARY: 32, _lib.CT_BVH_QUAD: 128, _lib.CT_BVH_WIDE8_Q8: 80}[layout]
         nodes = np.zeros(n * rec // 4, np.int32)
         prims = np.zeros(inf["prim_count"], np.uint32)
         check(self.ctx.lib.ct_bvh_export(self.h, layout, ptr(nodes), ptr(prims)))
         return nodes.reshape(n, rec // 4), prims
+
+    def wide_stats(self, reset: bool = False) -> dict:
+        """Query counters of a wide BVH: rays, FP64 re-tests, full FP64 traversals."""
+        a, b, c = ctypes.c_uint64(), ctypes.c_uint64(), ctypes.c_uint64()
+        check(self.ctx.lib.ct_bvh_wide_stats(self.ctx.h, self.h, ctypes.byref(a), ctypes.byref(b), ctypes.byref(c),
+                                             int(reset)), self.ctx.h)
+        return {"rays": a.value, "fp64_retests": b.value, "fp64_full": c.value}
 
     def trace_closest(self, org, dir, hit=None, t=None, tri_eps=1e-3, stream=None):
         """org/dir: (n,4) float32 CUDA tensors (dir.w = initial t). Returns (hit, t)."""

@@ -129,6 +129,10 @@ struct ct_bvh {
   int device = 0;
   void* d_quad = nullptr;
   uint32_t* d_prims = nullptr;
+  // 8-wide quantised tree (ct_bvh_build_wide): queries only
+  bool wide = false;
+  DevWBVH wdev{};
+  unsigned long long* d_wstats = nullptr;  // rays, FP64 re-tests, full FP64 traversals
 };
 
 struct ct_render {
@@ -556,6 +560,109 @@ ct_status ct_bvh_build_device(ct_ctx* ctx, const ct_scene* scene, void* stream, 
   return cleanup(CT_OK);
 }
 
+ct_status ct_bvh_build_wide(ct_ctx* ctx, const ct_scene* scene, void* stream, ct_bvh** out) {
+  if (!ctx || !scene || !out) return fail(ctx, CT_ERR_INVALID_ARGUMENT, "null argument");
+  *out = nullptr;
+  const uint32_t n = scene->nt;
+  if (n == 0 || n > (1u << 30)) return fail(ctx, CT_ERR_INVALID_ARGUMENT, "triangle count out of range for the device builder");
+  ct_status s = set_device(ctx);
+  if (s != CT_OK) return s;
+  cudaStream_t st = (cudaStream_t)stream;
+  const auto t0 = std::chrono::high_resolution_clock::now();
+  Allocs scratch_allocs;
+  void* scratch = nullptr;
+  void* scratch2 = nullptr;
+  uint32_t* hc = nullptr;
+  auto* b = new ct_bvh();
+  auto cleanup = [&](ct_status r) {
+    if (st) cudaStreamSynchronize(st);
+    else cudaDeviceSynchronize();
+    free_all(ctx, scratch_allocs);
+    if (hc) cudaFreeHost(hc);
+    if (r != CT_OK) {
+      free_all(ctx, b->allocs);
+      delete b;
+    }
+    return r;
+  };
+  if ((s = dev_alloc(ctx, scratch_allocs, &scratch, gpu_bvh_scratch_bytes(n))) != CT_OK) return cleanup(s);
+  cudaError_t e = cudaMallocHost((void**)&hc, 64);
+  if (e != cudaSuccess) return cleanup(cuda_fail(ctx, e, "cudaMallocHost"));
+  GpuBvhResult r;
+  e = gpu_bvh_build(scene->dev, scratch, hc, st, r, 1);
+  if (e != cudaSuccess) return cleanup(cuda_fail(ctx, e, "device BVH build"));
+  if (r.error & 1u)
+    return cleanup(fail(ctx, CT_ERR_UNSUPPORTED,
+                        "wide BVH build: a node of more than 2,048 primitives has no separating plane "
+                        "(coincident centroids) or the scene's extent makes the SAH cost overflow"));
+  if (r.error) return cleanup(fail(ctx, CT_ERR_CUDA, "wide BVH build: internal check failed (code " +
+                                                         std::to_string(r.error) + ")"));
+  const auto t1 = std::chrono::high_resolution_clock::now();
+  void* tris = nullptr;
+  void* stats = nullptr;
+  if ((s = dev_alloc(ctx, b->allocs, &tris, (size_t)n * 3 * sizeof(float4))) != CT_OK) return cleanup(s);
+  if ((s = upload(ctx, b->allocs, (unsigned long long**)&stats, nullptr, 4 * sizeof(unsigned long long))) != CT_OK)
+    return cleanup(s);
+  if ((s = dev_alloc(ctx, scratch_allocs, &scratch2, gpu_wbvh_scratch_bytes(r.binary_nodes))) != CT_OK)
+    return cleanup(s);
+  uint32_t nw = 0, depth = 0, werr = 0;
+  e = gpu_wbvh_collapse(scene->dev, scratch, scratch2, r.binary_nodes, (float4*)tris, hc, st, &nw, &depth, &werr);
+  if (e != cudaSuccess) return cleanup(cuda_fail(ctx, e, "wide BVH collapse"));
+  if (werr) return cleanup(fail(ctx, CT_ERR_UNSUPPORTED, "wide BVH collapse failed (code " + std::to_string(werr) +
+                                                              "): a leaf needs more than 8 slots or a box did not quantise"));
+  void* nodes = nullptr;
+  if ((s = dev_alloc(ctx, b->allocs, &nodes, (size_t)nw * sizeof(WNode8))) != CT_OK) return cleanup(s);
+  e = gpu_wbvh_copy_nodes(scratch2, r.binary_nodes, (WNode8*)nodes, nw, st);
+  if (e != cudaSuccess) return cleanup(cuda_fail(ctx, e, "wide BVH copy"));
+  e = st ? cudaStreamSynchronize(st) : cudaDeviceSynchronize();
+  if (e != cudaSuccess) return cleanup(cuda_fail(ctx, e, "wide BVH build"));
+  const auto t2 = std::chrono::high_resolution_clock::now();
+  b->wide = true;
+  b->device_built = true;
+  b->device = ctx->device;
+  b->wdev.nodes = (const WNode8*)nodes;
+  b->wdev.tris = (const float4*)tris;
+  b->wdev.node_count = nw;
+  b->wdev.prim_count = n;
+  b->wdev.depth = depth;
+  b->wdev.stack_entries = (int32_t)(7 * depth + 1);
+  b->d_wstats = (unsigned long long*)stats;
+  b->nt = n;
+  ct_bvh_info& i = b->info;
+  i.binary_node_count = r.binary_nodes;
+  i.quad_node_count = nw;
+  i.prim_count = n;
+  i.max_leaf_size = 3;
+  i.quad_depth = depth;
+  i.stack_entries = (uint32_t)b->wdev.stack_entries;
+  i.build_ms = std::chrono::duration<double, std::milli>(t1 - t0).count();
+  i.collapse_ms = std::chrono::duration<double, std::milli>(t2 - t1).count();
+  i.upload_ms = 0.0;
+  uint64_t bytes = 0;
+  for (auto& p : b->allocs.list) bytes += p.second;
+  i.device_bytes = bytes;
+  *out = b;
+  return cleanup(CT_OK);
+}
+
+ct_status ct_bvh_wide_stats(ct_ctx* ctx, const ct_bvh* bvh, uint64_t* rays, uint64_t* fp64_retests,
+                            uint64_t* fp64_full, int32_t reset) {
+  if (!ctx || !bvh || !bvh->wide) return fail(ctx, CT_ERR_INVALID_ARGUMENT, "not a wide BVH");
+  ct_status s = set_device(ctx);
+  if (s != CT_OK) return s;
+  unsigned long long h[4] = {0, 0, 0, 0};
+  CT_CUDA(ctx, cudaDeviceSynchronize());
+  CT_CUDA(ctx, cudaMemcpy(h, bvh->d_wstats, sizeof(h), cudaMemcpyDeviceToHost));
+  if (rays) *rays = h[0];
+  if (fp64_retests) *fp64_retests = h[1];
+  if (fp64_full) *fp64_full = h[2];
+  if (reset) {
+    CT_CUDA(ctx, cudaMemset(bvh->d_wstats, 0, sizeof(h)));
+    CT_CUDA(ctx, cudaStreamSynchronize(0));
+  }
+  return CT_OK;
+}
+
 ct_status ct_bvh_import_quad(ct_ctx* ctx, const ct_scene* scene, const void* nodes, uint32_t node_count,
                              const uint32_t* prim_indices, uint32_t prim_count, ct_bvh** out) {
   if (!ctx || !scene || !nodes || !prim_indices || !out) return fail(ctx, CT_ERR_INVALID_ARGUMENT, "null argument");
@@ -613,6 +720,21 @@ ct_status ct_bvh_info_get(const ct_bvh* bvh, ct_bvh_info* info) {
 
 ct_status ct_bvh_export(const ct_bvh* bvh, ct_bvh_layout layout, void* nodes, uint32_t* prim_indices) {
   if (!bvh) return CT_ERR_INVALID_ARGUMENT;
+  if (bvh->wide) {
+    if (layout != CT_BVH_WIDE8_Q8) return nodes ? CT_ERR_UNSUPPORTED : CT_OK;
+    if (cudaSetDevice(bvh->device) != cudaSuccess) return CT_ERR_CUDA;
+    if (nodes && cudaMemcpy(nodes, bvh->wdev.nodes, (size_t)bvh->wdev.node_count * sizeof(WNode8),
+                            cudaMemcpyDeviceToHost) != cudaSuccess)
+      return CT_ERR_CUDA;
+    if (prim_indices) {
+      std::vector<float4> tri((size_t)bvh->nt * 3);
+      if (cudaMemcpy(tri.data(), bvh->wdev.tris, tri.size() * sizeof(float4), cudaMemcpyDeviceToHost) != cudaSuccess)
+        return CT_ERR_CUDA;
+      for (uint32_t i = 0; i < bvh->nt; i++) std::memcpy(&prim_indices[i], &tri[3 * (size_t)i].w, 4);
+    }
+    return CT_OK;
+  }
+  if (layout == CT_BVH_WIDE8_Q8) return nodes ? CT_ERR_UNSUPPORTED : CT_OK;
   if (bvh->device_built) {
     if (layout == CT_BVH_BINARY) return nodes ? CT_ERR_UNSUPPORTED : CT_OK;
     if (layout != CT_BVH_QUAD) return CT_ERR_INVALID_ARGUMENT;
@@ -706,6 +828,11 @@ ct_status ct_trace_closest(ct_ctx* ctx, const ct_bvh* bvh, const float* org, con
   ct_status s = check_rays(ctx, bvh, org, dir, n);
   if (s != CT_OK) return s;
   if (n && (!hit || !t)) return fail(ctx, CT_ERR_INVALID_ARGUMENT, "null output buffer");
+  if (bvh->wide) {
+    CT_CUDA(ctx, launch_trace_wide_closest(bvh->wdev, (const float4*)org, (const float4*)dir, hit, t, n, ctx->d_error,
+                                           ctx->d_cursor, bvh->d_wstats, (cudaStream_t)stream));
+    return CT_OK;
+  }
   CT_CUDA(ctx, launch_trace_closest(bvh->dev, (const float4*)org, (const float4*)dir, hit, t, n, tri_eps, ctx->d_error,
                                     ctx->d_cursor, (cudaStream_t)stream));
   return CT_OK;
@@ -716,6 +843,11 @@ ct_status ct_trace_any(ct_ctx* ctx, const ct_bvh* bvh, const float* org, const f
   ct_status s = check_rays(ctx, bvh, org, dir, n);
   if (s != CT_OK) return s;
   if (n && !occluded) return fail(ctx, CT_ERR_INVALID_ARGUMENT, "null output buffer");
+  if (bvh->wide) {
+    CT_CUDA(ctx, launch_trace_wide_any(bvh->wdev, (const float4*)org, (const float4*)dir, occluded, n, ctx->d_error,
+                                       ctx->d_cursor, bvh->d_wstats, (cudaStream_t)stream));
+    return CT_OK;
+  }
   CT_CUDA(ctx, launch_trace_any(bvh->dev, (const float4*)org, (const float4*)dir, occluded, n, tri_eps, ctx->d_error,
                                 ctx->d_cursor, (cudaStream_t)stream));
   return CT_OK;
@@ -814,6 +946,7 @@ ct_status ct_render_accumulate(ct_ctx* ctx, const ct_scene* scene, const ct_bvh*
   if (p->width != r->w || p->height != r->h) return fail(ctx, CT_ERR_INVALID_ARGUMENT, "params size differs from the render job's");
   if (p->max_depth < 1 || p->max_depth > 64) return fail(ctx, CT_ERR_INVALID_ARGUMENT, "max_depth must be in [1, 64]");
   if (bvh->nt != scene->nt) return fail(ctx, CT_ERR_INVALID_ARGUMENT, "BVH was built for another scene");
+  if (bvh->wide) return fail(ctx, CT_ERR_UNSUPPORTED, "frames trace quad BVHs; the wide BVH serves ray queries");
   if (p->shading_mode != CT_SHADE_COMPAT && p->shading_mode != CT_SHADE_FULL)
     return fail(ctx, CT_ERR_INVALID_ARGUMENT, "unknown shading mode");
   if (p->texture_filter != CT_TEX_NEAREST && p->texture_filter != CT_TEX_BILINEAR)
@@ -894,6 +1027,7 @@ ct_status ct_render_accumulate_noalloc(ct_ctx* ctx, const ct_scene* scene, const
                     std::to_string(noalloc_max_pixels()) + " (CT_NOALLOC_MAX_PIXELS)");
   if (p->max_depth < 1 || p->max_depth > 64) return fail(ctx, CT_ERR_INVALID_ARGUMENT, "max_depth must be in [1, 64]");
   if (bvh->nt != scene->nt) return fail(ctx, CT_ERR_INVALID_ARGUMENT, "BVH was built for another scene");
+  if (bvh->wide) return fail(ctx, CT_ERR_UNSUPPORTED, "frames trace quad BVHs; the wide BVH serves ray queries");
   if (p->shading_mode != CT_SHADE_COMPAT && p->shading_mode != CT_SHADE_FULL)
     return fail(ctx, CT_ERR_INVALID_ARGUMENT, "unknown shading mode");
   if (p->texture_filter != CT_TEX_NEAREST && p->texture_filter != CT_TEX_BILINEAR)

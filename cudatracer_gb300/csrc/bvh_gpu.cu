@@ -248,17 +248,19 @@ __global__ void k_init(uint32_t* counters) {
 
 __global__ void __launch_bounds__(256) k_prep(const float4* __restrict__ v, const uint4* __restrict__ idx, uint32_t n,
                                               float4* __restrict__ lo, float4* __restrict__ hi,
-                                              uint32_t* __restrict__ prims, uint32_t* counters) {
+                                              uint32_t* __restrict__ prims, uint32_t* counters, int wide) {
   const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
   uint32_t kmn[3] = {fkey(1e34f), fkey(1e34f), fkey(1e34f)}, kmx[3] = {fkey(-1e34f), fkey(-1e34f), fkey(-1e34f)};
   if (i < n) {
     const uint4 t = idx[i];
     const float4 a = v[t.x], b = v[t.y], c = v[t.z];
-    // triangle::getBounds (src/Core/Triangle.cuh:59-65): min - 0.001, max + 0.01
-    const float mn[3] = {__fsub_rn(gmin(a.x, gmin(b.x, c.x)), 0.001f), __fsub_rn(gmin(a.y, gmin(b.y, c.y)), 0.001f),
-                         __fsub_rn(gmin(a.z, gmin(b.z, c.z)), 0.001f)};
-    const float mx[3] = {__fadd_rn(gmax(a.x, gmax(b.x, c.x)), 0.01f), __fadd_rn(gmax(a.y, gmax(b.y, c.y)), 0.01f),
-                         __fadd_rn(gmax(a.z, gmax(b.z, c.z)), 0.01f)};
+    // triangle::getBounds (src/Core/Triangle.cuh:59-65): min - 0.001, max + 0.01; the
+    // wide tree bounds the triangles exactly
+    const float plo = wide ? 0.0f : 0.001f, phi = wide ? 0.0f : 0.01f;
+    const float mn[3] = {__fsub_rn(gmin(a.x, gmin(b.x, c.x)), plo), __fsub_rn(gmin(a.y, gmin(b.y, c.y)), plo),
+                         __fsub_rn(gmin(a.z, gmin(b.z, c.z)), plo)};
+    const float mx[3] = {__fadd_rn(gmax(a.x, gmax(b.x, c.x)), phi), __fadd_rn(gmax(a.y, gmax(b.y, c.y)), phi),
+                         __fadd_rn(gmax(a.z, gmax(b.z, c.z)), phi)};
     lo[i] = make_float4(mn[0], mn[1], mn[2], 0.0f);
     hi[i] = make_float4(mx[0], mx[1], mx[2], 0.0f);
     prims[i] = i;
@@ -354,7 +356,7 @@ __device__ __forceinline__ void classify(int32_t id, uint32_t count, int32_t dep
 
 __global__ void __launch_bounds__(256) k_split(BNode* arena, const int32_t* __restrict__ large, uint32_t nl,
                                                const uint32_t* __restrict__ gbins, Split* split, int32_t* next_large,
-                                               int32_t* small, uint32_t* counters, uint32_t cap) {
+                                               int32_t* small, uint32_t* counters, uint32_t cap, int wide) {
   const uint32_t s = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
   const int lane = threadIdx.x & 31;
   if (s >= nl) return;  // whole warp
@@ -364,12 +366,13 @@ __global__ void __launch_bounds__(256) k_split(BNode* arena, const int32_t* __re
   const int best = choose_split(gbins + (size_t)s * kBinWords, lane, c);
   const float parent_cost = __fmul_rn(area3(nd.mn, nd.mx), __uint2float_rn((uint32_t)nd.count));
   if (best == 32) {
-    // no candidate below 1e34: a leaf unless the parent's cost is not below it either
-    if (!(parent_cost < 1e34f) && lane == 0) atomicOr(&counters[kError], kErrDegenerate);
+    // no candidate below 1e34: a leaf unless the parent's cost is not below it
+    // either (the wide tree must split every node above 3 primitives)
+    if ((wide || !(parent_cost < 1e34f)) && lane == 0) atomicOr(&counters[kError], kErrDegenerate);
     return;
   }
   bcast_cand(c, best);
-  if (parent_cost < c.cost) return;
+  if (!wide && parent_cost < c.cost) return;
   if (lane != 0) return;
   const int a = best / kPlanes, i = best % kPlanes + 1;
   const uint32_t cid = atomicAdd(&counters[kArenaCount], 2u);
@@ -487,11 +490,35 @@ __global__ void __launch_bounds__(256) k_part_copy(const Chunk* __restrict__ chu
   for (uint32_t k = ch.begin + threadIdx.x; k < ch.end; k += blockDim.x) prims[k] = tmp[k];
 }
 
+// Halve [first, first + count) in its current order; child boxes by warp reductions.
+__device__ __forceinline__ void median_split(const float4* lo, const float4* hi, const uint32_t* prims,
+                                             uint32_t first, uint32_t count, int lane, Cand& c) {
+  c.lc = count / 2;
+  c.rc = count - c.lc;
+  for (int side = 0; side < 2; side++) {
+    const uint32_t b = side ? c.lc : 0u, e = side ? count : c.lc;
+    uint32_t kmn[3] = {fkey(1e34f), fkey(1e34f), fkey(1e34f)}, kmx[3] = {fkey(-1e34f), fkey(-1e34f), fkey(-1e34f)};
+    for (uint32_t k = b + lane; k < e; k += 32) {
+      const uint32_t p = prims[first + k];
+      const float4 l = lo[p], h = hi[p];
+      kmn[0] = min(kmn[0], fkey(l.x)), kmn[1] = min(kmn[1], fkey(l.y)), kmn[2] = min(kmn[2], fkey(l.z));
+      kmx[0] = max(kmx[0], fkey(h.x)), kmx[1] = max(kmx[1], fkey(h.y)), kmx[2] = max(kmx[2], fkey(h.z));
+    }
+    for (int k = 0; k < 3; k++) {
+      const float mn = unkey(__reduce_min_sync(0xffffffffu, kmn[k]));
+      const float mx = unkey(__reduce_max_sync(0xffffffffu, kmx[k]));
+      if (side) c.rmn[k] = mn, c.rmx[k] = mx;
+      else c.lmn[k] = mn, c.lmx[k] = mx;
+    }
+  }
+  c.cost = 0.0f;
+}
+
 // ---------------------------------------------------------------- small subtrees, one warp each
 __global__ void __launch_bounds__(kSmallWarps * 32) k_small(BNode* arena, const int32_t* __restrict__ small,
                                                             const uint32_t* counters_ro, const float4* __restrict__ lo,
                                                             const float4* __restrict__ hi, uint32_t* prims,
-                                                            uint32_t* counters, uint32_t cap) {
+                                                            uint32_t* counters, uint32_t cap, int wide) {
   __shared__ uint32_t sbins[kSmallWarps][kBinWords];
   __shared__ float splanes[kSmallWarps][3 * kPlanes];
   __shared__ int32_t sstack[kSmallWarps][kSmallStack];
@@ -524,21 +551,25 @@ __global__ void __launch_bounds__(kSmallWarps * 32) k_small(BNode* arena, const 
       Cand c;
       const int best = choose_split(bins, lane, c);
       const float parent_cost = __fmul_rn(area3(nd.mn, nd.mx), __uint2float_rn(count));
-      if (best == 32) {
+      if (best == 32 && wide) {
+        // every centroid in one interval on all axes: halve the range as it lies
+        median_split(lo, hi, prims, first, count, lane, c);
+      } else if (best == 32) {
         if (!(parent_cost < 1e34f) && lane == 0) atomicOr(&counters[kError], kErrDegenerate);
         continue;
+      } else {
+        bcast_cand(c, best);
+        if (!wide && parent_cost < c.cost) continue;
       }
-      bcast_cand(c, best);
-      if (parent_cost < c.cost) continue;
-      const int a = best / kPlanes;
-      const float coord = planes[best];
-      // stable partition through shared memory
+      const int a = best == 32 ? 0 : best / kPlanes;
+      const float coord = best == 32 ? 0.0f : planes[best];
+      // stable partition through shared memory (the halving keeps the order)
       uint32_t nl = 0, nr = 0;
       for (uint32_t k0 = 0; k0 < count; k0 += 32) {
         const uint32_t k = k0 + lane;
         const bool in = k < count;
         const uint32_t p = in ? prims[first + k] : 0u;
-        const bool left = in && goes_left(lo, hi, p, a, coord);
+        const bool left = in && (best == 32 ? k < c.lc : goes_left(lo, hi, p, a, coord));
         const uint32_t bl = __ballot_sync(0xffffffffu, left), br = __ballot_sync(0xffffffffu, in && !left);
         if (left) tmp[nl + __popc(bl & lt)] = p;
         else if (in) tmp[kWarpMax + nr + __popc(br & lt)] = p;
@@ -711,7 +742,7 @@ unsigned blocks(uint64_t n, unsigned per) { return (unsigned)((n + per - 1) / pe
 size_t gpu_bvh_scratch_bytes(uint32_t n) { return Layout(n).total; }
 
 cudaError_t gpu_bvh_build(const DevScene& sc, void* scratch, uint32_t* host_counters, cudaStream_t s,
-                          GpuBvhResult& r) {
+                          GpuBvhResult& r, int wide) {
   const uint32_t n = sc.tri_count;
   const Layout L(n);
   uint32_t* counters = at<uint32_t>(scratch, L.counters);
@@ -731,7 +762,7 @@ cudaError_t gpu_bvh_build(const DevScene& sc, void* scratch, uint32_t* host_coun
   uint32_t* qidx = at<uint32_t>(scratch, L.qidx);
 
   k_init<<<1, 32, 0, s>>>(counters);
-  k_prep<<<blocks(n, 256), 256, 0, s>>>(sc.verts, sc.idx, n, lo, hi, prims, counters);
+  k_prep<<<blocks(n, 256), 256, 0, s>>>(sc.verts, sc.idx, n, lo, hi, prims, counters, wide);
   k_root<<<1, 1, 0, s>>>(arena, large[0], small, n, counters);
   GB_TRY(cudaGetLastError());
   GB_TRY(cudaMemcpyAsync(host_counters, counters, 4 * kCounterWords, cudaMemcpyDeviceToHost, s));
@@ -746,7 +777,7 @@ cudaError_t gpu_bvh_build(const DevScene& sc, void* scratch, uint32_t* host_coun
     const unsigned nchunk = (unsigned)std::min<uint64_t>((uint64_t)n / kChunk + nl + 1, L.max_chunks);
     k_bin<<<nchunk, 256, 0, s>>>(arena, large[cur], chunks, counters, lo, hi, prims, bins);
     k_split<<<blocks((uint64_t)nl * 32, 256), 256, 0, s>>>(arena, large[cur], nl, bins, split, large[cur ^ 1], small,
-                                                          counters, L.cap);
+                                                          counters, L.cap, wide);
     k_part_count<<<nchunk, 256, 0, s>>>(chunks, split, counters, lo, hi, prims, chunk_left);
     k_part_offsets<<<blocks((uint64_t)nl * 32, 256), 256, 0, s>>>(arena, large[cur], nl, split, chunk_left, chunk_loff,
                                                                  counters);
@@ -764,7 +795,7 @@ cudaError_t gpu_bvh_build(const DevScene& sc, void* scratch, uint32_t* host_coun
   if (nsmall > 0 && !host_counters[kError]) {
     const int sms = sm_count();
     const unsigned g = (unsigned)std::min<uint64_t>(blocks(nsmall, kSmallWarps), (uint64_t)sms * 8);
-    k_small<<<g, kSmallWarps * 32, 0, s>>>(arena, small, counters, lo, hi, prims, counters, L.cap);
+    k_small<<<g, kSmallWarps * 32, 0, s>>>(arena, small, counters, lo, hi, prims, counters, L.cap, wide);
     GB_TRY(cudaGetLastError());
   }
   GB_TRY(cudaMemsetAsync(arrive, 0, 4 * (size_t)L.cap, s));
@@ -807,6 +838,218 @@ cudaError_t gpu_bvh_emit(const DevScene& sc, void* scratch, const GpuBvhResult& 
   k_tris<<<blocks(n, 256), 256, 0, s>>>(sc.verts, sc.idx, prims, n, tris);
   GB_TRY(cudaGetLastError());
   GB_TRY(cudaMemcpyAsync(prims_out, prims, 4 * (size_t)n, cudaMemcpyDeviceToDevice, s));
+  return cudaSuccess;
+}
+
+
+// ================================================================ 8-wide quantised collapse
+namespace {
+
+enum WCounter : int { kWideCount = 0, kWidePrims = 1, kWideNext = 2, kWideError = 3, kWideCounterWords = 8 };
+enum : uint32_t { kWErrSlots = 1, kWErrCapacity = 2, kWErrQuant = 4 };
+
+struct WEntry {
+  uint32_t wide, bin;
+};
+
+struct WLayout {
+  size_t nodes, list0, list1, counters, total;
+  uint32_t cap;
+  explicit WLayout(uint32_t binary_nodes) {
+    cap = binary_nodes / 2 + 2;  // inner binary nodes + the root
+    size_t o = 0;
+    auto take = [&](size_t bytes) {
+      const size_t a = o;
+      o += (bytes + 255) & ~(size_t)255;
+      return a;
+    };
+    nodes = take(sizeof(WNode8) * (size_t)cap);
+    list0 = take(sizeof(WEntry) * (size_t)cap);
+    list1 = take(sizeof(WEntry) * (size_t)cap);
+    counters = take(4 * kWideCounterWords);
+    total = o;
+  }
+};
+
+__device__ __forceinline__ uint32_t leaf_slots(int32_t count) { return count <= 0 ? 1u : (uint32_t)(count + 2) / 3u; }
+__device__ __forceinline__ float pow2(int biased) { return __int_as_float(biased << 23); }
+
+// Smallest biased exponent whose 255 steps from p reach hi (fma as the traversal evaluates it).
+__device__ __forceinline__ int quant_exponent(float p, float hi) {
+  const float ext = __fsub_rn(hi, p);
+  int e = 1;
+  if (ext > 0.0f) {
+    int k = 0;
+    frexpf(__fdiv_rn(ext, 255.0f), &k);
+    e = max(1, min(254, k + 127));
+  }
+  while (e < 254 && __fmaf_rn(pow2(e), 255.0f, p) < hi) e++;
+  return e;
+}
+
+// Outward 8-bit bounds of [lo, hi] on the grid p + s*q; false if none fits.
+__device__ __forceinline__ bool quantise(float p, float s, float lo, float hi, uint8_t& qlo, uint8_t& qhi) {
+  float fl = floorf(__fdiv_rn(__fsub_rn(lo, p), s)), fh = ceilf(__fdiv_rn(__fsub_rn(hi, p), s));
+  int ql = (int)fminf(fmaxf(fl, 0.0f), 255.0f), qh = (int)fminf(fmaxf(fh, 0.0f), 255.0f);
+  while (ql > 0 && __fmaf_rn(s, (float)ql, p) > lo) ql--;
+  while (qh < 255 && __fmaf_rn(s, (float)qh, p) < hi) qh++;
+  qlo = (uint8_t)ql, qhi = (uint8_t)qh;
+  return __fmaf_rn(s, (float)ql, p) <= lo && __fmaf_rn(s, (float)qh, p) >= hi;
+}
+
+__global__ void __launch_bounds__(128) k_wcollapse(const BNode* __restrict__ arena, const uint32_t* __restrict__ bprims,
+                                                   const float4* __restrict__ v, const uint4* __restrict__ idx,
+                                                   const WEntry* __restrict__ in, uint32_t n_in, WEntry* out,
+                                                   uint32_t* counters, WNode8* wn, float4* wtris, uint32_t cap,
+                                                   uint32_t n_prims) {
+  const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n_in) return;
+  const WEntry en = in[i];
+  const BNode b = arena[en.bin];
+  // frontier of binary nodes under this wide node, in left-to-right order;
+  // open the inner entry of largest surface area while the slots last
+  int32_t F[8];
+  int nf = 0;
+  if (b.left < 0) {
+    F[nf++] = (int32_t)en.bin;
+  } else {
+    F[nf++] = b.left;
+    F[nf++] = b.left + 1;
+  }
+  auto usage = [&](int32_t x) {
+    const BNode& c = arena[x];
+    return c.left >= 0 ? 1u : leaf_slots(c.count);
+  };
+  uint32_t used = 0;
+  for (int k = 0; k < nf; k++) used += usage(F[k]);
+  while (true) {
+    int bi = -1;
+    float ba = -1.0f;
+    for (int k = 0; k < nf; k++) {
+      const BNode& c = arena[F[k]];
+      if (c.left < 0) continue;
+      const float a = area3(c.mn, c.mx);
+      if (a > ba) ba = a, bi = k;
+    }
+    if (bi < 0) break;
+    const int32_t l = arena[F[bi]].left;
+    const uint32_t nu = used - 1 + usage(l) + usage(l + 1);
+    if (nu > 8) break;
+    for (int k = nf; k > bi + 1; k--) F[k] = F[k - 1];
+    F[bi] = l;
+    F[bi + 1] = l + 1;
+    nf++;
+    used = nu;
+  }
+  if (used > 8) {
+    atomicOr(&counters[kWideError], kWErrSlots);
+    return;
+  }
+  uint32_t n_int = 0, n_tri = 0;
+  for (int k = 0; k < nf; k++) {
+    const BNode& c = arena[F[k]];
+    if (c.left >= 0) n_int++;
+    else n_tri += (uint32_t)c.count;
+  }
+  const uint32_t child_base = n_int ? atomicAdd(&counters[kWideCount], n_int) : 0u;
+  const uint32_t prim_base = n_tri ? atomicAdd(&counters[kWidePrims], n_tri) : 0u;
+  const uint32_t out_base = n_int ? atomicAdd(&counters[kWideNext], n_int) : 0u;
+  if (child_base + n_int > cap || prim_base + n_tri > n_prims || out_base + n_int > cap) {
+    atomicOr(&counters[kWideError], kWErrCapacity);
+    return;
+  }
+  WNode8 w;
+  memset(&w, 0, sizeof(w));
+  const float p[3] = {b.mn[0], b.mn[1], b.mn[2]};
+  float sc[3];
+  for (int a = 0; a < 3; a++) {
+    const int e = quant_exponent(p[a], b.mx[a]);
+    w.e[a] = (uint8_t)e;
+    sc[a] = pow2(e);
+  }
+  w.px = p[0], w.py = p[1], w.pz = p[2];
+  w.child_base = child_base;
+  w.prim_base = prim_base;
+  bool ok = true;
+  int slot = 0;
+  uint32_t rank = 0, off = 0;
+  for (int k = 0; k < nf; k++) {
+    const BNode& c = arena[F[k]];
+    if (c.left >= 0) {
+      for (int a = 0; a < 3; a++) ok &= quantise(p[a], sc[a], c.mn[a], c.mx[a], w.qlo[a][slot], w.qhi[a][slot]);
+      w.meta[slot] = (uint8_t)(0x80u | rank);
+      w.imask |= (uint8_t)(1u << slot);
+      out[out_base + rank] = WEntry{child_base + rank, (uint32_t)F[k]};
+      rank++, slot++;
+      continue;
+    }
+    for (int32_t j = 0; j < c.count; j += 3) {
+      const int cnt = min(3, c.count - j);
+      float mn[3] = {1e34f, 1e34f, 1e34f}, mx[3] = {-1e34f, -1e34f, -1e34f};
+      for (int t = 0; t < cnt; t++) {
+        const uint32_t prim = bprims[c.first + j + t];
+        const uint4 ti = idx[prim];
+        const float4 a = v[ti.x], bb = v[ti.y], cc = v[ti.z];
+        mn[0] = fminf(mn[0], fminf(a.x, fminf(bb.x, cc.x))), mx[0] = fmaxf(mx[0], fmaxf(a.x, fmaxf(bb.x, cc.x)));
+        mn[1] = fminf(mn[1], fminf(a.y, fminf(bb.y, cc.y))), mx[1] = fmaxf(mx[1], fmaxf(a.y, fmaxf(bb.y, cc.y)));
+        mn[2] = fminf(mn[2], fminf(a.z, fminf(bb.z, cc.z))), mx[2] = fmaxf(mx[2], fmaxf(a.z, fmaxf(bb.z, cc.z)));
+        float4* o = wtris + 3 * (size_t)(prim_base + off + t);
+        o[0] = make_float4(a.x, a.y, a.z, __uint_as_float(prim));
+        o[1] = make_float4(bb.x, bb.y, bb.z, 0.0f);
+        o[2] = make_float4(cc.x, cc.y, cc.z, 0.0f);
+      }
+      for (int a = 0; a < 3; a++) ok &= quantise(p[a], sc[a], mn[a], mx[a], w.qlo[a][slot], w.qhi[a][slot]);
+      w.meta[slot] = (uint8_t)(((uint32_t)cnt << 5) | off);
+      off += (uint32_t)cnt;
+      slot++;
+    }
+  }
+  if (!ok) atomicOr(&counters[kWideError], kWErrQuant);
+  wn[en.wide] = w;
+}
+
+}  // namespace
+
+size_t gpu_wbvh_scratch_bytes(uint32_t binary_nodes) { return WLayout(binary_nodes).total; }
+
+cudaError_t gpu_wbvh_collapse(const DevScene& sc, void* scratch, void* scratch2, uint32_t binary_nodes, float4* tris,
+                              uint32_t* host_counters, cudaStream_t s, uint32_t* wide_nodes, uint32_t* depth,
+                              uint32_t* error) {
+  const uint32_t n = sc.tri_count;
+  const Layout L(n);
+  const WLayout W(binary_nodes);
+  const BNode* arena = at<BNode>(scratch, L.arena);
+  const uint32_t* bprims = at<uint32_t>(scratch, L.prims);
+  WNode8* wn = at<WNode8>(scratch2, W.nodes);
+  WEntry* lists[2] = {at<WEntry>(scratch2, W.list0), at<WEntry>(scratch2, W.list1)};
+  uint32_t* counters = at<uint32_t>(scratch2, W.counters);
+  const uint32_t init[kWideCounterWords] = {1, 0, 0, 0, 0, 0, 0, 0};
+  const WEntry root{0, 0};
+  GB_TRY(cudaMemcpyAsync(counters, init, sizeof(init), cudaMemcpyHostToDevice, s));
+  GB_TRY(cudaMemcpyAsync(lists[0], &root, sizeof(root), cudaMemcpyHostToDevice, s));
+  uint32_t n_in = 1, levels = 0;
+  int cur = 0;
+  while (n_in > 0) {
+    GB_TRY(cudaMemsetAsync(counters + kWideNext, 0, 4, s));
+    k_wcollapse<<<blocks(n_in, 128), 128, 0, s>>>(arena, bprims, sc.verts, sc.idx, lists[cur], n_in, lists[cur ^ 1],
+                                                  counters, wn, tris, W.cap, n);
+    GB_TRY(cudaGetLastError());
+    GB_TRY(cudaMemcpyAsync(host_counters, counters, 4 * kWideCounterWords, cudaMemcpyDeviceToHost, s));
+    GB_TRY(cudaStreamSynchronize(s));
+    levels++;
+    if (host_counters[kWideError]) break;
+    n_in = host_counters[kWideNext];
+    cur ^= 1;
+  }
+  *wide_nodes = host_counters[kWideCount];
+  *depth = levels;
+  *error = host_counters[kWideError] | (host_counters[kWidePrims] != n ? kWErrCapacity : 0u);
+  return cudaSuccess;
+}
+
+cudaError_t gpu_wbvh_copy_nodes(void* scratch2, uint32_t binary_nodes, WNode8* out, uint32_t count, cudaStream_t s) {
+  const WLayout W(binary_nodes);
+  GB_TRY(cudaMemcpyAsync(out, at<WNode8>(scratch2, W.nodes), sizeof(WNode8) * (size_t)count, cudaMemcpyDeviceToDevice, s));
   return cudaSuccess;
 }
 

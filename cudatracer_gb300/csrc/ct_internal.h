@@ -31,6 +31,35 @@ constexpr int32_t kEmptyChild = -1;
 // The edges are the exact float differences the reference forms per test
 // (src/Core/Triangle.cuh:15-16), precomputed once.
 
+// 8-wide node with 8-bit child bounds, 80 bytes (five LDG.128). A child box
+// is lo = fma(2^(e - 127), qlo, p), hi = fma(2^(e - 127), qhi, p) per axis,
+// rounded outward when built, so it contains the child's exact bounds.
+//   meta[i] == 0          empty slot
+//   meta[i] & 0x80        inner child: node child_base + (meta & 7)
+//   otherwise             leaf: (meta >> 5) triangles (1..3) from prim_base + (meta & 31)
+struct __align__(16) WNode8 {
+  float px, py, pz;
+  uint8_t e[3];
+  uint8_t imask;
+  uint32_t child_base;
+  uint32_t prim_base;
+  uint8_t meta[8];
+  uint8_t qlo[3][8];
+  uint8_t qhi[3][8];
+};
+static_assert(sizeof(WNode8) == 80, "WNode8 is 80 bytes");
+
+// Triangles of the wide tree in leaf order, 48 bytes: {p0, prim id}, {p1, 0}, {p2, 0}
+// (raw vertices: the watertight test shears them per ray).
+struct DevWBVH {
+  const WNode8* nodes;
+  const float4* tris;
+  uint32_t node_count;
+  uint32_t prim_count;
+  uint32_t depth;          // levels of wide nodes
+  int32_t stack_entries;   // 7 per level + 1
+};
+
 struct DevBVH {
   const QNodeDev* nodes;
   const float4* tris;  // 3 float4 per leaf slot
@@ -134,9 +163,31 @@ struct GpuBvhResult {
   uint32_t levels = 0, small_roots = 0;
 };
 size_t gpu_bvh_scratch_bytes(uint32_t n);
-cudaError_t gpu_bvh_build(const DevScene& sc, void* scratch, uint32_t* host_counters, cudaStream_t s, GpuBvhResult& r);
+// wide = 1: the rules of the 8-wide quantised tree (exact triangle bounds, every
+// node above 3 primitives split, halving where no plane separates centroids).
+cudaError_t gpu_bvh_build(const DevScene& sc, void* scratch, uint32_t* host_counters, cudaStream_t s, GpuBvhResult& r,
+                          int wide = 0);
 cudaError_t gpu_bvh_emit(const DevScene& sc, void* scratch, const GpuBvhResult& r, uint32_t leaf_shift, void* quad,
                          QNodeDev* nodes, float4* tris, uint32_t* prims, cudaStream_t s);
+
+// Collapse of a wide-rule binary build (gpu_bvh_build with wide = 1) into
+// 8-wide quantised nodes. `scratch2` holds gpu_wbvh_scratch_bytes(binary_nodes);
+// nodes end up in scratch2 (read back their count in *wide_nodes, then copy
+// them out with gpu_wbvh_copy_nodes); triangles go straight to `tris` (n x 48 B).
+size_t gpu_wbvh_scratch_bytes(uint32_t binary_nodes);
+cudaError_t gpu_wbvh_collapse(const DevScene& sc, void* scratch, void* scratch2, uint32_t binary_nodes, float4* tris,
+                              uint32_t* host_counters, cudaStream_t s, uint32_t* wide_nodes, uint32_t* depth,
+                              uint32_t* error);
+cudaError_t gpu_wbvh_copy_nodes(void* scratch2, uint32_t binary_nodes, WNode8* out, uint32_t count, cudaStream_t s);
+
+// Wide-tree queries: FP32 watertight tests; hits within the FP32 error bound
+// of an edge or of another hit's t are settled by FP64 tests. stats (may be
+// null): [0] rays, [1] rays re-tested in FP64, [2] rays traced fully in FP64.
+cudaError_t launch_trace_wide_closest(const DevWBVH& b, const float4* org, const float4* dir, int32_t* hit, float* t,
+                                      uint32_t n, uint32_t* err, int* cursor, unsigned long long* stats,
+                                      cudaStream_t s);
+cudaError_t launch_trace_wide_any(const DevWBVH& b, const float4* org, const float4* dir, uint8_t* occ, uint32_t n,
+                                  uint32_t* err, int* cursor, unsigned long long* stats, cudaStream_t s);
 
 cudaError_t launch_fold(float4* accum, float4* frame, int n, cudaStream_t s);
 

@@ -1,0 +1,433 @@
+// Ray queries on the 8-wide quantised BVH (WNode8).
+//
+// Boxes: child bounds decoded as fma(2^e, q, p), which the builder rounded
+// outward, and a slab test whose far distance is scaled by 1 + 2*gamma(3)
+// (Ize 2013, "Robust BVH ray traversal"), so no box that the ray touches in
+// exact arithmetic is rejected.
+//
+// Triangles: the watertight test of Woop, Benthin and Wald (JCGT 2013) in FP32:
+// shear to ray space, edge functions U, V, W, no epsilon. Each edge function
+// carries a first-order bound of its FP32 rounding error (from the magnitudes
+// of its operands). A triangle is a certain hit when all three functions
+// exceed their bounds with one sign, a certain miss when two exceed them with
+// opposite signs, and uncertain otherwise. Uncertain triangles, and certain
+// hits whose t lies within the combined t error bound of the best hit, are
+// kept as candidates (up to kCand per ray); after traversal the best hit and
+// the candidates are re-tested with the same algorithm in FP64 and the
+// nearest FP64 hit wins (equal t: lower primitive id). A best hit whose t
+// error bound exceeds 4e-6 relative is re-tested the same way, so reported t
+// stay within 1e-5 of FP64. A ray with more candidates is traced again
+// entirely in FP64. The result therefore equals an FP64 watertight closest
+// hit over all triangles.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+
+#include "ct_internal.h"
+
+namespace ct {
+namespace {
+
+constexpr int kWStack = 128;  // local-memory stack entries per thread
+constexpr int kCand = 8;
+constexpr float kU = 5.9604645e-08f;          // 2^-24
+constexpr float kFarScale = 1.00000036f;      // 1 + 2 * gamma(3), gamma(n) = n u / (1 - n u)
+constexpr float kTRel = 4e-6f;                // a best hit whose t bound exceeds this (relative) is re-tested in FP64
+
+struct WRay {
+  float ox, oy, oz, dx, dy, dz;
+  float ix, iy, iz;   // reciprocal direction (zero components replaced by a huge value)
+  int kx, ky, kz;     // watertight axis permutation
+  float Sx, Sy, Sz;   // shear constants
+  float tmax;
+};
+
+__device__ __forceinline__ float comp3(float x, float y, float z, int k) { return k == 0 ? x : (k == 1 ? y : z); }
+
+__device__ __forceinline__ float safe_rcp(float d) {
+  return fabsf(d) > 1e-30f ? __frcp_rn(d) : copysignf(1e30f, d);
+}
+
+__device__ __forceinline__ void setup(const float4 o, const float4 d, WRay& r) {
+  r.ox = o.x, r.oy = o.y, r.oz = o.z, r.dx = d.x, r.dy = d.y, r.dz = d.z, r.tmax = d.w;
+  r.ix = safe_rcp(d.x), r.iy = safe_rcp(d.y), r.iz = safe_rcp(d.z);
+  const float ax = fabsf(d.x), ay = fabsf(d.y), az = fabsf(d.z);
+  r.kz = (ax > ay) ? (ax > az ? 0 : 2) : (ay > az ? 1 : 2);
+  r.kx = r.kz == 2 ? 0 : r.kz + 1;
+  r.ky = r.kx == 2 ? 0 : r.kx + 1;
+  if (comp3(d.x, d.y, d.z, r.kz) < 0.0f) {
+    const int t = r.kx;
+    r.kx = r.ky;
+    r.ky = t;
+  }
+  const float dz = comp3(d.x, d.y, d.z, r.kz);
+  r.Sx = __fdiv_rn(comp3(d.x, d.y, d.z, r.kx), dz);
+  r.Sy = __fdiv_rn(comp3(d.x, d.y, d.z, r.ky), dz);
+  r.Sz = __frcp_rn(dz);
+}
+
+// FP32 watertight test. Returns 0 certain miss, 1 certain hit, 2 uncertain;
+// t and terr (bound on |t - t_exact|) are set for 1 and 2 (for an uncertain
+// edge-on triangle t = 0, terr = +inf: any distance is possible).
+__device__ __forceinline__ int tri32(const WRay& r, const float4& a4, const float4& b4, const float4& c4, float& t,
+                                     float& terr) {
+  // ray-relative vertices, permuted to (kx, ky, kz), and magnitudes bounding their rounding
+  const float akx = comp3(a4.x, a4.y, a4.z, r.kx) - comp3(r.ox, r.oy, r.oz, r.kx);
+  const float aky = comp3(a4.x, a4.y, a4.z, r.ky) - comp3(r.ox, r.oy, r.oz, r.ky);
+  const float akz = comp3(a4.x, a4.y, a4.z, r.kz) - comp3(r.ox, r.oy, r.oz, r.kz);
+  const float bkx = comp3(b4.x, b4.y, b4.z, r.kx) - comp3(r.ox, r.oy, r.oz, r.kx);
+  const float bky = comp3(b4.x, b4.y, b4.z, r.ky) - comp3(r.ox, r.oy, r.oz, r.ky);
+  const float bkz = comp3(b4.x, b4.y, b4.z, r.kz) - comp3(r.ox, r.oy, r.oz, r.kz);
+  const float ckx = comp3(c4.x, c4.y, c4.z, r.kx) - comp3(r.ox, r.oy, r.oz, r.kx);
+  const float cky = comp3(c4.x, c4.y, c4.z, r.ky) - comp3(r.ox, r.oy, r.oz, r.ky);
+  const float ckz = comp3(c4.x, c4.y, c4.z, r.kz) - comp3(r.ox, r.oy, r.oz, r.kz);
+  const float mo_x = fabsf(comp3(r.ox, r.oy, r.oz, r.kx)), mo_y = fabsf(comp3(r.ox, r.oy, r.oz, r.ky));
+  const float mo_z = fabsf(comp3(r.ox, r.oy, r.oz, r.kz));
+  const float mAkx = fabsf(comp3(a4.x, a4.y, a4.z, r.kx)) + mo_x, mAky = fabsf(comp3(a4.x, a4.y, a4.z, r.ky)) + mo_y;
+  const float mAkz = fabsf(comp3(a4.x, a4.y, a4.z, r.kz)) + mo_z;
+  const float mBkx = fabsf(comp3(b4.x, b4.y, b4.z, r.kx)) + mo_x, mBky = fabsf(comp3(b4.x, b4.y, b4.z, r.ky)) + mo_y;
+  const float mBkz = fabsf(comp3(b4.x, b4.y, b4.z, r.kz)) + mo_z;
+  const float mCkx = fabsf(comp3(c4.x, c4.y, c4.z, r.kx)) + mo_x, mCky = fabsf(comp3(c4.x, c4.y, c4.z, r.ky)) + mo_y;
+  const float mCkz = fabsf(comp3(c4.x, c4.y, c4.z, r.kz)) + mo_z;
+  const float Ax = akx - r.Sx * akz, Ay = aky - r.Sy * akz;
+  const float Bx = bkx - r.Sx * bkz, By = bky - r.Sy * bkz;
+  const float Cx = ckx - r.Sx * ckz, Cy = cky - r.Sy * ckz;
+  const float aSx = fabsf(r.Sx), aSy = fabsf(r.Sy);
+  const float mAx = mAkx + aSx * mAkz, mAy = mAky + aSy * mAkz;
+  const float mBx = mBkx + aSx * mBkz, mBy = mBky + aSy * mBkz;
+  const float mCx = mCkx + aSx * mCkz, mCy = mCky + aSy * mCkz;
+  const float U = Cx * By - Cy * Bx;
+  const float V = Ax * Cy - Ay * Cx;
+  const float W = Bx * Ay - By * Ax;
+  // 4x the first-order bound: 3u per sheared coordinate, 2u for the products and difference
+  const float eU = (12.0f * kU) * (fabsf(Cx) * mBy + fabsf(By) * mCx + fabsf(Cy) * mBx + fabsf(Bx) * mCy) +
+                   (8.0f * kU) * (fabsf(Cx * By) + fabsf(Cy * Bx));
+  const float eV = (12.0f * kU) * (fabsf(Ax) * mCy + fabsf(Cy) * mAx + fabsf(Ay) * mCx + fabsf(Cx) * mAy) +
+                   (8.0f * kU) * (fabsf(Ax * Cy) + fabsf(Ay * Cx));
+  const float eW = (12.0f * kU) * (fabsf(Bx) * mAy + fabsf(Ay) * mBx + fabsf(By) * mAx + fabsf(Ax) * mBy) +
+                   (8.0f * kU) * (fabsf(Bx * Ay) + fabsf(By * Ax));
+  const bool up = U > eU, un = U < -eU, vp = V > eV, vn = V < -eV, wp = W > eW, wn = W < -eW;
+  if ((up || vp || wp) && (un || vn || wn)) return 0;
+  const bool certain = (up && vp && wp) || (un && vn && wn);
+  const float det = U + V + W;
+  if (!certain && fabsf(det) <= eU + eV + eW) {
+    t = 0.0f;
+    terr = __int_as_float(0x7f800000);
+    return 2;
+  }
+  const float Az = r.Sz * akz, Bz = r.Sz * bkz, Cz = r.Sz * ckz;
+  const float T = U * Az + V * Bz + W * Cz;
+  t = __fdiv_rn(T, det);
+  // t = Az + (V (Bz - Az) + W (Cz - Az)) / det: weight errors times the depth spread
+  const float spread = fmaxf(fabsf(Bz - Az), fabsf(Cz - Az));
+  const float mz = fabsf(r.Sz) * fmaxf(mAkz, fmaxf(mBkz, mCkz));
+  terr = 2.0f * (eU + eV + eW) * spread / fabsf(det) + (16.0f * kU) * (fabsf(t) + mz);
+  return certain ? 1 : 2;
+}
+
+__device__ __forceinline__ double comp3d(double x, double y, double z, int k) { return k == 0 ? x : (k == 1 ? y : z); }
+
+// The same test in FP64 (no contraction), the arbiter for candidates.
+__device__ __forceinline__ bool tri64(double ox, double oy, double oz, int kx, int ky, int kz, double Sx, double Sy,
+                                      double Sz, const float4& a4, const float4& b4, const float4& c4, double& t) {
+  const double akx = __dsub_rn(comp3d(a4.x, a4.y, a4.z, kx), comp3d(ox, oy, oz, kx));
+  const double aky = __dsub_rn(comp3d(a4.x, a4.y, a4.z, ky), comp3d(ox, oy, oz, ky));
+  const double akz = __dsub_rn(comp3d(a4.x, a4.y, a4.z, kz), comp3d(ox, oy, oz, kz));
+  const double bkx = __dsub_rn(comp3d(b4.x, b4.y, b4.z, kx), comp3d(ox, oy, oz, kx));
+  const double bky = __dsub_rn(comp3d(b4.x, b4.y, b4.z, ky), comp3d(ox, oy, oz, ky));
+  const double bkz = __dsub_rn(comp3d(b4.x, b4.y, b4.z, kz), comp3d(ox, oy, oz, kz));
+  const double ckx = __dsub_rn(comp3d(c4.x, c4.y, c4.z, kx), comp3d(ox, oy, oz, kx));
+  const double cky = __dsub_rn(comp3d(c4.x, c4.y, c4.z, ky), comp3d(ox, oy, oz, ky));
+  const double ckz = __dsub_rn(comp3d(c4.x, c4.y, c4.z, kz), comp3d(ox, oy, oz, kz));
+  const double Ax = __dsub_rn(akx, __dmul_rn(Sx, akz)), Ay = __dsub_rn(aky, __dmul_rn(Sy, akz));
+  const double Bx = __dsub_rn(bkx, __dmul_rn(Sx, bkz)), By = __dsub_rn(bky, __dmul_rn(Sy, bkz));
+  const double Cx = __dsub_rn(ckx, __dmul_rn(Sx, ckz)), Cy = __dsub_rn(cky, __dmul_rn(Sy, ckz));
+  const double U = __dsub_rn(__dmul_rn(Cx, By), __dmul_rn(Cy, Bx));
+  const double V = __dsub_rn(__dmul_rn(Ax, Cy), __dmul_rn(Ay, Cx));
+  const double W = __dsub_rn(__dmul_rn(Bx, Ay), __dmul_rn(By, Ax));
+  if ((U < 0.0 || V < 0.0 || W < 0.0) && (U > 0.0 || V > 0.0 || W > 0.0)) return false;
+  const double det = __dadd_rn(__dadd_rn(U, V), W);
+  if (det == 0.0) return false;
+  const double Az = __dmul_rn(Sz, akz), Bz = __dmul_rn(Sz, bkz), Cz = __dmul_rn(Sz, ckz);
+  const double T = __dadd_rn(__dadd_rn(__dmul_rn(U, Az), __dmul_rn(V, Bz)), __dmul_rn(W, Cz));
+  t = __ddiv_rn(T, det);
+  return t > 0.0;
+}
+
+struct Ray64 {
+  double ox, oy, oz, Sx, Sy, Sz, tmax;
+  int kx, ky, kz;
+};
+__device__ __forceinline__ Ray64 ray64(const WRay& r) {
+  Ray64 q;
+  q.ox = r.ox, q.oy = r.oy, q.oz = r.oz;
+  q.kx = r.kx, q.ky = r.ky, q.kz = r.kz;
+  const double dkz = comp3d(r.dx, r.dy, r.dz, r.kz);
+  q.Sx = __ddiv_rn(comp3d(r.dx, r.dy, r.dz, r.kx), dkz);
+  q.Sy = __ddiv_rn(comp3d(r.dx, r.dy, r.dz, r.ky), dkz);
+  q.Sz = __ddiv_rn(1.0, dkz);
+  q.tmax = r.tmax;
+  return q;
+}
+__device__ __forceinline__ bool tri64(const Ray64& q, const float4* tris, uint32_t slot, double& t) {
+  const float4* tr = tris + 3 * (size_t)slot;
+  return tri64(q.ox, q.oy, q.oz, q.kx, q.ky, q.kz, q.Sx, q.Sy, q.Sz, __ldg(tr), __ldg(tr + 1), __ldg(tr + 2), t) &&
+         t < q.tmax;
+}
+
+struct NodeBoxes {
+  float px, py, pz, sx, sy, sz;
+};
+
+// Slab test of slot i; returns the entry distance or +inf when missed.
+__device__ __forceinline__ float slot_box(const WRay& r, const WNode8& n, const NodeBoxes& nb, int i, float tfar) {
+  const float lx = __fmaf_rn(nb.sx, (float)n.qlo[0][i], nb.px), hx = __fmaf_rn(nb.sx, (float)n.qhi[0][i], nb.px);
+  const float ly = __fmaf_rn(nb.sy, (float)n.qlo[1][i], nb.py), hy = __fmaf_rn(nb.sy, (float)n.qhi[1][i], nb.py);
+  const float lz = __fmaf_rn(nb.sz, (float)n.qlo[2][i], nb.pz), hz = __fmaf_rn(nb.sz, (float)n.qhi[2][i], nb.pz);
+  const float t0x = (lx - r.ox) * r.ix, t1x = (hx - r.ox) * r.ix;
+  const float t0y = (ly - r.oy) * r.iy, t1y = (hy - r.oy) * r.iy;
+  const float t0z = (lz - r.oz) * r.iz, t1z = (hz - r.oz) * r.iz;
+  const float tn = fmaxf(fmaxf(fminf(t0x, t1x), fminf(t0y, t1y)), fmaxf(fminf(t0z, t1z), 0.0f));
+  const float tf = fminf(fminf(fmaxf(t0x, t1x), fmaxf(t0y, t1y)), fminf(fmaxf(t0z, t1z), tfar)) * kFarScale;
+  return tn <= tf ? tn : __int_as_float(0x7f800000);
+}
+
+__device__ __forceinline__ void load_node(const WNode8* nodes, uint32_t i, WNode8& n, NodeBoxes& nb) {
+  const float4* s = reinterpret_cast<const float4*>(nodes + i);
+  float4* d = reinterpret_cast<float4*>(&n);
+#pragma unroll
+  for (int k = 0; k < 5; k++) d[k] = __ldg(s + k);
+  nb.px = n.px, nb.py = n.py, nb.pz = n.pz;
+  nb.sx = __int_as_float((int)n.e[0] << 23);
+  nb.sy = __int_as_float((int)n.e[1] << 23);
+  nb.sz = __int_as_float((int)n.e[2] << 23);
+}
+
+__device__ __forceinline__ uint32_t meta_at(const WNode8& n, int i) {
+  const uint32_t* w = reinterpret_cast<const uint32_t*>(n.meta);
+  return ((i < 4 ? w[0] : w[1]) >> (8 * (i & 3))) & 0xffu;
+}
+
+// Whole traversal in FP64 triangle tests (boxes as above, culled with the FP64
+// best distance rounded up): the fallback for rays with too many candidates.
+template <bool ANY>
+__device__ bool trace_fp64(const DevWBVH& b, const WRay& r, uint32_t* st_node, float* st_t, uint32_t* err, int& best,
+                           double& tb) {
+  const Ray64 q = ray64(r);
+  best = -1;
+  tb = q.tmax;
+  int sp = 0;
+  st_node[sp] = 0, st_t[sp] = 0.0f, sp++;
+  while (sp > 0) {
+    sp--;
+    const uint32_t ni = st_node[sp];
+    const float far = __double2float_ru(tb) * kFarScale;
+    if (st_t[sp] > far) continue;
+    WNode8 n;
+    NodeBoxes nb;
+    load_node(b.nodes, ni, n, nb);
+    for (int i = 0; i < 8; i++) {
+      const uint32_t m = meta_at(n, i);
+      if (!m) continue;
+      const float tn = slot_box(r, n, nb, i, far);
+      if (!(tn <= far)) continue;
+      if (m & 0x80u) {
+        if (sp >= kWStack) {
+          atomicOr(err, kErrStackOverflow);
+          continue;
+        }
+        st_node[sp] = n.child_base + (m & 7u), st_t[sp] = tn, sp++;
+        continue;
+      }
+      const uint32_t cnt = m >> 5, off = m & 31u;
+      for (uint32_t k = 0; k < cnt; k++) {
+        double t;
+        const uint32_t slot = n.prim_base + off + k;
+        if (!tri64(q, b.tris, slot, t)) continue;
+        const int prim = __float_as_int(__ldg(b.tris + 3 * (size_t)slot).w);
+        if (ANY) {
+          best = prim;
+          tb = t;
+          return true;
+        }
+        if (t < tb || (t == tb && prim < best)) tb = t, best = prim;
+      }
+    }
+  }
+  return best >= 0;
+}
+
+template <bool ANY>
+__global__ void __launch_bounds__(128) k_trace_wide(const DevWBVH b, const float4* __restrict__ org,
+                                                    const float4* __restrict__ dir, int32_t* __restrict__ hit_out,
+                                                    float* __restrict__ t_out, uint8_t* __restrict__ occ_out,
+                                                    uint32_t n, uint32_t* err, int* cursor,
+                                                    unsigned long long* stats) {
+  uint32_t st_node[kWStack];
+  float st_t[kWStack];
+  const int lane = threadIdx.x & 31;
+  unsigned long long n_rays = 0, n_retest = 0, n_full = 0;
+  while (true) {
+    int base = 0;
+    if (lane == 0) base = atomicAdd(cursor, 32);
+    base = __shfl_sync(0xffffffffu, base, 0);
+    if ((uint32_t)base >= n) break;
+    const uint32_t ri = (uint32_t)base + lane;
+    if (ri >= n) continue;
+    n_rays++;
+    WRay r;
+    setup(__ldg(org + ri), __ldg(dir + ri), r);
+    int best = -1;                    // leaf slot of the certain best hit
+    float tb = r.tmax, tberr = 0.0f;  // its t and t error bound
+    uint32_t cand[kCand];
+    int nc = 0;
+    bool overflow = false, occluded = false;
+    int sp = 0;
+    st_node[sp] = 0, st_t[sp] = 0.0f, sp++;
+    while (sp > 0) {
+      sp--;
+      const uint32_t ni = st_node[sp];
+      const float far = (tb + tberr) * kFarScale;
+      if (st_t[sp] > far) continue;
+      WNode8 nd;
+      NodeBoxes nb;
+      load_node(b.nodes, ni, nd, nb);
+      const int sp0 = sp;
+      uint32_t leaves = 0;
+#pragma unroll
+      for (int i = 0; i < 8; i++) {
+        const uint32_t m = meta_at(nd, i);
+        if (!m) continue;
+        const float tn = slot_box(r, nd, nb, i, far);
+        if (!(tn <= far)) continue;
+        if (m & 0x80u) {
+          if (sp < kWStack) st_node[sp] = nd.child_base + (m & 7u), st_t[sp] = tn, sp++;
+          else atomicOr(err, kErrStackOverflow);
+        } else {
+          leaves |= 1u << i;
+        }
+      }
+      // nearest pushed child on top
+      if (sp - sp0 > 1) {
+        int bi = sp0;
+        for (int k = sp0 + 1; k < sp; k++)
+          if (st_t[k] < st_t[bi]) bi = k;
+        const uint32_t tnode = st_node[bi];
+        const float tt = st_t[bi];
+        st_node[bi] = st_node[sp - 1], st_t[bi] = st_t[sp - 1];
+        st_node[sp - 1] = tnode, st_t[sp - 1] = tt;
+      }
+      while (leaves) {
+        const int i = __ffs(leaves) - 1;
+        leaves &= leaves - 1;
+        const uint32_t m = meta_at(nd, i);
+        const uint32_t cnt = m >> 5, off = m & 31u;
+        for (uint32_t k = 0; k < cnt; k++) {
+          const uint32_t slot = nd.prim_base + off + k;
+          const float4* tr = b.tris + 3 * (size_t)slot;
+          float t, terr;
+          const int res = tri32(r, __ldg(tr), __ldg(tr + 1), __ldg(tr + 2), t, terr);
+          if (res == 0) continue;
+          if (res == 1 && t - terr > 0.0f && t + terr < tb - tberr) {
+            // certainly in range and certainly nearer than the best so far
+            best = (int)slot, tb = t, tberr = terr;
+            if (ANY) {
+              occluded = true;
+              break;
+            }
+            continue;
+          }
+          if (!(t - terr < tb + tberr)) continue;  // certainly beyond the best (or the ray's end)
+          if (res == 1 && t - terr > 0.0f && t < tb && t + terr < tb + tberr) {
+            // a certain hit nearer than the best within their errors: FP64 orders them
+            if (best >= 0) {
+              if (nc < kCand) cand[nc++] = (uint32_t)best;
+              else overflow = true;
+            }
+            best = (int)slot, tb = t, tberr = terr;
+            continue;
+          }
+          if (nc < kCand) cand[nc++] = slot;
+          else overflow = true;
+        }
+        if (ANY && occluded) break;
+      }
+      if (ANY && occluded) break;
+    }
+    int out_prim = best >= 0 ? __float_as_int(__ldg(b.tris + 3 * (size_t)best).w) : -1;
+    float out_t = best >= 0 ? tb : r.tmax;
+    if (ANY && !occluded && best >= 0) occluded = true;  // a certain hit within the ray's range
+    if (!(ANY && occluded) && overflow) {
+      n_full++;
+      double t64;
+      int prim;
+      const bool h = trace_fp64<ANY>(b, r, st_node, st_t, err, prim, t64);
+      out_prim = h ? prim : -1;
+      out_t = h ? (float)t64 : r.tmax;
+      occluded = h;
+    } else if (!(ANY && occluded) && (nc > 0 || (!ANY && best >= 0 && tberr > kTRel * tb))) {
+      // settle the candidates (and the best) in FP64
+      n_retest++;
+      const Ray64 q = ray64(r);
+      int bp = -1;
+      double bt = q.tmax;
+      auto consider = [&](uint32_t slot) {
+        double t;
+        if (!tri64(q, b.tris, slot, t)) return;
+        const int prim = __float_as_int(__ldg(b.tris + 3 * (size_t)slot).w);
+        if (t < bt || (t == bt && prim < bp)) bt = t, bp = prim;
+      };
+      if (best >= 0) consider((uint32_t)best);
+      for (int k = 0; k < nc; k++) consider(cand[k]);
+      out_prim = bp;
+      out_t = bp >= 0 ? (float)bt : r.tmax;
+      occluded = bp >= 0;
+    }
+    if (ANY) {
+      occ_out[ri] = occluded ? 1 : 0;
+    } else {
+      hit_out[ri] = out_prim;
+      t_out[ri] = out_t;
+    }
+  }
+  if (stats) {
+    atomicAdd(stats + 0, n_rays);
+    if (n_retest) atomicAdd(stats + 1, n_retest);
+    if (n_full) atomicAdd(stats + 2, n_full);
+  }
+}
+
+int wide_grid() {
+  static int g = 0;
+  if (!g) {
+    int per = 0;
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k_trace_wide<false>, 128, 0);
+    g = std::max(1, per) * sm_count();
+  }
+  return g;
+}
+
+}  // namespace
+
+cudaError_t launch_trace_wide_closest(const DevWBVH& b, const float4* org, const float4* dir, int32_t* hit, float* t,
+                                      uint32_t n, uint32_t* err, int* cursor, unsigned long long* stats,
+                                      cudaStream_t s) {
+  if (n == 0) return cudaSuccess;
+  cudaError_t e = cudaMemsetAsync(cursor, 0, sizeof(int), s);
+  if (e != cudaSuccess) return e;
+  const int g = std::min<int>(wide_grid(), (int)((n + 127) / 128));
+  k_trace_wide<false><<<g, 128, 0, s>>>(b, org, dir, hit, t, nullptr, n, err, cursor, stats);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_trace_wide_any(const DevWBVH& b, const float4* org, const float4* dir, uint8_t* occ, uint32_t n,
+                                  uint32_t* err, int* cursor, unsigned long long* stats, cudaStream_t s) {
+  if (n == 0) return cudaSuccess;
+  cudaError_t e = cudaMemsetAsync(cursor, 0, sizeof(int), s);
+  if (e != cudaSuccess) return e;
+  const int g = std::min<int>(wide_grid(), (int)((n + 127) / 128));
+  k_trace_wide<true><<<g, 128, 0, s>>>(b, org, dir, nullptr, nullptr, occ, n, err, cursor, stats);
+  return cudaGetLastError();
+}
+
+}  // namespace ct

@@ -94,7 +94,7 @@ typedef struct ct_scene_desc {
 
 /* BVH layouts. BINARY and QUAD are the reference's BVHNode (32 B) and
  * MBVHNode (128 B) trees (src/BVH/BVHNode.cuh:29-46, src/BVH/MBVHNode.cuh:35-63). */
-typedef enum ct_bvh_layout { CT_BVH_BINARY = 0, CT_BVH_QUAD = 1 } ct_bvh_layout;
+typedef enum ct_bvh_layout { CT_BVH_BINARY = 0, CT_BVH_QUAD = 1, CT_BVH_WIDE8_Q8 = 2 } ct_bvh_layout;
 
 typedef struct ct_bvh_info {
   uint32_t binary_node_count; /* 0 when the BVH was imported as a quad tree */
@@ -195,6 +195,23 @@ ct_status ct_bvh_import_binary(ct_ctx* ctx, const ct_scene* scene, const void* n
  * the SAH cost reach 1e34 (coordinates beyond ~1e14). Exports the QUAD layout
  * only (ct_bvh_export with CT_BVH_BINARY and non-NULL nodes fails). */
 ct_status ct_bvh_build_device(ct_ctx* ctx, const ct_scene* scene, void* stream, ct_bvh** out);
+/* 8-wide BVH with 8-bit quantised child bounds (no reference counterpart: the
+ * precision extension of the ray-query path). 80-byte nodes {quantisation
+ * origin p, three exponents, inner-child mask, first inner child, first
+ * triangle, 8 slot codes, 6 x 8 bytes of bounds}; child boxes are rounded
+ * outward, triangles are tested watertight in FP32 and the hits FP32 cannot
+ * settle (near an edge, near another hit's t) are re-tested in FP64, so
+ * ct_trace_closest/ct_trace_any on this tree give the FP64 closest hit (equal
+ * t: lower primitive id) and `tri_eps` is ignored. Built on the device from
+ * exact triangle bounds (every node above 3 triangles split). Frames need a
+ * quad BVH; export with CT_BVH_WIDE8_Q8 (80-byte nodes; prim_indices in leaf
+ * order). info.quad_node_count and info.quad_depth describe the wide tree. */
+ct_status ct_bvh_build_wide(ct_ctx* ctx, const ct_scene* scene, void* stream, ct_bvh** out);
+/* Counters of the wide tree's queries since the last reset: rays traced, rays
+ * whose result needed FP64 re-tests, rays traced entirely in FP64 (more than
+ * 8 unsettled triangles). Synchronises the device. */
+ct_status ct_bvh_wide_stats(ct_ctx* ctx, const ct_bvh* bvh, uint64_t* rays, uint64_t* fp64_retests,
+                            uint64_t* fp64_full, int32_t reset);
 ct_status ct_bvh_info_get(const ct_bvh* bvh, ct_bvh_info* info);
 /* Copy the host-side trees out in the reference layouts (NULL skips an array). */
 ct_status ct_bvh_export(const ct_bvh* bvh, ct_bvh_layout layout, void* nodes, uint32_t* prim_indices);

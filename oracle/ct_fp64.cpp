@@ -12,6 +12,11 @@
  * reference's sampling schemes, src/Core/Microfacet.cuh), one-light NEE with
  * the power heuristic, sky lookups (src/Core/SceneData.cuh:81-97). Converged
  * images from the GPU must agree with it within 3 standard errors.
+ *
+ * It also holds the FP64 closest-hit / any-hit oracle of the precision
+ * extension (fp64_trace): the watertight ray/triangle test of Woop, Benthin
+ * and Wald (JCGT 2013) evaluated in double, over the padded quad BVH, nearest
+ * t first and the lower primitive id on equal t.
  */
 #include <algorithm>
 #include <cmath>
@@ -572,4 +577,125 @@ void fp64_render(const Fp64Scene* desc, const float* pos, const float* cw, const
   for (auto& t : ts) t.join();
 }
 
+}  // extern "C"
+
+namespace {
+inline double c3(double x, double y, double z, int k) { return k == 0 ? x : (k == 1 ? y : z); }
+inline float c3f(float x, float y, float z, int k) { return k == 0 ? x : (k == 1 ? y : z); }
+
+struct WtRay {
+  double ox, oy, oz, Sx, Sy, Sz, tmax;
+  int kx, ky, kz;
+};
+
+// Axis choice and shear exactly as the GPU's ray setup (float comparisons).
+WtRay wt_ray(const float* o, const float* d) {
+  WtRay r;
+  r.ox = o[0], r.oy = o[1], r.oz = o[2], r.tmax = d[3];
+  const float ax = std::fabs(d[0]), ay = std::fabs(d[1]), az = std::fabs(d[2]);
+  r.kz = (ax > ay) ? (ax > az ? 0 : 2) : (ay > az ? 1 : 2);
+  r.kx = r.kz == 2 ? 0 : r.kz + 1;
+  r.ky = r.kx == 2 ? 0 : r.kx + 1;
+  if (c3f(d[0], d[1], d[2], r.kz) < 0.0f) std::swap(r.kx, r.ky);
+  const double dkz = c3f(d[0], d[1], d[2], r.kz);
+  r.Sx = (double)c3f(d[0], d[1], d[2], r.kx) / dkz;
+  r.Sy = (double)c3f(d[0], d[1], d[2], r.ky) / dkz;
+  r.Sz = 1.0 / dkz;
+  return r;
+}
+
+// Watertight test in double: the operation order of the GPU's FP64 arbiter.
+bool wt_hit(const WtRay& r, const float* a, const float* b, const float* c, double& t) {
+  const double akx = c3(a[0], a[1], a[2], r.kx) - c3(r.ox, r.oy, r.oz, r.kx);
+  const double aky = c3(a[0], a[1], a[2], r.ky) - c3(r.ox, r.oy, r.oz, r.ky);
+  const double akz = c3(a[0], a[1], a[2], r.kz) - c3(r.ox, r.oy, r.oz, r.kz);
+  const double bkx = c3(b[0], b[1], b[2], r.kx) - c3(r.ox, r.oy, r.oz, r.kx);
+  const double bky = c3(b[0], b[1], b[2], r.ky) - c3(r.ox, r.oy, r.oz, r.ky);
+  const double bkz = c3(b[0], b[1], b[2], r.kz) - c3(r.ox, r.oy, r.oz, r.kz);
+  const double ckx = c3(c[0], c[1], c[2], r.kx) - c3(r.ox, r.oy, r.oz, r.kx);
+  const double cky = c3(c[0], c[1], c[2], r.ky) - c3(r.ox, r.oy, r.oz, r.ky);
+  const double ckz = c3(c[0], c[1], c[2], r.kz) - c3(r.ox, r.oy, r.oz, r.kz);
+  const double Ax = akx - r.Sx * akz, Ay = aky - r.Sy * akz;
+  const double Bx = bkx - r.Sx * bkz, By = bky - r.Sy * bkz;
+  const double Cx = ckx - r.Sx * ckz, Cy = cky - r.Sy * ckz;
+  const double U = Cx * By - Cy * Bx;
+  const double V = Ax * Cy - Ay * Cx;
+  const double W = Bx * Ay - By * Ax;
+  if ((U < 0.0 || V < 0.0 || W < 0.0) && (U > 0.0 || V > 0.0 || W > 0.0)) return false;
+  const double det = (U + V) + W;
+  if (det == 0.0) return false;
+  const double Az = r.Sz * akz, Bz = r.Sz * bkz, Cz = r.Sz * ckz;
+  const double T = ((U * Az) + (V * Bz)) + (W * Cz);
+  t = T / det;
+  return t > 0.0 && t < r.tmax;
+}
+}  // namespace
+
+extern "C" {
+/* FP64 watertight closest hit (any_hit = 0) or occlusion (any_hit = 1) for n
+ * rays (org/dir float4, dir.w = tmax) over a quad BVH in the reference layout
+ * (padded boxes, so double slab tests lose nothing). hit: primitive or -1;
+ * t: its double distance (tmax on a miss). */
+void fp64_trace(const float* verts, const uint32_t* idx, const void* qnodes, const uint32_t* prims, const float* org,
+                const float* dir, uint32_t n, int any_hit, int32_t* hit, double* t_out, int nthreads) {
+  const QNode* Q = (const QNode*)qnodes;
+  auto work = [&](uint32_t b, uint32_t e) {
+    std::vector<int> stk(4096);
+    for (uint32_t i = b; i < e; i++) {
+      const float* o = org + 4 * (size_t)i;
+      const float* d = dir + 4 * (size_t)i;
+      const WtRay r = wt_ray(o, d);
+      const double inv[3] = {1.0 / (double)d[0], 1.0 / (double)d[1], 1.0 / (double)d[2]};
+      const double oo[3] = {o[0], o[1], o[2]};
+      int best = -1;
+      double tb = r.tmax;
+      int sp = 0;
+      stk[sp++] = 0;
+      bool done = false;
+      while (sp > 0 && !done) {
+        const QNode& nd = Q[stk[--sp]];
+        for (int c = 0; c < 4 && !done; c++) {
+          if (nd.counts[c] == 0) continue;
+          double t0 = 0.0, t1 = tb;
+          const double lo[3] = {nd.bminx[c], nd.bminy[c], nd.bminz[c]}, hi[3] = {nd.bmaxx[c], nd.bmaxy[c], nd.bmaxz[c]};
+          bool ok = true;
+          for (int a = 0; a < 3 && ok; a++) {
+            double ta = (lo[a] - oo[a]) * inv[a], tb2 = (hi[a] - oo[a]) * inv[a];
+            if (std::isnan(ta) || std::isnan(tb2)) continue;
+            if (ta > tb2) std::swap(ta, tb2);
+            t0 = std::max(t0, ta);
+            t1 = std::min(t1, tb2);
+            ok = t0 <= t1;
+          }
+          if (!ok) continue;
+          if (nd.counts[c] == -1) {
+            if (sp < (int)stk.size()) stk[sp++] = nd.childs[c];
+            continue;
+          }
+          for (int k = 0; k < nd.counts[c]; k++) {
+            const uint32_t prim = prims[nd.childs[c] + k];
+            const uint32_t* ix = idx + 3 * (size_t)prim;
+            double tt;
+            if (!wt_hit(r, verts + 3 * (size_t)ix[0], verts + 3 * (size_t)ix[1], verts + 3 * (size_t)ix[2], tt)) continue;
+            if (tt < tb || (tt == tb && (int)prim < best)) tb = tt, best = (int)prim;
+            if (any_hit) {
+              done = true;
+              break;
+            }
+          }
+        }
+      }
+      hit[i] = best;
+      t_out[i] = best >= 0 ? tb : r.tmax;
+    }
+  };
+  nthreads = std::max(1, nthreads);
+  std::vector<std::thread> ts;
+  const uint32_t chunk = (n + nthreads - 1) / nthreads;
+  for (int k = 0; k < nthreads; k++) {
+    const uint32_t b = k * chunk, e = std::min(n, b + chunk);
+    if (b < e) ts.emplace_back(work, b, e);
+  }
+  for (auto& th : ts) th.join();
+}
 }  // extern "C"

@@ -82,8 +82,25 @@ def fp64() -> ctypes.CDLL:
         L.fp64_microfacet.argtypes = [ctypes.c_int, ctypes.c_double, P, ctypes.c_double, ctypes.c_double, P, P, P]
         L.fp64_roughness_to_alpha.restype = ctypes.c_double
         L.fp64_roughness_to_alpha.argtypes = [ctypes.c_double]
+        L.fp64_trace.argtypes = [P, P, P, P, P, P, ctypes.c_uint32, ctypes.c_int, P, P, ctypes.c_int]
         _fp64 = L
     return _fp64
+
+
+def trace_fp64(vertices, indices, quad, prims, org, dir, any_hit: bool = False, nthreads: int = 8):
+    """FP64 watertight closest hit (or occlusion) over the padded quad BVH:
+    returns (hit int32, t float64); equal t resolves to the lower primitive id."""
+    v = np.ascontiguousarray(vertices, np.float32)
+    ix = np.ascontiguousarray(indices, np.uint32)
+    q = np.ascontiguousarray(quad)
+    pr = np.ascontiguousarray(prims, np.uint32)
+    o = np.ascontiguousarray(org, np.float32)
+    d = np.ascontiguousarray(dir, np.float32)
+    n = o.shape[0]
+    hit = np.empty(n, np.int32)
+    t = np.empty(n, np.float64)
+    fp64().fp64_trace(_p(v), _p(ix), _p(q), _p(pr), _p(o), _p(d), n, int(any_hit), _p(hit), _p(t), nthreads)
+    return hit, t
 
 
 def render_fp64(arrays: dict, materials: np.ndarray, quad, prims, camera: dict, width: int, height: int, spp: int,
