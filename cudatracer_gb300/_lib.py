@@ -106,7 +106,8 @@ SIGNATURES = {
     "ct_host_bvh_destroy": (c_int32, [P]),
     "ct_bvh_build_device": (c_int32, [P, P, P, PP]),
     "ct_bvh_build_wide": (c_int32, [P, P, P, PP]),
-    "ct_bvh_wide_stats": (c_int32, [P, P, POINTER(c_uint64), POINTER(c_uint64), POINTER(c_uint64), c_int32]),
+    "ct_bvh_wide_stats": (c_int32, [P, P, POINTER(c_uint64), POINTER(c_uint64), POINTER(c_uint64), POINTER(c_uint64),
+                                    c_int32]),
     "ct_mesh_load_obj": (c_int32, [c_char_p, c_int32, PP]),
     "ct_mesh_info": (c_int32, [P, POINTER(c_uint32), POINTER(c_uint32), POINTER(c_uint32)]),
     "ct_mesh_arrays": (c_int32, [P, P, P, P, P, P]),

@@ -449,11 +449,12 @@ class BVH:
         return nodes.reshape(n, rec // 4), prims
 
     def wide_stats(self, reset: bool = False) -> dict:
-        """Query counters of a wide BVH: rays, FP64 re-tests, full FP64 traversals."""
-        a, b, c = ctypes.c_uint64(), ctypes.c_uint64(), ctypes.c_uint64()
+        """Query counters of a wide BVH: rays, FP64 re-tests (of which only to
+        tighten t), full FP64 traversals."""
+        a, b, c, d = ctypes.c_uint64(), ctypes.c_uint64(), ctypes.c_uint64(), ctypes.c_uint64()
         check(self.ctx.lib.ct_bvh_wide_stats(self.ctx.h, self.h, ctypes.byref(a), ctypes.byref(b), ctypes.byref(c),
-                                             int(reset)), self.ctx.h)
-        return {"rays": a.value, "fp64_retests": b.value, "fp64_full": c.value}
+                                             ctypes.byref(d), int(reset)), self.ctx.h)
+        return {"rays": a.value, "fp64_retests": b.value, "fp64_t_only": c.value, "fp64_full": d.value}
 
     def trace_closest(self, org, dir, hit=None, t=None, tri_eps=1e-3, stream=None):
         """org/dir: (n,4) float32 CUDA tensors (dir.w = initial t). Returns (hit, t)."""

@@ -646,7 +646,7 @@ ct_status ct_bvh_build_wide(ct_ctx* ctx, const ct_scene* scene, void* stream, ct
 }
 
 ct_status ct_bvh_wide_stats(ct_ctx* ctx, const ct_bvh* bvh, uint64_t* rays, uint64_t* fp64_retests,
-                            uint64_t* fp64_full, int32_t reset) {
+                            uint64_t* fp64_t_only, uint64_t* fp64_full, int32_t reset) {
   if (!ctx || !bvh || !bvh->wide) return fail(ctx, CT_ERR_INVALID_ARGUMENT, "not a wide BVH");
   ct_status s = set_device(ctx);
   if (s != CT_OK) return s;
@@ -656,6 +656,7 @@ ct_status ct_bvh_wide_stats(ct_ctx* ctx, const ct_bvh* bvh, uint64_t* rays, uint
   if (rays) *rays = h[0];
   if (fp64_retests) *fp64_retests = h[1];
   if (fp64_full) *fp64_full = h[2];
+  if (fp64_t_only) *fp64_t_only = h[3];
   if (reset) {
     CT_CUDA(ctx, cudaMemset(bvh->d_wstats, 0, sizeof(h)));
     CT_CUDA(ctx, cudaStreamSynchronize(0));

@@ -182,7 +182,8 @@ cudaError_t gpu_wbvh_copy_nodes(void* scratch2, uint32_t binary_nodes, WNode8* o
 
 // Wide-tree queries: FP32 watertight tests; hits within the FP32 error bound
 // of an edge or of another hit's t are settled by FP64 tests. stats (may be
-// null): [0] rays, [1] rays re-tested in FP64, [2] rays traced fully in FP64.
+// null): [0] rays, [1] rays re-tested in FP64, [2] rays traced fully in FP64,
+// [3] of [1], rays re-tested only because the best hit's t bound was loose.
 cudaError_t launch_trace_wide_closest(const DevWBVH& b, const float4* org, const float4* dir, int32_t* hit, float* t,
                                       uint32_t n, uint32_t* err, int* cursor, unsigned long long* stats,
                                       cudaStream_t s);

@@ -15,8 +15,8 @@
 // kept as candidates (up to kCand per ray); after traversal the best hit and
 // the candidates are re-tested with the same algorithm in FP64 and the
 // nearest FP64 hit wins (equal t: lower primitive id). A best hit whose t
-// error bound exceeds 4e-6 relative is re-tested the same way, so reported t
-// stay within 1e-5 of FP64. A ray with more candidates is traced again
+// error bound exceeds 9e-6 relative is re-tested the same way, so reported t
+// stay within 1e-5 of the exact distance. A ray with more candidates is traced again
 // entirely in FP64. The result therefore equals an FP64 watertight closest
 // hit over all triangles.
 #include <cuda_runtime.h>
@@ -32,7 +32,7 @@ constexpr int kWStack = 128;  // local-memory stack entries per thread
 constexpr int kCand = 8;
 constexpr float kU = 5.9604645e-08f;          // 2^-24
 constexpr float kFarScale = 1.00000036f;      // 1 + 2 * gamma(3), gamma(n) = n u / (1 - n u)
-constexpr float kTRel = 4e-6f;                // a best hit whose t bound exceeds this (relative) is re-tested in FP64
+constexpr float kTRel = 9e-6f;                // a best hit whose t bound exceeds this (relative) is re-tested in FP64
 
 struct WRay {
   float ox, oy, oz, dx, dy, dz;
@@ -71,7 +71,7 @@ __device__ __forceinline__ void setup(const float4 o, const float4 d, WRay& r) {
 // edge-on triangle t = 0, terr = +inf: any distance is possible).
 __device__ __forceinline__ int tri32(const WRay& r, const float4& a4, const float4& b4, const float4& c4, float& t,
                                      float& terr) {
-  // ray-relative vertices, permuted to (kx, ky, kz), and magnitudes bounding their rounding
+  // ray-relative vertices, permuted to (kx, ky, kz)
   const float akx = comp3(a4.x, a4.y, a4.z, r.kx) - comp3(r.ox, r.oy, r.oz, r.kx);
   const float aky = comp3(a4.x, a4.y, a4.z, r.ky) - comp3(r.ox, r.oy, r.oz, r.ky);
   const float akz = comp3(a4.x, a4.y, a4.z, r.kz) - comp3(r.ox, r.oy, r.oz, r.kz);
@@ -81,14 +81,11 @@ __device__ __forceinline__ int tri32(const WRay& r, const float4& a4, const floa
   const float ckx = comp3(c4.x, c4.y, c4.z, r.kx) - comp3(r.ox, r.oy, r.oz, r.kx);
   const float cky = comp3(c4.x, c4.y, c4.z, r.ky) - comp3(r.ox, r.oy, r.oz, r.ky);
   const float ckz = comp3(c4.x, c4.y, c4.z, r.kz) - comp3(r.ox, r.oy, r.oz, r.kz);
-  const float mo_x = fabsf(comp3(r.ox, r.oy, r.oz, r.kx)), mo_y = fabsf(comp3(r.ox, r.oy, r.oz, r.ky));
-  const float mo_z = fabsf(comp3(r.ox, r.oy, r.oz, r.kz));
-  const float mAkx = fabsf(comp3(a4.x, a4.y, a4.z, r.kx)) + mo_x, mAky = fabsf(comp3(a4.x, a4.y, a4.z, r.ky)) + mo_y;
-  const float mAkz = fabsf(comp3(a4.x, a4.y, a4.z, r.kz)) + mo_z;
-  const float mBkx = fabsf(comp3(b4.x, b4.y, b4.z, r.kx)) + mo_x, mBky = fabsf(comp3(b4.x, b4.y, b4.z, r.ky)) + mo_y;
-  const float mBkz = fabsf(comp3(b4.x, b4.y, b4.z, r.kz)) + mo_z;
-  const float mCkx = fabsf(comp3(c4.x, c4.y, c4.z, r.kx)) + mo_x, mCky = fabsf(comp3(c4.x, c4.y, c4.z, r.ky)) + mo_y;
-  const float mCkz = fabsf(comp3(c4.x, c4.y, c4.z, r.kz)) + mo_z;
+  // a difference of two floats is rounded once, relative to its own value:
+  // the ray-relative coordinates carry u |x| of error
+  const float mAkx = fabsf(akx), mAky = fabsf(aky), mAkz = fabsf(akz);
+  const float mBkx = fabsf(bkx), mBky = fabsf(bky), mBkz = fabsf(bkz);
+  const float mCkx = fabsf(ckx), mCky = fabsf(cky), mCkz = fabsf(ckz);
   const float Ax = akx - r.Sx * akz, Ay = aky - r.Sy * akz;
   const float Bx = bkx - r.Sx * bkz, By = bky - r.Sy * bkz;
   const float Cx = ckx - r.Sx * ckz, Cy = cky - r.Sy * ckz;
@@ -109,19 +106,30 @@ __device__ __forceinline__ int tri32(const WRay& r, const float4& a4, const floa
   const bool up = U > eU, un = U < -eU, vp = V > eV, vn = V < -eV, wp = W > eW, wn = W < -eW;
   if ((up || vp || wp) && (un || vn || wn)) return 0;
   const bool certain = (up && vp && wp) || (un && vn && wn);
-  const float det = U + V + W;
-  if (!certain && fabsf(det) <= eU + eV + eW) {
+  // distance from the triangle's plane, t = ((a - o) . n) / (d . n) with
+  // n = (b - a) x (c - a), and a first-order bound of its rounding (x2)
+  const float e1x = b4.x - a4.x, e1y = b4.y - a4.y, e1z = b4.z - a4.z;
+  const float e2x = c4.x - a4.x, e2y = c4.y - a4.y, e2z = c4.z - a4.z;
+  const float nx = e1y * e2z - e1z * e2y, ny = e1z * e2x - e1x * e2z, nz = e1x * e2y - e1y * e2x;
+  const float enx = (6.0f * kU) * (fabsf(e1y * e2z) + fabsf(e1z * e2y));
+  const float eny = (6.0f * kU) * (fabsf(e1z * e2x) + fabsf(e1x * e2z));
+  const float enz = (6.0f * kU) * (fabsf(e1x * e2y) + fabsf(e1y * e2x));
+  const float aox = a4.x - r.ox, aoy = a4.y - r.oy, aoz = a4.z - r.oz;
+  const float num = aox * nx + aoy * ny + aoz * nz;
+  const float den = r.dx * nx + r.dy * ny + r.dz * nz;
+  const float enum_ = fabsf(aox) * enx + fabsf(aoy) * eny + fabsf(aoz) * enz +
+                      (4.0f * kU) * (fabsf(aox * nx) + fabsf(aoy * ny) + fabsf(aoz * nz));
+  const float eden = fabsf(r.dx) * enx + fabsf(r.dy) * eny + fabsf(r.dz) * enz +
+                     (3.0f * kU) * (fabsf(r.dx * nx) + fabsf(r.dy * ny) + fabsf(r.dz * nz));
+  if (!(fabsf(den) > 2.0f * eden)) {
+    // (nearly) parallel to the plane in FP32: distance unknown
     t = 0.0f;
     terr = __int_as_float(0x7f800000);
     return 2;
   }
-  const float Az = r.Sz * akz, Bz = r.Sz * bkz, Cz = r.Sz * ckz;
-  const float T = U * Az + V * Bz + W * Cz;
-  t = __fdiv_rn(T, det);
-  // t = Az + (V (Bz - Az) + W (Cz - Az)) / det: weight errors times the depth spread
-  const float spread = fmaxf(fabsf(Bz - Az), fabsf(Cz - Az));
-  const float mz = fabsf(r.Sz) * fmaxf(mAkz, fmaxf(mBkz, mCkz));
-  terr = 2.0f * (eU + eV + eW) * spread / fabsf(det) + (16.0f * kU) * (fabsf(t) + mz);
+  t = __fdiv_rn(num, den);
+  terr = fabsf(t) * (2.0f * (enum_ / fmaxf(fabsf(num), 1e-37f) + eden / fabsf(den)) + 4.0f * kU);
+  if (!(enum_ < fabsf(num))) terr = fmaxf(terr, 2.0f * enum_ / fabsf(den));  // t near zero
   return certain ? 1 : 2;
 }
 
@@ -266,7 +274,7 @@ __global__ void __launch_bounds__(128) k_trace_wide(const DevWBVH b, const float
   uint32_t st_node[kWStack];
   float st_t[kWStack];
   const int lane = threadIdx.x & 31;
-  unsigned long long n_rays = 0, n_retest = 0, n_full = 0;
+  unsigned long long n_rays = 0, n_retest = 0, n_full = 0, n_tbound = 0;
   while (true) {
     int base = 0;
     if (lane == 0) base = atomicAdd(cursor, 32);
@@ -280,6 +288,7 @@ __global__ void __launch_bounds__(128) k_trace_wide(const DevWBVH b, const float
     int best = -1;                    // leaf slot of the certain best hit
     float tb = r.tmax, tberr = 0.0f;  // its t and t error bound
     uint32_t cand[kCand];
+    float cand_lo[kCand];  // lower bound of each candidate's t
     int nc = 0;
     bool overflow = false, occluded = false;
     int sp = 0;
@@ -341,18 +350,25 @@ __global__ void __launch_bounds__(128) k_trace_wide(const DevWBVH b, const float
           if (res == 1 && t - terr > 0.0f && t < tb && t + terr < tb + tberr) {
             // a certain hit nearer than the best within their errors: FP64 orders them
             if (best >= 0) {
-              if (nc < kCand) cand[nc++] = (uint32_t)best;
+              if (nc < kCand) cand[nc] = (uint32_t)best, cand_lo[nc] = tb - tberr, nc++;
               else overflow = true;
             }
             best = (int)slot, tb = t, tberr = terr;
             continue;
           }
-          if (nc < kCand) cand[nc++] = slot;
+          if (nc < kCand) cand[nc] = slot, cand_lo[nc] = t - terr, nc++;
           else overflow = true;
         }
         if (ANY && occluded) break;
       }
       if (ANY && occluded) break;
+    }
+    // candidates recorded before a nearer certain hit was found may now be out of reach
+    if (!overflow) {
+      int k2 = 0;
+      for (int k = 0; k < nc; k++)
+        if (cand_lo[k] < tb + tberr) cand[k2] = cand[k], cand_lo[k2] = cand_lo[k], k2++;
+      nc = k2;
     }
     int out_prim = best >= 0 ? __float_as_int(__ldg(b.tris + 3 * (size_t)best).w) : -1;
     float out_t = best >= 0 ? tb : r.tmax;
@@ -368,6 +384,7 @@ __global__ void __launch_bounds__(128) k_trace_wide(const DevWBVH b, const float
     } else if (!(ANY && occluded) && (nc > 0 || (!ANY && best >= 0 && tberr > kTRel * tb))) {
       // settle the candidates (and the best) in FP64
       n_retest++;
+      n_tbound += nc == 0;
       const Ray64 q = ray64(r);
       int bp = -1;
       double bt = q.tmax;
@@ -394,6 +411,7 @@ __global__ void __launch_bounds__(128) k_trace_wide(const DevWBVH b, const float
     atomicAdd(stats + 0, n_rays);
     if (n_retest) atomicAdd(stats + 1, n_retest);
     if (n_full) atomicAdd(stats + 2, n_full);
+    if (n_tbound) atomicAdd(stats + 3, n_tbound);
   }
 }
 

@@ -208,10 +208,11 @@ ct_status ct_bvh_build_device(ct_ctx* ctx, const ct_scene* scene, void* stream, 
  * order). info.quad_node_count and info.quad_depth describe the wide tree. */
 ct_status ct_bvh_build_wide(ct_ctx* ctx, const ct_scene* scene, void* stream, ct_bvh** out);
 /* Counters of the wide tree's queries since the last reset: rays traced, rays
- * whose result needed FP64 re-tests, rays traced entirely in FP64 (more than
- * 8 unsettled triangles). Synchronises the device. */
+ * whose result needed FP64 re-tests, of those the ones re-tested only to
+ * tighten the reported t, and rays traced entirely in FP64 (more than 8
+ * unsettled triangles). NULL skips a counter. Synchronises the device. */
 ct_status ct_bvh_wide_stats(ct_ctx* ctx, const ct_bvh* bvh, uint64_t* rays, uint64_t* fp64_retests,
-                            uint64_t* fp64_full, int32_t reset);
+                            uint64_t* fp64_t_only, uint64_t* fp64_full, int32_t reset);
 ct_status ct_bvh_info_get(const ct_bvh* bvh, ct_bvh_info* info);
 /* Copy the host-side trees out in the reference layouts (NULL skips an array). */
 ct_status ct_bvh_export(const ct_bvh* bvh, ct_bvh_layout layout, void* nodes, uint32_t* prim_indices);
