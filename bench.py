@@ -50,6 +50,8 @@ def parse_args():
     ap.add_argument("--height", type=int, default=1080)
     ap.add_argument("--skip-extras", action="store_true",
                     help="only the timed frames: no e2e pass, roofline model, CPU baseline or sphere query")
+    ap.add_argument("--skip-precision", action="store_true",
+                    help="leave out the 10M-triangle precision workload (wide vs quad BVH against FP64)")
     args = ap.parse_args()
     global W, H
     W, H = args.width, args.height
@@ -270,6 +272,82 @@ def gpu_closest_hit_c1(ctx):
             "workload": "81,920-tri sphere, 256x256 pinhole rays x64, ct_trace_closest"}
 
 
+def precision_c3(ctx, ntri: int = 10_000_000, nray: int = 16_000_000, sample_every: int = 8) -> dict:
+    """The precision workload: a 10M-triangle seeded soup (centroids U[0,1]^3,
+    edges log-uniform 1e-4..1e-2) and 16M incoherent rays. Closest-hit Mrays/s
+    of the plain quad BVH (reference Moller-Trumbore, epsilon 1e-12 since the
+    reference's 1e-3 culls every soup triangle) and of the 8-wide quantised BVH
+    (watertight FP32 + FP64 settlement); ids, lost hits and t error of both
+    against the FP64 watertight oracle on every 8th ray."""
+    import numpy as np
+    import torch
+
+    import oracle
+    from cudatracer_gb300 import api, scenes
+
+    s = scenes.soup_scene(ntri, seed=3)
+    o, d = scenes.incoherent_rays(nray, seed=5)
+    arr = {"vertices": s.vertices, "normals": np.tile(np.array([[0, 0, 1]], np.float32), (s.vertices.shape[0], 1)),
+           "indices": s.indices}
+    sc = ctx.scene(arr, [api.Material()])
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    qb = sc.build_bvh_device()
+    q_ms = (time.perf_counter() - t0) * 1e3
+    t0 = time.perf_counter()
+    wb = sc.build_bvh_wide()
+    w_ms = (time.perf_counter() - t0) * 1e3
+    org, dirs = torch.from_numpy(o).cuda(), torch.from_numpy(d).cuda()
+    hit = torch.empty(nray, dtype=torch.int32, device="cuda")
+    t = torch.empty(nray, device="cuda")
+
+    def timed(fn, k=5):
+        for _ in range(3):
+            fn()
+        torch.cuda.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record()
+        for _ in range(k):
+            fn()
+        e1.record()
+        torch.cuda.synchronize()
+        return e0.elapsed_time(e1) / k
+
+    q_trace = timed(lambda: qb.trace_closest(org, dirs, hit, t, tri_eps=1e-12))
+    hq, tq = hit.cpu().numpy().copy(), t.cpu().numpy().copy()
+    wb.wide_stats(reset=True)
+    w_trace = timed(lambda: wb.trace_closest(org, dirs, hit, t))
+    st = wb.wide_stats(reset=True)
+    hw, tw = hit.cpu().numpy().copy(), t.cpu().numpy().copy()
+    ctx.check()
+    quad, prims = qb.export()
+    sel = slice(0, nray, sample_every)
+    ho, to = oracle.trace_fp64(s.vertices, s.indices, quad, prims, o[sel], d[sel], nthreads=os.cpu_count() or 1)
+
+    def against(h, tt):
+        h, tt = h[sel], tt[sel]
+        both = (h >= 0) & (h == ho)
+        rel = np.abs(tt[both].astype(np.float64) - to[both]) / to[both]
+        return {"id_mismatches": int((h != ho).sum()), "lost_hits": int(((ho >= 0) & (h < 0)).sum()),
+                "false_hits": int(((ho < 0) & (h >= 0)).sum()), "mismatch_rate": float((h != ho).mean()),
+                "max_rel_t_err": float(rel.max()) if rel.size else 0.0}
+
+    out = {
+        "workload": f"{ntri:,}-triangle soup, {nray:,} incoherent rays (origins U[0,1]^3, directions uniform)",
+        "plain_quad_fp32": {"mrays_per_s": nray / q_trace / 1e3, "build_ms": q_ms, **against(hq, tq)},
+        "wide8_q8": {"mrays_per_s": nray / w_trace / 1e3, "build_ms": w_ms, "nodes": wb.info()["quad_node_count"],
+                     "node_bytes": 80, "fp64_retest_frac": st["fp64_retests"] / max(1, st["rays"]),
+                     "fp64_full_traversals": st["fp64_full"], **against(hw, tw)},
+        "oracle_sample": f"FP64 watertight closest hit on every {sample_every}th ray ({ho.shape[0]:,} rays, "
+                         f"{int((ho >= 0).sum()):,} hits)",
+    }
+    out["speedup_wide_vs_plain"] = out["wide8_q8"]["mrays_per_s"] / out["plain_quad_fp32"]["mrays_per_s"]
+    qb.close()
+    wb.close()
+    sc.close()
+    return out
+
+
 def run_ours(args, world, rank, local):
     import numpy as np
     import torch
@@ -428,6 +506,7 @@ def run_ours(args, world, rank, local):
     full = {"msamples_per_s": W * H / full_ms / 1e3, "ms_per_frame": full_ms, "frames": full_frames,
             "shading": "full materials (Lambert, mirror, dielectric IOR 1.5, GGX) with MIS"}
     c1 = gpu_closest_hit_c1(ctx) if rank == 0 else None
+    c3 = precision_c3(ctx) if (rank == 0 and not args.skip_precision) else None
     launches = sum(v["launches"] for v in prof.values())
     line = {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
@@ -442,7 +521,7 @@ def run_ours(args, world, rank, local):
         "stage_ms": {k: v["ms"] for k, v in prof.items()},
         "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": h2d_bytes, "d2h_bytes_per_step": d2h_bytes},
         "gpu_launches": launches,
-        "roofline": roofline, "cpu_baseline": cpu_base, "closest_hit": c1, "full_materials": full, "clocks": clk,
+        "roofline": roofline, "cpu_baseline": cpu_base, "closest_hit": c1, "precision": c3, "full_materials": full, "clocks": clk,
         "setup": {"scene_and_bvh_s": setup_s, "quad_nodes": info["quad_node_count"],
                   "bvh_device_build_ms": min(dev_build),
                   "bvh_host_build_ms": (hinfo["build_ms"] + hinfo["collapse_ms"] + hinfo["upload_ms"]) if hinfo else None,

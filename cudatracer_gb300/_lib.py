@@ -74,6 +74,16 @@ class ct_frame_stats(Structure):
     _fields_ = [("extension_rays", c_uint64), ("shadow_rays", c_uint64), ("samples", c_uint64), ("frames", c_uint32)]
 
 
+class ct_batch_job(Structure):
+    _fields_ = [("scene", c_void_p), ("bvh", c_void_p), ("camera", ct_camera), ("params", ct_render_params),
+                ("spp", c_uint32)]
+
+
+class ct_batch_tuning(Structure):
+    _fields_ = [("extend_block", c_int32), ("connect_block", c_int32), ("shade_waves", c_int32),
+                ("use_graph", c_int32)]
+
+
 class ct_stage_times(Structure):
     _fields_ = [("ms", c_double * 4), ("launches", c_uint32 * 4)]
 
@@ -127,6 +137,14 @@ SIGNATURES = {
     "ct_render_profile": (c_int32, [P, P, c_int32]),
     "ct_render_profile_read": (c_int32, [P, P, POINTER(ct_stage_times), c_int32]),
     "ct_render_accumulate_noalloc": (c_int32, [P, P, P, POINTER(ct_camera), POINTER(ct_render_params), P, P]),
+    "ct_batch_create": (c_int32, [P, POINTER(ct_batch_job), c_uint32, c_int32, PP]),
+    "ct_batch_destroy": (c_int32, [P, P]),
+    "ct_batch_run": (c_int32, [P, P, P]),
+    "ct_batch_accum": (c_int32, [P, c_uint32, PP, POINTER(c_uint32)]),
+    "ct_batch_set_tuning": (c_int32, [P, P, POINTER(ct_batch_tuning)]),
+    "ct_batch_get_tuning": (c_int32, [P, POINTER(ct_batch_tuning)]),
+    "ct_batch_autotune": (c_int32, [P, P, P, POINTER(ct_batch_tuning), POINTER(c_double)]),
+    "ct_batch_stats": (c_int32, [P, P, POINTER(ct_frame_stats), c_int32, P]),
 }
 
 _lib = None

@@ -642,3 +642,69 @@ def launch_kernels(job: RenderJob, scene: Scene, bvh: BVH, params: Params, prese
     params.samples += 2
     if present_out is not None:
         job.present(params.samples, present_out, stream)
+
+
+class Batch:
+    """Many render jobs in one queue set (ct_batch_*): every stage is one
+    launch over all jobs' rays, iterations replayed from a CUDA graph.
+
+    jobs: sequence of dicts with scene (Scene), bvh (quad BVH), camera
+    (Camera), params (ct_render_params, e.g. Params.to_ct()) and spp."""
+
+    def __init__(self, ctx: Context, jobs, exact_math: bool = False):
+        self.ctx = ctx
+        arr = (_lib.ct_batch_job * len(jobs))()
+        self._keep = []
+        for k, j in enumerate(jobs):
+            a = arr[k]
+            a.scene, a.bvh = j["scene"].h, j["bvh"].h
+            a.camera = j["camera"].to_ct()
+            a.params = j["params"]
+            a.spp = int(j["spp"])
+            self._keep.append((j["scene"], j["bvh"]))
+        self.sizes = [(int(j["params"].width), int(j["params"].height)) for j in jobs]
+        self.h = ctypes.c_void_p()
+        check(ctx.lib.ct_batch_create(ctx.h, arr, len(jobs), int(exact_math), ctypes.byref(self.h)), ctx.h)
+
+    def close(self):
+        if self.h:
+            self.ctx.lib.ct_batch_destroy(self.ctx.h, self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def run(self, stream=None):
+        check(self.ctx.lib.ct_batch_run(self.ctx.h, self.h, _stream(stream)), self.ctx.h)
+
+    def accum_tensor(self, job: int):
+        """Job `job`'s float4 accumulation as a (h*w, 4) torch view (no copy)."""
+        import torch
+
+        p, n = ctypes.c_void_p(), ctypes.c_uint32()
+        check(self.ctx.lib.ct_batch_accum(self.h, job, ctypes.byref(p), ctypes.byref(n)))
+        return _device_view(p.value, n.value * 4, torch.float32).view(-1, 4)
+
+    @property
+    def tuning(self) -> dict:
+        t = _lib.ct_batch_tuning()
+        check(self.ctx.lib.ct_batch_get_tuning(self.h, ctypes.byref(t)))
+        return {k: getattr(t, k) for k, _ in t._fields_}
+
+    def set_tuning(self, extend_block=128, connect_block=128, shade_waves=1, use_graph=1):
+        t = _lib.ct_batch_tuning(extend_block, connect_block, shade_waves, use_graph)
+        check(self.ctx.lib.ct_batch_set_tuning(self.ctx.h, self.h, ctypes.byref(t)), self.ctx.h)
+
+    def autotune(self, stream=None) -> tuple[dict, float]:
+        t, ms = _lib.ct_batch_tuning(), ctypes.c_double()
+        check(self.ctx.lib.ct_batch_autotune(self.ctx.h, self.h, _stream(stream), ctypes.byref(t), ctypes.byref(ms)),
+              self.ctx.h)
+        return {k: getattr(t, k) for k, _ in t._fields_}, ms.value
+
+    def stats(self, reset=False, stream=None) -> dict:
+        s = _lib.ct_frame_stats()
+        check(self.ctx.lib.ct_batch_stats(self.ctx.h, self.h, ctypes.byref(s), int(reset), _stream(stream)), self.ctx.h)
+        return {k: getattr(s, k) for k, _ in s._fields_}

@@ -1138,3 +1138,309 @@ ct_status ct_render_profile_read(ct_ctx* ctx, ct_render* r, ct_stage_times* out,
 }
 
 }  // extern "C"
+
+// ============================================================ batches
+struct ct_batch {
+  int32_t n = 0;
+  int32_t exact = 0;
+  int32_t max_depth = 1;
+  uint32_t max_spp = 0;
+  DevQueues q{};
+  DevBatch dev{};
+  Allocs allocs;
+  std::vector<BatchJob> jobs0;  // job table at the first sample
+  std::vector<int32_t> bases;
+  ct_batch_tuning tune{128, 128, 1, 1};
+  cudaStream_t cap = nullptr;  // capture stream
+  cudaGraphExec_t exec = nullptr;
+  ct_batch_tuning exec_tune{0, 0, 0, 0};
+  ~ct_batch() {
+    if (exec) cudaGraphExecDestroy(exec);
+    if (cap) cudaStreamDestroy(cap);
+  }
+};
+
+namespace {
+
+// core::Camera + sample() basis (Camera.cpp:11-16, Kernel.cu:274-290), as ct_render_accumulate derives it.
+FrameConst batch_frame_const(const ct_camera* cam, const ct_render_params* p) {
+  const float dist = tanf((cam->fov_deg * 0.5f) * 0.01745329251994329576923690768489f);
+  const float* w = cam->forward;
+  const float* up = cam->up;
+  float u[3] = {w[1] * up[2] - up[1] * w[2], w[2] * up[0] - up[2] * w[0], w[0] * up[1] - up[0] * w[1]};
+  float inv = 1.0f / std::sqrt((u[0] * u[0] + u[1] * u[1]) + u[2] * u[2]);
+  u[0] *= inv, u[1] *= inv, u[2] *= inv;
+  float v[3] = {u[1] * w[2] - w[1] * u[2], u[2] * w[0] - w[2] * u[0], u[0] * w[1] - w[0] * u[1]};
+  inv = 1.0f / std::sqrt((v[0] * v[0] + v[1] * v[1]) + v[2] * v[2]);
+  v[0] *= inv, v[1] *= inv, v[2] *= inv;
+  float hor[3] = {u[0] * dist, u[1] * dist, u[2] * dist};
+  float ver[3] = {v[0] * dist, v[1] * dist, v[2] * dist};
+  const float aspect = (float)p->width / (float)p->height;
+  if (p->width > p->height)
+    hor[0] *= aspect, hor[1] *= aspect, hor[2] *= aspect;
+  else
+    ver[0] *= aspect, ver[1] *= aspect, ver[2] *= aspect;
+  FrameConst f;
+  f.cam_pos = make_float3(cam->position[0], cam->position[1], cam->position[2]);
+  f.cam_w = make_float3(w[0], w[1], w[2]);
+  f.hor = make_float3(hor[0], hor[1], hor[2]);
+  f.ver = make_float3(ver[0], ver[1], ver[2]);
+  f.width = p->width;
+  f.height = p->height;
+  f.frame = p->frame_index;
+  f.normal_eps = p->normal_eps;
+  f.dist_eps = p->dist_eps;
+  f.tri_eps = p->tri_eps;
+  f.shadow = p->shadow;
+  f.indirect = p->indirect;
+  f.sky = p->sky;
+  f.shading_mode = p->shading_mode;
+  f.tex_filter = p->texture_filter;
+  return f;
+}
+
+// One iteration: every job that still takes samples traces one more.
+cudaError_t batch_iteration(ct_batch* b, const ct_batch_tuning& t, cudaStream_t st) {
+  cudaError_t e = launch_batch_raygen(b->dev, b->q, b->exact, st);
+  for (int pass = 0; pass < b->max_depth && e == cudaSuccess; pass++) {
+    const int cur = pass & 1;
+    const uint32_t path_length = pass == 0 ? 0u : (uint32_t)pass + 1u;  // Kernel.cu:306, 330
+    e = launch_batch_extend(b->dev, b->q, cur, !b->exact, t.extend_block, st);
+    if (e == cudaSuccess) e = launch_batch_shade(b->dev, b->q, cur, path_length, pass, b->exact, t.shade_waves, st);
+    if (e == cudaSuccess) e = launch_batch_connect(b->dev, b->q, !b->exact, t.connect_block, st);
+  }
+  if (e == cudaSuccess) e = launch_batch_advance(b->dev, b->q, st);
+  return e;
+}
+
+cudaError_t batch_graph(ct_batch* b) {
+  if (b->exec && std::memcmp(&b->exec_tune, &b->tune, sizeof(b->tune)) == 0) return cudaSuccess;
+  if (b->exec) {
+    cudaGraphExecDestroy(b->exec);
+    b->exec = nullptr;
+  }
+  cudaError_t e = cudaSuccess;
+  if (!b->cap) e = cudaStreamCreateWithFlags(&b->cap, cudaStreamNonBlocking);
+  if (e != cudaSuccess) return e;
+  e = cudaStreamBeginCapture(b->cap, cudaStreamCaptureModeRelaxed);
+  if (e != cudaSuccess) return e;
+  const cudaError_t le = batch_iteration(b, b->tune, b->cap);
+  cudaGraph_t g = nullptr;
+  e = cudaStreamEndCapture(b->cap, &g);
+  if (le != cudaSuccess) e = le;
+  if (e == cudaSuccess) e = cudaGraphInstantiate(&b->exec, g, 0);
+  if (g) cudaGraphDestroy(g);
+  if (e == cudaSuccess) b->exec_tune = b->tune;
+  return e;
+}
+
+// Reset the job table to the first sample and the queues' counters.
+cudaError_t batch_reset(ct_batch* b, cudaStream_t st, bool zero_accum) {
+  cudaError_t e = cudaMemcpyAsync(b->dev.jobs, b->jobs0.data(), b->jobs0.size() * sizeof(BatchJob),
+                                  cudaMemcpyHostToDevice, st);
+  if (e == cudaSuccess) e = cudaMemsetAsync(b->q.counts, 0, 16 * sizeof(int32_t), st);
+  if (e == cudaSuccess && zero_accum)
+    e = cudaMemsetAsync(b->q.accum, 0, (size_t)b->dev.total_pix * sizeof(float4), st);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(st);  // jobs0 is pageable host memory
+  return e;
+}
+
+cudaError_t batch_iterations(ct_batch* b, uint32_t iters, cudaStream_t st) {
+  cudaError_t e = cudaSuccess;
+  if (b->tune.use_graph) {
+    e = batch_graph(b);
+    for (uint32_t k = 0; k < iters && e == cudaSuccess; k++) e = cudaGraphLaunch(b->exec, st);
+  } else {
+    for (uint32_t k = 0; k < iters && e == cudaSuccess; k++) e = batch_iteration(b, b->tune, st);
+  }
+  return e;
+}
+
+bool tuning_ok(const ct_batch_tuning& t) {
+  auto blk = [](int32_t v) { return v == 64 || v == 128 || v == 256; };
+  return blk(t.extend_block) && blk(t.connect_block) && t.shade_waves >= 1 && t.shade_waves <= 8 &&
+         (t.use_graph == 0 || t.use_graph == 1);
+}
+
+}  // namespace
+
+extern "C" {
+
+ct_status ct_batch_create(ct_ctx* ctx, const ct_batch_job* jobs, uint32_t n, int32_t exact_math, ct_batch** out) {
+  if (!ctx || !jobs || !out || n == 0) return fail(ctx, CT_ERR_INVALID_ARGUMENT, "null argument or empty batch");
+  *out = nullptr;
+  int64_t total = 0;
+  int32_t max_stack = 1, max_depth = 1;
+  uint32_t max_spp = 0;
+  for (uint32_t j = 0; j < n; j++) {
+    const ct_batch_job& J = jobs[j];
+    const ct_render_params* p = &J.params;
+    const std::string at = "job " + std::to_string(j) + ": ";
+    if (!J.scene || !J.bvh) return fail(ctx, CT_ERR_INVALID_ARGUMENT, at + "null scene or BVH");
+    if (J.bvh->nt != J.scene->nt) return fail(ctx, CT_ERR_INVALID_ARGUMENT, at + "BVH was built for another scene");
+    if (J.bvh->wide) return fail(ctx, CT_ERR_UNSUPPORTED, at + "frames trace quad BVHs");
+    if (p->width <= 0 || p->height <= 0 || (int64_t)p->width * p->height > (1 << 26))
+      return fail(ctx, CT_ERR_INVALID_ARGUMENT, at + "bad frame size");
+    if (p->max_depth < 1 || p->max_depth > 64) return fail(ctx, CT_ERR_INVALID_ARGUMENT, at + "max_depth must be in [1, 64]");
+    if (p->shading_mode != CT_SHADE_COMPAT && p->shading_mode != CT_SHADE_FULL)
+      return fail(ctx, CT_ERR_INVALID_ARGUMENT, at + "unknown shading mode");
+    if (p->texture_filter != CT_TEX_NEAREST && p->texture_filter != CT_TEX_BILINEAR)
+      return fail(ctx, CT_ERR_INVALID_ARGUMENT, at + "unknown texture filter");
+    if (J.spp == 0) return fail(ctx, CT_ERR_INVALID_ARGUMENT, at + "spp must be at least 1");
+    if (!finite3(J.camera.position) || !finite3(J.camera.forward) || !finite3(J.camera.up) ||
+        !std::isfinite(J.camera.fov_deg))
+      return fail(ctx, CT_ERR_INVALID_ARGUMENT, at + "non-finite camera");
+    total += (int64_t)p->width * p->height;
+    max_stack = std::max(max_stack, J.bvh->dev.stack_entries);
+    max_depth = std::max(max_depth, p->max_depth);
+    max_spp = std::max(max_spp, J.spp);
+  }
+  if (total > (int64_t)INT32_MAX / 2) return fail(ctx, CT_ERR_INVALID_ARGUMENT, "batch has too many pixels");
+  ct_status s = set_device(ctx);
+  if (s != CT_OK) return s;
+  auto* b = new ct_batch();
+  b->n = (int32_t)n;
+  b->exact = exact_math ? 1 : 0;
+  b->max_depth = max_depth;
+  b->max_spp = max_spp;
+  b->jobs0.resize(n);
+  b->bases.resize(n + 1);
+  int32_t base = 0;
+  for (uint32_t j = 0; j < n; j++) {
+    const ct_batch_job& J = jobs[j];
+    BatchJob& d = b->jobs0[j];
+    std::memset(&d, 0, sizeof(d));
+    d.sc = J.scene->dev;
+    d.bvh = J.bvh->dev;
+    d.f = batch_frame_const(&J.camera, &J.params);
+    d.pix_base = base;
+    d.max_depth = J.params.max_depth;
+    d.spp_left = (int32_t)J.spp;
+    d.exact = b->exact;
+    b->bases[j] = base;
+    base += J.params.width * J.params.height;
+  }
+  b->bases[n] = base;
+  BatchJob* djobs = nullptr;
+  int32_t* dbases = nullptr;
+  if ((s = alloc_queues(ctx, b->allocs, (size_t)base, b->q)) != CT_OK ||
+      (s = upload(ctx, b->allocs, &djobs, b->jobs0.data(), n * sizeof(BatchJob))) != CT_OK ||
+      (s = upload(ctx, b->allocs, &dbases, b->bases.data(), (n + 1) * sizeof(int32_t))) != CT_OK) {
+    free_all(ctx, b->allocs);
+    delete b;
+    return s;
+  }
+  b->dev.jobs = djobs;
+  b->dev.bases = dbases;
+  b->dev.n_jobs = (int32_t)n;
+  b->dev.total_pix = base;
+  b->dev.max_stack = max_stack;
+  *out = b;
+  return CT_OK;
+}
+
+ct_status ct_batch_destroy(ct_ctx* ctx, ct_batch* b) {
+  if (!ctx || !b) return CT_ERR_INVALID_ARGUMENT;
+  set_device(ctx);
+  cudaDeviceSynchronize();
+  free_all(ctx, b->allocs);
+  delete b;
+  return CT_OK;
+}
+
+ct_status ct_batch_run(ct_ctx* ctx, ct_batch* b, void* stream) {
+  if (!ctx || !b) return fail(ctx, CT_ERR_INVALID_ARGUMENT, "null argument");
+  ct_status s = set_device(ctx);
+  if (s != CT_OK) return s;
+  cudaStream_t st = (cudaStream_t)stream;
+  CT_CUDA(ctx, batch_reset(b, st, true));
+  CT_CUDA(ctx, batch_iterations(b, b->max_spp, st));
+  return CT_OK;
+}
+
+ct_status ct_batch_accum(const ct_batch* b, uint32_t job, float** accum_device, uint32_t* pixels) {
+  if (!b || job >= (uint32_t)b->n) return CT_ERR_INVALID_ARGUMENT;
+  if (accum_device) *accum_device = (float*)(b->q.accum + b->bases[job]);
+  if (pixels) *pixels = (uint32_t)(b->bases[job + 1] - b->bases[job]);
+  return CT_OK;
+}
+
+ct_status ct_batch_set_tuning(ct_ctx* ctx, ct_batch* b, const ct_batch_tuning* t) {
+  if (!b || !t) return fail(ctx, CT_ERR_INVALID_ARGUMENT, "null argument");
+  if (!tuning_ok(*t)) return fail(ctx, CT_ERR_INVALID_ARGUMENT, "tuning out of range");
+  b->tune = *t;
+  return CT_OK;
+}
+
+ct_status ct_batch_get_tuning(const ct_batch* b, ct_batch_tuning* t) {
+  if (!b || !t) return CT_ERR_INVALID_ARGUMENT;
+  *t = b->tune;
+  return CT_OK;
+}
+
+ct_status ct_batch_autotune(ct_ctx* ctx, ct_batch* b, void* stream, ct_batch_tuning* chosen, double* ms_per_iteration) {
+  if (!ctx || !b) return fail(ctx, CT_ERR_INVALID_ARGUMENT, "null argument");
+  ct_status s = set_device(ctx);
+  if (s != CT_OK) return s;
+  cudaStream_t st = (cudaStream_t)stream;
+  cudaEvent_t e0 = nullptr, e1 = nullptr;
+  CT_CUDA(ctx, cudaEventCreate(&e0));
+  CT_CUDA(ctx, cudaEventCreate(&e1));
+  // time `iters` iterations of the first samples of every job under tuning t
+  const uint32_t iters = std::max<uint32_t>(1, std::min<uint32_t>(2, b->max_spp));
+  auto measure = [&](const ct_batch_tuning& t, float& ms) -> cudaError_t {
+    b->tune = t;
+    cudaError_t e = batch_reset(b, st, false);
+    if (e == cudaSuccess) e = batch_iterations(b, 1, st);  // warm-up (and graph instantiation)
+    if (e == cudaSuccess) e = batch_reset(b, st, false);
+    if (e == cudaSuccess) e = cudaEventRecord(e0, st);
+    if (e == cudaSuccess) e = batch_iterations(b, iters, st);
+    if (e == cudaSuccess) e = cudaEventRecord(e1, st);
+    if (e == cudaSuccess) e = cudaEventSynchronize(e1);
+    if (e == cudaSuccess) e = cudaEventElapsedTime(&ms, e0, e1);
+    ms /= (float)iters;
+    return e;
+  };
+  ct_batch_tuning best = b->tune;
+  float best_ms = 1e30f;
+  cudaError_t err = cudaSuccess;
+  auto trial = [&](const ct_batch_tuning& t) {
+    if (err != cudaSuccess) return;
+    float ms = 0.0f;
+    err = measure(t, ms);
+    if (err == cudaSuccess && ms < best_ms) best_ms = ms, best = t;
+  };
+  // coordinate search: traversal block sizes, then shade waves, then graph replay
+  for (int eb : {64, 128, 256})
+    for (int cb : {128, 256}) trial(ct_batch_tuning{eb, cb, 1, 1});
+  trial(ct_batch_tuning{best.extend_block, best.connect_block, 2, 1});
+  trial(ct_batch_tuning{best.extend_block, best.connect_block, best.shade_waves, 0});
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  if (err != cudaSuccess) return cuda_fail(ctx, err, "batch autotune");
+  b->tune = best;
+  if (chosen) *chosen = best;
+  if (ms_per_iteration) *ms_per_iteration = best_ms;
+  return CT_OK;
+}
+
+ct_status ct_batch_stats(ct_ctx* ctx, ct_batch* b, ct_frame_stats* out, int32_t reset, void* stream) {
+  if (!ctx || !b || !out) return fail(ctx, CT_ERR_INVALID_ARGUMENT, "null argument");
+  ct_status s = set_device(ctx);
+  if (s != CT_OK) return s;
+  cudaStream_t st = (cudaStream_t)stream;
+  unsigned long long h[8] = {0};
+  CT_CUDA(ctx, cudaMemcpyAsync(h, b->q.stats, sizeof(h), cudaMemcpyDeviceToHost, st));
+  CT_CUDA(ctx, cudaStreamSynchronize(st));
+  out->extension_rays = h[0];
+  out->shadow_rays = h[1];
+  out->samples = h[2];
+  out->frames = (uint32_t)h[3];
+  if (reset) {
+    CT_CUDA(ctx, cudaMemsetAsync(b->q.stats, 0, sizeof(h), st));
+    CT_CUDA(ctx, cudaStreamSynchronize(st));
+  }
+  return CT_OK;
+}
+
+}  // extern "C"

@@ -130,6 +130,40 @@ struct FrameConst {
 enum : uint32_t { kErrStackOverflow = 1u };
 
 // ---------------------------------------------------------------------------
+// Batches: many render jobs share one queue set and one launch per stage.
+// A ray's pixel index (origin.w) is global to the batch; the job owning it is
+// found by binary search over the jobs' first pixels.
+// ---------------------------------------------------------------------------
+struct BatchJob {
+  DevScene sc;
+  DevBVH bvh;
+  FrameConst f;         // f.frame advances by 2 per sample, as launchKernels does
+  int32_t pix_base;     // first pixel of the job in the batch
+  int32_t max_depth;
+  int32_t spp_left;     // samples still to take; the job traces while > 0
+  int32_t exact;        // unused by the kernels (the batch picks one math mode)
+};
+struct DevBatch {
+  BatchJob* jobs;
+  const int32_t* bases;  // n_jobs + 1 ascending first pixels; bases[n_jobs] = total
+  int32_t n_jobs;
+  int32_t total_pix;
+  int32_t max_stack;     // largest traversal stack among the jobs' BVHs
+  int32_t pad;
+};
+#ifdef __CUDACC__
+__device__ __forceinline__ int batch_job_of(const int32_t* __restrict__ bases, int n, int pix) {
+  int lo = 0, hi = n - 1;  // largest j with bases[j] <= pix
+  while (lo < hi) {
+    const int mid = (lo + hi + 1) >> 1;
+    if (__ldg(bases + mid) <= pix) lo = mid;
+    else hi = mid - 1;
+  }
+  return lo;
+}
+#endif
+
+// ---------------------------------------------------------------------------
 // Kernel launchers (defined in the .cu files)
 // ---------------------------------------------------------------------------
 int sm_count();
@@ -189,6 +223,16 @@ cudaError_t launch_trace_wide_closest(const DevWBVH& b, const float4* org, const
                                       cudaStream_t s);
 cudaError_t launch_trace_wide_any(const DevWBVH& b, const float4* org, const float4* dir, uint8_t* occ, uint32_t n,
                                   uint32_t* err, int* cursor, unsigned long long* stats, cudaStream_t s);
+
+// Batch stages (one launch each for every job of the batch). The queue
+// capacity is the batch's total pixel count; counts[0] must be zero before
+// raygen (launch_batch_advance leaves it so).
+cudaError_t launch_batch_raygen(const DevBatch& b, const DevQueues& q, int exact, cudaStream_t s);
+cudaError_t launch_batch_extend(const DevBatch& b, const DevQueues& q, int queue, bool fast, int block, cudaStream_t s);
+cudaError_t launch_batch_shade(const DevBatch& b, const DevQueues& q, int queue, uint32_t path_length, int pass,
+                               int exact, int grid_mult, cudaStream_t s);
+cudaError_t launch_batch_connect(const DevBatch& b, const DevQueues& q, bool fast, int block, cudaStream_t s);
+cudaError_t launch_batch_advance(const DevBatch& b, const DevQueues& q, cudaStream_t s);
 
 cudaError_t launch_fold(float4* accum, float4* frame, int n, cudaStream_t s);
 

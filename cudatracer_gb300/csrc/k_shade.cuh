@@ -135,8 +135,10 @@ struct Emit {
 };
 
 // One ray of the compat shade stage.
+// pix_base: first pixel of the job in a batch (0 for a single job); seeds use
+// the job's own pixel index so a job renders the same alone and in a batch.
 __device__ __forceinline__ void shade_compat(const DevScene& sc, const DevQueues& q, const FrameConst& f, int cur,
-                                             int i, uint32_t path_length, Emit& e) {
+                                             int i, uint32_t path_length, Emit& e, int pix_base = 0) {
   const float4 o4 = q.org_q(cur)[i], d4 = q.dir_q(cur)[i], t4 = q.thr_q(cur)[i];
   const int2 h = q.hit[i];
   const int pix = __float_as_int(o4.w);
@@ -190,7 +192,7 @@ __device__ __forceinline__ void shade_compat(const DevScene& sc, const DevQueues
   const float flip = dot(dir, N) > 0 ? -1.0f : 1.0f;
   N = N * flip;
   iN = iN * flip;
-  uint32_t seed = wang_hash((uint32_t)pix * 16789u + f.frame * 1791u + path_length * 720898027u);
+  uint32_t seed = wang_hash((uint32_t)(pix - pix_base) * 16789u + f.frame * 1791u + path_length * 720898027u);
   V3 color = v3(alb);
   if (mtex.x >= 0) color = v3(tex_color(sc, mtex.x, tu, tv, f.tex_filter));
   // SampleBSDF (BSDF.h:33-63); its two random numbers are drawn left to right
@@ -311,7 +313,7 @@ __device__ __forceinline__ void onb(V3 n, V3& t, V3& b) {
 }
 
 __device__ __forceinline__ void shade_full(const DevScene& sc, const DevQueues& q, const FrameConst& f, int cur, int i,
-                                           uint32_t path_length, Emit& e) {
+                                           uint32_t path_length, Emit& e, int pix_base = 0) {
   const float4 o4 = q.org_q(cur)[i], d4 = q.dir_q(cur)[i], t4 = q.thr_q(cur)[i];
   const int2 h = q.hit[i];
   const int pix = __float_as_int(o4.w);
@@ -374,7 +376,7 @@ __device__ __forceinline__ void shade_full(const DevScene& sc, const DevQueues& 
   const V3 wo_l = v3(dot(wo, Tt), dot(wo, Bt), dot(wo, N));
   V3 color = v3(alb);
   if (mtex.x >= 0) color = v3(tex_color(sc, mtex.x, tu, tv, f.tex_filter));
-  uint32_t seed = wang_hash((uint32_t)pix * 16789u + f.frame * 1791u + path_length * 720898027u);
+  uint32_t seed = wang_hash((uint32_t)(pix - pix_base) * 16789u + f.frame * 1791u + path_length * 720898027u);
   const float u1 = rnd_float(seed), u2 = rnd_float(seed), u3 = rnd_float(seed);
   const float rough = tr.y;
   const float alpha = full::roughness_to_alpha(rough);
@@ -496,6 +498,101 @@ __global__ void __launch_bounds__(kBlock) k_raygen(DevQueues q, FrameConst f) {
     q.org_q(0)[i] = make_float4(f.cam_pos.x, f.cam_pos.y, f.cam_pos.z, __int_as_float(i));
     q.dir_q(0)[i] = f4(normalize(p), __int_as_float(0));  // lastBounceType = SPECULAR
     q.thr_q(0)[i] = make_float4(1.0f, 1.0f, 1.0f, 1.0f);  // throughput 1, lastBsdfPDF 1
+  }
+}
+
+// ---- batches: one launch per stage for every job (see DevBatch)
+
+// Primary rays of the jobs that still take samples, appended to queue 0.
+__global__ void __launch_bounds__(kBlock) k_batch_raygen(DevBatch bt, DevQueues q) {
+  if (blockIdx.x == 0 && threadIdx.x == 0) q.counts[4] = 0;
+  for (int base = blockIdx.x * kBlock + (threadIdx.x & ~31); base < bt.total_pix; base += gridDim.x * kBlock) {
+    const int g = base + (threadIdx.x & 31);
+    bool want = false;
+    float4 o, d;
+    if (g < bt.total_pix) {
+      const BatchJob& J = bt.jobs[batch_job_of(bt.bases, bt.n_jobs, g)];
+      if (J.spp_left > 0) {
+        const FrameConst& f = J.f;
+        const int i = g - J.pix_base;
+        uint32_t seed = ((uint32_t)i + f.frame * 147565741u) * 720898027u;
+        const int x = i % f.width, y = (i / f.width) % f.height;
+        const float invw = 1.0f / (float)f.width, invh = 1.0f / (float)f.height;
+        const float px = ((float)x + rnd_float(seed)) - 0.5f;
+        const float py = ((float)y + rnd_float(seed)) - 0.5f;
+        const float sx = 2.0f * (px * invw) - 1.0f;
+        const float sy = 1.0f - 2.0f * (py * invh);
+        const V3 w = v3(f.cam_w.x, f.cam_w.y, f.cam_w.z), hor = v3(f.hor.x, f.hor.y, f.hor.z),
+                 ver = v3(f.ver.x, f.ver.y, f.ver.z);
+        const V3 p = (w + hor * sx) + ver * sy;
+        o = make_float4(f.cam_pos.x, f.cam_pos.y, f.cam_pos.z, __int_as_float(g));
+        d = f4(normalize(p), __int_as_float(0));
+        want = true;
+      }
+    }
+    const int k = warp_append(want, &q.counts[0]);
+    if (k >= 0) {
+      q.org_q(0)[k] = o;
+      q.dir_q(0)[k] = d;
+      q.thr_q(0)[k] = make_float4(1.0f, 1.0f, 1.0f, 1.0f);
+    }
+  }
+}
+
+// Shade every ray of the batch with its job's scene and frame constants; a
+// job's paths stop after its own max_depth passes.
+__global__ void __launch_bounds__(kBlock) k_batch_shade(DevBatch bt, DevQueues q, int cur, uint32_t path_length,
+                                                        int pass) {
+  const int n = q.counts[cur];
+  const int nxt = cur ^ 1;
+  if (blockIdx.x == 0 && threadIdx.x == 0) q.counts[4] = 0;
+  const int lane = threadIdx.x & 31;
+  const int stride = gridDim.x * kBlock;
+  for (int base = blockIdx.x * kBlock + (threadIdx.x & ~31); base < n; base += stride) {
+    const int i = base + lane;
+    Emit e;
+    e.cont = false;
+    e.shadow = false;
+    if (i < n) {
+      const int pix = __float_as_int(q.org_q(cur)[i].w);
+      const BatchJob& J = bt.jobs[batch_job_of(bt.bases, bt.n_jobs, pix)];
+      if (J.f.shading_mode == CT_MODE_FULL)
+        shade_full(J.sc, q, J.f, cur, i, path_length, e, J.pix_base);
+      else
+        shade_compat(J.sc, q, J.f, cur, i, path_length, e, J.pix_base);
+      if (pass + 1 >= J.max_depth) e.cont = false;
+    }
+    const int si = warp_append(e.shadow, &q.counts[2]);
+    if (si >= 0) {
+      q.sorg[si] = e.so;
+      q.sdir[si] = e.sd;
+      q.scol[si] = e.sc;
+    }
+    const int ci = warp_append(e.cont, &q.counts[nxt]);
+    if (ci >= 0) {
+      q.org_q(nxt)[ci] = e.no;
+      q.dir_q(nxt)[ci] = e.nd;
+      q.thr_q(nxt)[ci] = e.nt;
+    }
+  }
+}
+
+// End of a batch iteration: each job that took a sample advances its frame
+// seed by 2 (launchKernels' samples += 2) and counts the sample; queue 0 is
+// emptied for the next raygen.
+__global__ void k_batch_advance(DevBatch bt, DevQueues q) {
+  const int j = blockIdx.x * blockDim.x + threadIdx.x;
+  if (j == 0) {
+    q.counts[0] = 0;
+    q.counts[4] = 0;
+    atomicAdd(&q.stats[3], 1ull);
+  }
+  if (j >= bt.n_jobs) return;
+  BatchJob& J = bt.jobs[j];
+  if (J.spp_left > 0) {
+    atomicAdd(&q.stats[2], (unsigned long long)(J.f.width * J.f.height));
+    J.spp_left -= 1;
+    J.f.frame += 2;
   }
 }
 

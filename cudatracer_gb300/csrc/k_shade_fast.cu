@@ -8,6 +8,9 @@ namespace ct {
 namespace exact {
 __global__ void __launch_bounds__(128) k_shade(DevScene sc, DevQueues q, FrameConst f, int cur, uint32_t path_length);
 __global__ void __launch_bounds__(128) k_raygen(DevQueues q, FrameConst f);
+__global__ void __launch_bounds__(128) k_batch_raygen(DevBatch bt, DevQueues q);
+__global__ void __launch_bounds__(128) k_batch_shade(DevBatch bt, DevQueues q, int cur, uint32_t path_length, int pass);
+__global__ void k_batch_advance(DevBatch bt, DevQueues q);
 }  // namespace exact
 
 namespace {
@@ -78,4 +81,29 @@ cudaError_t launch_present(const float4* accum, float4* out, int n, float sample
   return cudaGetLastError();
 }
 
+
+cudaError_t launch_batch_raygen(const DevBatch& b, const DevQueues& q, int exact, cudaStream_t s) {
+  if (exact)
+    exact::k_batch_raygen<<<fill_grid(exact::k_batch_raygen, b.total_pix), kBlock, 0, s>>>(b, q);
+  else
+    fast::k_batch_raygen<<<fill_grid(fast::k_batch_raygen, b.total_pix), kBlock, 0, s>>>(b, q);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_batch_shade(const DevBatch& b, const DevQueues& q, int queue, uint32_t path_length, int pass,
+                               int exact, int grid_mult, cudaStream_t s) {
+  // the live count is on the device: size the grid for the capacity, up to grid_mult waves
+  auto k = exact ? exact::k_batch_shade : fast::k_batch_shade;
+  int per_sm = 0;
+  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k, kBlock, 0);
+  const int cap_blocks = (q.capacity + kBlock - 1) / kBlock;
+  const int grid = std::max(1, std::min(cap_blocks, std::max(1, per_sm) * sm_count() * std::max(1, grid_mult)));
+  k<<<grid, kBlock, 0, s>>>(b, q, queue, path_length, pass);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_batch_advance(const DevBatch& b, const DevQueues& q, cudaStream_t s) {
+  fast::k_batch_advance<<<(b.n_jobs + 127) / 128, 128, 0, s>>>(b, q);
+  return cudaGetLastError();
+}
 }  // namespace ct

@@ -191,4 +191,122 @@ cudaError_t launch_connect(const DevBVH& b, const DevQueues& q, float eps, bool 
   return cudaGetLastError();
 }
 
+
+// ---------------------------------------------------------------- batches
+namespace {
+
+struct BatchExtendIO {
+  const float4* __restrict__ org;
+  const float4* __restrict__ dir;
+  int2* hit;
+  uint32_t* err;
+  const BatchJob* jobs;
+  const int32_t* bases;
+  int n_jobs;
+  __device__ void load(int i, float4& o, float4& d, float& t0, DevBVH& b, float& eps) {
+    o = __ldg(org + i);
+    d = __ldg(dir + i);
+    t0 = kMaxDistance;
+    const BatchJob& J = jobs[batch_job_of(bases, n_jobs, __float_as_int(o.w))];
+    b = J.bvh;
+    eps = J.f.tri_eps;
+  }
+  __device__ void store(int i, const RayState& r, bool overflow) {
+    if (overflow) {
+      atomicOr(err, kErrStackOverflow);
+      hit[i] = make_int2(-1, __float_as_int(kMaxDistance));
+      return;
+    }
+    hit[i] = make_int2(r.hit, __float_as_int(r.t));
+  }
+};
+
+template <bool FASTMM, int BLOCK>
+__global__ void __launch_bounds__(BLOCK) k_batch_extend(DevBatch bt, DevQueues q, int qi) {
+  extern __shared__ int s_stack[];
+  const int n = q.counts[qi];
+  if (blockIdx.x == 0 && threadIdx.x == 0) {
+    q.counts[qi ^ 1] = 0;
+    q.counts[2] = 0;
+    atomicAdd(&q.stats[0], (unsigned long long)n);
+  }
+  BatchExtendIO io{q.org_q(qi), q.dir_q(qi), q.hit, q.error, bt.jobs, bt.bases, bt.n_jobs};
+  trace_persistent_batch<false, FASTMM>(n, q.counts + 4, io, s_stack + threadIdx.x, BLOCK);
+}
+
+template <bool FASTMM, int BLOCK>
+__global__ void __launch_bounds__(BLOCK) k_batch_connect(DevBatch bt, DevQueues q) {
+  extern __shared__ int s_stack[];
+  int* stack = s_stack + threadIdx.x;
+  const int n = q.counts[2];
+  if (blockIdx.x == 0 && threadIdx.x == 0) atomicAdd(&q.stats[1], (unsigned long long)n);
+  for (int i = blockIdx.x * BLOCK + threadIdx.x; i < n; i += gridDim.x * BLOCK) {
+    const float4 o = __ldg(q.sorg + i), d = __ldg(q.sdir + i);
+    const int pix = __float_as_int(o.w);
+    const BatchJob& J = bt.jobs[batch_job_of(bt.bases, bt.n_jobs, pix)];
+    const DevBVH b = J.bvh;
+    RayState r;
+    ray_begin(r, o, d, d.w);
+    if (!traverse<true, FASTMM>(b, r, J.f.tri_eps, stack, BLOCK)) {
+      atomicOr(q.error, kErrStackOverflow);
+      continue;
+    }
+    if (r.hit < 0) {
+      const float4 c = __ldg(q.scol + i);
+      float4 a = q.accum[pix];
+      a.x = __fadd_rn(a.x, c.x);
+      a.y = __fadd_rn(a.y, c.y);
+      a.z = __fadd_rn(a.z, c.z);
+      a.w = __fadd_rn(a.w, 1.0f);
+      q.accum[pix] = a;
+    }
+  }
+}
+
+template <bool FASTMM, int BLOCK>
+cudaError_t batch_extend(const DevBatch& b, const DevQueues& q, int queue, cudaStream_t s) {
+  const size_t smem = (size_t)b.max_stack * BLOCK * sizeof(int);
+  auto kernel = k_batch_extend<FASTMM, BLOCK>;
+  if (smem > 48 * 1024) {
+    cudaError_t e = cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (e != cudaSuccess) return e;
+  }
+  int per_sm = 0;
+  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kernel, BLOCK, smem);
+  const int cap_blocks = (q.capacity + BLOCK - 1) / BLOCK;
+  const int grid = std::max(1, std::min(cap_blocks, std::max(1, per_sm) * sm_count()));
+  kernel<<<grid, BLOCK, smem, s>>>(b, q, queue);
+  return cudaGetLastError();
+}
+
+template <bool FASTMM, int BLOCK>
+cudaError_t batch_connect(const DevBatch& b, const DevQueues& q, cudaStream_t s) {
+  const size_t smem = (size_t)b.max_stack * BLOCK * sizeof(int);
+  auto kernel = k_batch_connect<FASTMM, BLOCK>;
+  if (smem > 48 * 1024) {
+    cudaError_t e = cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (e != cudaSuccess) return e;
+  }
+  int per_sm = 0;
+  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kernel, BLOCK, smem);
+  const int cap_blocks = (q.capacity + BLOCK - 1) / BLOCK;
+  const int grid = std::max(1, std::min(cap_blocks, std::max(1, per_sm) * sm_count()));
+  kernel<<<grid, BLOCK, smem, s>>>(b, q);
+  return cudaGetLastError();
+}
+
+}  // namespace
+
+cudaError_t launch_batch_extend(const DevBatch& b, const DevQueues& q, int queue, bool fast, int block, cudaStream_t s) {
+  if (block == 64) return fast ? batch_extend<true, 64>(b, q, queue, s) : batch_extend<false, 64>(b, q, queue, s);
+  if (block == 256) return fast ? batch_extend<true, 256>(b, q, queue, s) : batch_extend<false, 256>(b, q, queue, s);
+  return fast ? batch_extend<true, 128>(b, q, queue, s) : batch_extend<false, 128>(b, q, queue, s);
+}
+
+cudaError_t launch_batch_connect(const DevBatch& b, const DevQueues& q, bool fast, int block, cudaStream_t s) {
+  if (block == 64) return fast ? batch_connect<true, 64>(b, q, s) : batch_connect<false, 64>(b, q, s);
+  if (block == 256) return fast ? batch_connect<true, 256>(b, q, s) : batch_connect<false, 256>(b, q, s);
+  return fast ? batch_connect<true, 128>(b, q, s) : batch_connect<false, 128>(b, q, s);
+}
+
 }  // namespace ct

@@ -249,4 +249,49 @@ __device__ __forceinline__ void trace_persistent(const DevBVH& b, int n, int* cu
   }
 }
 
+// trace_persistent with a BVH and epsilon per lane: io.load(i, o, d, t0, b, eps)
+// supplies the ray and the tree it is traced against (batches of jobs).
+template <bool ANY, bool FASTMM, class IO>
+__device__ __forceinline__ void trace_persistent_batch(int n, int* cursor, IO& io, int* stack, int stride) {
+  const unsigned FULL = 0xffffffffu;
+  const int lane = threadIdx.x & 31;
+  const unsigned below = (1u << lane) - 1u;
+  int rid = -1;
+  bool exhausted = false;
+  RayState r;
+  r.ref = kEmptyChild;
+  DevBVH b;
+  float eps = 0.0f;
+  while (true) {
+    if (!exhausted) {
+      const unsigned m = __ballot_sync(FULL, rid < 0);
+      if (m) {
+        const int leader = __ffs(m) - 1;
+        int base = 0;
+        if (lane == leader) base = atomicAdd(cursor, __popc(m));
+        base = __shfl_sync(FULL, base, leader);
+        if (base + __popc(m) >= n) exhausted = true;
+        if (rid < 0) {
+          const int my = base + __popc(m & below);
+          if (my < n) {
+            float4 o, d;
+            float t0;
+            io.load(my, o, d, t0, b, eps);
+            ray_begin(r, o, d, t0);
+            rid = my;
+          }
+        }
+      }
+    }
+    if (__ballot_sync(FULL, rid >= 0) == 0) break;
+    if (rid < 0) continue;
+    const StepResult s =
+        r.ref >= 0 ? inner_step<FASTMM>(b, r, stack, stride, b.stack_entries) : leaf_step<ANY>(b, r, eps, stack, stride);
+    if (s != kContinue) {
+      io.store(rid, r, s == kOverflow);
+      rid = -1;
+    }
+  }
+}
+
 }  // namespace ct

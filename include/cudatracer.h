@@ -277,6 +277,49 @@ ct_status ct_trace_closest(ct_ctx* ctx, const ct_bvh* bvh, const float* org, con
 ct_status ct_trace_any(ct_ctx* ctx, const ct_bvh* bvh, const float* org, const float* dir, uint8_t* occluded,
                        uint32_t n, float tri_eps, void* stream);
 
+/* ---- batches (no reference counterpart: the reference renders one job per
+ * launchKernels call). Many render jobs of different scenes, BVHs,
+ * resolutions, depths and sample counts share one queue set: every stage is
+ * one launch over the rays of all jobs, and one iteration (ray generation,
+ * max_depth x (closest hit, shade, shadow any-hit), bookkeeping) is captured
+ * once in a CUDA graph and replayed until every job has its samples. A job's
+ * result does not depend on the other jobs in the batch: its pixels use its
+ * own seeds, and each pixel's contributions arrive in the same order. */
+typedef struct ct_batch ct_batch;
+typedef struct ct_batch_job {
+  const ct_scene* scene;
+  const ct_bvh* bvh;            /* a quad BVH of that scene */
+  ct_camera camera;
+  ct_render_params params;      /* size, max_depth, frame_index of the first sample, shading,
+                                   flags, epsilons, texture filter; exact_math is the batch's */
+  uint32_t spp;                 /* samples to accumulate (frame_index advances by 2 per sample) */
+} ct_batch_job;
+/* Launch shapes the autotuner chooses between (extend/connect block sizes
+ * 64, 128 or 256; shade grid in waves of resident blocks; graph replay on/off). */
+typedef struct ct_batch_tuning {
+  int32_t extend_block;
+  int32_t connect_block;
+  int32_t shade_waves;
+  int32_t use_graph;
+} ct_batch_tuning;
+/* Copies the job table; allocates queues for every job's pixels at once and
+ * one FP32 RGBA accumulation buffer holding all jobs' images back to back. */
+ct_status ct_batch_create(ct_ctx* ctx, const ct_batch_job* jobs, uint32_t n, int32_t exact_math, ct_batch** out);
+ct_status ct_batch_destroy(ct_ctx* ctx, ct_batch* b);
+/* Zero the accumulation, reset every job to its first sample, and render all
+ * samples of all jobs. Asynchronous on `stream`. */
+ct_status ct_batch_run(ct_ctx* ctx, ct_batch* b, void* stream);
+/* Device pointer to job j's float4 accumulation (width*height entries). */
+ct_status ct_batch_accum(const ct_batch* b, uint32_t job, float** accum_device, uint32_t* pixels);
+ct_status ct_batch_set_tuning(ct_ctx* ctx, ct_batch* b, const ct_batch_tuning* t);
+ct_status ct_batch_get_tuning(const ct_batch* b, ct_batch_tuning* t);
+/* Time candidate launch shapes on this batch (a few iterations each) and keep
+ * the fastest; `chosen` (may be NULL) receives it and ms_per_iteration its
+ * time. Leaves the accumulation undefined: call ct_batch_run afterwards. */
+ct_status ct_batch_autotune(ct_ctx* ctx, ct_batch* b, void* stream, ct_batch_tuning* chosen, double* ms_per_iteration);
+/* Ray and sample counters of the batch (frames = iterations). */
+ct_status ct_batch_stats(ct_ctx* ctx, ct_batch* b, ct_frame_stats* out, int32_t reset, void* stream);
+
 /* ---- rendering: replaces launchKernels (src/CUDA/Kernel.cu:355) and its
  * buffers (Application::allocateBuffers, src/Application.cpp:141-154).
  * A ct_render holds one job's resident state: ray queues, shadow queue,
