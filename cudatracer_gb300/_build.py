@@ -26,6 +26,7 @@ SOURCES = {
     "api.cpp": [],
     "bvh_build.cpp": [],
     "mesh_io.cpp": [],
+    "server.cpp": [],
     "k_trace.cu": [],
     "bvh_gpu.cu": [],
     "k_trace_wide.cu": [],

@@ -84,6 +84,21 @@ class ct_batch_tuning(Structure):
                 ("use_graph", c_int32)]
 
 
+class ct_server_config(Structure):
+    _fields_ = [("hbm_budget", c_uint64), ("max_inflight_pixels", c_uint32), ("exact_math", c_int32)]
+
+
+class ct_request_info(Structure):
+    _fields_ = [("status", c_int32), ("kind", c_int32), ("submit_s", c_double), ("admit_s", c_double),
+                ("done_s", c_double), ("device_bytes", c_uint64)]
+
+
+class ct_server_stats(Structure):
+    _fields_ = [("submitted", c_uint64), ("completed", c_uint64), ("failed", c_uint64), ("iterations", c_uint64),
+                ("peak_bytes", c_uint64), ("extension_rays", c_uint64), ("shadow_rays", c_uint64),
+                ("query_rays", c_uint64)]
+
+
 class ct_stage_times(Structure):
     _fields_ = [("ms", c_double * 4), ("launches", c_uint32 * 4)]
 
@@ -145,6 +160,12 @@ SIGNATURES = {
     "ct_batch_get_tuning": (c_int32, [P, POINTER(ct_batch_tuning)]),
     "ct_batch_autotune": (c_int32, [P, P, P, POINTER(ct_batch_tuning), POINTER(c_double)]),
     "ct_batch_stats": (c_int32, [P, P, POINTER(ct_frame_stats), c_int32, P]),
+    "ct_server_create": (c_int32, [P, POINTER(ct_server_config), PP]),
+    "ct_server_destroy": (c_int32, [P]),
+    "ct_server_submit_render": (c_int32, [P, POINTER(ct_batch_job), P, POINTER(c_uint64)]),
+    "ct_server_submit_query": (c_int32, [P, P, P, P, c_uint32, c_float, c_int32, P, P, P, POINTER(c_uint64)]),
+    "ct_server_wait": (c_int32, [P, c_uint64, c_double, POINTER(ct_request_info)]),
+    "ct_server_get_stats": (c_int32, [P, POINTER(ct_server_stats)]),
 }
 
 _lib = None

@@ -708,3 +708,96 @@ class Batch:
         s = _lib.ct_frame_stats()
         check(self.ctx.lib.ct_batch_stats(self.ctx.h, self.h, ctypes.byref(s), int(reset), _stream(stream)), self.ctx.h)
         return {k: getattr(s, k) for k, _ in s._fields_}
+
+
+class Server:
+    """The serving loop (ct_server_*): render jobs and ray queries admitted as
+    they arrive against an HBM budget, render jobs continuously batched, ray
+    queries overlapping on a second stream. Results land in pinned host
+    buffers owned here until the request is waited for."""
+
+    def __init__(self, ctx: Context, hbm_budget: int = 0, max_inflight_pixels: int = 1 << 22,
+                 exact_math: bool = False):
+        self.ctx = ctx
+        cfg = _lib.ct_server_config(int(hbm_budget), int(max_inflight_pixels), int(exact_math))
+        self.h = ctypes.c_void_p()
+        check(ctx.lib.ct_server_create(ctx.h, ctypes.byref(cfg), ctypes.byref(self.h)), ctx.h)
+        self._req = {}
+
+    def close(self):
+        if self.h:
+            self.ctx.lib.ct_server_destroy(self.h)
+            self.h = None
+            self._req.clear()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    @staticmethod
+    def _pinned(shape, dtype):
+        import torch
+
+        return torch.empty(shape, dtype=dtype, pin_memory=True)
+
+    def submit_render(self, job: dict) -> int:
+        import torch
+
+        W, H = int(job["params"].width), int(job["params"].height)
+        out = self._pinned((W * H, 4), torch.float32)
+        j = _lib.ct_batch_job()
+        j.scene, j.bvh = job["scene"].h, job["bvh"].h
+        j.camera = job["camera"].to_ct()
+        j.params = job["params"]
+        j.spp = int(job["spp"])
+        rid = ctypes.c_uint64()
+        check(self.ctx.lib.ct_server_submit_render(self.h, ctypes.byref(j), out.data_ptr(), ctypes.byref(rid)),
+              self.ctx.h)
+        self._req[rid.value] = ("render", out, job)
+        return rid.value
+
+    def submit_query(self, bvh: "BVH", org: np.ndarray, dir: np.ndarray, any_hit: bool = False,
+                     tri_eps: float = 1e-3) -> int:
+        import torch
+
+        n = int(org.shape[0])
+        o = self._pinned((n, 4), torch.float32)
+        d = self._pinned((n, 4), torch.float32)
+        o.numpy()[:] = org
+        d.numpy()[:] = dir
+        rid = ctypes.c_uint64()
+        if any_hit:
+            occ = self._pinned((n,), torch.uint8)
+            check(self.ctx.lib.ct_server_submit_query(self.h, bvh.h, o.data_ptr(), d.data_ptr(), n, float(tri_eps), 1,
+                                                      None, None, occ.data_ptr(), ctypes.byref(rid)), self.ctx.h)
+            self._req[rid.value] = ("any", (o, d, occ), bvh)
+        else:
+            hit = self._pinned((n,), torch.int32)
+            t = self._pinned((n,), torch.float32)
+            check(self.ctx.lib.ct_server_submit_query(self.h, bvh.h, o.data_ptr(), d.data_ptr(), n, float(tri_eps), 0,
+                                                      hit.data_ptr(), t.data_ptr(), None, ctypes.byref(rid)),
+                  self.ctx.h)
+            self._req[rid.value] = ("closest", (o, d, hit, t), bvh)
+        return rid.value
+
+    def wait(self, rid: int, timeout: float = -1.0):
+        """(info dict, result): result is the (h*w, 4) accumulation, (hit, t)
+        or the occlusion flags, as numpy arrays."""
+        info = _lib.ct_request_info()
+        st = self.ctx.lib.ct_server_wait(self.h, rid, float(timeout), ctypes.byref(info))
+        kind, bufs, _ = self._req.pop(rid)
+        d = {k: getattr(info, k) for k, _ in info._fields_}
+        if st != _lib.CT_OK:
+            raise _lib.CTError(st, f"request {rid} failed")
+        if kind == "render":
+            return d, bufs.numpy().copy()
+        if kind == "any":
+            return d, bufs[2].numpy().copy()
+        return d, (bufs[2].numpy().copy(), bufs[3].numpy().copy())
+
+    def stats(self) -> dict:
+        s = _lib.ct_server_stats()
+        check(self.ctx.lib.ct_server_get_stats(self.h, ctypes.byref(s)))
+        return {k: getattr(s, k) for k, _ in s._fields_}

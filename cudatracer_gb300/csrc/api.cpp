@@ -1330,6 +1330,14 @@ ct_status ct_batch_create(ct_ctx* ctx, const ct_batch_job* jobs, uint32_t n, int
     delete b;
     return s;
   }
+  for (uint32_t j = 0; j < n; j++) b->jobs0[j].accum = b->q.accum + b->bases[j];
+  cudaError_t e = cudaMemcpy(djobs, b->jobs0.data(), n * sizeof(BatchJob), cudaMemcpyHostToDevice);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(0);
+  if (e != cudaSuccess) {
+    free_all(ctx, b->allocs);
+    delete b;
+    return cuda_fail(ctx, e, "batch job table");
+  }
   b->dev.jobs = djobs;
   b->dev.bases = dbases;
   b->dev.n_jobs = (int32_t)n;
@@ -1444,3 +1452,68 @@ ct_status ct_batch_stats(ct_ctx* ctx, ct_batch* b, ct_frame_stats* out, int32_t 
 }
 
 }  // extern "C"
+
+// ============================================================ accessors for the serving loop (server.cpp)
+namespace ct {
+const DevScene& rt_scene_dev(const ct_scene* s) { return s->dev; }
+uint32_t rt_scene_tris(const ct_scene* s) { return s->nt; }
+const DevBVH& rt_bvh_dev(const ct_bvh* b) { return b->dev; }
+bool rt_bvh_wide(const ct_bvh* b) { return b->wide; }
+uint32_t rt_bvh_tris(const ct_bvh* b) { return b->nt; }
+int rt_ctx_device(const ct_ctx* c) { return c->device; }
+uint32_t* rt_ctx_error(const ct_ctx* c) { return c->d_error; }
+ct_status rt_fail(ct_ctx* c, ct_status s, const std::string& msg) { return fail(c, s, msg); }
+ct_status rt_alloc(ct_ctx* c, size_t bytes, void** p) {
+  Allocs a;
+  const ct_status s = dev_alloc(c, a, p, bytes);
+  return s;
+}
+void rt_free(ct_ctx* c, void* p, size_t bytes) {
+  if (!p) return;
+  bytes = (bytes == 0 ? 16 : bytes);
+  bytes = (bytes + 255) & ~(size_t)255;
+  cudaFree(p);
+  c->bytes -= bytes;
+}
+ct_status rt_alloc_queues(ct_ctx* c, size_t n, DevQueues& q, std::vector<std::pair<void*, size_t>>& owned) {
+  Allocs a;
+  const ct_status s = alloc_queues(c, a, n, q);
+  owned = a.list;
+  if (s != CT_OK) {
+    free_all(c, a);
+    owned.clear();
+  }
+  return s;
+}
+void rt_free_list(ct_ctx* c, std::vector<std::pair<void*, size_t>>& owned) {
+  Allocs a;
+  a.list = owned;
+  free_all(c, a);
+  owned.clear();
+}
+FrameConst rt_frame_const(const ct_camera* cam, const ct_render_params* p) { return batch_frame_const(cam, p); }
+const DevWBVH& rt_bvh_wdev(const ct_bvh* b) { return b->wdev; }
+bool rt_account(ct_ctx* c, int64_t delta) {
+  if (delta > 0 && c->budget && c->bytes.load() + (uint64_t)delta > c->budget) return false;
+  c->bytes += (uint64_t)delta;
+  return true;
+}
+ct_status rt_check_job(ct_ctx* ctx, const ct_batch_job& J) {
+  const ct_render_params* p = &J.params;
+  if (!J.scene || !J.bvh) return fail(ctx, CT_ERR_INVALID_ARGUMENT, "null scene or BVH");
+  if (J.bvh->nt != J.scene->nt) return fail(ctx, CT_ERR_INVALID_ARGUMENT, "BVH was built for another scene");
+  if (J.bvh->wide) return fail(ctx, CT_ERR_UNSUPPORTED, "frames trace quad BVHs");
+  if (p->width <= 0 || p->height <= 0 || (int64_t)p->width * p->height > (1 << 26))
+    return fail(ctx, CT_ERR_INVALID_ARGUMENT, "bad frame size");
+  if (p->max_depth < 1 || p->max_depth > 64) return fail(ctx, CT_ERR_INVALID_ARGUMENT, "max_depth must be in [1, 64]");
+  if (p->shading_mode != CT_SHADE_COMPAT && p->shading_mode != CT_SHADE_FULL)
+    return fail(ctx, CT_ERR_INVALID_ARGUMENT, "unknown shading mode");
+  if (p->texture_filter != CT_TEX_NEAREST && p->texture_filter != CT_TEX_BILINEAR)
+    return fail(ctx, CT_ERR_INVALID_ARGUMENT, "unknown texture filter");
+  if (J.spp == 0) return fail(ctx, CT_ERR_INVALID_ARGUMENT, "spp must be at least 1");
+  if (!finite3(J.camera.position) || !finite3(J.camera.forward) || !finite3(J.camera.up) ||
+      !std::isfinite(J.camera.fov_deg))
+    return fail(ctx, CT_ERR_INVALID_ARGUMENT, "non-finite camera");
+  return CT_OK;
+}
+}  // namespace ct

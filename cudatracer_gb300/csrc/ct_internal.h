@@ -138,6 +138,7 @@ struct BatchJob {
   DevScene sc;
   DevBVH bvh;
   FrameConst f;         // f.frame advances by 2 per sample, as launchKernels does
+  float4* accum;        // the job's own width*height accumulation
   int32_t pix_base;     // first pixel of the job in the batch
   int32_t max_depth;
   int32_t spp_left;     // samples still to take; the job traces while > 0
@@ -241,4 +242,33 @@ uint32_t noalloc_max_pixels();
 cudaError_t noalloc_render(int device, const DevScene& sc, const DevBVH& bvh, const FrameConst& f, int max_depth,
                            int exact_math, float4* accum, uint32_t* err, cudaStream_t s);
 
+
+}  // namespace ct
+
+// Host-side accessors of the runtime objects (api.cpp), for the serving loop.
+#include <string>
+#include <utility>
+#include <vector>
+
+#include "../../include/cudatracer.h"
+
+namespace ct {
+const DevScene& rt_scene_dev(const ct_scene* s);
+uint32_t rt_scene_tris(const ct_scene* s);
+const DevBVH& rt_bvh_dev(const ct_bvh* b);
+bool rt_bvh_wide(const ct_bvh* b);
+uint32_t rt_bvh_tris(const ct_bvh* b);
+int rt_ctx_device(const ct_ctx* c);
+uint32_t* rt_ctx_error(const ct_ctx* c);
+ct_status rt_fail(ct_ctx* c, ct_status s, const std::string& msg);
+// device allocation counted against the context's budget (rt_free gives it back)
+ct_status rt_alloc(ct_ctx* c, size_t bytes, void** p);
+void rt_free(ct_ctx* c, void* p, size_t bytes);
+ct_status rt_alloc_queues(ct_ctx* c, size_t n, DevQueues& q, std::vector<std::pair<void*, size_t>>& owned);
+void rt_free_list(ct_ctx* c, std::vector<std::pair<void*, size_t>>& owned);
+FrameConst rt_frame_const(const ct_camera* cam, const ct_render_params* p);
+const DevWBVH& rt_bvh_wdev(const ct_bvh* b);
+// count stream-ordered allocations against the context's budget (false: over budget)
+bool rt_account(ct_ctx* c, int64_t delta);
+ct_status rt_check_job(ct_ctx* ctx, const ct_batch_job& J);
 }  // namespace ct

@@ -137,8 +137,10 @@ struct Emit {
 // One ray of the compat shade stage.
 // pix_base: first pixel of the job in a batch (0 for a single job); seeds use
 // the job's own pixel index so a job renders the same alone and in a batch.
+// acc: where the job's pixels accumulate (q.accum when null); indexed by pix - pix_base.
 __device__ __forceinline__ void shade_compat(const DevScene& sc, const DevQueues& q, const FrameConst& f, int cur,
-                                             int i, uint32_t path_length, Emit& e, int pix_base = 0) {
+                                             int i, uint32_t path_length, Emit& e, int pix_base = 0,
+                                             float4* acc = nullptr) {
   const float4 o4 = q.org_q(cur)[i], d4 = q.dir_q(cur)[i], t4 = q.thr_q(cur)[i];
   const int2 h = q.hit[i];
   const int pix = __float_as_int(o4.w);
@@ -151,7 +153,7 @@ __device__ __forceinline__ void shade_compat(const DevScene& sc, const DevQueues
       const float u = 1.0f + (xatan2(dir.x, -dir.z) * kOneOverPi) * 0.5f;
       const float v = 1.0f - xacos(dir.y) * kOneOverPi;
       const float4 tc = tex_color(sc, sc.sky_tex, u, v, f.tex_filter);
-      accum_add(q.accum, pix, (T / last_pdf) * v3(tc));
+      accum_add(acc ? acc : q.accum, acc ? pix - pix_base : pix, (T / last_pdf) * v3(tc));
     }
     return;
   }
@@ -184,7 +186,7 @@ __device__ __forceinline__ void shade_compat(const DevScene& sc, const DevQueues
       const float lightPDF = ((t * t) / (DdotNL * tri_area(p0, p1, p2))) * (float)sc.light_count;
       c = (T * v3(alb)) * (1.0f / (last_pdf + lightPDF));
     }
-    accum_add(q.accum, pix, vmax0(c));
+    accum_add(acc ? acc : q.accum, acc ? pix - pix_base : pix, vmax0(c));
     return;
   }
   org = org + dir * t;  // getHitpoint
@@ -313,7 +315,8 @@ __device__ __forceinline__ void onb(V3 n, V3& t, V3& b) {
 }
 
 __device__ __forceinline__ void shade_full(const DevScene& sc, const DevQueues& q, const FrameConst& f, int cur, int i,
-                                           uint32_t path_length, Emit& e, int pix_base = 0) {
+                                           uint32_t path_length, Emit& e, int pix_base = 0,
+                                           float4* acc = nullptr) {
   const float4 o4 = q.org_q(cur)[i], d4 = q.dir_q(cur)[i], t4 = q.thr_q(cur)[i];
   const int2 h = q.hit[i];
   const int pix = __float_as_int(o4.w);
@@ -326,7 +329,7 @@ __device__ __forceinline__ void shade_full(const DevScene& sc, const DevQueues& 
     if (f.sky && sc.sky_tex >= 0) {
       const float u = 1.0f + (xatan2(dir.x, -dir.z) * kOneOverPi) * 0.5f;
       const float v = 1.0f - xacos(fminf(fmaxf(dir.y, -1.0f), 1.0f)) * kOneOverPi;
-      accum_add(q.accum, pix, T * v3(tex_color(sc, sc.sky_tex, u, v, f.tex_filter)));
+      accum_add(acc ? acc : q.accum, acc ? pix - pix_base : pix, T * v3(tex_color(sc, sc.sky_tex, u, v, f.tex_filter)));
     }
     return;
   }
@@ -362,7 +365,7 @@ __device__ __forceinline__ void shade_full(const DevScene& sc, const DevQueues& 
       const float light_pdf = (t * t) / (cos_l * 0.5f * area2 * (float)sc.light_count);
       w = (last_pdf * last_pdf) / (last_pdf * last_pdf + light_pdf * light_pdf);
     }
-    accum_add(q.accum, pix, vmax0(T * v3(alb) * w));
+    accum_add(acc ? acc : q.accum, acc ? pix - pix_base : pix, vmax0(T * v3(alb) * w));
     return;
   }
   const bool dielectric = full::is_dielectric(mtype);
@@ -557,9 +560,9 @@ __global__ void __launch_bounds__(kBlock) k_batch_shade(DevBatch bt, DevQueues q
       const int pix = __float_as_int(q.org_q(cur)[i].w);
       const BatchJob& J = bt.jobs[batch_job_of(bt.bases, bt.n_jobs, pix)];
       if (J.f.shading_mode == CT_MODE_FULL)
-        shade_full(J.sc, q, J.f, cur, i, path_length, e, J.pix_base);
+        shade_full(J.sc, q, J.f, cur, i, path_length, e, J.pix_base, J.accum);
       else
-        shade_compat(J.sc, q, J.f, cur, i, path_length, e, J.pix_base);
+        shade_compat(J.sc, q, J.f, cur, i, path_length, e, J.pix_base, J.accum);
       if (pass + 1 >= J.max_depth) e.cont = false;
     }
     const int si = warp_append(e.shadow, &q.counts[2]);

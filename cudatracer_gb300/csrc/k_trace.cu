@@ -253,12 +253,13 @@ __global__ void __launch_bounds__(BLOCK) k_batch_connect(DevBatch bt, DevQueues 
     }
     if (r.hit < 0) {
       const float4 c = __ldg(q.scol + i);
-      float4 a = q.accum[pix];
+      float4* acc = J.accum + (pix - J.pix_base);
+      float4 a = *acc;
       a.x = __fadd_rn(a.x, c.x);
       a.y = __fadd_rn(a.y, c.y);
       a.z = __fadd_rn(a.z, c.z);
       a.w = __fadd_rn(a.w, 1.0f);
-      q.accum[pix] = a;
+      *acc = a;
     }
   }
 }

@@ -1,0 +1,519 @@
+// Serving loop: continuous batching of render jobs and ray queries on one GPU.
+//
+// One scheduler thread owns the device work. Each turn it
+//   1. admits pending requests in arrival order while the HBM budget and the
+//      shared queue capacity allow (render: its accumulation buffer and its
+//      pixels of the queues; query: its ray and result buffers);
+//   2. starts admitted queries on the query stream (copy in, trace, copy out);
+//   3. runs one batched iteration of all admitted render jobs on the render
+//      stream (one sample each, the ct_batch kernels with a job table built
+//      for this iteration), at most two iterations ahead of the device;
+//   4. retires requests whose completion events have fired, freeing their
+//      device state and waking waiters.
+// Jobs arriving while others are on the GPU join at the next iteration; a
+// job's samples, seeds and per-pixel accumulation order do not depend on the
+// other jobs, so its result equals the job rendered alone.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <chrono>
+#include <condition_variable>
+#include <cstring>
+#include <deque>
+#include <mutex>
+#include <thread>
+#include <unordered_map>
+#include <vector>
+
+#include "../../include/cudatracer.h"
+#include "ct_internal.h"
+
+using namespace ct;
+
+namespace {
+
+enum Kind { kRender = 0, kClosest = 1, kAny = 2 };
+enum State { kPending, kActive, kFinishing, kDone };
+
+struct Request {
+  uint64_t id = 0;
+  Kind kind = kRender;
+  State state = kPending;
+  ct_status status = CT_OK;
+  // render
+  ct_batch_job job{};
+  float* host_out = nullptr;
+  uint32_t done_spp = 0;
+  // query
+  const ct_bvh* bvh = nullptr;
+  const float* horg = nullptr;
+  const float* hdir = nullptr;
+  uint32_t n = 0;
+  float tri_eps = 1e-3f;
+  int32_t* hhit = nullptr;
+  float* ht = nullptr;
+  uint8_t* hocc = nullptr;
+  // device state
+  void* dmem = nullptr;
+  size_t bytes = 0;
+  uint32_t pixels = 0;
+  cudaEvent_t ev = nullptr;
+  double t_submit = 0, t_admit = 0, t_done = 0;
+};
+
+size_t request_bytes(const Request& r) {
+  if (r.kind == kRender) return (size_t)r.pixels * sizeof(float4);
+  // org + dir + hit/occluded + t + cursor, each 256-byte aligned
+  auto al = [](size_t b) { return (b + 255) & ~(size_t)255; };
+  return al((size_t)r.n * 16) * 2 + al((size_t)r.n * 4) * 2 + 256;
+}
+
+}  // namespace
+
+struct ct_server {
+  ct_ctx* ctx = nullptr;
+  ct_server_config cfg{};
+  int device = 0;
+  std::thread th;
+  std::mutex mu;
+  std::condition_variable cv;       // work for the scheduler
+  std::condition_variable done_cv;  // completions for waiters
+  bool stop = false;
+  uint64_t next_id = 1;
+  std::deque<Request*> pending;                // guarded by mu
+  std::unordered_map<uint64_t, Request*> all;  // guarded by mu
+  ct_server_stats stats{};                     // guarded by mu
+  // scheduler-thread state
+  std::vector<Request*> render;     // admitted render jobs
+  std::vector<Request*> finishing;  // waiting for their completion event
+  size_t used_bytes = 0;
+  uint32_t inflight_pixels = 0;
+  std::chrono::steady_clock::time_point t0;
+  DevQueues q{};
+  std::vector<std::pair<void*, size_t>> q_owned;
+  int32_t max_stack = 1;
+  BatchJob* d_table[2] = {nullptr, nullptr};
+  int32_t* d_bases[2] = {nullptr, nullptr};
+  BatchJob* h_table[2] = {nullptr, nullptr};  // pinned staging
+  int32_t* h_bases[2] = {nullptr, nullptr};
+  uint32_t table_cap = 0;
+  cudaEvent_t table_ev[2] = {nullptr, nullptr};
+  int slot = 0;
+  cudaStream_t rs = nullptr, qs = nullptr;
+
+  double now() const { return std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count(); }
+  void loop();
+  void start(Request* r);
+  void start_query(Request* r);
+  cudaError_t render_iteration(std::vector<Request*>& finished);
+  void retire_locked();
+  void free_tables();
+};
+
+// Device state of an admitted request: stream-ordered allocation on the stream
+// that uses it, so freeing never waits for the whole device.
+void ct_server::start(Request* r) {
+  cudaStream_t st = r->kind == kRender ? rs : qs;
+  cudaError_t e = cudaMallocAsync(&r->dmem, r->bytes, st);
+  if (e != cudaSuccess) {
+    cudaGetLastError();
+    r->dmem = nullptr;
+    r->status = CT_ERR_OUT_OF_MEMORY;
+    return;
+  }
+  if (cudaEventCreateWithFlags(&r->ev, cudaEventDisableTiming) != cudaSuccess) {
+    r->status = CT_ERR_CUDA;
+    cudaFreeAsync(r->dmem, st);
+    r->dmem = nullptr;
+    return;
+  }
+  if (r->kind == kRender) {
+    if (cudaMemsetAsync(r->dmem, 0, r->bytes, rs) != cudaSuccess) {
+      r->status = CT_ERR_CUDA;
+      cudaFreeAsync(r->dmem, rs);
+      r->dmem = nullptr;
+    }
+  } else {
+    start_query(r);
+  }
+}
+
+void ct_server::start_query(Request* r) {
+  auto al = [](size_t b) { return (b + 255) & ~(size_t)255; };
+  char* m = (char*)r->dmem;
+  float4* org = (float4*)m;
+  float4* dir = (float4*)(m + al((size_t)r->n * 16));
+  int32_t* hit = (int32_t*)(m + 2 * al((size_t)r->n * 16));
+  float* t = (float*)(m + 2 * al((size_t)r->n * 16) + al((size_t)r->n * 4));
+  int* cursor = (int*)(m + 2 * al((size_t)r->n * 16) + 2 * al((size_t)r->n * 4));
+  cudaError_t e = cudaMemcpyAsync(org, r->horg, (size_t)r->n * 16, cudaMemcpyHostToDevice, qs);
+  if (e == cudaSuccess) e = cudaMemcpyAsync(dir, r->hdir, (size_t)r->n * 16, cudaMemcpyHostToDevice, qs);
+  if (e == cudaSuccess) {
+    uint32_t* err = rt_ctx_error(ctx);
+    if (rt_bvh_wide(r->bvh)) {
+      e = r->kind == kClosest
+              ? launch_trace_wide_closest(rt_bvh_wdev(r->bvh), org, dir, hit, t, r->n, err, cursor, nullptr, qs)
+              : launch_trace_wide_any(rt_bvh_wdev(r->bvh), org, dir, (uint8_t*)hit, r->n, err, cursor, nullptr, qs);
+    } else {
+      e = r->kind == kClosest
+              ? launch_trace_closest(rt_bvh_dev(r->bvh), org, dir, hit, t, r->n, r->tri_eps, err, cursor, qs)
+              : launch_trace_any(rt_bvh_dev(r->bvh), org, dir, (uint8_t*)hit, r->n, r->tri_eps, err, cursor, qs);
+    }
+  }
+  if (e == cudaSuccess) {
+    if (r->kind == kClosest) {
+      e = cudaMemcpyAsync(r->hhit, hit, (size_t)r->n * 4, cudaMemcpyDeviceToHost, qs);
+      if (e == cudaSuccess) e = cudaMemcpyAsync(r->ht, t, (size_t)r->n * 4, cudaMemcpyDeviceToHost, qs);
+    } else {
+      e = cudaMemcpyAsync(r->hocc, hit, (size_t)r->n, cudaMemcpyDeviceToHost, qs);
+    }
+  }
+  const cudaError_t fe = cudaFreeAsync(r->dmem, qs);  // after the copies, in stream order
+  r->dmem = nullptr;
+  if (e == cudaSuccess) e = fe;
+  if (e == cudaSuccess) e = cudaEventRecord(r->ev, qs);
+  if (e != cudaSuccess) {
+    cudaGetLastError();
+    r->status = CT_ERR_CUDA;
+  }
+}
+
+void ct_server::free_tables() {
+  for (int k = 0; k < 2; k++) {
+    if (d_table[k]) rt_free(ctx, d_table[k], (size_t)table_cap * sizeof(BatchJob));
+    if (d_bases[k]) rt_free(ctx, d_bases[k], (size_t)(table_cap + 1) * 4);
+    if (h_table[k]) cudaFreeHost(h_table[k]);
+    if (h_bases[k]) cudaFreeHost(h_bases[k]);
+    d_table[k] = nullptr, d_bases[k] = nullptr, h_table[k] = nullptr, h_bases[k] = nullptr;
+  }
+  table_cap = 0;
+}
+
+// One sample for every admitted render job. `finished` receives the jobs that
+// took their last one (their images are being copied out).
+cudaError_t ct_server::render_iteration(std::vector<Request*>& finished) {
+  const uint32_t n = (uint32_t)render.size();
+  // the table slot is free once the iteration that used it has finished
+  cudaError_t e = cudaEventSynchronize(table_ev[slot]);
+  if (e != cudaSuccess) return e;
+  if (n > table_cap) {
+    if ((e = cudaStreamSynchronize(rs)) != cudaSuccess) return e;  // the other slot may be in use
+    free_tables();
+    const uint32_t cap = std::max<uint32_t>(64, n * 2);
+    for (int k = 0; k < 2; k++) {
+      if (rt_alloc(ctx, (size_t)cap * sizeof(BatchJob), (void**)&d_table[k]) != CT_OK ||
+          rt_alloc(ctx, (size_t)(cap + 1) * 4, (void**)&d_bases[k]) != CT_OK)
+        return cudaErrorMemoryAllocation;
+      if ((e = cudaMallocHost((void**)&h_table[k], (size_t)cap * sizeof(BatchJob))) != cudaSuccess) return e;
+      if ((e = cudaMallocHost((void**)&h_bases[k], (size_t)(cap + 1) * 4)) != cudaSuccess) return e;
+    }
+    table_cap = cap;
+  }
+  BatchJob* ht = h_table[slot];
+  int32_t* hb = h_bases[slot];
+  int32_t base = 0, depth = 1;
+  for (uint32_t j = 0; j < n; j++) {
+    Request* r = render[j];
+    BatchJob& J = ht[j];
+    std::memset(&J, 0, sizeof(J));
+    J.sc = rt_scene_dev(r->job.scene);
+    J.bvh = rt_bvh_dev(r->job.bvh);
+    J.f = rt_frame_const(&r->job.camera, &r->job.params);
+    J.f.frame = r->job.params.frame_index + 2u * r->done_spp;
+    J.accum = (float4*)r->dmem;
+    J.pix_base = base;
+    J.max_depth = r->job.params.max_depth;
+    J.spp_left = 1;
+    J.exact = cfg.exact_math;
+    hb[j] = base;
+    base += (int32_t)r->pixels;
+    depth = std::max(depth, r->job.params.max_depth);
+    max_stack = std::max(max_stack, J.bvh.stack_entries);
+  }
+  hb[n] = base;
+  if ((e = cudaMemcpyAsync(d_table[slot], ht, (size_t)n * sizeof(BatchJob), cudaMemcpyHostToDevice, rs)) != cudaSuccess)
+    return e;
+  if ((e = cudaMemcpyAsync(d_bases[slot], hb, (size_t)(n + 1) * 4, cudaMemcpyHostToDevice, rs)) != cudaSuccess) return e;
+  if ((e = cudaMemsetAsync(q.counts, 0, 16 * sizeof(int32_t), rs)) != cudaSuccess) return e;
+  DevBatch b{d_table[slot], d_bases[slot], (int32_t)n, base, max_stack, 0};
+  const bool fast = !cfg.exact_math;
+  e = launch_batch_raygen(b, q, cfg.exact_math, rs);
+  for (int pass = 0; pass < depth && e == cudaSuccess; pass++) {
+    const int cur = pass & 1;
+    const uint32_t path_length = pass == 0 ? 0u : (uint32_t)pass + 1u;  // Kernel.cu:306, 330
+    e = launch_batch_extend(b, q, cur, fast, 128, rs);
+    if (e == cudaSuccess) e = launch_batch_shade(b, q, cur, path_length, pass, cfg.exact_math, 1, rs);
+    if (e == cudaSuccess) e = launch_batch_connect(b, q, fast, 128, rs);
+  }
+  if (e == cudaSuccess) e = cudaEventRecord(table_ev[slot], rs);
+  slot ^= 1;
+  std::vector<Request*> keep;
+  for (Request* r : render) {
+    r->done_spp++;
+    if (r->done_spp < r->job.spp) {
+      keep.push_back(r);
+      continue;
+    }
+    if (e == cudaSuccess)
+      e = cudaMemcpyAsync(r->host_out, r->dmem, (size_t)r->pixels * sizeof(float4), cudaMemcpyDeviceToHost, rs);
+    if (e == cudaSuccess) e = cudaFreeAsync(r->dmem, rs);
+    if (e == cudaSuccess) e = cudaEventRecord(r->ev, rs);
+    inflight_pixels -= r->pixels;  // later iterations are ordered after this one on the stream
+    finished.push_back(r);
+  }
+  render.swap(keep);
+  return e;
+}
+
+void ct_server::retire_locked() {
+  std::vector<Request*> keep;
+  bool any = false;
+  for (Request* r : finishing) {
+    const cudaError_t qr = r->ev ? cudaEventQuery(r->ev) : cudaSuccess;
+    if (qr == cudaErrorNotReady) {
+      keep.push_back(r);
+      continue;
+    }
+    if (qr != cudaSuccess && r->status == CT_OK) r->status = CT_ERR_CUDA;
+    if (r->t_admit > 0 || r->bytes) {
+      used_bytes -= r->bytes;
+      rt_account(ctx, -(int64_t)r->bytes);
+    }
+    r->dmem = nullptr;
+    if (r->ev) cudaEventDestroy(r->ev), r->ev = nullptr;
+    r->t_done = now();
+    r->state = kDone;
+    if (r->status == CT_OK) stats.completed++;
+    else stats.failed++;
+    any = true;
+  }
+  finishing.swap(keep);
+  if (any) done_cv.notify_all();
+}
+
+void ct_server::loop() {
+  cudaSetDevice(device);
+  std::unique_lock<std::mutex> lk(mu);
+  while (true) {
+    if (pending.empty() && render.empty() && finishing.empty()) {
+      if (stop) break;
+      cv.wait(lk, [&] { return stop || !pending.empty(); });
+      continue;
+    }
+    // admissions in arrival order (accounting under the lock, device work outside)
+    std::vector<Request*> admitted;
+    while (!pending.empty()) {
+      Request* r = pending.front();
+      r->bytes = request_bytes(*r);
+      const bool fits_budget = cfg.hbm_budget == 0 || used_bytes + r->bytes <= cfg.hbm_budget;
+      const bool fits_queue = r->kind != kRender || inflight_pixels + r->pixels <= cfg.max_inflight_pixels;
+      if (!fits_budget || !fits_queue) {
+        if (render.empty() && finishing.empty() && admitted.empty()) {
+          // cannot fit even with nothing else admitted
+          pending.pop_front();
+          r->status = CT_ERR_OUT_OF_MEMORY;
+          r->bytes = 0;
+          r->state = kFinishing;
+          finishing.push_back(r);
+          continue;
+        }
+        break;
+      }
+      if (!rt_account(ctx, (int64_t)r->bytes)) {
+        pending.pop_front();
+        r->status = CT_ERR_OUT_OF_MEMORY;
+        r->bytes = 0;
+        r->state = kFinishing;
+        finishing.push_back(r);
+        continue;
+      }
+      pending.pop_front();
+      used_bytes += r->bytes;
+      stats.peak_bytes = std::max<uint64_t>(stats.peak_bytes, used_bytes);
+      if (r->kind == kRender) inflight_pixels += r->pixels;
+      else stats.query_rays += r->n;
+      r->t_admit = now();
+      admitted.push_back(r);
+    }
+    lk.unlock();
+    for (Request* r : admitted) start(r);
+    std::vector<Request*> finished;
+    for (Request* r : admitted) {
+      if (r->status != CT_OK) {
+        if (r->kind == kRender) inflight_pixels -= r->pixels;
+        finished.push_back(r);
+      } else if (r->kind == kRender) {
+        render.push_back(r);
+      } else {
+        finished.push_back(r);  // completion event recorded on the query stream
+      }
+    }
+    bool iterated = false;
+    if (!render.empty()) {
+      const cudaError_t e = render_iteration(finished);
+      iterated = true;
+      if (e != cudaSuccess) {
+        cudaGetLastError();
+        for (Request* r : render) r->status = CT_ERR_CUDA, finished.push_back(r);
+        render.clear();
+      }
+    }
+    lk.lock();
+    if (iterated) stats.iterations++;
+    for (Request* r : finished) r->state = kFinishing, finishing.push_back(r);
+    retire_locked();
+    if (render.empty() && !finishing.empty() && pending.empty()) {
+      // only completions outstanding: wait briefly instead of spinning
+      lk.unlock();
+      std::this_thread::sleep_for(std::chrono::microseconds(50));
+      lk.lock();
+    }
+  }
+}
+
+extern "C" {
+
+ct_status ct_server_create(ct_ctx* ctx, const ct_server_config* cfg, ct_server** out) {
+  if (!ctx || !cfg || !out || cfg->max_inflight_pixels == 0) return rt_fail(ctx, CT_ERR_INVALID_ARGUMENT, "bad server config");
+  *out = nullptr;
+  if (cudaSetDevice(rt_ctx_device(ctx)) != cudaSuccess) return rt_fail(ctx, CT_ERR_CUDA, "cudaSetDevice");
+  auto* s = new ct_server();
+  s->ctx = ctx;
+  s->cfg = *cfg;
+  s->device = rt_ctx_device(ctx);
+  s->t0 = std::chrono::steady_clock::now();
+  ct_status st = rt_alloc_queues(ctx, cfg->max_inflight_pixels, s->q, s->q_owned);
+  cudaError_t e = cudaSuccess;
+  // keep freed request memory in the device's pool between requests
+  cudaMemPool_t pool = nullptr;
+  if (cudaDeviceGetDefaultMemPool(&pool, s->device) == cudaSuccess) {
+    uint64_t keep = ~0ull;
+    cudaMemPoolSetAttribute(pool, cudaMemPoolAttrReleaseThreshold, &keep);
+  }
+  if (st == CT_OK) e = cudaStreamCreateWithFlags(&s->rs, cudaStreamNonBlocking);
+  if (st == CT_OK && e == cudaSuccess) e = cudaStreamCreateWithFlags(&s->qs, cudaStreamNonBlocking);
+  for (int k = 0; k < 2 && st == CT_OK && e == cudaSuccess; k++) {
+    e = cudaEventCreateWithFlags(&s->table_ev[k], cudaEventDisableTiming);
+    if (e == cudaSuccess) e = cudaEventRecord(s->table_ev[k], s->rs);
+  }
+  if (st != CT_OK || e != cudaSuccess) {
+    rt_free_list(ctx, s->q_owned);
+    delete s;
+    return st != CT_OK ? st : rt_fail(ctx, CT_ERR_CUDA, cudaGetErrorString(e));
+  }
+  s->th = std::thread([s] { s->loop(); });
+  *out = s;
+  return CT_OK;
+}
+
+ct_status ct_server_destroy(ct_server* s) {
+  if (!s) return CT_ERR_INVALID_ARGUMENT;
+  {
+    std::lock_guard<std::mutex> g(s->mu);
+    s->stop = true;
+  }
+  s->cv.notify_all();
+  s->th.join();
+  cudaSetDevice(s->device);
+  cudaDeviceSynchronize();
+  for (auto& kv : s->all) delete kv.second;
+  s->free_tables();
+  for (int k = 0; k < 2; k++)
+    if (s->table_ev[k]) cudaEventDestroy(s->table_ev[k]);
+  rt_free_list(s->ctx, s->q_owned);
+  if (s->rs) cudaStreamDestroy(s->rs);
+  if (s->qs) cudaStreamDestroy(s->qs);
+  delete s;
+  return CT_OK;
+}
+
+ct_status ct_server_submit_render(ct_server* s, const ct_batch_job* job, float* host_out, uint64_t* request_id) {
+  if (!s || !job || !host_out || !request_id) return CT_ERR_INVALID_ARGUMENT;
+  const ct_status st = rt_check_job(s->ctx, *job);
+  if (st != CT_OK) return st;
+  auto* r = new Request();
+  r->kind = kRender;
+  r->job = *job;
+  r->host_out = host_out;
+  r->pixels = (uint32_t)(job->params.width * job->params.height);
+  {
+    std::lock_guard<std::mutex> g(s->mu);
+    r->id = s->next_id++;
+    r->t_submit = s->now();
+    s->all[r->id] = r;
+    s->pending.push_back(r);
+    s->stats.submitted++;
+  }
+  s->cv.notify_all();
+  *request_id = r->id;
+  return CT_OK;
+}
+
+ct_status ct_server_submit_query(ct_server* s, const ct_bvh* bvh, const float* host_org, const float* host_dir,
+                                 uint32_t n, float tri_eps, int32_t any_hit, int32_t* host_hit, float* host_t,
+                                 uint8_t* host_occluded, uint64_t* request_id) {
+  if (!s || !bvh || !host_org || !host_dir || !request_id || n == 0) return CT_ERR_INVALID_ARGUMENT;
+  if (any_hit ? !host_occluded : (!host_hit || !host_t)) return CT_ERR_INVALID_ARGUMENT;
+  auto* r = new Request();
+  r->kind = any_hit ? kAny : kClosest;
+  r->bvh = bvh;
+  r->horg = host_org;
+  r->hdir = host_dir;
+  r->n = n;
+  r->tri_eps = tri_eps;
+  r->hhit = host_hit;
+  r->ht = host_t;
+  r->hocc = host_occluded;
+  {
+    std::lock_guard<std::mutex> g(s->mu);
+    r->id = s->next_id++;
+    r->t_submit = s->now();
+    s->all[r->id] = r;
+    s->pending.push_back(r);
+    s->stats.submitted++;
+  }
+  s->cv.notify_all();
+  *request_id = r->id;
+  return CT_OK;
+}
+
+ct_status ct_server_wait(ct_server* s, uint64_t id, double timeout_s, ct_request_info* info) {
+  if (!s) return CT_ERR_INVALID_ARGUMENT;
+  std::unique_lock<std::mutex> lk(s->mu);
+  auto it = s->all.find(id);
+  if (it == s->all.end()) return CT_ERR_INVALID_ARGUMENT;
+  Request* r = it->second;
+  auto done = [&] { return r->state == kDone; };
+  if (timeout_s < 0) {
+    s->done_cv.wait(lk, done);
+  } else if (!s->done_cv.wait_for(lk, std::chrono::duration<double>(timeout_s), done)) {
+    return CT_ERR_TIMEOUT;
+  }
+  if (info) {
+    info->status = r->status;
+    info->kind = (int32_t)r->kind;
+    info->submit_s = r->t_submit;
+    info->admit_s = r->t_admit;
+    info->done_s = r->t_done;
+    info->device_bytes = r->bytes;
+  }
+  const ct_status st = r->status;
+  s->all.erase(it);
+  delete r;
+  return st;
+}
+
+ct_status ct_server_get_stats(ct_server* s, ct_server_stats* out) {
+  if (!s || !out) return CT_ERR_INVALID_ARGUMENT;
+  unsigned long long h[8] = {0};
+  cudaSetDevice(s->device);
+  // ray counters of the render iterations (current when no iteration is running)
+  if (cudaMemcpy(h, s->q.stats, sizeof(h), cudaMemcpyDeviceToHost) != cudaSuccess) return CT_ERR_CUDA;
+  std::lock_guard<std::mutex> g(s->mu);
+  *out = s->stats;
+  out->extension_rays = h[0];
+  out->shadow_rays = h[1];
+  return CT_OK;
+}
+
+}  // extern "C"

@@ -320,6 +320,51 @@ ct_status ct_batch_autotune(ct_ctx* ctx, ct_batch* b, void* stream, ct_batch_tun
 /* Ray and sample counters of the batch (frames = iterations). */
 ct_status ct_batch_stats(ct_ctx* ctx, ct_batch* b, ct_frame_stats* out, int32_t reset, void* stream);
 
+/* ---- serving (no reference counterpart): a scheduler thread that admits
+ * render jobs and ray queries as they arrive, against an HBM budget, and
+ * keeps the GPU busy with all admitted work at once. Render jobs join the
+ * batched iterations (one sample per job per iteration, as ct_batch) at the
+ * next iteration boundary and leave when their samples are done; ray queries
+ * run on a second stream, overlapping the iterations. Requests are admitted
+ * in arrival order; one that can never fit fails with CT_ERR_OUT_OF_MEMORY.
+ * Results are the same as the request alone (a render job's pixels use their
+ * own seeds; queries are per ray). Host buffers given to the server must stay
+ * valid until the request is waited for; pinned buffers let copies overlap. */
+typedef struct ct_server ct_server;
+typedef struct ct_server_config {
+  uint64_t hbm_budget;          /* bytes of per-request device state admitted at once (0 = no limit) */
+  uint32_t max_inflight_pixels; /* shared ray-queue capacity: pixels of all render jobs in flight */
+  int32_t exact_math;           /* math mode of every render job */
+} ct_server_config;
+typedef struct ct_request_info {
+  ct_status status;
+  int32_t kind;                 /* 0 render, 1 closest-hit query, 2 any-hit query */
+  double submit_s, admit_s, done_s;  /* seconds since the server started */
+  uint64_t device_bytes;        /* device state the request held */
+} ct_request_info;
+typedef struct ct_server_stats {
+  uint64_t submitted, completed, failed;
+  uint64_t iterations;          /* batched render iterations run */
+  uint64_t peak_bytes;          /* largest per-request device state admitted at once */
+  uint64_t extension_rays, shadow_rays, query_rays;
+} ct_server_stats;
+ct_status ct_server_create(ct_ctx* ctx, const ct_server_config* cfg, ct_server** out);
+/* Stops admitting, finishes every admitted request, joins the thread. */
+ct_status ct_server_destroy(ct_server* srv);
+/* A render job (as in a batch); at completion the float4 accumulation
+ * (width*height*4 floats) is copied to host_out. */
+ct_status ct_server_submit_render(ct_server* srv, const ct_batch_job* job, float* host_out, uint64_t* request_id);
+/* n rays from host buffers (org/dir float4 as for ct_trace_closest) against a
+ * resident BVH (quad or wide); closest hit into host_hit/host_t, or with
+ * any_hit occlusion (uint8) into host_occluded. */
+ct_status ct_server_submit_query(ct_server* srv, const ct_bvh* bvh, const float* host_org, const float* host_dir,
+                                 uint32_t n, float tri_eps, int32_t any_hit, int32_t* host_hit, float* host_t,
+                                 uint8_t* host_occluded, uint64_t* request_id);
+/* Block until the request is done (timeout_s < 0: no limit); the request is
+ * forgotten afterwards. CT_ERR_TIMEOUT when the time runs out first. */
+ct_status ct_server_wait(ct_server* srv, uint64_t request_id, double timeout_s, ct_request_info* info);
+ct_status ct_server_get_stats(ct_server* srv, ct_server_stats* out);
+
 /* ---- rendering: replaces launchKernels (src/CUDA/Kernel.cu:355) and its
  * buffers (Application::allocateBuffers, src/Application.cpp:141-154).
  * A ct_render holds one job's resident state: ray queues, shadow queue,

@@ -1,0 +1,152 @@
+"""The serving loop (ct_server_*): requests admitted as they arrive against an
+HBM budget, render jobs batched continuously, ray queries overlapping.
+
+Each result must be the same alone and in the mix: a request served by
+itself and the same request submitted together with many others (renders of
+other scenes, sizes, depths and sample counts; closest-hit and any-hit
+queries on quad and wide BVHs) give identical bytes."""
+import time
+
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.fixture(scope="module")
+def world(gpu_ctx):
+    from cudatracer_gb300 import api, scenes
+
+    out = {"render": [], "query": []}
+    for k, (grid, spheres, seed) in enumerate([(48, 6, 11), (96, 10, 12), (32, 3, 13)]):
+        ts, cam = scenes.terrain_scene(grid=grid, spheres=spheres, seed=seed, extent=60.0, sky_size=(128, 64))
+        sc = gpu_ctx.scene(scenes.scene_arrays(ts), [api.Material(**m) for m in ts.materials], ts.textures,
+                           ts.skybox_texture)
+        out["render"].append(dict(sc=sc, bvh=sc.build_bvh_device(), cam=dict(cam, position=(0.0, 14.0, 34.0))))
+    s = scenes.soup_scene(100000, seed=14)
+    arr = {"vertices": s.vertices, "normals": np.tile(np.array([[0, 0, 1]], np.float32), (s.vertices.shape[0], 1)),
+           "indices": s.indices}
+    sq = gpu_ctx.scene(arr, [api.Material()])
+    out["query"] = [sq.build_bvh_device(), sq.build_bvh_wide()]
+    out["soup_scene"] = sq
+    return out
+
+
+def _render_job(S, W, H, depth, spp, shading=0):
+    from cudatracer_gb300 import api
+
+    cam = S["cam"]
+    p = api.default_params(W, H)
+    p.max_depth, p.shading_mode = depth, shading
+    return dict(scene=S["sc"], bvh=S["bvh"], camera=api.Camera(W, H, cam["fov"], cam["position"], cam["forward"],
+                                                                cam["up"]), params=p, spp=spp)
+
+
+def _requests(world):
+    from cudatracer_gb300 import scenes
+
+    R = world["render"]
+    reqs = [
+        ("render", _render_job(R[0], 48, 32, 5, 3)),
+        ("render", _render_job(R[1], 64, 64, 8, 6, shading=1)),
+        ("render", _render_job(R[2], 20, 30, 4, 9)),
+        ("render", _render_job(R[0], 96, 48, 12, 2)),
+        ("render", _render_job(R[1], 16, 16, 6, 12)),
+    ]
+    for k in range(6):
+        o, d = scenes.incoherent_rays(5000 * (k + 1), seed=30 + k)
+        if k % 2:
+            d[:, 3] = 0.05 * (k + 1)
+        reqs.append(("query", dict(bvh=world["query"][k % 2], org=o, dir=d, any_hit=bool(k % 2), tri_eps=1e-12)))
+    return reqs
+
+
+def _submit(srv, kind, r):
+    if kind == "render":
+        return srv.submit_render(r)
+    return srv.submit_query(r["bvh"], r["org"], r["dir"], any_hit=r["any_hit"], tri_eps=r["tri_eps"])
+
+
+def _same(a, b):
+    if isinstance(a, tuple):
+        return all(_same(x, y) for x, y in zip(a, b))
+    return np.array_equal(np.ascontiguousarray(a).view(np.uint8), np.ascontiguousarray(b).view(np.uint8))
+
+
+def test_each_result_same_alone_and_in_mix(gpu_ctx, world):
+    from cudatracer_gb300 import api
+
+    reqs = _requests(world)
+    srv = api.Server(gpu_ctx, max_inflight_pixels=1 << 16)
+    alone = []
+    for kind, r in reqs:
+        rid = _submit(srv, kind, r)
+        alone.append(srv.wait(rid)[1])
+    srv.close()
+    # all at once, in a shuffled order, some arriving while others run
+    srv = api.Server(gpu_ctx, max_inflight_pixels=1 << 16)
+    order = np.random.default_rng(5).permutation(len(reqs))
+    ids = {}
+    for k, i in enumerate(order):
+        ids[i] = _submit(srv, *reqs[i])
+        if k % 3 == 2:
+            time.sleep(0.002)
+    mixed = {i: srv.wait(ids[i]) for i in order}
+    st = srv.stats()
+    srv.close()
+    gpu_ctx.check()
+    for i in range(len(reqs)):
+        assert _same(alone[i], mixed[i][1]), i
+        info = mixed[i][0]
+        assert info["status"] == 0 and info["submit_s"] <= info["admit_s"] <= info["done_s"]
+    assert st["completed"] == len(reqs) and st["failed"] == 0
+    assert st["iterations"] >= 12  # the longest render job's samples
+
+
+def test_render_equals_batch_and_queries_equal_direct_calls(gpu_ctx, world):
+    import torch
+
+    from cudatracer_gb300 import api
+
+    reqs = _requests(world)
+    srv = api.Server(gpu_ctx)
+    ids = [_submit(srv, *r) for r in reqs]
+    res = [srv.wait(i)[1] for i in ids]
+    srv.close()
+    for (kind, r), got in zip(reqs, res):
+        if kind == "render":
+            b = api.Batch(gpu_ctx, [r])
+            b.run()
+            torch.cuda.synchronize()
+            assert _same(b.accum_tensor(0).cpu().numpy(), got)
+            b.close()
+        else:
+            o, d = torch.from_numpy(r["org"]).cuda(), torch.from_numpy(r["dir"]).cuda()
+            if r["any_hit"]:
+                ref = r["bvh"].trace_any(o, d, tri_eps=r["tri_eps"]).cpu().numpy()
+            else:
+                h, t = r["bvh"].trace_closest(o, d, tri_eps=r["tri_eps"])
+                ref = (h.cpu().numpy(), t.cpu().numpy())
+            assert _same(ref, got)
+
+
+def test_admission_respects_the_budget(gpu_ctx, world):
+    from cudatracer_gb300 import _lib, api
+
+    reqs = _requests(world)
+    sizes = [r["params"].width * r["params"].height * 16 if k == "render" else r["org"].shape[0] * 40 + 2048
+             for k, r in reqs]
+    budget = max(sizes) + 4096
+    srv = api.Server(gpu_ctx, hbm_budget=budget, max_inflight_pixels=1 << 16)
+    ids = [_submit(srv, *r) for r in reqs]
+    for i in ids:
+        srv.wait(i)
+    st = srv.stats()
+    assert 0 < st["peak_bytes"] <= budget and st["completed"] == len(reqs)
+    # a request that can never fit fails instead of waiting forever
+    big = _render_job(world["render"][0], 512, 512, 4, 1)
+    rid = srv.submit_render(big)
+    with pytest.raises(_lib.CTError) as e:
+        srv.wait(rid, timeout=30.0)
+    assert e.value.status == _lib.CT_ERR_OUT_OF_MEMORY
+    srv.close()
