@@ -50,6 +50,8 @@ def parse_args():
     ap.add_argument("--height", type=int, default=1080)
     ap.add_argument("--skip-extras", action="store_true",
                     help="only the timed frames: no e2e pass, roofline model, CPU baseline or sphere query")
+    ap.add_argument("--skip-serving", action="store_true",
+                    help="leave out the 256-job batching and the Poisson serving workloads")
     ap.add_argument("--skip-precision", action="store_true",
                     help="leave out the 10M-triangle precision workload (wide vs quad BVH against FP64)")
     args = ap.parse_args()
@@ -348,6 +350,208 @@ def precision_c3(ctx, ntri: int = 10_000_000, nray: int = 16_000_000, sample_eve
     return out
 
 
+def batching_c4(ctx, n_jobs: int = 256, seed: int = 2024) -> dict:
+    """The batching workload: n_jobs render jobs of the terrain-plus-spheres
+    kind, triangle counts log-uniform 10k..2M, square resolutions log-uniform
+    64..1024, spp log-uniform 1..64, depth uniform 4..12, all in one batch
+    (autotuned launch shapes, graph-replayed iterations); against the same
+    jobs rendered one after another through the plain per-job path."""
+    import numpy as np
+    import torch
+
+    from cudatracer_gb300 import api, scenes
+
+    rng = np.random.default_rng(seed)
+    jobs, tris = [], 0
+    t0 = time.perf_counter()
+    for _ in range(n_jobs):
+        tri = float(np.exp(rng.uniform(np.log(1e4), np.log(2e6))))
+        sph = int(rng.integers(2, 40))
+        grid = int(max(16, np.sqrt(max(1.0, tri - sph * 5120) / 2) + 1))
+        side = int(np.exp(rng.uniform(np.log(64), np.log(1024))))
+        spp = int(np.exp(rng.uniform(0.0, np.log(64))))
+        depth = int(rng.integers(4, 13))
+        ts, cam = scenes.terrain_scene(grid=grid, spheres=sph, seed=int(rng.integers(1, 100000)), extent=200.0,
+                                       sky_size=(256, 128))
+        sc = ctx.scene(scenes.scene_arrays(ts), [api.Material(**m) for m in ts.materials], ts.textures,
+                       ts.skybox_texture)
+        p = api.default_params(side, side)
+        p.max_depth = depth
+        jobs.append(dict(scene=sc, bvh=sc.build_bvh_device(), params=p, spp=spp,
+                         camera=api.Camera(side, side, cam["fov"], cam["position"], cam["forward"], cam["up"])))
+        tris += ts.indices.shape[0]
+    setup_s = time.perf_counter() - t0
+    samples = sum(j["spp"] * j["params"].width * j["params"].height for j in jobs)
+    b = api.Batch(ctx, jobs)
+    tuning, tune_ms = b.autotune()
+    b.run()
+    torch.cuda.synchronize()
+    b.stats(reset=True)
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record()
+    b.run()
+    e1.record()
+    torch.cuda.synchronize()
+    ms = e0.elapsed_time(e1)
+    st = b.stats(reset=True)
+    ctx.check()
+    b.close()
+    # the same jobs, one after another, through ct_render_accumulate
+    e0.record()
+    for j in jobs:
+        W, H = j["params"].width, j["params"].height
+        rj = api.RenderJob(ctx, W, H)
+        pp = api.Params(W, H, camera=j["camera"], max_depth=j["params"].max_depth)
+        pp.reset(rj)
+        for _ in range(j["spp"]):
+            api.launch_kernels(rj, j["scene"], j["bvh"], pp)
+    e1.record()
+    torch.cuda.synchronize()
+    serial_ms = e0.elapsed_time(e1)
+    for j in jobs:
+        j["bvh"].close()
+        j["scene"].close()
+    return {
+        "workload": f"{n_jobs} jobs, {tris:,} triangles, {samples:,} samples (res 64..1024, spp 1..64, depth 4..12)",
+        "msamples_per_s": samples / ms / 1e3, "mrays_per_s": (st["extension_rays"] + st["shadow_rays"]) / ms / 1e3,
+        "ms": ms, "iterations": st["frames"], "tuning": tuning, "autotune_ms_per_iteration": tune_ms,
+        "serial_plain_ms": serial_ms, "serial_plain_msamples_per_s": samples / serial_ms / 1e3,
+        "speedup_vs_serial": serial_ms / ms, "setup_s": setup_s,
+    }
+
+
+def serving_c5(ctx, rate: float = 100.0, duration_s: float = 5.0, seed: int = 77) -> dict:
+    """The serving workload: a Poisson request stream (rate req/s for
+    duration_s) mixing render jobs (config-4 distribution over 16 resident
+    terrain scenes) and ray queries (10k..4M incoherent rays against resident
+    wide BVHs of 10k..10M-triangle soups), through ct_server with a 150 GB
+    HBM budget. Latency = completion - submission. Serial plain execution: the
+    same requests' service times measured one at a time through the plain
+    per-request path, queued FIFO at the same arrival times."""
+    import threading
+
+    import numpy as np
+    import torch
+
+    from cudatracer_gb300 import api, scenes
+
+    rng = np.random.default_rng(seed)
+    t0 = time.perf_counter()
+    rscenes = []
+    for k in range(16):
+        tri = float(np.exp(rng.uniform(np.log(1e4), np.log(2e6))))
+        sph = int(rng.integers(2, 40))
+        grid = int(max(16, np.sqrt(max(1.0, tri - sph * 5120) / 2) + 1))
+        ts, cam = scenes.terrain_scene(grid=grid, spheres=sph, seed=100 + k, extent=200.0, sky_size=(256, 128))
+        sc = ctx.scene(scenes.scene_arrays(ts), [api.Material(**m) for m in ts.materials], ts.textures,
+                       ts.skybox_texture)
+        rscenes.append((sc, sc.build_bvh_device(), cam))
+    qbvhs = []
+    for k, ntri in enumerate([10_000, 100_000, 1_000_000, 10_000_000]):
+        s = scenes.soup_scene(ntri, seed=200 + k)
+        arr = {"vertices": s.vertices, "normals": np.tile(np.array([[0, 0, 1]], np.float32), (s.vertices.shape[0], 1)),
+               "indices": s.indices}
+        sq = ctx.scene(arr, [api.Material()])
+        qbvhs.append((sq, sq.build_bvh_wide()))
+    ray_o, ray_d = scenes.incoherent_rays(4_000_000, seed=seed)
+    setup_s = time.perf_counter() - t0
+    # the request list
+    n_req = int(rate * duration_s)
+    arrivals = np.cumsum(rng.exponential(1.0 / rate, n_req))
+    reqs = []
+    for _ in range(n_req):
+        if rng.uniform() < 0.5:
+            sc, bvh, cam = rscenes[int(rng.integers(0, len(rscenes)))]
+            side = int(np.exp(rng.uniform(np.log(64), np.log(1024))))
+            p = api.default_params(side, side)
+            p.max_depth = int(rng.integers(4, 13))
+            reqs.append(("render", dict(scene=sc, bvh=bvh, params=p, spp=int(np.exp(rng.uniform(0.0, np.log(64)))),
+                                        camera=api.Camera(side, side, cam["fov"], cam["position"], cam["forward"],
+                                                          cam["up"]))))
+        else:
+            n = int(np.exp(rng.uniform(np.log(1e4), np.log(4e6))))
+            off = int(rng.integers(0, ray_o.shape[0] - n + 1))
+            reqs.append(("query", dict(bvh=qbvhs[int(rng.integers(0, len(qbvhs)))][1], n=n, off=off)))
+
+    def submit(srv, kind, r):
+        if kind == "render":
+            return srv.submit_render(r)
+        return srv.submit_query(r["bvh"], ray_o[r["off"]:r["off"] + r["n"]], ray_d[r["off"]:r["off"] + r["n"]])
+
+    srv = api.Server(ctx, hbm_budget=150 << 30, max_inflight_pixels=1 << 24)
+    ids = [None] * n_req
+
+    def client():
+        start = time.perf_counter()
+        for i, (kind, r) in enumerate(reqs):
+            delay = arrivals[i] - (time.perf_counter() - start)
+            if delay > 0:
+                time.sleep(delay)
+            ids[i] = submit(srv, kind, r)
+
+    th = threading.Thread(target=client)
+    w0 = time.perf_counter()
+    th.start()
+    th.join()
+    infos = []
+    for i in range(n_req):
+        infos.append(srv.wait(ids[i])[0])
+    wall = time.perf_counter() - w0
+    st = srv.stats()
+    srv.close()
+    ctx.check()
+    lat = np.array([x["done_s"] - x["submit_s"] for x in infos]) * 1e3
+    kinds = np.array([k == "render" for k, _ in reqs])
+    rays = st["extension_rays"] + st["shadow_rays"] + st["query_rays"]
+    # serial plain execution: each request alone through the plain path
+    svc = []
+    for kind, r in reqs:
+        torch.cuda.synchronize()
+        a = time.perf_counter()
+        if kind == "render":
+            W, H = r["params"].width, r["params"].height
+            rj = api.RenderJob(ctx, W, H)
+            pp = api.Params(W, H, camera=r["camera"], max_depth=r["params"].max_depth)
+            pp.reset(rj)
+            for _ in range(r["spp"]):
+                api.launch_kernels(rj, r["scene"], r["bvh"], pp)
+            rj.accum_tensor().cpu()
+        else:
+            o = torch.from_numpy(ray_o[r["off"]:r["off"] + r["n"]]).cuda()
+            d = torch.from_numpy(ray_d[r["off"]:r["off"] + r["n"]]).cuda()
+            h, t = r["bvh"].trace_closest(o, d)
+            h.cpu(), t.cpu()
+        torch.cuda.synchronize()
+        svc.append(time.perf_counter() - a)
+    finish, slat = 0.0, []
+    for a_t, s_t in zip(arrivals, svc):
+        finish = max(finish, a_t) + s_t
+        slat.append((finish - a_t) * 1e3)
+    slat = np.array(slat)
+
+    def pct(x):
+        return {"p50": float(np.percentile(x, 50)), "p95": float(np.percentile(x, 95)),
+                "p99": float(np.percentile(x, 99))}
+
+    for sc, bvh, _ in rscenes:
+        bvh.close()
+        sc.close()
+    for sq, b in qbvhs:
+        b.close()
+        sq.close()
+    return {
+        "workload": f"Poisson {rate:g} req/s for {duration_s:g} s: {n_req} requests, {int(kinds.sum())} renders "
+                    f"(res 64..1024, spp 1..64, depth 4..12 over 16 resident scenes of 10k..2M triangles), "
+                    f"{int((~kinds).sum())} closest-hit queries (10k..4M incoherent rays, wide BVHs of 10k..10M "
+                    f"triangles); HBM budget 150 GB",
+        "latency_ms": pct(lat), "latency_ms_render": pct(lat[kinds]), "latency_ms_query": pct(lat[~kinds]),
+        "mrays_per_s": rays / wall / 1e6, "wall_s": wall, "completed": st["completed"], "failed": st["failed"],
+        "peak_request_bytes": st["peak_bytes"], "iterations": st["iterations"],
+        "serial_plain_latency_ms": pct(slat), "serial_plain_busy_s": float(sum(svc)),
+        "setup_s": setup_s,
+    }
+
+
 def run_ours(args, world, rank, local):
     import numpy as np
     import torch
@@ -507,6 +711,8 @@ def run_ours(args, world, rank, local):
             "shading": "full materials (Lambert, mirror, dielectric IOR 1.5, GGX) with MIS"}
     c1 = gpu_closest_hit_c1(ctx) if rank == 0 else None
     c3 = precision_c3(ctx) if (rank == 0 and not args.skip_precision) else None
+    c4 = batching_c4(ctx) if (rank == 0 and not args.skip_serving) else None
+    c5 = serving_c5(ctx) if (rank == 0 and not args.skip_serving) else None
     launches = sum(v["launches"] for v in prof.values())
     line = {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
@@ -521,7 +727,7 @@ def run_ours(args, world, rank, local):
         "stage_ms": {k: v["ms"] for k, v in prof.items()},
         "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": h2d_bytes, "d2h_bytes_per_step": d2h_bytes},
         "gpu_launches": launches,
-        "roofline": roofline, "cpu_baseline": cpu_base, "closest_hit": c1, "precision": c3, "full_materials": full, "clocks": clk,
+        "roofline": roofline, "cpu_baseline": cpu_base, "closest_hit": c1, "precision": c3, "batching": c4, "serving": c5, "full_materials": full, "clocks": clk,
         "setup": {"scene_and_bvh_s": setup_s, "quad_nodes": info["quad_node_count"],
                   "bvh_device_build_ms": min(dev_build),
                   "bvh_host_build_ms": (hinfo["build_ms"] + hinfo["collapse_ms"] + hinfo["upload_ms"]) if hinfo else None,

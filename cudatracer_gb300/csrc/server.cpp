@@ -12,7 +12,10 @@
 //      device state and waking waiters.
 // Jobs arriving while others are on the GPU join at the next iteration; a
 // job's samples, seeds and per-pixel accumulation order do not depend on the
-// other jobs, so its result equals the job rendered alone.
+// other jobs, so its result equals the job rendered alone. A small job takes
+// k = min(spp, kIterPixels / pixels) samples per iteration, each into its own
+// slot buffer (sample i into slot i mod k), and its slots are added in slot
+// order when it finishes; k depends only on the job itself.
 #include <cuda_runtime.h>
 
 #include <algorithm>
@@ -32,6 +35,8 @@ using namespace ct;
 
 namespace {
 
+constexpr uint32_t kIterPixels = 65536;  // pixel-samples a small job may take per iteration
+
 enum Kind { kRender = 0, kClosest = 1, kAny = 2 };
 enum State { kPending, kActive, kFinishing, kDone };
 
@@ -44,6 +49,7 @@ struct Request {
   ct_batch_job job{};
   float* host_out = nullptr;
   uint32_t done_spp = 0;
+  uint32_t k = 1;  // samples per iteration (slot buffers)
   // query
   const ct_bvh* bvh = nullptr;
   const float* horg = nullptr;
@@ -62,7 +68,7 @@ struct Request {
 };
 
 size_t request_bytes(const Request& r) {
-  if (r.kind == kRender) return (size_t)r.pixels * sizeof(float4);
+  if (r.kind == kRender) return (size_t)r.k * r.pixels * sizeof(float4);
   // org + dir + hit/occluded + t + cursor, each 256-byte aligned
   auto al = [](size_t b) { return (b + 255) & ~(size_t)255; };
   return al((size_t)r.n * 16) * 2 + al((size_t)r.n * 4) * 2 + 256;
@@ -192,7 +198,9 @@ void ct_server::free_tables() {
 // One sample for every admitted render job. `finished` receives the jobs that
 // took their last one (their images are being copied out).
 cudaError_t ct_server::render_iteration(std::vector<Request*>& finished) {
-  const uint32_t n = (uint32_t)render.size();
+  // one table entry per (job, sample) taken this iteration
+  uint32_t n = 0;
+  for (Request* r : render) n += std::min(r->k, r->job.spp - r->done_spp);
   // the table slot is free once the iteration that used it has finished
   cudaError_t e = cudaEventSynchronize(table_ev[slot]);
   if (e != cudaSuccess) return e;
@@ -212,23 +220,29 @@ cudaError_t ct_server::render_iteration(std::vector<Request*>& finished) {
   BatchJob* ht = h_table[slot];
   int32_t* hb = h_bases[slot];
   int32_t base = 0, depth = 1;
-  for (uint32_t j = 0; j < n; j++) {
-    Request* r = render[j];
-    BatchJob& J = ht[j];
+  uint32_t j = 0;
+  for (Request* r : render) {
+    const uint32_t m = std::min(r->k, r->job.spp - r->done_spp);
+    BatchJob J;
     std::memset(&J, 0, sizeof(J));
     J.sc = rt_scene_dev(r->job.scene);
     J.bvh = rt_bvh_dev(r->job.bvh);
     J.f = rt_frame_const(&r->job.camera, &r->job.params);
-    J.f.frame = r->job.params.frame_index + 2u * r->done_spp;
-    J.accum = (float4*)r->dmem;
-    J.pix_base = base;
     J.max_depth = r->job.params.max_depth;
     J.spp_left = 1;
     J.exact = cfg.exact_math;
-    hb[j] = base;
-    base += (int32_t)r->pixels;
+    for (uint32_t s = 0; s < m; s++, j++) {
+      const uint32_t i = r->done_spp + s;  // sample index
+      ht[j] = J;
+      ht[j].f.frame = r->job.params.frame_index + 2u * i;
+      ht[j].accum = (float4*)r->dmem + (size_t)(i % r->k) * r->pixels;
+      ht[j].pix_base = base;
+      hb[j] = base;
+      base += (int32_t)r->pixels;
+    }
     depth = std::max(depth, r->job.params.max_depth);
     max_stack = std::max(max_stack, J.bvh.stack_entries);
+    r->done_spp += m;
   }
   hb[n] = base;
   if ((e = cudaMemcpyAsync(d_table[slot], ht, (size_t)n * sizeof(BatchJob), cudaMemcpyHostToDevice, rs)) != cudaSuccess)
@@ -249,16 +263,19 @@ cudaError_t ct_server::render_iteration(std::vector<Request*>& finished) {
   slot ^= 1;
   std::vector<Request*> keep;
   for (Request* r : render) {
-    r->done_spp++;
     if (r->done_spp < r->job.spp) {
       keep.push_back(r);
       continue;
     }
+    // add the slot buffers in slot order, copy the image out, free in stream order
+    float4* acc = (float4*)r->dmem;
+    for (uint32_t s = 1; s < r->k && e == cudaSuccess; s++)
+      e = launch_fold(acc, acc + (size_t)s * r->pixels, (int)r->pixels, rs);
     if (e == cudaSuccess)
       e = cudaMemcpyAsync(r->host_out, r->dmem, (size_t)r->pixels * sizeof(float4), cudaMemcpyDeviceToHost, rs);
     if (e == cudaSuccess) e = cudaFreeAsync(r->dmem, rs);
     if (e == cudaSuccess) e = cudaEventRecord(r->ev, rs);
-    inflight_pixels -= r->pixels;  // later iterations are ordered after this one on the stream
+    inflight_pixels -= r->k * r->pixels;  // later iterations are ordered after this one on the stream
     finished.push_back(r);
   }
   render.swap(keep);
@@ -306,7 +323,7 @@ void ct_server::loop() {
       Request* r = pending.front();
       r->bytes = request_bytes(*r);
       const bool fits_budget = cfg.hbm_budget == 0 || used_bytes + r->bytes <= cfg.hbm_budget;
-      const bool fits_queue = r->kind != kRender || inflight_pixels + r->pixels <= cfg.max_inflight_pixels;
+      const bool fits_queue = r->kind != kRender || inflight_pixels + r->k * r->pixels <= cfg.max_inflight_pixels;
       if (!fits_budget || !fits_queue) {
         if (render.empty() && finishing.empty() && admitted.empty()) {
           // cannot fit even with nothing else admitted
@@ -330,7 +347,7 @@ void ct_server::loop() {
       pending.pop_front();
       used_bytes += r->bytes;
       stats.peak_bytes = std::max<uint64_t>(stats.peak_bytes, used_bytes);
-      if (r->kind == kRender) inflight_pixels += r->pixels;
+      if (r->kind == kRender) inflight_pixels += r->k * r->pixels;
       else stats.query_rays += r->n;
       r->t_admit = now();
       admitted.push_back(r);
@@ -340,7 +357,7 @@ void ct_server::loop() {
     std::vector<Request*> finished;
     for (Request* r : admitted) {
       if (r->status != CT_OK) {
-        if (r->kind == kRender) inflight_pixels -= r->pixels;
+        if (r->kind == kRender) inflight_pixels -= r->k * r->pixels;
         finished.push_back(r);
       } else if (r->kind == kRender) {
         render.push_back(r);
@@ -436,6 +453,7 @@ ct_status ct_server_submit_render(ct_server* s, const ct_batch_job* job, float* 
   r->job = *job;
   r->host_out = host_out;
   r->pixels = (uint32_t)(job->params.width * job->params.height);
+  r->k = std::max<uint32_t>(1, std::min<uint32_t>(job->spp, kIterPixels / r->pixels));
   {
     std::lock_guard<std::mutex> g(s->mu);
     r->id = s->next_id++;

@@ -323,12 +323,17 @@ ct_status ct_batch_stats(ct_ctx* ctx, ct_batch* b, ct_frame_stats* out, int32_t 
 /* ---- serving (no reference counterpart): a scheduler thread that admits
  * render jobs and ray queries as they arrive, against an HBM budget, and
  * keeps the GPU busy with all admitted work at once. Render jobs join the
- * batched iterations (one sample per job per iteration, as ct_batch) at the
- * next iteration boundary and leave when their samples are done; ray queries
+ * batched iterations at the next iteration boundary (a job of p pixels takes
+ * min(spp, 65536 / p) samples per iteration, at least one, into private
+ * per-slot buffers added in order at the end) and leave when their samples
+ * are done; ray queries
  * run on a second stream, overlapping the iterations. Requests are admitted
  * in arrival order; one that can never fit fails with CT_ERR_OUT_OF_MEMORY.
  * Results are the same as the request alone (a render job's pixels use their
- * own seeds; queries are per ray). Host buffers given to the server must stay
+ * own seeds and its samples' summation order depends on the job only;
+ * queries are per ray). A render result equals ct_batch's for the same job
+ * up to that summation order (the same bits when it takes one sample per
+ * iteration). Host buffers given to the server must stay
  * valid until the request is waited for; pinned buffers let copies overlap. */
 typedef struct ct_server ct_server;
 typedef struct ct_server_config {

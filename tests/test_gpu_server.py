@@ -100,10 +100,12 @@ def test_each_result_same_alone_and_in_mix(gpu_ctx, world):
         info = mixed[i][0]
         assert info["status"] == 0 and info["submit_s"] <= info["admit_s"] <= info["done_s"]
     assert st["completed"] == len(reqs) and st["failed"] == 0
-    assert st["iterations"] >= 12  # the longest render job's samples
+    # small jobs take min(spp, 65536 // pixels) samples per iteration
+    assert st["iterations"] >= max(-(-r["spp"] // max(1, min(r["spp"], 65536 // (r["params"].width * r["params"].height))))
+                                   for k, r in reqs if k == "render")
 
 
-def test_render_equals_batch_and_queries_equal_direct_calls(gpu_ctx, world):
+def test_render_matches_batch_and_queries_equal_direct_calls(gpu_ctx, world):
     import torch
 
     from cudatracer_gb300 import api
@@ -118,8 +120,12 @@ def test_render_equals_batch_and_queries_equal_direct_calls(gpu_ctx, world):
             b = api.Batch(gpu_ctx, [r])
             b.run()
             torch.cuda.synchronize()
-            assert _same(b.accum_tensor(0).cpu().numpy(), got)
+            ref = b.accum_tensor(0).cpu().numpy()
             b.close()
+            # small jobs take several samples per iteration into slot buffers
+            # added at the end: the same samples, summed in another order
+            assert np.allclose(got, ref, rtol=1e-5, atol=1e-6)
+            assert np.array_equal(got[:, 3], ref[:, 3])
         else:
             o, d = torch.from_numpy(r["org"]).cuda(), torch.from_numpy(r["dir"]).cuda()
             if r["any_hit"]:
@@ -134,8 +140,11 @@ def test_admission_respects_the_budget(gpu_ctx, world):
     from cudatracer_gb300 import _lib, api
 
     reqs = _requests(world)
-    sizes = [r["params"].width * r["params"].height * 16 if k == "render" else r["org"].shape[0] * 40 + 2048
-             for k, r in reqs]
+    def render_bytes(r):
+        px = r["params"].width * r["params"].height
+        return max(1, min(r["spp"], 65536 // px)) * px * 16
+
+    sizes = [render_bytes(r) if k == "render" else r["org"].shape[0] * 40 + 2048 for k, r in reqs]
     budget = max(sizes) + 4096
     srv = api.Server(gpu_ctx, hbm_budget=budget, max_inflight_pixels=1 << 16)
     ids = [_submit(srv, *r) for r in reqs]
