@@ -166,6 +166,51 @@ __device__ __forceinline__ StepResult inner_step(const DevBVH& b, RayState& r, i
   return kContinue;
 }
 
+
+// Any-hit variant of inner_step: whether the ray is occluded does not depend
+// on the order in which hit children are visited (every node whose packed
+// interval passes the reference's test is visited until a triangle hits), so
+// the order network is skipped: the lowest hit slot continues, the others are
+// pushed.
+template <bool FASTMM>
+__device__ __forceinline__ StepResult inner_step_any(const DevBVH& b, RayState& r, int* stack, int stride, int limit) {
+  const QNodeDev* n = b.nodes + r.ref;
+  const float4 nx0 = __ldg(&n->bminx), nx1 = __ldg(&n->bmaxx);
+  const float4 ny0 = __ldg(&n->bminy), ny1 = __ldg(&n->bmaxy);
+  const float4 nz0 = __ldg(&n->bminz), nz1 = __ldg(&n->bmaxz);
+  const int4 ch = __ldg(&n->child);
+  float tn0, tn1, tn2, tn3, tf0, tf1, tf2, tf3;
+  slab<FASTMM>(nx0.x, nx1.x, ny0.x, ny1.x, nz0.x, nz1.x, r.ox, r.oy, r.oz, r.ix, r.iy, r.iz, tn0, tf0);
+  slab<FASTMM>(nx0.y, nx1.y, ny0.y, ny1.y, nz0.y, nz1.y, r.ox, r.oy, r.oz, r.ix, r.iy, r.iz, tn1, tf1);
+  slab<FASTMM>(nx0.z, nx1.z, ny0.z, ny1.z, nz0.z, nz1.z, r.ox, r.oy, r.oz, r.ix, r.iy, r.iz, tn2, tf2);
+  slab<FASTMM>(nx0.w, nx1.w, ny0.w, ny1.w, nz0.w, nz1.w, r.ox, r.oy, r.oz, r.ix, r.iy, r.iz, tn3, tf3);
+  const float p0 = __int_as_float((__float_as_int(tn0) & ~3) | 0);
+  const float p1 = __int_as_float((__float_as_int(tn1) & ~3) | 1);
+  const float p2 = __int_as_float((__float_as_int(tn2) & ~3) | 2);
+  const float p3 = __int_as_float((__float_as_int(tn3) & ~3) | 3);
+  const float t = r.t;
+  unsigned vm = ((tf0 > 0.0f && p0 <= tf0 && p0 < t && ch.x != kEmptyChild) ? 1u : 0u) |
+                ((tf1 > 0.0f && p1 <= tf1 && p1 < t && ch.y != kEmptyChild) ? 2u : 0u) |
+                ((tf2 > 0.0f && p2 <= tf2 && p2 < t && ch.z != kEmptyChild) ? 4u : 0u) |
+                ((tf3 > 0.0f && p3 <= tf3 && p3 < t && ch.w != kEmptyChild) ? 8u : 0u);
+  if (vm == 0) {
+    if (r.sp == 0) return kDone;
+    r.ref = stack[--r.sp * stride];
+    return kContinue;
+  }
+  const int first = __ffs(vm) - 1;
+  vm &= vm - 1;
+  while (vm) {
+    const int c = __ffs(vm) - 1;
+    vm &= vm - 1;
+    if (r.sp >= limit) return kOverflow;
+    stack[r.sp * stride] = sel4(ch.x, ch.y, ch.z, ch.w, c);
+    r.sp++;
+  }
+  r.ref = sel4(ch.x, ch.y, ch.z, ch.w, first);
+  return kContinue;
+}
+
 // Test the leaf r.ref's triangles in primitive order, then pop.
 template <bool ANY>
 __device__ __forceinline__ StepResult leaf_step(const DevBVH& b, RayState& r, float eps, int* stack, int stride) {
@@ -193,7 +238,7 @@ template <bool ANY, bool FASTMM>
 __device__ __forceinline__ bool traverse(const DevBVH& b, RayState& r, float eps, int* stack, int stride) {
   const int limit = b.stack_entries;
   while (true) {
-    const StepResult s = r.ref >= 0 ? inner_step<FASTMM>(b, r, stack, stride, limit) : leaf_step<ANY>(b, r, eps, stack, stride);
+    const StepResult s = r.ref >= 0 ? (ANY ? inner_step_any<FASTMM>(b, r, stack, stride, limit) : inner_step<FASTMM>(b, r, stack, stride, limit)) : leaf_step<ANY>(b, r, eps, stack, stride);
     if (s == kDone) return true;
     if (s == kOverflow) return false;
   }
@@ -241,7 +286,7 @@ __device__ __forceinline__ void trace_persistent(const DevBVH& b, int n, int* cu
     }
     if (__ballot_sync(FULL, rid >= 0) == 0) break;
     if (rid < 0) continue;
-    const StepResult s = r.ref >= 0 ? inner_step<FASTMM>(b, r, stack, stride, limit) : leaf_step<ANY>(b, r, eps, stack, stride);
+    const StepResult s = r.ref >= 0 ? (ANY ? inner_step_any<FASTMM>(b, r, stack, stride, limit) : inner_step<FASTMM>(b, r, stack, stride, limit)) : leaf_step<ANY>(b, r, eps, stack, stride);
     if (s != kContinue) {
       io.store(rid, r, s == kOverflow);
       rid = -1;
@@ -286,7 +331,7 @@ __device__ __forceinline__ void trace_persistent_batch(int n, int* cursor, IO& i
     if (__ballot_sync(FULL, rid >= 0) == 0) break;
     if (rid < 0) continue;
     const StepResult s =
-        r.ref >= 0 ? inner_step<FASTMM>(b, r, stack, stride, b.stack_entries) : leaf_step<ANY>(b, r, eps, stack, stride);
+        r.ref >= 0 ? (ANY ? inner_step_any<FASTMM>(b, r, stack, stride, b.stack_entries) : inner_step<FASTMM>(b, r, stack, stride, b.stack_entries)) : leaf_step<ANY>(b, r, eps, stack, stride);
     if (s != kContinue) {
       io.store(rid, r, s == kOverflow);
       rid = -1;
