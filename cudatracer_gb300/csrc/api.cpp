@@ -570,7 +570,8 @@ ct_status ct_bvh_build_wide(ct_ctx* ctx, const ct_scene* scene, void* stream, ct
   if (!ctx || !scene || !out) return fail(ctx, CT_ERR_INVALID_ARGUMENT, "null argument");
   *out = nullptr;
   const uint32_t n = scene->nt;
-  if (n == 0 || n > (1u << 30)) return fail(ctx, CT_ERR_INVALID_ARGUMENT, "triangle count out of range for the device builder");
+  // traversal stack entries hold a leaf group's first triangle in 29 bits
+  if (n == 0 || n > (1u << 29)) return fail(ctx, CT_ERR_INVALID_ARGUMENT, "triangle count out of range for the wide BVH");
   ct_status s = set_device(ctx);
   if (s != CT_OK) return s;
   cudaStream_t st = (cudaStream_t)stream;

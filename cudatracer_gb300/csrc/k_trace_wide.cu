@@ -265,6 +265,14 @@ __device__ bool trace_fp64(const DevWBVH& b, const WRay& r, uint32_t* st_node, f
   return best >= 0;
 }
 
+constexpr uint32_t kLeafEntry = 0x80000000u;  // stack entry: bit 31 leaf, bits 29-30 count, 0-28 first triangle
+
+// Persistent traversal: each lane owns a ray and takes one step per round —
+// an inner node (eight slab tests; inner children and leaf groups pushed,
+// the nearest on top) or one leaf group (up to three triangle tests) — so
+// the warp's lanes do similar work each round; a lane whose ray is done takes
+// the next ray from the device cursor (one atomicAdd per warp). A ray that
+// would overflow the stack is traced again entirely in FP64.
 template <bool ANY>
 __global__ void __launch_bounds__(128) k_trace_wide(const DevWBVH b, const float4* __restrict__ org,
                                                     const float4* __restrict__ dir, int32_t* __restrict__ hit_out,
@@ -273,66 +281,51 @@ __global__ void __launch_bounds__(128) k_trace_wide(const DevWBVH b, const float
                                                     unsigned long long* stats) {
   uint32_t st_node[kWStack];
   float st_t[kWStack];
+  const unsigned FULL = 0xffffffffu;
   const int lane = threadIdx.x & 31;
+  const unsigned below = (1u << lane) - 1u;
   unsigned long long n_rays = 0, n_retest = 0, n_full = 0, n_tbound = 0;
+  int rid = -1;
+  bool exhausted = false;
+  WRay r;
+  int best = -1, nc = 0, sp = 0;
+  float tb = 0.0f, tberr = 0.0f;
+  bool overflow = false, occluded = false;
+  uint32_t cand[kCand];
+  float cand_lo[kCand];
   while (true) {
-    int base = 0;
-    if (lane == 0) base = atomicAdd(cursor, 32);
-    base = __shfl_sync(0xffffffffu, base, 0);
-    if ((uint32_t)base >= n) break;
-    const uint32_t ri = (uint32_t)base + lane;
-    if (ri >= n) continue;
-    n_rays++;
-    WRay r;
-    setup(__ldg(org + ri), __ldg(dir + ri), r);
-    int best = -1;                    // leaf slot of the certain best hit
-    float tb = r.tmax, tberr = 0.0f;  // its t and t error bound
-    uint32_t cand[kCand];
-    float cand_lo[kCand];  // lower bound of each candidate's t
-    int nc = 0;
-    bool overflow = false, occluded = false;
-    int sp = 0;
-    st_node[sp] = 0, st_t[sp] = 0.0f, sp++;
-    while (sp > 0) {
-      sp--;
-      const uint32_t ni = st_node[sp];
-      const float far = (tb + tberr) * kFarScale;
-      if (st_t[sp] > far) continue;
-      WNode8 nd;
-      NodeBoxes nb;
-      load_node(b.nodes, ni, nd, nb);
-      const int sp0 = sp;
-      uint32_t leaves = 0;
-#pragma unroll
-      for (int i = 0; i < 8; i++) {
-        const uint32_t m = meta_at(nd, i);
-        if (!m) continue;
-        const float tn = slot_box(r, nd, nb, i, far);
-        if (!(tn <= far)) continue;
-        if (m & 0x80u) {
-          if (sp < kWStack) st_node[sp] = nd.child_base + (m & 7u), st_t[sp] = tn, sp++;
-          else atomicOr(err, kErrStackOverflow);
-        } else {
-          leaves |= 1u << i;
+    if (!exhausted) {
+      const unsigned m = __ballot_sync(FULL, rid < 0);
+      if (m) {
+        const int leader = __ffs(m) - 1;
+        int base = 0;
+        if (lane == leader) base = atomicAdd(cursor, __popc(m));
+        base = __shfl_sync(FULL, base, leader);
+        if ((uint32_t)(base + __popc(m)) >= n) exhausted = true;
+        if (rid < 0) {
+          const int my = base + __popc(m & below);
+          if ((uint32_t)my < n) {
+            setup(__ldg(org + my), __ldg(dir + my), r);
+            rid = my;
+            n_rays++;
+            best = -1, nc = 0, tb = r.tmax, tberr = 0.0f, overflow = false, occluded = false;
+            st_node[0] = 0, st_t[0] = 0.0f, sp = 1;
+          }
         }
       }
-      // nearest pushed child on top
-      if (sp - sp0 > 1) {
-        int bi = sp0;
-        for (int k = sp0 + 1; k < sp; k++)
-          if (st_t[k] < st_t[bi]) bi = k;
-        const uint32_t tnode = st_node[bi];
-        const float tt = st_t[bi];
-        st_node[bi] = st_node[sp - 1], st_t[bi] = st_t[sp - 1];
-        st_node[sp - 1] = tnode, st_t[sp - 1] = tt;
-      }
-      while (leaves) {
-        const int i = __ffs(leaves) - 1;
-        leaves &= leaves - 1;
-        const uint32_t m = meta_at(nd, i);
-        const uint32_t cnt = m >> 5, off = m & 31u;
+    }
+    if (__ballot_sync(FULL, rid >= 0) == 0) break;
+    if (rid < 0) continue;
+    // ---- one step
+    const float far = (tb + tberr) * kFarScale;
+    while (sp > 0 && st_t[sp - 1] > far) sp--;  // culled entries
+    bool finished = sp == 0 || overflow || (ANY && occluded);
+    if (!finished) {
+      const uint32_t ent = st_node[--sp];
+      if (ent & kLeafEntry) {
+        const uint32_t cnt = (ent >> 29) & 3u, first = ent & 0x1fffffffu;
         for (uint32_t k = 0; k < cnt; k++) {
-          const uint32_t slot = nd.prim_base + off + k;
+          const uint32_t slot = first + k;
           const float4* tr = b.tris + 3 * (size_t)slot;
           float t, terr;
           const int res = tri32(r, __ldg(tr), __ldg(tr + 1), __ldg(tr + 2), t, terr);
@@ -359,11 +352,40 @@ __global__ void __launch_bounds__(128) k_trace_wide(const DevWBVH b, const float
           if (nc < kCand) cand[nc] = slot, cand_lo[nc] = t - terr, nc++;
           else overflow = true;
         }
-        if (ANY && occluded) break;
+      } else {
+        WNode8 nd;
+        NodeBoxes nb;
+        load_node(b.nodes, ent, nd, nb);
+        const int sp0 = sp;
+#pragma unroll
+        for (int i = 0; i < 8; i++) {
+          const uint32_t m = meta_at(nd, i);
+          if (!m) continue;
+          const float tn = slot_box(r, nd, nb, i, far);
+          if (!(tn <= far)) continue;
+          if (sp >= kWStack) {
+            overflow = true;  // settled by the full FP64 traversal
+            continue;
+          }
+          st_node[sp] = (m & 0x80u) ? nd.child_base + (m & 7u)
+                                    : (kLeafEntry | ((m >> 5) << 29) | (nd.prim_base + (m & 31u)));
+          st_t[sp] = tn;
+          sp++;
+        }
+        if (sp - sp0 > 1) {
+          int bi = sp0;
+          for (int k = sp0 + 1; k < sp; k++)
+            if (st_t[k] < st_t[bi]) bi = k;
+          const uint32_t tnode = st_node[bi];
+          const float tt = st_t[bi];
+          st_node[bi] = st_node[sp - 1], st_t[bi] = st_t[sp - 1];
+          st_node[sp - 1] = tnode, st_t[sp - 1] = tt;
+        }
       }
-      if (ANY && occluded) break;
+      finished = sp == 0 || overflow || (ANY && occluded);
     }
-    // candidates recorded before a nearer certain hit was found may now be out of reach
+    if (!finished) continue;
+    // ---- the ray is done: settle what FP32 could not
     if (!overflow) {
       int k2 = 0;
       for (int k = 0; k < nc; k++)
@@ -372,7 +394,7 @@ __global__ void __launch_bounds__(128) k_trace_wide(const DevWBVH b, const float
     }
     int out_prim = best >= 0 ? __float_as_int(__ldg(b.tris + 3 * (size_t)best).w) : -1;
     float out_t = best >= 0 ? tb : r.tmax;
-    if (ANY && !occluded && best >= 0) occluded = true;  // a certain hit within the ray's range
+    if (ANY && !occluded && best >= 0) occluded = true;
     if (!(ANY && occluded) && overflow) {
       n_full++;
       double t64;
@@ -382,7 +404,6 @@ __global__ void __launch_bounds__(128) k_trace_wide(const DevWBVH b, const float
       out_t = h ? (float)t64 : r.tmax;
       occluded = h;
     } else if (!(ANY && occluded) && (nc > 0 || (!ANY && best >= 0 && tberr > kTRel * tb))) {
-      // settle the candidates (and the best) in FP64
       n_retest++;
       n_tbound += nc == 0;
       const Ray64 q = ray64(r);
@@ -401,11 +422,12 @@ __global__ void __launch_bounds__(128) k_trace_wide(const DevWBVH b, const float
       occluded = bp >= 0;
     }
     if (ANY) {
-      occ_out[ri] = occluded ? 1 : 0;
+      occ_out[rid] = occluded ? 1 : 0;
     } else {
-      hit_out[ri] = out_prim;
-      t_out[ri] = out_t;
+      hit_out[rid] = out_prim;
+      t_out[rid] = out_t;
     }
+    rid = -1;
   }
   if (stats) {
     atomicAdd(stats + 0, n_rays);
