@@ -50,6 +50,11 @@ def parse_args():
     ap.add_argument("--height", type=int, default=1080)
     ap.add_argument("--skip-extras", action="store_true",
                     help="only the timed frames: no e2e pass, roofline model, CPU baseline or sphere query")
+    ap.add_argument("--case", choices=["soup"], default=None,
+                    help="profiling case instead of the benchmark: 'soup' builds the quad and the wide BVH of "
+                         "a seeded soup and traces incoherent rays twice through each (prints timings)")
+    ap.add_argument("--soup-tris", type=int, default=4_000_000)
+    ap.add_argument("--soup-rays", type=int, default=2_000_000)
     ap.add_argument("--skip-serving", action="store_true",
                     help="leave out the 256-job batching and the Poisson serving workloads")
     ap.add_argument("--skip-precision", action="store_true",
@@ -552,6 +557,39 @@ def serving_c5(ctx, rate: float = 100.0, duration_s: float = 5.0, seed: int = 77
     }
 
 
+def soup_case(args) -> None:
+    """Profiling case: quad and wide BVH of a seeded soup, incoherent closest-hit
+    queries traced twice through each (the second launch of each is the one to
+    capture)."""
+    import numpy as np
+    import torch
+
+    from cudatracer_gb300 import _build, api, scenes
+
+    _build.build()
+    ctx = api.Context(0)
+    s = scenes.soup_scene(args.soup_tris, seed=3)
+    o, d = scenes.incoherent_rays(args.soup_rays, seed=5)
+    arr = {"vertices": s.vertices, "normals": np.tile(np.array([[0, 0, 1]], np.float32), (s.vertices.shape[0], 1)),
+           "indices": s.indices}
+    sc = ctx.scene(arr, [api.Material()])
+    wb, qb = sc.build_bvh_wide(), sc.build_bvh_device()
+    org, dirs = torch.from_numpy(o).cuda(), torch.from_numpy(d).cuda()
+    out = {}
+    for name, fn in (("wide", lambda: wb.trace_closest(org, dirs)),
+                     ("quad", lambda: qb.trace_closest(org, dirs, tri_eps=1e-12))):
+        for _ in range(2):
+            torch.cuda.synchronize()
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record()
+            fn()
+            e1.record()
+            torch.cuda.synchronize()
+        out[name + "_mrays_per_s"] = args.soup_rays / e0.elapsed_time(e1) / 1e3
+    ctx.check()
+    print(json.dumps({"case": "soup", "triangles": args.soup_tris, "rays": args.soup_rays, **out}), flush=True)
+
+
 def run_ours(args, world, rank, local):
     import numpy as np
     import torch
@@ -802,6 +840,9 @@ def run_reference(args, world, rank):
 
 def main():
     args = parse_args()
+    if args.case == "soup":
+        soup_case(args)
+        return
     world, rank, local = dist_setup(args)
     if args.impl == "reference":
         run_reference(args, world, rank)
