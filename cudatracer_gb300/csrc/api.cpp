@@ -933,9 +933,17 @@ static ct_status emit_frame(ct_ctx* ctx, ct_render* r, const DevQueues& q, const
   for (int pass = 0; pass < p->max_depth; pass++) {
     const int cur = pass & 1;
     const int path_length = pass == 0 ? 0 : pass + 1;  // Kernel.cu:306, 330
-    CT_CUDA(ctx, staged(r, 1, st, [&] { return launch_extend(bvh->dev, q, cur, p->tri_eps, fast, st); }));
+    if (bvh->wide)
+      CT_CUDA(ctx, staged(r, 1, st, [&] { return launch_extend_wide(bvh->wdev, q, cur, p->tri_eps, st); }));
+    else
+      CT_CUDA(ctx, staged(r, 1, st, [&] { return launch_extend(bvh->dev, q, cur, p->tri_eps, fast, st); }));
     CT_CUDA(ctx, staged(r, 2, st, [&] { return launch_shade(scene->dev, q, f, cur, path_length, p->exact_math, st); }));
-    if (p->shadow) CT_CUDA(ctx, staged(r, 3, st, [&] { return launch_connect(bvh->dev, q, p->tri_eps, fast, st); }));
+    if (p->shadow) {
+      if (bvh->wide)
+        CT_CUDA(ctx, staged(r, 3, st, [&] { return launch_connect_wide(bvh->wdev, q, p->tri_eps, st); }));
+      else
+        CT_CUDA(ctx, staged(r, 3, st, [&] { return launch_connect(bvh->dev, q, p->tri_eps, fast, st); }));
+    }
   }
   return CT_OK;
 }
@@ -954,7 +962,6 @@ ct_status ct_render_accumulate(ct_ctx* ctx, const ct_scene* scene, const ct_bvh*
   if (p->width != r->w || p->height != r->h) return fail(ctx, CT_ERR_INVALID_ARGUMENT, "params size differs from the render job's");
   if (p->max_depth < 1 || p->max_depth > 64) return fail(ctx, CT_ERR_INVALID_ARGUMENT, "max_depth must be in [1, 64]");
   if (bvh->nt != scene->nt) return fail(ctx, CT_ERR_INVALID_ARGUMENT, "BVH was built for another scene");
-  if (bvh->wide) return fail(ctx, CT_ERR_UNSUPPORTED, "frames trace quad BVHs; the wide BVH serves ray queries");
   if (p->shading_mode != CT_SHADE_COMPAT && p->shading_mode != CT_SHADE_FULL)
     return fail(ctx, CT_ERR_INVALID_ARGUMENT, "unknown shading mode");
   if (p->texture_filter != CT_TEX_NEAREST && p->texture_filter != CT_TEX_BILINEAR)
@@ -1215,9 +1222,12 @@ cudaError_t batch_iteration(ct_batch* b, const ct_batch_tuning& t, cudaStream_t 
   for (int pass = 0; pass < b->max_depth && e == cudaSuccess; pass++) {
     const int cur = pass & 1;
     const uint32_t path_length = pass == 0 ? 0u : (uint32_t)pass + 1u;  // Kernel.cu:306, 330
-    e = launch_batch_extend(b->dev, b->q, cur, !b->exact, t.extend_block, st);
+    e = b->dev.wide ? launch_batch_extend_wide(b->dev, b->q, cur, st)
+                    : launch_batch_extend(b->dev, b->q, cur, !b->exact, t.extend_block, st);
     if (e == cudaSuccess) e = launch_batch_shade(b->dev, b->q, cur, path_length, pass, b->exact, t.shade_waves, st);
-    if (e == cudaSuccess) e = launch_batch_connect(b->dev, b->q, !b->exact, t.connect_block, st);
+    if (e == cudaSuccess)
+      e = b->dev.wide ? launch_batch_connect_wide(b->dev, b->q, st)
+                      : launch_batch_connect(b->dev, b->q, !b->exact, t.connect_block, st);
   }
   if (e == cudaSuccess) e = launch_batch_advance(b->dev, b->q, st);
   return e;
@@ -1288,7 +1298,8 @@ ct_status ct_batch_create(ct_ctx* ctx, const ct_batch_job* jobs, uint32_t n, int
     const std::string at = "job " + std::to_string(j) + ": ";
     if (!J.scene || !J.bvh) return fail(ctx, CT_ERR_INVALID_ARGUMENT, at + "null scene or BVH");
     if (J.bvh->nt != J.scene->nt) return fail(ctx, CT_ERR_INVALID_ARGUMENT, at + "BVH was built for another scene");
-    if (J.bvh->wide) return fail(ctx, CT_ERR_UNSUPPORTED, at + "frames trace quad BVHs");
+    if (J.bvh->wide != jobs[0].bvh->wide)
+      return fail(ctx, CT_ERR_UNSUPPORTED, at + "a batch traces either quad or wide BVHs, not both");
     if (p->width <= 0 || p->height <= 0 || (int64_t)p->width * p->height > (1 << 26))
       return fail(ctx, CT_ERR_INVALID_ARGUMENT, at + "bad frame size");
     if (p->max_depth < 1 || p->max_depth > 64) return fail(ctx, CT_ERR_INVALID_ARGUMENT, at + "max_depth must be in [1, 64]");
@@ -1322,6 +1333,7 @@ ct_status ct_batch_create(ct_ctx* ctx, const ct_batch_job* jobs, uint32_t n, int
     std::memset(&d, 0, sizeof(d));
     d.sc = J.scene->dev;
     d.bvh = J.bvh->dev;
+    d.wbvh = J.bvh->wdev;
     d.f = batch_frame_const(&J.camera, &J.params);
     d.pix_base = base;
     d.max_depth = J.params.max_depth;
@@ -1353,6 +1365,7 @@ ct_status ct_batch_create(ct_ctx* ctx, const ct_batch_job* jobs, uint32_t n, int
   b->dev.n_jobs = (int32_t)n;
   b->dev.total_pix = base;
   b->dev.max_stack = max_stack;
+  b->dev.wide = jobs[0].bvh->wide ? 1 : 0;
   *out = b;
   return CT_OK;
 }
@@ -1512,7 +1525,7 @@ ct_status rt_check_job(ct_ctx* ctx, const ct_batch_job& J) {
   const ct_render_params* p = &J.params;
   if (!J.scene || !J.bvh) return fail(ctx, CT_ERR_INVALID_ARGUMENT, "null scene or BVH");
   if (J.bvh->nt != J.scene->nt) return fail(ctx, CT_ERR_INVALID_ARGUMENT, "BVH was built for another scene");
-  if (J.bvh->wide) return fail(ctx, CT_ERR_UNSUPPORTED, "frames trace quad BVHs");
+  if (J.bvh->wide) return fail(ctx, CT_ERR_UNSUPPORTED, "the serving loop renders on quad BVHs");
   if (p->width <= 0 || p->height <= 0 || (int64_t)p->width * p->height > (1 << 26))
     return fail(ctx, CT_ERR_INVALID_ARGUMENT, "bad frame size");
   if (p->max_depth < 1 || p->max_depth > 64) return fail(ctx, CT_ERR_INVALID_ARGUMENT, "max_depth must be in [1, 64]");

@@ -137,6 +137,7 @@ enum : uint32_t { kErrStackOverflow = 1u };
 struct BatchJob {
   DevScene sc;
   DevBVH bvh;
+  DevWBVH wbvh;         // the job's tree when the batch traces wide BVHs
   FrameConst f;         // f.frame advances by 2 per sample, as launchKernels does
   float4* accum;        // the job's own width*height accumulation
   int32_t pix_base;     // first pixel of the job in the batch
@@ -150,7 +151,7 @@ struct DevBatch {
   int32_t n_jobs;
   int32_t total_pix;
   int32_t max_stack;     // largest traversal stack among the jobs' BVHs
-  int32_t pad;
+  int32_t wide;          // 1: every job traces its wide BVH (fast-math frames on the quantised tree)
 };
 #ifdef __CUDACC__
 __device__ __forceinline__ int batch_job_of(const int32_t* __restrict__ bases, int n, int pix) {
@@ -234,6 +235,13 @@ cudaError_t launch_batch_shade(const DevBatch& b, const DevQueues& q, int queue,
                                int exact, int grid_mult, cudaStream_t s);
 cudaError_t launch_batch_connect(const DevBatch& b, const DevQueues& q, bool fast, int block, cudaStream_t s);
 cudaError_t launch_batch_advance(const DevBatch& b, const DevQueues& q, cudaStream_t s);
+
+// Frame stages on a wide (quantised) BVH: the reference's Moller-Trumbore test
+// and epsilon over conservative 8-bit boxes (k_trace_wide.cu).
+cudaError_t launch_extend_wide(const DevWBVH& b, const DevQueues& q, int queue, float eps, cudaStream_t s);
+cudaError_t launch_connect_wide(const DevWBVH& b, const DevQueues& q, float eps, cudaStream_t s);
+cudaError_t launch_batch_extend_wide(const DevBatch& b, const DevQueues& q, int queue, cudaStream_t s);
+cudaError_t launch_batch_connect_wide(const DevBatch& b, const DevQueues& q, cudaStream_t s);
 
 cudaError_t launch_fold(float4* accum, float4* frame, int n, cudaStream_t s);
 

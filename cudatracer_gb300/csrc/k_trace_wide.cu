@@ -24,6 +24,7 @@
 #include <algorithm>
 
 #include "ct_internal.h"
+#include "trace.cuh"
 
 namespace ct {
 namespace {
@@ -437,6 +438,295 @@ __global__ void __launch_bounds__(128) k_trace_wide(const DevWBVH b, const float
   }
 }
 
+// ---------------------------------------------------------------- frames on the wide tree
+// The wavefront's closest-hit and shadow stages on the quantised tree, with the
+// reference's Moller-Trumbore test and triangle epsilon (src/Core/Triangle.cuh:13-44,
+// edges formed as p1 - p0 and p2 - p0 exactly as the quad layout stores them)
+// instead of the watertight FP32/FP64 pair: the boxes are conservative, so the
+// set of triangles a ray can hit is the reference's; only the visit order (and
+// with it the winner of an exact t tie) differs.
+struct MRay {
+  float ox, oy, oz, dx, dy, dz, ix, iy, iz;
+};
+
+__device__ __forceinline__ float mslot_box(const MRay& r, const WNode8& n, const NodeBoxes& nb, int i, float tfar) {
+  const float lx = __fmaf_rn(nb.sx, (float)n.qlo[0][i], nb.px), hx = __fmaf_rn(nb.sx, (float)n.qhi[0][i], nb.px);
+  const float ly = __fmaf_rn(nb.sy, (float)n.qlo[1][i], nb.py), hy = __fmaf_rn(nb.sy, (float)n.qhi[1][i], nb.py);
+  const float lz = __fmaf_rn(nb.sz, (float)n.qlo[2][i], nb.pz), hz = __fmaf_rn(nb.sz, (float)n.qhi[2][i], nb.pz);
+  const float t0x = (lx - r.ox) * r.ix, t1x = (hx - r.ox) * r.ix;
+  const float t0y = (ly - r.oy) * r.iy, t1y = (hy - r.oy) * r.iy;
+  const float t0z = (lz - r.oz) * r.iz, t1z = (hz - r.oz) * r.iz;
+  const float tn = fmaxf(fmaxf(fminf(t0x, t1x), fminf(t0y, t1y)), fmaxf(fminf(t0z, t1z), 0.0f));
+  const float tf = fminf(fminf(fmaxf(t0x, t1x), fmaxf(t0y, t1y)), fminf(fmaxf(t0z, t1z), tfar)) * kFarScale;
+  return tn <= tf ? tn : __int_as_float(0x7f800000);
+}
+
+// Persistent, one step per round (as k_trace_wide). IO::load(i, o, d, t0, bvh, eps),
+// IO::store(i, hit, t, overflow).
+template <bool ANY, class IO>
+__device__ __forceinline__ void trace_wide_mt(int n, int* cursor, IO& io, uint32_t* st_node, float* st_t) {
+  const unsigned FULL = 0xffffffffu;
+  const int lane = threadIdx.x & 31;
+  const unsigned below = (1u << lane) - 1u;
+  int rid = -1;
+  bool exhausted = false;
+  MRay r;
+  DevWBVH b;
+  float eps = 0.0f, t = 0.0f;
+  int hit = -1, sp = 0;
+  bool overflow = false;
+  while (true) {
+    if (!exhausted) {
+      const unsigned m = __ballot_sync(FULL, rid < 0);
+      if (m) {
+        const int leader = __ffs(m) - 1;
+        int base = 0;
+        if (lane == leader) base = atomicAdd(cursor, __popc(m));
+        base = __shfl_sync(FULL, base, leader);
+        if (base + __popc(m) >= n) exhausted = true;
+        if (rid < 0) {
+          const int my = base + __popc(m & below);
+          if (my < n) {
+            float4 o, d;
+            io.load(my, o, d, t, b, eps);
+            r.ox = o.x, r.oy = o.y, r.oz = o.z, r.dx = d.x, r.dy = d.y, r.dz = d.z;
+            r.ix = safe_rcp(d.x), r.iy = safe_rcp(d.y), r.iz = safe_rcp(d.z);
+            hit = -1, overflow = false;
+            st_node[0] = 0, st_t[0] = 0.0f, sp = 1;
+            rid = my;
+          }
+        }
+      }
+    }
+    if (__ballot_sync(FULL, rid >= 0) == 0) break;
+    if (rid < 0) continue;
+    const float far = t * kFarScale;
+    while (sp > 0 && st_t[sp - 1] > far) sp--;
+    bool finished = sp == 0;
+    if (!finished) {
+      const uint32_t ent = st_node[--sp];
+      if (ent & kLeafEntry) {
+        const uint32_t cnt = (ent >> 29) & 3u, first = ent & 0x1fffffffu;
+        for (uint32_t k = 0; k < cnt; k++) {
+          const float4* tr = b.tris + 3 * (size_t)(first + k);
+          const float4 a = __ldg(tr), p1 = __ldg(tr + 1), p2 = __ldg(tr + 2);
+          const float4 e1 = make_float4(__fsub_rn(p1.x, a.x), __fsub_rn(p1.y, a.y), __fsub_rn(p1.z, a.z), 0.0f);
+          const float4 e2 = make_float4(__fsub_rn(p2.x, a.x), __fsub_rn(p2.y, a.y), __fsub_rn(p2.z, a.z), 0.0f);
+          if (tri_test(a, e1, e2, r.ox, r.oy, r.oz, r.dx, r.dy, r.dz, eps, t)) {
+            hit = __float_as_int(a.w);
+            if (ANY) break;
+          }
+        }
+        finished = ANY && hit >= 0;
+      } else {
+        WNode8 nd;
+        NodeBoxes nb;
+        load_node(b.nodes, ent, nd, nb);
+        const int sp0 = sp;
+#pragma unroll
+        for (int i = 0; i < 8; i++) {
+          const uint32_t m = meta_at(nd, i);
+          if (!m) continue;
+          const float tn = mslot_box(r, nd, nb, i, far);
+          if (!(tn <= far)) continue;
+          if (sp >= kWStack) {
+            overflow = true;
+            continue;
+          }
+          st_node[sp] = (m & 0x80u) ? nd.child_base + (m & 7u)
+                                    : (kLeafEntry | ((m >> 5) << 29) | (nd.prim_base + (m & 31u)));
+          st_t[sp] = tn;
+          sp++;
+        }
+        if (!ANY && sp - sp0 > 1) {
+          int bi = sp0;
+          for (int k = sp0 + 1; k < sp; k++)
+            if (st_t[k] < st_t[bi]) bi = k;
+          const uint32_t tnode = st_node[bi];
+          const float tt = st_t[bi];
+          st_node[bi] = st_node[sp - 1], st_t[bi] = st_t[sp - 1];
+          st_node[sp - 1] = tnode, st_t[sp - 1] = tt;
+        }
+      }
+      finished = finished || sp == 0 || overflow;
+    }
+    if (!finished) continue;
+    io.store(rid, hit, t, overflow);
+    rid = -1;
+  }
+}
+
+struct WExtendIO {
+  const float4* __restrict__ org;
+  const float4* __restrict__ dir;
+  int2* hit;
+  uint32_t* err;
+  DevWBVH bvh;
+  float eps;
+  __device__ void load(int i, float4& o, float4& d, float& t0, DevWBVH& b, float& e) {
+    o = __ldg(org + i);
+    d = __ldg(dir + i);
+    t0 = 1e34f;  // MAX_DISTANCE, src/Core/Ray.cuh:13
+    b = bvh;
+    e = eps;
+  }
+  __device__ void store(int i, int h, float t, bool overflow) {
+    if (overflow) {
+      atomicOr(err, kErrStackOverflow);
+      hit[i] = make_int2(-1, __float_as_int(1e34f));
+      return;
+    }
+    hit[i] = make_int2(h, __float_as_int(t));
+  }
+};
+
+struct WConnectIO {
+  const float4* __restrict__ sorg;
+  const float4* __restrict__ sdir;
+  const float4* __restrict__ scol;
+  float4* accum;
+  uint32_t* err;
+  DevWBVH bvh;
+  float eps;
+  __device__ void load(int i, float4& o, float4& d, float& t0, DevWBVH& b, float& e) {
+    o = __ldg(sorg + i);
+    d = __ldg(sdir + i);
+    t0 = d.w;
+    b = bvh;
+    e = eps;
+  }
+  __device__ void store(int i, int h, float, bool overflow) {
+    if (overflow) {
+      atomicOr(err, kErrStackOverflow);
+      return;
+    }
+    if (h >= 0) return;
+    const float4 c = __ldg(scol + i);
+    const int pix = __float_as_int(__ldg(&sorg[i].w));
+    float4 a = accum[pix];
+    a.x = __fadd_rn(a.x, c.x);
+    a.y = __fadd_rn(a.y, c.y);
+    a.z = __fadd_rn(a.z, c.z);
+    a.w = __fadd_rn(a.w, 1.0f);
+    accum[pix] = a;
+  }
+};
+
+struct WBatchExtendIO {
+  const float4* __restrict__ org;
+  const float4* __restrict__ dir;
+  int2* hit;
+  uint32_t* err;
+  const BatchJob* jobs;
+  const int32_t* bases;
+  int n_jobs;
+  __device__ void load(int i, float4& o, float4& d, float& t0, DevWBVH& b, float& e) {
+    o = __ldg(org + i);
+    d = __ldg(dir + i);
+    t0 = 1e34f;
+    const BatchJob& J = jobs[batch_job_of(bases, n_jobs, __float_as_int(o.w))];
+    b = J.wbvh;
+    e = J.f.tri_eps;
+  }
+  __device__ void store(int i, int h, float t, bool overflow) {
+    if (overflow) {
+      atomicOr(err, kErrStackOverflow);
+      hit[i] = make_int2(-1, __float_as_int(1e34f));
+      return;
+    }
+    hit[i] = make_int2(h, __float_as_int(t));
+  }
+};
+
+struct WBatchConnectIO {
+  const float4* __restrict__ sorg;
+  const float4* __restrict__ sdir;
+  const float4* __restrict__ scol;
+  uint32_t* err;
+  const BatchJob* jobs;
+  const int32_t* bases;
+  int n_jobs;
+  __device__ void load(int i, float4& o, float4& d, float& t0, DevWBVH& b, float& e) {
+    o = __ldg(sorg + i);
+    d = __ldg(sdir + i);
+    t0 = d.w;
+    const BatchJob& J = jobs[batch_job_of(bases, n_jobs, __float_as_int(o.w))];
+    b = J.wbvh;
+    e = J.f.tri_eps;
+  }
+  __device__ void store(int i, int h, float, bool overflow) {
+    if (overflow) {
+      atomicOr(err, kErrStackOverflow);
+      return;
+    }
+    if (h >= 0) return;
+    const float4 c = __ldg(scol + i);
+    const int pix = __float_as_int(__ldg(&sorg[i].w));
+    const BatchJob& J = jobs[batch_job_of(bases, n_jobs, pix)];
+    float4* acc = J.accum + (pix - J.pix_base);
+    float4 a = *acc;
+    a.x = __fadd_rn(a.x, c.x);
+    a.y = __fadd_rn(a.y, c.y);
+    a.z = __fadd_rn(a.z, c.z);
+    a.w = __fadd_rn(a.w, 1.0f);
+    *acc = a;
+  }
+};
+
+__global__ void __launch_bounds__(128) k_extend_wide(DevWBVH b, DevQueues q, int qi, float eps) {
+  uint32_t st_node[kWStack];
+  float st_t[kWStack];
+  const int n = q.counts[qi];
+  if (blockIdx.x == 0 && threadIdx.x == 0) {
+    q.counts[qi ^ 1] = 0;
+    q.counts[2] = 0;
+    q.counts[5] = 0;  // fetch cursor of the connect that follows
+    atomicAdd(&q.stats[0], (unsigned long long)n);
+  }
+  WExtendIO io{q.org_q(qi), q.dir_q(qi), q.hit, q.error, b, eps};
+  trace_wide_mt<false>(n, q.counts + 4, io, st_node, st_t);
+}
+
+__global__ void __launch_bounds__(128) k_connect_wide(DevWBVH b, DevQueues q, float eps) {
+  uint32_t st_node[kWStack];
+  float st_t[kWStack];
+  const int n = q.counts[2];
+  if (blockIdx.x == 0 && threadIdx.x == 0) atomicAdd(&q.stats[1], (unsigned long long)n);
+  WConnectIO io{q.sorg, q.sdir, q.scol, q.accum, q.error, b, eps};
+  trace_wide_mt<true>(n, q.counts + 5, io, st_node, st_t);
+}
+
+__global__ void __launch_bounds__(128) k_batch_extend_wide(DevBatch bt, DevQueues q, int qi) {
+  uint32_t st_node[kWStack];
+  float st_t[kWStack];
+  const int n = q.counts[qi];
+  if (blockIdx.x == 0 && threadIdx.x == 0) {
+    q.counts[qi ^ 1] = 0;
+    q.counts[2] = 0;
+    q.counts[5] = 0;
+    atomicAdd(&q.stats[0], (unsigned long long)n);
+  }
+  WBatchExtendIO io{q.org_q(qi), q.dir_q(qi), q.hit, q.error, bt.jobs, bt.bases, bt.n_jobs};
+  trace_wide_mt<false>(n, q.counts + 4, io, st_node, st_t);
+}
+
+__global__ void __launch_bounds__(128) k_batch_connect_wide(DevBatch bt, DevQueues q) {
+  uint32_t st_node[kWStack];
+  float st_t[kWStack];
+  const int n = q.counts[2];
+  if (blockIdx.x == 0 && threadIdx.x == 0) atomicAdd(&q.stats[1], (unsigned long long)n);
+  WBatchConnectIO io{q.sorg, q.sdir, q.scol, q.error, bt.jobs, bt.bases, bt.n_jobs};
+  trace_wide_mt<true>(n, q.counts + 5, io, st_node, st_t);
+}
+
+template <typename K>
+int mt_grid(K kernel, int capacity) {
+  int per = 0;
+  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, kernel, 128, 0);
+  const int cap_blocks = (capacity + 127) / 128;
+  return std::max(1, std::min(cap_blocks, std::max(1, per) * sm_count()));
+}
+
 int wide_grid() {
   static int g = 0;
   if (!g) {
@@ -467,6 +757,24 @@ cudaError_t launch_trace_wide_any(const DevWBVH& b, const float4* org, const flo
   if (e != cudaSuccess) return e;
   const int g = std::min<int>(wide_grid(), (int)((n + 127) / 128));
   k_trace_wide<true><<<g, 128, 0, s>>>(b, org, dir, nullptr, nullptr, occ, n, err, cursor, stats);
+  return cudaGetLastError();
+}
+
+
+cudaError_t launch_extend_wide(const DevWBVH& b, const DevQueues& q, int queue, float eps, cudaStream_t s) {
+  k_extend_wide<<<mt_grid(k_extend_wide, q.capacity), 128, 0, s>>>(b, q, queue, eps);
+  return cudaGetLastError();
+}
+cudaError_t launch_connect_wide(const DevWBVH& b, const DevQueues& q, float eps, cudaStream_t s) {
+  k_connect_wide<<<mt_grid(k_connect_wide, q.capacity), 128, 0, s>>>(b, q, eps);
+  return cudaGetLastError();
+}
+cudaError_t launch_batch_extend_wide(const DevBatch& b, const DevQueues& q, int queue, cudaStream_t s) {
+  k_batch_extend_wide<<<mt_grid(k_batch_extend_wide, q.capacity), 128, 0, s>>>(b, q, queue);
+  return cudaGetLastError();
+}
+cudaError_t launch_batch_connect_wide(const DevBatch& b, const DevQueues& q, cudaStream_t s) {
+  k_batch_connect_wide<<<mt_grid(k_batch_connect_wide, q.capacity), 128, 0, s>>>(b, q);
   return cudaGetLastError();
 }
 

@@ -249,7 +249,7 @@ cudaError_t ct_server::render_iteration(std::vector<Request*>& finished) {
     return e;
   if ((e = cudaMemcpyAsync(d_bases[slot], hb, (size_t)(n + 1) * 4, cudaMemcpyHostToDevice, rs)) != cudaSuccess) return e;
   if ((e = cudaMemsetAsync(q.counts, 0, 16 * sizeof(int32_t), rs)) != cudaSuccess) return e;
-  DevBatch b{d_table[slot], d_bases[slot], (int32_t)n, base, max_stack, 0};
+  DevBatch b{d_table[slot], d_bases[slot], (int32_t)n, base, max_stack, 0};  // quad BVHs
   const bool fast = !cfg.exact_math;
   e = launch_batch_raygen(b, q, cfg.exact_math, rs);
   for (int pass = 0; pass < depth && e == cudaSuccess; pass++) {

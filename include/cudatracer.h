@@ -203,9 +203,12 @@ ct_status ct_bvh_build_device(ct_ctx* ctx, const ct_scene* scene, void* stream, 
  * settle (near an edge, near another hit's t) are re-tested in FP64, so
  * ct_trace_closest/ct_trace_any on this tree give the FP64 closest hit (equal
  * t: lower primitive id) and `tri_eps` is ignored. Built on the device from
- * exact triangle bounds (every node above 3 triangles split). Frames need a
- * quad BVH; export with CT_BVH_WIDE8_Q8 (80-byte nodes; prim_indices in leaf
- * order). info.quad_node_count and info.quad_depth describe the wide tree. */
+ * exact triangle bounds (every node above 3 triangles split). Frames
+ * (ct_render_accumulate, ct_batch) may trace it too: there the triangle test
+ * is the reference's Moller-Trumbore with tri_eps, so the hits are the quad
+ * tree's up to the winner of an exact t tie. Export with CT_BVH_WIDE8_Q8
+ * (80-byte nodes; prim_indices in leaf order). info.quad_node_count and
+ * info.quad_depth describe the wide tree. */
 ct_status ct_bvh_build_wide(ct_ctx* ctx, const ct_scene* scene, void* stream, ct_bvh** out);
 /* Counters of the wide tree's queries since the last reset: rays traced, rays
  * whose result needed FP64 re-tests, of those the ones re-tested only to

@@ -147,6 +147,18 @@ def test_batch_validation(gpu_ctx, scenes_):
            "indices": s.indices}
     sc = gpu_ctx.scene(arr, [api.Material()])
     j = _job(scenes_[0], 16, 16, 4, 1)
-    j["bvh"] = sc.build_bvh_wide()
+    j["bvh"] = scenes_[0]["sc"].build_bvh_wide()
     with pytest.raises(_lib.CTError):
-        api.Batch(gpu_ctx, [j])
+        api.Batch(gpu_ctx, [j, _job(scenes_[1], 16, 16, 4, 1)])  # quad and wide trees in one batch
+
+
+def test_wide_batch_job_alone_equals_job_in_mix(gpu_ctx, scenes_):
+    """Batches on the quantised trees: the same independence from the mix."""
+    jobs = _mix(scenes_)
+    wide = {id(S["sc"]): S["sc"].build_bvh_wide() for S in scenes_}
+    for j in jobs:
+        j["bvh"] = wide[id(j["scene"])]
+    mixed, _ = _run(gpu_ctx, jobs)
+    for k in (0, 3, 5):
+        alone, _ = _run(gpu_ctx, [jobs[k]])
+        assert np.array_equal(alone[0].view(np.int32), mixed[k].view(np.int32)), k

@@ -214,16 +214,35 @@ def test_wide_axis_parallel_rays(gpu_ctx, orc):
     assert mism == 0 and lost == 0 and rel <= 1e-5
 
 
-def test_wide_bvh_rejected_by_frames(gpu_ctx):
-    from cudatracer_gb300 import _lib, api, scenes
+def test_frames_on_the_wide_tree(gpu_ctx, orc):
+    """Frames traced through the wide tree use the reference's triangle test:
+    with exact math they match the oracle (traced through the quad tree) up to
+    exact t ties, and fast-math frames match the quad tree's fast frames."""
+    from cudatracer_gb300 import api, scenes
 
-    s = scenes.soup_scene(1000, seed=1)
-    sc = _scene(gpu_ctx, s.vertices, s.indices)
-    wb = sc.build_bvh_wide()
-    job = api.RenderJob(gpu_ctx, 16, 16)
-    p = api.Params(16, 16, camera=api.Camera(16, 16, 60.0, (0.5, 0.5, 3.0)))
-    with pytest.raises(_lib.CTError) as e:
-        job.accumulate(sc, wb, p.camera, p.to_ct())
-    assert e.value.status == _lib.CT_ERR_UNSUPPORTED
-    with pytest.raises(_lib.CTError):
-        wb.export(_lib.CT_BVH_QUAD)
+    ts, cam = scenes.terrain_scene(grid=128, spheres=12, sky_size=(256, 128))
+    arr = scenes.scene_arrays(ts)
+    sc = gpu_ctx.scene(arr, [api.Material(**m) for m in ts.materials], ts.textures, ts.skybox_texture)
+    qb, wb = sc.build_bvh_device(), sc.build_bvh_wide()
+    W, H = 96, 64
+    camera = api.Camera(W, H, cam["fov"], cam["position"], cam["forward"], cam["up"])
+
+    def render(bvh, exact, frames=2):
+        job = api.RenderJob(gpu_ctx, W, H)
+        p = api.Params(W, H, camera=camera, max_depth=5, exact_math=exact)
+        p.reset(job)
+        for _ in range(frames):
+            api.launch_kernels(job, sc, bvh, p)
+        gpu_ctx.check()
+        return job.accum_tensor().cpu().numpy().copy()
+
+    a = render(wb, True)
+    ob = orc.bvh_build(ts.vertices, ts.indices)
+    o = orc.render_frames(arr, orc.pack_materials(ts.materials), ob["quad"], ob["prims"], cam, W, H, [0, 2], 5,
+                          exact_math=True, textures=ts.textures, sky_tex=0)
+    rel = np.abs(a - o) / np.maximum(np.abs(o), 1e-6)
+    assert (rel > 1e-4).any(axis=1).mean() < 1e-3
+    assert (a.view(np.int32) == o.view(np.int32)).all(axis=1).mean() >= 0.999
+    f_w, f_q = render(wb, False), render(qb, False)
+    rel = np.abs(f_w - f_q) / np.maximum(np.abs(f_q), 1e-6)
+    assert (rel > 1e-4).any(axis=1).mean() < 1e-3
