@@ -1014,7 +1014,8 @@ ct_status ct_render_accumulate(ct_ctx* ctx, const ct_scene* scene, const ct_bvh*
   f.sky = p->sky;
   f.shading_mode = p->shading_mode;
   f.tex_filter = p->texture_filter;
-  if (p->exact_math) return emit_frame(ctx, r, r->q, scene, bvh, f, p, st);  // strictly sequential accumulation
+  // exact math accumulates strictly in sequence; profiling times kernels alone
+  if (p->exact_math || r->profile) return emit_frame(ctx, r, r->q, scene, bvh, f, p, st);
   // Fast-math frames overlap: the frame renders into one of kFrameSlots
   // private slots (queues + accumulation) on the slot's own stream, so its
   // first passes can run while earlier frames' last bounces are still

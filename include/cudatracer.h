@@ -395,9 +395,11 @@ ct_status ct_render_stats(ct_ctx* ctx, ct_render* r, ct_frame_stats* stats, int3
 
 /* Per-stage GPU timing (no reference counterpart; the reference prints host
  * build times only, src/BVH/BVHTree.cpp:53): when enabled, every stage launch
- * of ct_render_accumulate is bracketed by CUDA events on its stream. Reading
- * synchronises on the recorded events. Stage index: 0 raygen, 1 extend
- * (closest hit), 2 shade, 3 connect (shadow any hit). */
+ * of ct_render_accumulate is bracketed by CUDA events on its stream, and
+ * fast-math frames run one after another on the caller's stream (no frames in
+ * flight), so each interval is one kernel running alone. Reading synchronises
+ * on the recorded events. Stage index: 0 raygen, 1 extend (closest hit),
+ * 2 shade, 3 connect (shadow any hit). */
 typedef struct ct_stage_times {
   double ms[4];
   uint32_t launches[4];
