@@ -243,7 +243,7 @@ def reference_traversal_baseline() -> dict | None:
     return out
 
 
-def gpu_closest_hit_c1(ctx):
+def sphere_closest_hit(ctx):
     """Mrays/s of ct_trace_closest on the 81,920-triangle sphere, 256x256 rays x 64."""
     import numpy as np
     import torch
@@ -279,7 +279,7 @@ def gpu_closest_hit_c1(ctx):
             "workload": "81,920-tri sphere, 256x256 pinhole rays x64, ct_trace_closest"}
 
 
-def precision_c3(ctx, ntri: int = 10_000_000, nray: int = 16_000_000, sample_every: int = 8) -> dict:
+def precision_soup(ctx, ntri: int = 10_000_000, nray: int = 16_000_000, sample_every: int = 8) -> dict:
     """The precision workload: a 10M-triangle seeded soup (centroids U[0,1]^3,
     edges log-uniform 1e-4..1e-2) and 16M incoherent rays. Closest-hit Mrays/s
     of the plain quad BVH (reference Moller-Trumbore, epsilon 1e-12 since the
@@ -355,7 +355,7 @@ def precision_c3(ctx, ntri: int = 10_000_000, nray: int = 16_000_000, sample_eve
     return out
 
 
-def batching_c4(ctx, n_jobs: int = 256, seed: int = 2024) -> dict:
+def batching_jobs(ctx, n_jobs: int = 256, seed: int = 2024) -> dict:
     """The batching workload: n_jobs render jobs of the terrain-plus-spheres
     kind, triangle counts log-uniform 10k..2M, square resolutions log-uniform
     64..1024, spp log-uniform 1..64, depth uniform 4..12, all in one batch
@@ -401,8 +401,10 @@ def batching_c4(ctx, n_jobs: int = 256, seed: int = 2024) -> dict:
     st = b.stats(reset=True)
     ctx.check()
     b.close()
-    # the same jobs, one after another, through ct_render_accumulate
+    # the same jobs, one after another, through ct_render_accumulate (each
+    # job's device state is freed after the timed region)
     e0.record()
+    done = []
     for j in jobs:
         W, H = j["params"].width, j["params"].height
         rj = api.RenderJob(ctx, W, H)
@@ -410,9 +412,12 @@ def batching_c4(ctx, n_jobs: int = 256, seed: int = 2024) -> dict:
         pp.reset(rj)
         for _ in range(j["spp"]):
             api.launch_kernels(rj, j["scene"], j["bvh"], pp)
+        done.append(rj)
     e1.record()
     torch.cuda.synchronize()
     serial_ms = e0.elapsed_time(e1)
+    for rj in done:
+        rj.close()
     for j in jobs:
         j["bvh"].close()
         j["scene"].close()
@@ -425,10 +430,10 @@ def batching_c4(ctx, n_jobs: int = 256, seed: int = 2024) -> dict:
     }
 
 
-def serving_c5(ctx, rate: float = 100.0, duration_s: float = 5.0, seed: int = 77) -> dict:
+def serving_poisson(ctx, rate: float = 100.0, duration_s: float = 5.0, seed: int = 77, iter_pixels: int = 0) -> dict:
     """The serving workload: a Poisson request stream (rate req/s for
-    duration_s) mixing render jobs (config-4 distribution over 16 resident
-    terrain scenes) and ray queries (10k..4M incoherent rays against resident
+    duration_s) mixing render jobs (the batching workload's job distribution over 16
+    resident terrain scenes) and ray queries (10k..4M incoherent rays against resident
     wide BVHs of 10k..10M-triangle soups), through ct_server with a 150 GB
     HBM budget. Latency = completion - submission. Serial plain execution: the
     same requests' service times measured one at a time through the plain
@@ -483,7 +488,7 @@ def serving_c5(ctx, rate: float = 100.0, duration_s: float = 5.0, seed: int = 77
             return srv.submit_render(r)
         return srv.submit_query(r["bvh"], ray_o[r["off"]:r["off"] + r["n"]], ray_d[r["off"]:r["off"] + r["n"]])
 
-    srv = api.Server(ctx, hbm_budget=150 << 30, max_inflight_pixels=1 << 24)
+    srv = api.Server(ctx, hbm_budget=150 << 30, max_inflight_pixels=1 << 24, iter_pixels=iter_pixels)
     ids = [None] * n_req
 
     def client():
@@ -528,6 +533,8 @@ def serving_c5(ctx, rate: float = 100.0, duration_s: float = 5.0, seed: int = 77
             h.cpu(), t.cpu()
         torch.cuda.synchronize()
         svc.append(time.perf_counter() - a)
+        if kind == "render":
+            rj.close()  # outside the service time
     finish, slat = 0.0, []
     for a_t, s_t in zip(arrivals, svc):
         finish = max(finish, a_t) + s_t
@@ -553,7 +560,7 @@ def serving_c5(ctx, rate: float = 100.0, duration_s: float = 5.0, seed: int = 77
         "mrays_per_s": rays / wall / 1e6, "wall_s": wall, "completed": st["completed"], "failed": st["failed"],
         "peak_request_bytes": st["peak_bytes"], "iterations": st["iterations"],
         "serial_plain_latency_ms": pct(slat), "serial_plain_busy_s": float(sum(svc)),
-        "setup_s": setup_s,
+        "iter_pixels": iter_pixels or (1 << 22), "setup_s": setup_s,
     }
 
 
@@ -754,10 +761,12 @@ def run_ours(args, world, rank, local):
     full_ms = e0.elapsed_time(e1) / full_frames
     full = {"msamples_per_s": W * H / full_ms / 1e3, "ms_per_frame": full_ms, "frames": full_frames,
             "shading": "full materials (Lambert, mirror, dielectric IOR 1.5, GGX) with MIS"}
-    c1 = gpu_closest_hit_c1(ctx) if rank == 0 else None
-    c3 = precision_c3(ctx) if (rank == 0 and not args.skip_precision) else None
-    c4 = batching_c4(ctx) if (rank == 0 and not args.skip_serving) else None
-    c5 = serving_c5(ctx) if (rank == 0 and not args.skip_serving) else None
+    c1 = sphere_closest_hit(ctx) if rank == 0 else None
+    c3 = precision_soup(ctx) if (rank == 0 and not args.skip_precision) else None
+    c4 = batching_jobs(ctx) if (rank == 0 and not args.skip_serving) else None
+    # the light end of the request-rate range and one where serial execution saturates
+    c5 = ([serving_poisson(ctx), serving_poisson(ctx, rate=400.0, duration_s=2.0)]
+          if (rank == 0 and not args.skip_serving) else None)
     launches = sum(v["launches"] for v in prof.values())
     line = {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,

@@ -85,7 +85,8 @@ class ct_batch_tuning(Structure):
 
 
 class ct_server_config(Structure):
-    _fields_ = [("hbm_budget", c_uint64), ("max_inflight_pixels", c_uint32), ("exact_math", c_int32)]
+    _fields_ = [("hbm_budget", c_uint64), ("max_inflight_pixels", c_uint32), ("exact_math", c_int32),
+                ("iter_pixels", c_uint32)]
 
 
 class ct_request_info(Structure):

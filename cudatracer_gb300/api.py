@@ -544,6 +544,12 @@ class RenderJob:
             self.ctx.lib.ct_render_destroy(self.ctx.h, self.h)
             self.h = None
 
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
     def reset(self, stream=None):
         check(self.ctx.lib.ct_render_reset(self.ctx.h, self.h, _stream(stream)), self.ctx.h)
 
@@ -717,9 +723,9 @@ class Server:
     buffers owned here until the request is waited for."""
 
     def __init__(self, ctx: Context, hbm_budget: int = 0, max_inflight_pixels: int = 1 << 22,
-                 exact_math: bool = False):
+                 exact_math: bool = False, iter_pixels: int = 0):
         self.ctx = ctx
-        cfg = _lib.ct_server_config(int(hbm_budget), int(max_inflight_pixels), int(exact_math))
+        cfg = _lib.ct_server_config(int(hbm_budget), int(max_inflight_pixels), int(exact_math), int(iter_pixels))
         self.h = ctypes.c_void_p()
         check(ctx.lib.ct_server_create(ctx.h, ctypes.byref(cfg), ctypes.byref(self.h)), ctx.h)
         self._req = {}

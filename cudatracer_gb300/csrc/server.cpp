@@ -6,16 +6,18 @@
 //      pixels of the queues; query: its ray and result buffers);
 //   2. starts admitted queries on the query stream (copy in, trace, copy out);
 //   3. runs one batched iteration of all admitted render jobs on the render
-//      stream (one sample each, the ct_batch kernels with a job table built
+//      stream (up to k samples each, the ct_batch kernels with a job table built
 //      for this iteration), at most two iterations ahead of the device;
 //   4. retires requests whose completion events have fired, freeing their
 //      device state and waking waiters.
 // Jobs arriving while others are on the GPU join at the next iteration; a
 // job's samples, seeds and per-pixel accumulation order do not depend on the
-// other jobs, so its result equals the job rendered alone. A small job takes
-// k = min(spp, kIterPixels / pixels) samples per iteration, each into its own
-// slot buffer (sample i into slot i mod k), and its slots are added in slot
-// order when it finishes; k depends only on the job itself.
+// other jobs, so its result equals the job rendered alone. A job has
+// k = min(spp, I / pixels) slot buffers, I = min(iter_pixels,
+// max_inflight_pixels), at least one; it takes up to k samples per iteration,
+// sample i into slot i mod k, and its slots are added in slot order when it
+// finishes. Each slot sums its samples in sample order however many samples an
+// iteration takes, and k depends only on the job and the configuration.
 #include <cuda_runtime.h>
 
 #include <algorithm>
@@ -35,7 +37,7 @@ using namespace ct;
 
 namespace {
 
-constexpr uint32_t kIterPixels = 65536;  // pixel-samples a small job may take per iteration
+constexpr uint32_t kIterPixels = 1u << 22;  // default pixel-samples a job may take per iteration
 
 enum Kind { kRender = 0, kClosest = 1, kAny = 2 };
 enum State { kPending, kActive, kFinishing, kDone };
@@ -195,7 +197,7 @@ void ct_server::free_tables() {
   table_cap = 0;
 }
 
-// One sample for every admitted render job. `finished` receives the jobs that
+// Up to k samples of every admitted render job. `finished` receives the jobs that
 // took their last one (their images are being copied out).
 cudaError_t ct_server::render_iteration(std::vector<Request*>& finished) {
   // one table entry per (job, sample) taken this iteration
@@ -453,7 +455,8 @@ ct_status ct_server_submit_render(ct_server* s, const ct_batch_job* job, float* 
   r->job = *job;
   r->host_out = host_out;
   r->pixels = (uint32_t)(job->params.width * job->params.height);
-  r->k = std::max<uint32_t>(1, std::min<uint32_t>(job->spp, kIterPixels / r->pixels));
+  const uint32_t per_iter = std::min(s->cfg.iter_pixels ? s->cfg.iter_pixels : kIterPixels, s->cfg.max_inflight_pixels);
+  r->k = std::max<uint32_t>(1, std::min<uint32_t>(job->spp, per_iter / r->pixels));
   {
     std::lock_guard<std::mutex> g(s->mu);
     r->id = s->next_id++;

@@ -327,22 +327,26 @@ ct_status ct_batch_stats(ct_ctx* ctx, ct_batch* b, ct_frame_stats* out, int32_t 
  * render jobs and ray queries as they arrive, against an HBM budget, and
  * keeps the GPU busy with all admitted work at once. Render jobs join the
  * batched iterations at the next iteration boundary (a job of p pixels takes
- * min(spp, 65536 / p) samples per iteration, at least one, into private
- * per-slot buffers added in order at the end) and leave when their samples
- * are done; ray queries
+ * up to k = min(spp, I / p) samples per iteration, at least one, where
+ * I = min(iter_pixels, max_inflight_pixels); sample i goes to private slot
+ * buffer i mod k and the k slots are added in order at the end) and leave
+ * when their samples are done; ray queries
  * run on a second stream, overlapping the iterations. Requests are admitted
  * in arrival order; one that can never fit fails with CT_ERR_OUT_OF_MEMORY.
  * Results are the same as the request alone (a render job's pixels use their
  * own seeds and its samples' summation order depends on the job only;
- * queries are per ray). A render result equals ct_batch's for the same job
- * up to that summation order (the same bits when it takes one sample per
- * iteration). Host buffers given to the server must stay
+ * queries are per ray; k depends on the job and the server's configuration
+ * only). A render result equals ct_batch's for the same job up to that
+ * summation order (the same bits when k = 1). Host buffers given to the server must stay
  * valid until the request is waited for; pinned buffers let copies overlap. */
 typedef struct ct_server ct_server;
 typedef struct ct_server_config {
   uint64_t hbm_budget;          /* bytes of per-request device state admitted at once (0 = no limit) */
   uint32_t max_inflight_pixels; /* shared ray-queue capacity: pixels of all render jobs in flight */
   int32_t exact_math;           /* math mode of every render job */
+  uint32_t iter_pixels;         /* pixel-samples a render job may take per iteration (0 = 4,194,304):
+                                   larger values finish big jobs in fewer, larger iterations and
+                                   cost k * p * 16 bytes of slot buffers per job */
 } ct_server_config;
 typedef struct ct_request_info {
   ct_status status;

@@ -159,3 +159,40 @@ def test_admission_respects_the_budget(gpu_ctx, world):
         srv.wait(rid, timeout=30.0)
     assert e.value.status == _lib.CT_ERR_OUT_OF_MEMORY
     srv.close()
+
+
+def test_larger_iterations_same_alone_and_in_mix(gpu_ctx, world):
+    """With a larger per-iteration budget every job here takes several samples
+    per iteration (k = min(spp, iter_pixels / pixels) slot buffers); results are
+    still identical alone and in the mix, and equal ct_batch's up to the
+    summation order of the slots."""
+    import torch
+
+    from cudatracer_gb300 import api
+
+    R = world["render"]
+    reqs = [("render", _render_job(R[0], 160, 120, 6, 5)), ("render", _render_job(R[1], 128, 128, 8, 7, shading=1)),
+            ("render", _render_job(R[2], 64, 48, 5, 9))] + [q for q in _requests(world) if q[0] == "query"][:3]
+    cfg = dict(max_inflight_pixels=1 << 17, iter_pixels=1 << 16)
+    srv = api.Server(gpu_ctx, **cfg)
+    alone = [srv.wait(_submit(srv, *r))[1] for r in reqs]
+    srv.close()
+    srv = api.Server(gpu_ctx, **cfg)
+    order = (5, 2, 0, 3, 1, 4)
+    ids = [_submit(srv, *reqs[i]) for i in order]
+    mixed = dict(zip(order, (srv.wait(i) for i in ids)))
+    st = srv.stats()
+    srv.close()
+    gpu_ctx.check()
+    for i in range(len(reqs)):
+        assert _same(alone[i], mixed[i][1]), i
+    # 160x120 takes 3 samples per iteration (2 iterations), 128x128 4 (2), 64x48 9 (1)
+    assert 2 <= st["iterations"] <= 6
+    for (kind, r), got in zip(reqs[:3], alone[:3]):
+        b = api.Batch(gpu_ctx, [r])
+        b.run()
+        torch.cuda.synchronize()
+        ref = b.accum_tensor(0).cpu().numpy()
+        b.close()
+        assert np.allclose(got, ref, rtol=1e-5, atol=1e-6)
+        assert np.array_equal(got[:, 3], ref[:, 3])
