@@ -22,6 +22,7 @@ globals().update({name: code for code, name in STATUS_NAMES.items()})
 CT_BVH_BINARY, CT_BVH_QUAD, CT_BVH_WIDE8_Q8 = 0, 1, 2
 CT_SHADE_COMPAT, CT_SHADE_FULL = 0, 1
 CT_TEX_NEAREST, CT_TEX_BILINEAR = 0, 1
+CT_SORT_NONE, CT_SORT_OCTANT, CT_SORT_FACE_CELLS = 0, 1, 2
 
 
 class CTError(RuntimeError):
@@ -66,7 +67,7 @@ class ct_render_params(Structure):
         ("width", c_int32), ("height", c_int32), ("max_depth", c_int32), ("frame_index", c_uint32),
         ("shading_mode", c_int32), ("exact_math", c_int32), ("shadow", c_int32), ("indirect", c_int32),
         ("sky", c_int32), ("normal_eps", c_float), ("dist_eps", c_float), ("tri_eps", c_float),
-        ("texture_filter", c_int32),
+        ("texture_filter", c_int32), ("ray_sort", c_int32),
     ]
 
 
@@ -81,7 +82,7 @@ class ct_batch_job(Structure):
 
 class ct_batch_tuning(Structure):
     _fields_ = [("extend_block", c_int32), ("connect_block", c_int32), ("shade_waves", c_int32),
-                ("use_graph", c_int32)]
+                ("use_graph", c_int32), ("sort_key", c_int32)]
 
 
 class ct_server_config(Structure):

@@ -623,6 +623,7 @@ class Params:
     tri_eps: float = 1e-3
     shading_mode: int = _lib.CT_SHADE_COMPAT
     texture_filter: int = _lib.CT_TEX_NEAREST
+    ray_sort: int = _lib.CT_SORT_NONE
 
     def reset(self, job: RenderJob, stream=None):
         """Params::reset: clear the accumulation buffer and the sample count."""
@@ -637,6 +638,7 @@ class Params:
         p.shadow, p.indirect, p.sky = int(self.shadow), int(self.indirect), int(self.sky)
         p.normal_eps, p.dist_eps, p.tri_eps = self.normal_eps, self.dist_eps, self.tri_eps
         p.shading_mode, p.texture_filter = int(self.shading_mode), int(self.texture_filter)
+        p.ray_sort = int(self.ray_sort)
         return p
 
 
@@ -700,8 +702,8 @@ class Batch:
         check(self.ctx.lib.ct_batch_get_tuning(self.h, ctypes.byref(t)))
         return {k: getattr(t, k) for k, _ in t._fields_}
 
-    def set_tuning(self, extend_block=128, connect_block=128, shade_waves=1, use_graph=1):
-        t = _lib.ct_batch_tuning(extend_block, connect_block, shade_waves, use_graph)
+    def set_tuning(self, extend_block=128, connect_block=128, shade_waves=1, use_graph=1, sort_key=0):
+        t = _lib.ct_batch_tuning(extend_block, connect_block, shade_waves, use_graph, sort_key)
         check(self.ctx.lib.ct_batch_set_tuning(self.ctx.h, self.h, ctypes.byref(t)), self.ctx.h)
 
     def autotune(self, stream=None) -> tuple[dict, float]:

@@ -869,10 +869,12 @@ static ct_status alloc_queues(ct_ctx* ctx, Allocs& a, size_t n, DevQueues& q) {
       (s = alloc4(&q.dir[1])) != CT_OK || (s = alloc4(&q.thr[0])) != CT_OK || (s = alloc4(&q.thr[1])) != CT_OK ||
       (s = alloc4(&q.sorg)) != CT_OK || (s = alloc4(&q.sdir)) != CT_OK || (s = alloc4(&q.scol)) != CT_OK ||
       (s = alloc4(&q.accum)) != CT_OK || (s = upload(ctx, a, &q.hit, nullptr, n * sizeof(int2))) != CT_OK ||
+      (s = upload(ctx, a, &q.perm_buf, nullptr, n * sizeof(int32_t))) != CT_OK ||
       (s = upload(ctx, a, &q.counts, nullptr, 16 * sizeof(int32_t))) != CT_OK ||
       (s = upload(ctx, a, &q.stats, nullptr, 8 * sizeof(unsigned long long))) != CT_OK)
     return s;
   q.error = ctx->d_error;
+  q.perm = nullptr;  // queue order unless a stage sorted the queue
   return CT_OK;
 }
 
@@ -933,10 +935,15 @@ static ct_status emit_frame(ct_ctx* ctx, ct_render* r, const DevQueues& q, const
   for (int pass = 0; pass < p->max_depth; pass++) {
     const int cur = pass & 1;
     const int path_length = pass == 0 ? 0 : pass + 1;  // Kernel.cu:306, 330
+    DevQueues qx = q;  // extend's view: sorted order for bounce rays when asked
+    if (pass > 0 && p->ray_sort != CT_SORT_NONE && q.perm_buf) {
+      CT_CUDA(ctx, staged(r, 1, st, [&] { return launch_ray_sort(q, cur, p->ray_sort, st); }));
+      qx.perm = q.perm_buf;
+    }
     if (bvh->wide)
-      CT_CUDA(ctx, staged(r, 1, st, [&] { return launch_extend_wide(bvh->wdev, q, cur, p->tri_eps, st); }));
+      CT_CUDA(ctx, staged(r, 1, st, [&] { return launch_extend_wide(bvh->wdev, qx, cur, p->tri_eps, st); }));
     else
-      CT_CUDA(ctx, staged(r, 1, st, [&] { return launch_extend(bvh->dev, q, cur, p->tri_eps, fast, st); }));
+      CT_CUDA(ctx, staged(r, 1, st, [&] { return launch_extend(bvh->dev, qx, cur, p->tri_eps, fast, st); }));
     CT_CUDA(ctx, staged(r, 2, st, [&] { return launch_shade(scene->dev, q, f, cur, path_length, p->exact_math, st); }));
     if (p->shadow) {
       if (bvh->wide)
@@ -966,6 +973,8 @@ ct_status ct_render_accumulate(ct_ctx* ctx, const ct_scene* scene, const ct_bvh*
     return fail(ctx, CT_ERR_INVALID_ARGUMENT, "unknown shading mode");
   if (p->texture_filter != CT_TEX_NEAREST && p->texture_filter != CT_TEX_BILINEAR)
     return fail(ctx, CT_ERR_INVALID_ARGUMENT, "unknown texture filter");
+  if (p->ray_sort < CT_SORT_NONE || p->ray_sort > CT_SORT_FACE_CELLS)
+    return fail(ctx, CT_ERR_INVALID_ARGUMENT, "unknown ray-sort key");
   if (!finite3(cam->position) || !finite3(cam->forward) || !finite3(cam->up) || !std::isfinite(cam->fov_deg))
     return fail(ctx, CT_ERR_INVALID_ARGUMENT, "non-finite camera");
   ct_status s = set_device(ctx);
@@ -1168,10 +1177,10 @@ struct ct_batch {
   Allocs allocs;
   std::vector<BatchJob> jobs0;  // job table at the first sample
   std::vector<int32_t> bases;
-  ct_batch_tuning tune{128, 128, 1, 1};
+  ct_batch_tuning tune{128, 128, 1, 1, CT_SORT_NONE};
   cudaStream_t cap = nullptr;  // capture stream
   cudaGraphExec_t exec = nullptr;
-  ct_batch_tuning exec_tune{0, 0, 0, 0};
+  ct_batch_tuning exec_tune{0, 0, 0, 0, 0};
   ~ct_batch() {
     if (exec) cudaGraphExecDestroy(exec);
     if (cap) cudaStreamDestroy(cap);
@@ -1223,8 +1232,14 @@ cudaError_t batch_iteration(ct_batch* b, const ct_batch_tuning& t, cudaStream_t 
   for (int pass = 0; pass < b->max_depth && e == cudaSuccess; pass++) {
     const int cur = pass & 1;
     const uint32_t path_length = pass == 0 ? 0u : (uint32_t)pass + 1u;  // Kernel.cu:306, 330
-    e = b->dev.wide ? launch_batch_extend_wide(b->dev, b->q, cur, st)
-                    : launch_batch_extend(b->dev, b->q, cur, !b->exact, t.extend_block, st);
+    DevQueues qx = b->q;
+    if (pass > 0 && t.sort_key != CT_SORT_NONE) {
+      e = launch_ray_sort(b->q, cur, t.sort_key, st);
+      qx.perm = b->q.perm_buf;
+    }
+    if (e == cudaSuccess)
+      e = b->dev.wide ? launch_batch_extend_wide(b->dev, qx, cur, st)
+                      : launch_batch_extend(b->dev, qx, cur, !b->exact, t.extend_block, st);
     if (e == cudaSuccess) e = launch_batch_shade(b->dev, b->q, cur, path_length, pass, b->exact, t.shade_waves, st);
     if (e == cudaSuccess)
       e = b->dev.wide ? launch_batch_connect_wide(b->dev, b->q, st)
@@ -1280,7 +1295,7 @@ cudaError_t batch_iterations(ct_batch* b, uint32_t iters, cudaStream_t st) {
 bool tuning_ok(const ct_batch_tuning& t) {
   auto blk = [](int32_t v) { return v == 64 || v == 128 || v == 256; };
   return blk(t.extend_block) && blk(t.connect_block) && t.shade_waves >= 1 && t.shade_waves <= 8 &&
-         (t.use_graph == 0 || t.use_graph == 1);
+         (t.use_graph == 0 || t.use_graph == 1) && t.sort_key >= CT_SORT_NONE && t.sort_key <= CT_SORT_FACE_CELLS;
 }
 
 }  // namespace
@@ -1308,6 +1323,8 @@ ct_status ct_batch_create(ct_ctx* ctx, const ct_batch_job* jobs, uint32_t n, int
       return fail(ctx, CT_ERR_INVALID_ARGUMENT, at + "unknown shading mode");
     if (p->texture_filter != CT_TEX_NEAREST && p->texture_filter != CT_TEX_BILINEAR)
       return fail(ctx, CT_ERR_INVALID_ARGUMENT, at + "unknown texture filter");
+    if (p->ray_sort < CT_SORT_NONE || p->ray_sort > CT_SORT_FACE_CELLS)
+      return fail(ctx, CT_ERR_INVALID_ARGUMENT, at + "unknown ray-sort key");
     if (J.spp == 0) return fail(ctx, CT_ERR_INVALID_ARGUMENT, at + "spp must be at least 1");
     if (!finite3(J.camera.position) || !finite3(J.camera.forward) || !finite3(J.camera.up) ||
         !std::isfinite(J.camera.fov_deg))
@@ -1442,11 +1459,14 @@ ct_status ct_batch_autotune(ct_ctx* ctx, ct_batch* b, void* stream, ct_batch_tun
     err = measure(t, ms);
     if (err == cudaSuccess && ms < best_ms) best_ms = ms, best = t;
   };
-  // coordinate search: traversal block sizes, then shade waves, then graph replay
+  // coordinate search: traversal block sizes, then the ray-sort key, shade
+  // waves and graph replay
   for (int eb : {64, 128, 256})
-    for (int cb : {128, 256}) trial(ct_batch_tuning{eb, cb, 1, 1});
-  trial(ct_batch_tuning{best.extend_block, best.connect_block, 2, 1});
-  trial(ct_batch_tuning{best.extend_block, best.connect_block, best.shade_waves, 0});
+    for (int cb : {128, 256}) trial(ct_batch_tuning{eb, cb, 1, 1, CT_SORT_NONE});
+  for (int key : {CT_SORT_OCTANT, CT_SORT_FACE_CELLS})
+    trial(ct_batch_tuning{best.extend_block, best.connect_block, 1, 1, key});
+  trial(ct_batch_tuning{best.extend_block, best.connect_block, 2, 1, best.sort_key});
+  trial(ct_batch_tuning{best.extend_block, best.connect_block, best.shade_waves, 0, best.sort_key});
   cudaEventDestroy(e0);
   cudaEventDestroy(e1);
   if (err != cudaSuccess) return cuda_fail(ctx, err, "batch autotune");
@@ -1534,6 +1554,8 @@ ct_status rt_check_job(ct_ctx* ctx, const ct_batch_job& J) {
     return fail(ctx, CT_ERR_INVALID_ARGUMENT, "unknown shading mode");
   if (p->texture_filter != CT_TEX_NEAREST && p->texture_filter != CT_TEX_BILINEAR)
     return fail(ctx, CT_ERR_INVALID_ARGUMENT, "unknown texture filter");
+  if (p->ray_sort < CT_SORT_NONE || p->ray_sort > CT_SORT_FACE_CELLS)
+    return fail(ctx, CT_ERR_INVALID_ARGUMENT, "unknown ray-sort key");
   if (J.spp == 0) return fail(ctx, CT_ERR_INVALID_ARGUMENT, "spp must be at least 1");
   if (!finite3(J.camera.position) || !finite3(J.camera.forward) || !finite3(J.camera.up) ||
       !std::isfinite(J.camera.fov_deg))

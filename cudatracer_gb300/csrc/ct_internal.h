@@ -110,6 +110,10 @@ struct DevQueues {
   int32_t* counts;   // [0],[1] ray queue sizes, [2] shadow queue size, [4] extend fetch cursor
   unsigned long long* stats;  // [0] extension rays, [1] shadow rays, [2] samples, [3] frames
   uint32_t* error;   // error bits (1 = stack overflow)
+  int32_t* perm;     // order in which extend takes the queue's rays (nullptr = queue order); a
+                     // stage that sorted the queue passes perm = perm_buf. It never changes a
+                     // result, only which rays share a warp
+  int32_t* perm_buf; // capacity entries, written by launch_ray_sort
   int32_t capacity;
   // queue selection without dynamic indexing into the (by-value) parameter struct
   __host__ __device__ float4* org_q(int i) const { return i ? org[1] : org[0]; }
@@ -241,6 +245,10 @@ cudaError_t launch_batch_advance(const DevBatch& b, const DevQueues& q, cudaStre
 cudaError_t launch_extend_wide(const DevWBVH& b, const DevQueues& q, int queue, float eps, cudaStream_t s);
 cudaError_t launch_connect_wide(const DevWBVH& b, const DevQueues& q, float eps, cudaStream_t s);
 cudaError_t launch_batch_extend_wide(const DevBatch& b, const DevQueues& q, int queue, cudaStream_t s);
+// Order the rays of queue `queue` within windows of kSortWindow by direction
+// class into q.perm_buf (key 1: octant; key 2: cube face x 4x4 cells; 0: nothing).
+constexpr int kSortWindow = 2048;
+cudaError_t launch_ray_sort(const DevQueues& q, int queue, int key, cudaStream_t s);
 cudaError_t launch_batch_connect_wide(const DevBatch& b, const DevQueues& q, cudaStream_t s);
 
 cudaError_t launch_fold(float4* accum, float4* frame, int n, cudaStream_t s);

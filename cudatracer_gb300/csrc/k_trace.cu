@@ -80,12 +80,15 @@ struct ExtendIO {
   const float4* __restrict__ dir;
   int2* hit;
   uint32_t* err;
+  const int32_t* __restrict__ perm;
   __device__ void load(int i, float4& o, float4& d, float& t0) {
+    if (perm) i = __ldg(perm + i);
     o = __ldg(org + i);
     d = __ldg(dir + i);
     t0 = kMaxDistance;
   }
   __device__ void store(int i, const RayState& r, bool overflow) {
+    if (perm) i = __ldg(perm + i);
     if (overflow) {
       atomicOr(err, kErrStackOverflow);
       hit[i] = make_int2(-1, __float_as_int(kMaxDistance));
@@ -111,7 +114,7 @@ __global__ void __launch_bounds__(kBlock) k_extend(DevBVH b, DevQueues q, int qi
     q.counts[2] = 0;
     atomicAdd(&q.stats[0], (unsigned long long)n);
   }
-  ExtendIO io{q.org_q(qi), q.dir_q(qi), q.hit, q.error};
+  ExtendIO io{q.org_q(qi), q.dir_q(qi), q.hit, q.error, q.perm};
   trace_persistent<false, FASTMM>(b, n, q.counts + 4, eps, io, s_stack + threadIdx.x, kBlock);
 }
 
@@ -192,6 +195,104 @@ cudaError_t launch_connect(const DevBVH& b, const DevQueues& q, float eps, bool 
 }
 
 
+// ------------------------------------------------------------- ray sorting
+// Windows of kSortWindow consecutive queue entries are counting-sorted by a
+// direction class in shared memory; q.perm_buf[base + rank] = queue index.
+// Sorting them by direction puts rays that traverse alike into one warp (the
+// queue is roughly in pixel order, so a window's rays already start close
+// together). A ray's result does not depend on the order (extend writes each
+// hit at its own queue index), so every key gives identical frames.
+namespace {
+
+constexpr int kSortThreads = 256;
+
+template <int KEY>
+__device__ __forceinline__ int ray_class(float4 d) {
+  if (KEY == 1) return (d.x < 0.0f ? 1 : 0) | (d.y < 0.0f ? 2 : 0) | (d.z < 0.0f ? 4 : 0);
+  // cube face of the direction and a 4x4 cell grid on that face
+  const float ax = fabsf(d.x), ay = fabsf(d.y), az = fabsf(d.z);
+  int face;
+  float u, v, m;
+  if (ax >= ay && ax >= az) {
+    face = d.x < 0.0f ? 1 : 0, u = d.y, v = d.z, m = ax;
+  } else if (ay >= az) {
+    face = d.y < 0.0f ? 3 : 2, u = d.x, v = d.z, m = ay;
+  } else {
+    face = d.z < 0.0f ? 5 : 4, u = d.x, v = d.y, m = az;
+  }
+  const float sc = m > 0.0f ? 2.0f / m : 0.0f;  // u / m in [-1, 1] -> [0, 4]
+  const int cu = min(3, max(0, (int)(u * sc + 2.0f)));
+  const int cv = min(3, max(0, (int)(v * sc + 2.0f)));
+  return face * 16 + cv * 4 + cu;
+}
+
+template <int KEY>
+__global__ void __launch_bounds__(kSortThreads) k_ray_sort(DevQueues q, int qi) {
+  constexpr int NB = KEY == 1 ? 8 : 96;
+  constexpr int PER = kSortWindow / kSortThreads;
+  constexpr int BPL = (NB + 31) / 32;  // bins per lane of the scan
+  __shared__ int bins[NB];
+  const int n = q.counts[qi];
+  const int base = blockIdx.x * kSortWindow;
+  if (base >= n) return;
+  const int cnt = min(kSortWindow, n - base);
+  for (int b = threadIdx.x; b < NB; b += kSortThreads) bins[b] = 0;
+  __syncthreads();
+  const float4* dir = q.dir_q(qi) + base;
+  int key[PER], rank[PER];
+#pragma unroll
+  for (int k = 0; k < PER; k++) {
+    const int i = k * kSortThreads + threadIdx.x;
+    key[k] = -1;
+    rank[k] = 0;
+    if (i < cnt) {
+      key[k] = ray_class<KEY>(__ldg(dir + i));
+      rank[k] = atomicAdd(&bins[key[k]], 1);
+    }
+  }
+  __syncthreads();
+  if (threadIdx.x < 32) {  // exclusive scan of the bin counts
+    const int lane = threadIdx.x;
+    int c[BPL], sum = 0;
+#pragma unroll
+    for (int j = 0; j < BPL; j++) {
+      const int b = lane * BPL + j;
+      c[j] = b < NB ? bins[b] : 0;
+      sum += c[j];
+    }
+    int inc = sum;
+#pragma unroll
+    for (int off = 1; off < 32; off <<= 1) {
+      const int y = __shfl_up_sync(0xffffffffu, inc, off);
+      if (lane >= off) inc += y;
+    }
+    int run = inc - sum;
+#pragma unroll
+    for (int j = 0; j < BPL; j++) {
+      const int b = lane * BPL + j;
+      if (b < NB) bins[b] = run;
+      run += c[j];
+    }
+  }
+  __syncthreads();
+  int32_t* perm = q.perm_buf + base;
+#pragma unroll
+  for (int k = 0; k < PER; k++)
+    if (key[k] >= 0) perm[bins[key[k]] + rank[k]] = base + k * kSortThreads + threadIdx.x;
+}
+
+}  // namespace
+
+cudaError_t launch_ray_sort(const DevQueues& q, int queue, int key, cudaStream_t s) {
+  if (key == 0 || !q.perm_buf) return cudaSuccess;
+  const int grid = std::max(1, (q.capacity + kSortWindow - 1) / kSortWindow);
+  if (key == 1)
+    k_ray_sort<1><<<grid, kSortThreads, 0, s>>>(q, queue);
+  else
+    k_ray_sort<2><<<grid, kSortThreads, 0, s>>>(q, queue);
+  return cudaGetLastError();
+}
+
 // ---------------------------------------------------------------- batches
 namespace {
 
@@ -203,7 +304,9 @@ struct BatchExtendIO {
   const BatchJob* jobs;
   const int32_t* bases;
   int n_jobs;
+  const int32_t* __restrict__ perm;
   __device__ void load(int i, float4& o, float4& d, float& t0, DevBVH& b, float& eps) {
+    if (perm) i = __ldg(perm + i);
     o = __ldg(org + i);
     d = __ldg(dir + i);
     t0 = kMaxDistance;
@@ -212,6 +315,7 @@ struct BatchExtendIO {
     eps = J.f.tri_eps;
   }
   __device__ void store(int i, const RayState& r, bool overflow) {
+    if (perm) i = __ldg(perm + i);
     if (overflow) {
       atomicOr(err, kErrStackOverflow);
       hit[i] = make_int2(-1, __float_as_int(kMaxDistance));
@@ -230,7 +334,7 @@ __global__ void __launch_bounds__(BLOCK) k_batch_extend(DevBatch bt, DevQueues q
     q.counts[2] = 0;
     atomicAdd(&q.stats[0], (unsigned long long)n);
   }
-  BatchExtendIO io{q.org_q(qi), q.dir_q(qi), q.hit, q.error, bt.jobs, bt.bases, bt.n_jobs};
+  BatchExtendIO io{q.org_q(qi), q.dir_q(qi), q.hit, q.error, bt.jobs, bt.bases, bt.n_jobs, q.perm};
   trace_persistent_batch<false, FASTMM>(n, q.counts + 4, io, s_stack + threadIdx.x, BLOCK);
 }
 

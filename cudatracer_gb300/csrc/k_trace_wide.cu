@@ -563,7 +563,9 @@ struct WExtendIO {
   uint32_t* err;
   DevWBVH bvh;
   float eps;
+  const int32_t* __restrict__ perm;
   __device__ void load(int i, float4& o, float4& d, float& t0, DevWBVH& b, float& e) {
+    if (perm) i = __ldg(perm + i);
     o = __ldg(org + i);
     d = __ldg(dir + i);
     t0 = 1e34f;  // MAX_DISTANCE, src/Core/Ray.cuh:13
@@ -571,6 +573,7 @@ struct WExtendIO {
     e = eps;
   }
   __device__ void store(int i, int h, float t, bool overflow) {
+    if (perm) i = __ldg(perm + i);
     if (overflow) {
       atomicOr(err, kErrStackOverflow);
       hit[i] = make_int2(-1, __float_as_int(1e34f));
@@ -620,7 +623,9 @@ struct WBatchExtendIO {
   const BatchJob* jobs;
   const int32_t* bases;
   int n_jobs;
+  const int32_t* __restrict__ perm;
   __device__ void load(int i, float4& o, float4& d, float& t0, DevWBVH& b, float& e) {
+    if (perm) i = __ldg(perm + i);
     o = __ldg(org + i);
     d = __ldg(dir + i);
     t0 = 1e34f;
@@ -629,6 +634,7 @@ struct WBatchExtendIO {
     e = J.f.tri_eps;
   }
   __device__ void store(int i, int h, float t, bool overflow) {
+    if (perm) i = __ldg(perm + i);
     if (overflow) {
       atomicOr(err, kErrStackOverflow);
       hit[i] = make_int2(-1, __float_as_int(1e34f));
@@ -683,7 +689,7 @@ __global__ void __launch_bounds__(128) k_extend_wide(DevWBVH b, DevQueues q, int
     q.counts[5] = 0;  // fetch cursor of the connect that follows
     atomicAdd(&q.stats[0], (unsigned long long)n);
   }
-  WExtendIO io{q.org_q(qi), q.dir_q(qi), q.hit, q.error, b, eps};
+  WExtendIO io{q.org_q(qi), q.dir_q(qi), q.hit, q.error, b, eps, q.perm};
   trace_wide_mt<false>(n, q.counts + 4, io, st_node, st_t);
 }
 
@@ -706,7 +712,7 @@ __global__ void __launch_bounds__(128) k_batch_extend_wide(DevBatch bt, DevQueue
     q.counts[5] = 0;
     atomicAdd(&q.stats[0], (unsigned long long)n);
   }
-  WBatchExtendIO io{q.org_q(qi), q.dir_q(qi), q.hit, q.error, bt.jobs, bt.bases, bt.n_jobs};
+  WBatchExtendIO io{q.org_q(qi), q.dir_q(qi), q.hit, q.error, bt.jobs, bt.bases, bt.n_jobs, q.perm};
   trace_wide_mt<false>(n, q.counts + 4, io, st_node, st_t);
 }
 

@@ -124,6 +124,12 @@ enum { CT_SHADE_COMPAT = 0, CT_SHADE_FULL = 1 };
  * src/Core/SceneData.cuh:81-116), or bilinear over the same texel grid
  * (texel centres at u*(width-1), v*(height-1), clamped at the edges). */
 enum { CT_TEX_NEAREST = 0, CT_TEX_BILINEAR = 1 };
+/* Ray-sort keys for the bounce queues (no reference counterpart): before each
+ * closest-hit pass after the first, windows of 2048 queued rays are ordered by
+ * direction octant (CT_SORT_OCTANT) or by cube face and a 4x4 cell on it
+ * (CT_SORT_FACE_CELLS), so rays that traverse alike share a warp. Results are
+ * identical with every key: only the traversal order of the queue changes. */
+enum { CT_SORT_NONE = 0, CT_SORT_OCTANT = 1, CT_SORT_FACE_CELLS = 2 };
 
 /* Per-frame parameters: the reference `Params` (src/CUDA/Kernel.cuh:23-72) and
  * SceneData flags/epsilons (src/Core/SceneData.cuh:19-45). Defaults from
@@ -143,6 +149,7 @@ typedef struct ct_render_params {
   float dist_eps;        /* SceneData::distEpsilon */
   float tri_eps;         /* SceneData::triangleEpsilon */
   int32_t texture_filter; /* CT_TEX_NEAREST (reference) or CT_TEX_BILINEAR */
+  int32_t ray_sort;      /* CT_SORT_*: order of bounce rays before closest-hit traversal (no result changes) */
 } ct_render_params;
 
 typedef struct ct_frame_stats {
@@ -304,6 +311,7 @@ typedef struct ct_batch_tuning {
   int32_t connect_block;
   int32_t shade_waves;
   int32_t use_graph;
+  int32_t sort_key;      /* CT_SORT_*: ray-sort key of the bounce queues */
 } ct_batch_tuning;
 /* Copies the job table; allocates queues for every job's pixels at once and
  * one FP32 RGBA accumulation buffer holding all jobs' images back to back. */

@@ -110,7 +110,9 @@ def test_graph_replay_and_tunings_do_not_change_results(gpu_ctx, scenes_):
     jobs = _mix(scenes_)
     ref, _ = _run(gpu_ctx, jobs, tuning=dict(extend_block=128, connect_block=128, shade_waves=1, use_graph=0))
     for t in (dict(extend_block=64, connect_block=256, shade_waves=2, use_graph=1),
-              dict(extend_block=256, connect_block=128, shade_waves=1, use_graph=1)):
+              dict(extend_block=256, connect_block=128, shade_waves=1, use_graph=1),
+              dict(extend_block=128, connect_block=128, shade_waves=1, use_graph=1, sort_key=1),
+              dict(extend_block=64, connect_block=128, shade_waves=2, use_graph=0, sort_key=2)):
         out, _ = _run(gpu_ctx, jobs, tuning=t)
         for a, b in zip(ref, out):
             assert np.array_equal(a.view(np.int32), b.view(np.int32))
@@ -125,7 +127,7 @@ def test_autotune_picks_a_valid_shape(gpu_ctx, scenes_):
     b = api.Batch(gpu_ctx, jobs)
     t, ms = b.autotune()
     assert t["extend_block"] in (64, 128, 256) and t["connect_block"] in (64, 128, 256)
-    assert t["shade_waves"] in (1, 2) and t["use_graph"] in (0, 1) and ms > 0
+    assert t["shade_waves"] in (1, 2) and t["use_graph"] in (0, 1) and t["sort_key"] in (0, 1, 2) and ms > 0
     assert b.tuning == t
     b.run()
     torch.cuda.synchronize()
@@ -162,3 +164,7 @@ def test_wide_batch_job_alone_equals_job_in_mix(gpu_ctx, scenes_):
     for k in (0, 3, 5):
         alone, _ = _run(gpu_ctx, [jobs[k]])
         assert np.array_equal(alone[0].view(np.int32), mixed[k].view(np.int32)), k
+    srt, _ = _run(gpu_ctx, jobs, tuning=dict(extend_block=128, connect_block=128, shade_waves=1, use_graph=1,
+                                             sort_key=2))
+    for a, b in zip(mixed, srt):
+        assert np.array_equal(a.view(np.int32), b.view(np.int32))

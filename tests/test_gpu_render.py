@@ -69,6 +69,26 @@ def test_exact_frames_flags(gpu_ctx, orc, small, flags):
     assert _bad(acc, oacc).sum() == 0
 
 
+@pytest.mark.parametrize("exact", [True, False])
+def test_ray_sort_keys_do_not_change_frames(gpu_ctx, orc, small, exact):
+    """Sorting the bounce queues by direction class changes which rays share a
+    warp, never a result: every key gives the same accumulation bit for bit,
+    and exact frames still equal the oracle."""
+    from cudatracer_gb300 import _lib, api
+
+    W, H = 96, 64
+    outs = [_render(gpu_ctx, small, W, H, 3, 5, exact, ray_sort=k)[2]
+            for k in (_lib.CT_SORT_NONE, _lib.CT_SORT_OCTANT, _lib.CT_SORT_FACE_CELLS)]
+    for o in outs[1:]:
+        assert np.array_equal(outs[0].view(np.int32), o.view(np.int32))
+    if exact:
+        assert _bad(outs[2], _oracle(orc, small, W, H, 3, 5, True)).sum() == 0
+    job = api.RenderJob(gpu_ctx, W, H)
+    p = api.Params(W, H, camera=api.Camera(W, H, 60.0, (0, 5, 20), (0, 0, -1), (0, 1, 0)), ray_sort=3)
+    with pytest.raises(_lib.CTError):
+        api.launch_kernels(job, small["sc"], small["bvh"], p)
+
+
 def test_fast_math_frames_close_to_oracle(gpu_ctx, orc, small):
     W, H = 96, 64
     _, _, acc = _render(gpu_ctx, small, W, H, 4, 5, False)
