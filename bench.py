@@ -709,7 +709,9 @@ def run_ours(args, world, rank, local):
         oracle.build_oracle()
         quad, prims = bvh.export()
         omats = oracle.pack_materials(ts.materials)
-        # traversal work per extension ray on sampled rows (the reference's traverseMBVH counts)
+        # traversal work per extension ray on sampled rows: the reference's traverseMBVH
+        # counts, in the child order the GPU frames use (full distance order in fast math)
+        oracle.set_full_sort(not args.exact_math)
         oracle.work_read(reset=True)
         acc = np.zeros((W * H, 4), np.float32)
         for r0 in range(0, H, 135):
@@ -717,6 +719,7 @@ def run_ours(args, world, rank, local):
                                  textures=ts.textures, sky_tex=0, pixels=(r0 * W, (r0 + 2) * W),
                                  nthreads=os.cpu_count() or 1)
         work = oracle.work_read(reset=True)
+        oracle.set_full_sort(False)
         v_node = work["ext_nodes"] / max(1, work["ext_rays"])
         v_tri = work["ext_tris"] / max(1, work["ext_rays"])
         b_ray = 32 + v_node * 128 + v_tri * 52

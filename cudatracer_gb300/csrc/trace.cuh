@@ -12,6 +12,9 @@
 // a slab term is NaN (a zero direction component with the origin exactly on a
 // bounding plane) or when two zeros of opposite sign meet (an origin on two
 // planes). The fast-math render path uses FASTMM; exact paths never do.
+// FASTMM closest-hit traversal also visits hit children in true distance order
+// (inner_step_sorted) instead of the reference's partial order network: the
+// same nearest hit (up to exact ties), fewer node visits and instructions.
 #pragma once
 
 #include "ct_internal.h"
@@ -101,6 +104,64 @@ __device__ __forceinline__ void ray_begin(RayState& r, float4 o, float4 d, float
 }
 
 enum StepResult { kContinue = 0, kDone = 1, kOverflow = 2 };
+
+// Compare-and-swap of (distance, child) pairs: the nearer pair goes first.
+__device__ __forceinline__ void cas_pair(float& ka, int& ca, float& kb, int& cb) {
+  const bool sw = kb < ka;
+  const float k = sw ? kb : ka;
+  const int c = sw ? cb : ca;
+  kb = sw ? ka : kb;
+  cb = sw ? ca : cb;
+  ka = k;
+  ca = c;
+}
+
+// Fast-math closest-hit node step: the hit children in true distance order (a
+// full 4-sort of (tmin, child) pairs, misses last as +inf), nearest visited
+// next and the others pushed far to near with predicated stores. Frames in
+// fast math do not reproduce the reference's visiting order, only its nearest
+// hit, which no order changes beyond exact ties.
+__device__ __forceinline__ StepResult inner_step_sorted(const DevBVH& b, RayState& r, int* stack, int stride,
+                                                        int limit) {
+  const QNodeDev* n = b.nodes + r.ref;
+  const float4 nx0 = __ldg(&n->bminx), nx1 = __ldg(&n->bmaxx);
+  const float4 ny0 = __ldg(&n->bminy), ny1 = __ldg(&n->bmaxy);
+  const float4 nz0 = __ldg(&n->bminz), nz1 = __ldg(&n->bmaxz);
+  const int4 ch = __ldg(&n->child);
+  float tn0, tn1, tn2, tn3, tf0, tf1, tf2, tf3;
+  slab<true>(nx0.x, nx1.x, ny0.x, ny1.x, nz0.x, nz1.x, r.ox, r.oy, r.oz, r.ix, r.iy, r.iz, tn0, tf0);
+  slab<true>(nx0.y, nx1.y, ny0.y, ny1.y, nz0.y, nz1.y, r.ox, r.oy, r.oz, r.ix, r.iy, r.iz, tn1, tf1);
+  slab<true>(nx0.z, nx1.z, ny0.z, ny1.z, nz0.z, nz1.z, r.ox, r.oy, r.oz, r.ix, r.iy, r.iz, tn2, tf2);
+  slab<true>(nx0.w, nx1.w, ny0.w, ny1.w, nz0.w, nz1.w, r.ox, r.oy, r.oz, r.ix, r.iy, r.iz, tn3, tf3);
+  const float t = r.t, inf = __int_as_float(0x7f800000);
+  const bool h0 = tf0 > 0.0f && tn0 <= tf0 && tn0 < t && ch.x != kEmptyChild;
+  const bool h1 = tf1 > 0.0f && tn1 <= tf1 && tn1 < t && ch.y != kEmptyChild;
+  const bool h2 = tf2 > 0.0f && tn2 <= tf2 && tn2 < t && ch.z != kEmptyChild;
+  const bool h3 = tf3 > 0.0f && tn3 <= tf3 && tn3 < t && ch.w != kEmptyChild;
+  const int cnt = (int)h0 + (int)h1 + (int)h2 + (int)h3;
+  if (cnt == 0) {
+    if (r.sp == 0) return kDone;
+    r.ref = stack[--r.sp * stride];
+    return kContinue;
+  }
+  float k0 = h0 ? tn0 : inf, k1 = h1 ? tn1 : inf, k2 = h2 ? tn2 : inf, k3 = h3 ? tn3 : inf;
+  int c0 = ch.x, c1 = ch.y, c2 = ch.z, c3 = ch.w;
+  if (cnt > 1) {
+    cas_pair(k0, c0, k1, c1);
+    cas_pair(k2, c2, k3, c3);
+    cas_pair(k0, c0, k2, c2);
+    cas_pair(k1, c1, k3, c3);
+    cas_pair(k1, c1, k2, c2);
+    if (r.sp + cnt - 1 > limit) return kOverflow;
+    if (cnt > 3) stack[r.sp++ * stride] = c3;
+    if (cnt > 2) stack[r.sp++ * stride] = c2;
+    stack[r.sp++ * stride] = c1;
+  } else {
+    c0 = h0 ? ch.x : (h1 ? ch.y : (h2 ? ch.z : ch.w));
+  }
+  r.ref = c0;
+  return kContinue;
+}
 
 // Visit the inner node r.ref: slab-test the four children (MBVHNode.cuh:69-110),
 // then continue with the nearest hit child and push the others far to near
@@ -238,7 +299,10 @@ template <bool ANY, bool FASTMM>
 __device__ __forceinline__ bool traverse(const DevBVH& b, RayState& r, float eps, int* stack, int stride) {
   const int limit = b.stack_entries;
   while (true) {
-    const StepResult s = r.ref >= 0 ? (ANY ? inner_step_any<FASTMM>(b, r, stack, stride, limit) : inner_step<FASTMM>(b, r, stack, stride, limit)) : leaf_step<ANY>(b, r, eps, stack, stride);
+    const StepResult s = r.ref >= 0 ? (ANY ? inner_step_any<FASTMM>(b, r, stack, stride, limit)
+                                           : (FASTMM ? inner_step_sorted(b, r, stack, stride, limit)
+                                                     : inner_step<false>(b, r, stack, stride, limit)))
+                                    : leaf_step<ANY>(b, r, eps, stack, stride);
     if (s == kDone) return true;
     if (s == kOverflow) return false;
   }
@@ -286,7 +350,10 @@ __device__ __forceinline__ void trace_persistent(const DevBVH& b, int n, int* cu
     }
     if (__ballot_sync(FULL, rid >= 0) == 0) break;
     if (rid < 0) continue;
-    const StepResult s = r.ref >= 0 ? (ANY ? inner_step_any<FASTMM>(b, r, stack, stride, limit) : inner_step<FASTMM>(b, r, stack, stride, limit)) : leaf_step<ANY>(b, r, eps, stack, stride);
+    const StepResult s = r.ref >= 0 ? (ANY ? inner_step_any<FASTMM>(b, r, stack, stride, limit)
+                                           : (FASTMM ? inner_step_sorted(b, r, stack, stride, limit)
+                                                     : inner_step<false>(b, r, stack, stride, limit)))
+                                    : leaf_step<ANY>(b, r, eps, stack, stride);
     if (s != kContinue) {
       io.store(rid, r, s == kOverflow);
       rid = -1;
@@ -331,7 +398,10 @@ __device__ __forceinline__ void trace_persistent_batch(int n, int* cursor, IO& i
     if (__ballot_sync(FULL, rid >= 0) == 0) break;
     if (rid < 0) continue;
     const StepResult s =
-        r.ref >= 0 ? (ANY ? inner_step_any<FASTMM>(b, r, stack, stride, b.stack_entries) : inner_step<FASTMM>(b, r, stack, stride, b.stack_entries)) : leaf_step<ANY>(b, r, eps, stack, stride);
+        r.ref >= 0 ? (ANY ? inner_step_any<FASTMM>(b, r, stack, stride, b.stack_entries)
+                          : (FASTMM ? inner_step_sorted(b, r, stack, stride, b.stack_entries)
+                                    : inner_step<false>(b, r, stack, stride, b.stack_entries)))
+                   : leaf_step<ANY>(b, r, eps, stack, stride);
     if (s != kContinue) {
       io.store(rid, r, s == kOverflow);
       rid = -1;

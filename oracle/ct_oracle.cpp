@@ -329,6 +329,13 @@ inline bool tri_intersect(V3 org, V3 dir, float* rayt, V3 p0, V3 p1, V3 p2, floa
   return false;
 }
 
+// Child order after the slab tests: the reference's 5-exchange network, whose
+// last pair is (2,3) and which leaves (1,2) unordered (MBVHNode.cuh:98-107), or,
+// when g_full_sort is set, a full 4-sort with last pair (1,2) as the fast-math
+// GPU frames use. Only the visiting order differs, hence only the work counts
+// (and exact-tie choices); every parity test runs with the reference's order.
+static std::atomic<int> g_full_sort{0};
+
 // MBVHNode::intersect (src/BVH/MBVHNode.cuh:69-110)
 inline void quad_intersect(const QNode& n, V3 o, V3 inv, float t, float tmin[4], bool res[4]) {
   float tmax[4];
@@ -352,7 +359,10 @@ inline void quad_intersect(const QNode& n, V3 o, V3 inv, float t, float tmin[4],
   cs(2, 3);
   cs(0, 2);
   cs(1, 3);
-  cs(2, 3);
+  if (g_full_sort.load(std::memory_order_relaxed))
+    cs(1, 2);
+  else
+    cs(2, 3);
 }
 
 struct Geo {
@@ -1006,6 +1016,10 @@ void or_work_read(uint64_t* out, int reset) {
     if (reset) g_work[k] = 0;
   }
 }
+
+/* Child order of the quad traversal for the frames that follow: 0 the
+ * reference's network (default), 1 a full sort (fast-math GPU frames). */
+void or_set_full_sort(int on) { g_full_sort = on ? 1 : 0; }
 
 /* ---- per-function entry points for the known-answer tests ---- */
 void or_sample_bsdf(const float* color, float roughness, const float* iN, const float* N, const float* wi, float r3,

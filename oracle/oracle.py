@@ -330,6 +330,14 @@ def work_read(reset: bool = True) -> dict:
     return {k: int(v) for k, v in zip(keys, w)}
 
 
+def set_full_sort(on: bool) -> None:
+    """Visit quad children in full distance order (as fast-math GPU frames do)
+    instead of the reference's partial order; changes work counts only."""
+    L = lib()
+    L.or_set_full_sort.argtypes = [ctypes.c_int]
+    L.or_set_full_sort(int(on))
+
+
 def camera_basis(forward, up, fov_deg, width, height):
     L = lib()
     fw = np.asarray(forward, np.float32)
