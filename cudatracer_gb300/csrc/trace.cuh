@@ -12,9 +12,11 @@
 // a slab term is NaN (a zero direction component with the origin exactly on a
 // bounding plane) or when two zeros of opposite sign meet (an origin on two
 // planes). The fast-math render path uses FASTMM; exact paths never do.
-// FASTMM closest-hit traversal also visits hit children in true distance order
+// FASTMM traversal also computes each slab plane with one fused multiply-add
+// and, for closest hit, visits hit children in true distance order
 // (inner_step_sorted) instead of the reference's partial order network: the
-// same nearest hit (up to exact ties), fewer node visits and instructions.
+// same nearest hit up to exact ties and the rounding of box distances, fewer
+// instructions per node.
 #pragma once
 
 #include "ct_internal.h"
@@ -58,6 +60,19 @@ __device__ __forceinline__ void slab(float bminx, float bmaxx, float bminy, floa
   tmax = mn<FASTMM>(tmax, mx<FASTMM>(t1, t2));
 }
 
+// Fast-math slab: one fused multiply-add per plane, b * inv + (-o * inv). A
+// zero direction component makes that axis NaN, which the hardware min/max
+// drop: the axis then culls nothing (more boxes visited, never a hit lost).
+__device__ __forceinline__ void slab_fma(float bminx, float bmaxx, float bminy, float bmaxy, float bminz,
+                                         float bmaxz, float nox, float noy, float noz, float ix, float iy, float iz,
+                                         float& tmin, float& tmax) {
+  const float x1 = fmaf(bminx, ix, nox), x2 = fmaf(bmaxx, ix, nox);
+  const float y1 = fmaf(bminy, iy, noy), y2 = fmaf(bmaxy, iy, noy);
+  const float z1 = fmaf(bminz, iz, noz), z2 = fmaf(bmaxz, iz, noz);
+  tmin = fmaxf(fmaxf(fminf(x1, x2), fminf(y1, y2)), fminf(z1, z2));
+  tmax = fminf(fminf(fmaxf(x1, x2), fmaxf(y1, y2)), fmaxf(z1, z2));
+}
+
 // Moller-Trumbore with the reference's absolute epsilon. Returns the new t
 // through `t` when the hit is closer (t' > eps && t > t').
 __device__ __forceinline__ bool tri_test(const float4 a, const float4 e1v, const float4 e2v, float ox, float oy,
@@ -91,12 +106,14 @@ __device__ __forceinline__ bool tri_test(const float4 a, const float4 e1v, const
 // Per-ray traversal state.
 struct RayState {
   float ox, oy, oz, dx, dy, dz, ix, iy, iz, t;
+  float nox, noy, noz;  // -o * inv, read by the fast-math slab only
   int hit, sp, ref;
 };
 
 __device__ __forceinline__ void ray_begin(RayState& r, float4 o, float4 d, float t0) {
   r.ox = o.x, r.oy = o.y, r.oz = o.z, r.dx = d.x, r.dy = d.y, r.dz = d.z;
   r.ix = __frcp_rn(d.x), r.iy = __frcp_rn(d.y), r.iz = __frcp_rn(d.z);
+  r.nox = -o.x * r.ix, r.noy = -o.y * r.iy, r.noz = -o.z * r.iz;
   r.t = t0;
   r.hit = -1;
   r.sp = 0;
@@ -104,6 +121,17 @@ __device__ __forceinline__ void ray_begin(RayState& r, float4 o, float4 d, float
 }
 
 enum StepResult { kContinue = 0, kDone = 1, kOverflow = 2 };
+
+// The four child intervals of a node in fast math.
+__device__ __forceinline__ void fast_slab4(const float4& nx0, const float4& nx1, const float4& ny0, const float4& ny1,
+                                           const float4& nz0, const float4& nz1, const RayState& r, float& tn0,
+                                           float& tn1, float& tn2, float& tn3, float& tf0, float& tf1, float& tf2,
+                                           float& tf3) {
+  slab_fma(nx0.x, nx1.x, ny0.x, ny1.x, nz0.x, nz1.x, r.nox, r.noy, r.noz, r.ix, r.iy, r.iz, tn0, tf0);
+  slab_fma(nx0.y, nx1.y, ny0.y, ny1.y, nz0.y, nz1.y, r.nox, r.noy, r.noz, r.ix, r.iy, r.iz, tn1, tf1);
+  slab_fma(nx0.z, nx1.z, ny0.z, ny1.z, nz0.z, nz1.z, r.nox, r.noy, r.noz, r.ix, r.iy, r.iz, tn2, tf2);
+  slab_fma(nx0.w, nx1.w, ny0.w, ny1.w, nz0.w, nz1.w, r.nox, r.noy, r.noz, r.ix, r.iy, r.iz, tn3, tf3);
+}
 
 // Compare-and-swap of (distance, child) pairs: the nearer pair goes first.
 __device__ __forceinline__ void cas_pair(float& ka, int& ca, float& kb, int& cb) {
@@ -129,10 +157,7 @@ __device__ __forceinline__ StepResult inner_step_sorted(const DevBVH& b, RayStat
   const float4 nz0 = __ldg(&n->bminz), nz1 = __ldg(&n->bmaxz);
   const int4 ch = __ldg(&n->child);
   float tn0, tn1, tn2, tn3, tf0, tf1, tf2, tf3;
-  slab<true>(nx0.x, nx1.x, ny0.x, ny1.x, nz0.x, nz1.x, r.ox, r.oy, r.oz, r.ix, r.iy, r.iz, tn0, tf0);
-  slab<true>(nx0.y, nx1.y, ny0.y, ny1.y, nz0.y, nz1.y, r.ox, r.oy, r.oz, r.ix, r.iy, r.iz, tn1, tf1);
-  slab<true>(nx0.z, nx1.z, ny0.z, ny1.z, nz0.z, nz1.z, r.ox, r.oy, r.oz, r.ix, r.iy, r.iz, tn2, tf2);
-  slab<true>(nx0.w, nx1.w, ny0.w, ny1.w, nz0.w, nz1.w, r.ox, r.oy, r.oz, r.ix, r.iy, r.iz, tn3, tf3);
+  fast_slab4(nx0, nx1, ny0, ny1, nz0, nz1, r, tn0, tn1, tn2, tn3, tf0, tf1, tf2, tf3);
   const float t = r.t, inf = __int_as_float(0x7f800000);
   const bool h0 = tf0 > 0.0f && tn0 <= tf0 && tn0 < t && ch.x != kEmptyChild;
   const bool h1 = tf1 > 0.0f && tn1 <= tf1 && tn1 < t && ch.y != kEmptyChild;
@@ -241,10 +266,14 @@ __device__ __forceinline__ StepResult inner_step_any(const DevBVH& b, RayState& 
   const float4 nz0 = __ldg(&n->bminz), nz1 = __ldg(&n->bmaxz);
   const int4 ch = __ldg(&n->child);
   float tn0, tn1, tn2, tn3, tf0, tf1, tf2, tf3;
-  slab<FASTMM>(nx0.x, nx1.x, ny0.x, ny1.x, nz0.x, nz1.x, r.ox, r.oy, r.oz, r.ix, r.iy, r.iz, tn0, tf0);
-  slab<FASTMM>(nx0.y, nx1.y, ny0.y, ny1.y, nz0.y, nz1.y, r.ox, r.oy, r.oz, r.ix, r.iy, r.iz, tn1, tf1);
-  slab<FASTMM>(nx0.z, nx1.z, ny0.z, ny1.z, nz0.z, nz1.z, r.ox, r.oy, r.oz, r.ix, r.iy, r.iz, tn2, tf2);
-  slab<FASTMM>(nx0.w, nx1.w, ny0.w, ny1.w, nz0.w, nz1.w, r.ox, r.oy, r.oz, r.ix, r.iy, r.iz, tn3, tf3);
+  if (FASTMM) {
+    fast_slab4(nx0, nx1, ny0, ny1, nz0, nz1, r, tn0, tn1, tn2, tn3, tf0, tf1, tf2, tf3);
+  } else {
+    slab<false>(nx0.x, nx1.x, ny0.x, ny1.x, nz0.x, nz1.x, r.ox, r.oy, r.oz, r.ix, r.iy, r.iz, tn0, tf0);
+    slab<false>(nx0.y, nx1.y, ny0.y, ny1.y, nz0.y, nz1.y, r.ox, r.oy, r.oz, r.ix, r.iy, r.iz, tn1, tf1);
+    slab<false>(nx0.z, nx1.z, ny0.z, ny1.z, nz0.z, nz1.z, r.ox, r.oy, r.oz, r.ix, r.iy, r.iz, tn2, tf2);
+    slab<false>(nx0.w, nx1.w, ny0.w, ny1.w, nz0.w, nz1.w, r.ox, r.oy, r.oz, r.ix, r.iy, r.iz, tn3, tf3);
+  }
   const float p0 = __int_as_float((__float_as_int(tn0) & ~3) | 0);
   const float p1 = __int_as_float((__float_as_int(tn1) & ~3) | 1);
   const float p2 = __int_as_float((__float_as_int(tn2) & ~3) | 2);
@@ -259,16 +288,13 @@ __device__ __forceinline__ StepResult inner_step_any(const DevBVH& b, RayState& 
     r.ref = stack[--r.sp * stride];
     return kContinue;
   }
-  const int first = __ffs(vm) - 1;
-  vm &= vm - 1;
-  while (vm) {
-    const int c = __ffs(vm) - 1;
-    vm &= vm - 1;
-    if (r.sp >= limit) return kOverflow;
-    stack[r.sp * stride] = sel4(ch.x, ch.y, ch.z, ch.w, c);
-    r.sp++;
-  }
-  r.ref = sel4(ch.x, ch.y, ch.z, ch.w, first);
+  // the lowest hit slot continues; the others (never slot 0) are pushed in slot order
+  const unsigned rest = vm & (vm - 1);
+  if (r.sp + __popc(rest) > limit) return kOverflow;
+  if (rest & 2u) stack[r.sp++ * stride] = ch.y;
+  if (rest & 4u) stack[r.sp++ * stride] = ch.z;
+  if (rest & 8u) stack[r.sp++ * stride] = ch.w;
+  r.ref = (vm & 1u) ? ch.x : ((vm & 2u) ? ch.y : ((vm & 4u) ? ch.z : ch.w));
   return kContinue;
 }
 
