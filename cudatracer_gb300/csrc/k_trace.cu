@@ -13,6 +13,8 @@
 namespace ct {
 
 constexpr int kBlock = 128;
+constexpr int kExtendRefill = 24;  // idle lanes that make an extend warp refill (of 32)
+constexpr int kQueryRefill = 8;    // the same for ray queries (shorter, often coherent)
 constexpr float kMaxDistance = 1e34f;  // MAX_DISTANCE, src/Core/Ray.cuh:13
 
 int sm_count() {
@@ -101,7 +103,7 @@ struct ExtendIO {
 template <bool ANY>
 __global__ void __launch_bounds__(kBlock) k_query(DevBVH b, QueryIO io, int n, int* cursor, float eps) {
   extern __shared__ int s_stack[];
-  trace_persistent<ANY, false>(b, n, cursor, eps, io, s_stack + threadIdx.x, kBlock);
+  trace_persistent<ANY, false, kQueryRefill>(b, n, cursor, eps, io, s_stack + threadIdx.x, kBlock);
 }
 
 template <bool FASTMM>
@@ -115,7 +117,7 @@ __global__ void __launch_bounds__(kBlock) k_extend(DevBVH b, DevQueues q, int qi
     atomicAdd(&q.stats[0], (unsigned long long)n);
   }
   ExtendIO io{q.org_q(qi), q.dir_q(qi), q.hit, q.error, q.perm};
-  trace_persistent<false, FASTMM>(b, n, q.counts + 4, eps, io, s_stack + threadIdx.x, kBlock);
+  trace_persistent<false, FASTMM, kExtendRefill>(b, n, q.counts + 4, eps, io, s_stack + threadIdx.x, kBlock);
 }
 
 // connect (src/CUDA/Kernel.cu:247-256): unoccluded shadow rays add their
@@ -335,7 +337,7 @@ __global__ void __launch_bounds__(BLOCK) k_batch_extend(DevBatch bt, DevQueues q
     atomicAdd(&q.stats[0], (unsigned long long)n);
   }
   BatchExtendIO io{q.org_q(qi), q.dir_q(qi), q.hit, q.error, bt.jobs, bt.bases, bt.n_jobs, q.perm};
-  trace_persistent_batch<false, FASTMM>(n, q.counts + 4, io, s_stack + threadIdx.x, BLOCK);
+  trace_persistent_batch<false, FASTMM, kExtendRefill>(n, q.counts + 4, io, s_stack + threadIdx.x, BLOCK);
 }
 
 template <bool FASTMM, int BLOCK>

@@ -337,12 +337,17 @@ __device__ __forceinline__ bool traverse(const DevBVH& b, RayState& r, float eps
 // Persistent traversal with per-warp dynamic ray fetch. Each lane owns a ray
 // and performs one step (an inner node or a leaf) per round; lanes whose ray
 // finished take the next rays from a device cursor (one atomicAdd per warp),
-// so a warp is not held back by its longest ray. Every ray still performs the
+// so a warp is not held back by its longest ray. A warp refills once at least
+// REFILL of its lanes are idle (or all are): refilling costs a cursor atomic
+// shared by every warp, a ballot and the new rays' loads and reciprocals, run
+// by the whole warp for the lanes that refill, so batching refills pays for
+// long incoherent traversals (the wavefront's extend) while short coherent
+// queries refill at the first idle lane. Every ray still performs the
 // reference's exact sequence of node tests, pushes, pops and triangle tests:
 // only the interleaving across lanes changes.
 //   IO::load(int i, float4& org, float4& dir, float& t0)
 //   IO::store(int i, const RayState& r, bool overflow)
-template <bool ANY, bool FASTMM, class IO>
+template <bool ANY, bool FASTMM, int REFILL, class IO>
 __device__ __forceinline__ void trace_persistent(const DevBVH& b, int n, int* cursor, float eps, IO& io, int* stack,
                                                  int stride) {
   const unsigned FULL = 0xffffffffu;
@@ -356,7 +361,7 @@ __device__ __forceinline__ void trace_persistent(const DevBVH& b, int n, int* cu
   while (true) {
     if (!exhausted) {
       const unsigned m = __ballot_sync(FULL, rid < 0);
-      if (m) {
+      if (m == FULL || __popc(m) >= REFILL) {
         const int leader = __ffs(m) - 1;
         int base = 0;
         if (lane == leader) base = atomicAdd(cursor, __popc(m));
@@ -389,7 +394,7 @@ __device__ __forceinline__ void trace_persistent(const DevBVH& b, int n, int* cu
 
 // trace_persistent with a BVH and epsilon per lane: io.load(i, o, d, t0, b, eps)
 // supplies the ray and the tree it is traced against (batches of jobs).
-template <bool ANY, bool FASTMM, class IO>
+template <bool ANY, bool FASTMM, int REFILL, class IO>
 __device__ __forceinline__ void trace_persistent_batch(int n, int* cursor, IO& io, int* stack, int stride) {
   const unsigned FULL = 0xffffffffu;
   const int lane = threadIdx.x & 31;
@@ -403,7 +408,7 @@ __device__ __forceinline__ void trace_persistent_batch(int n, int* cursor, IO& i
   while (true) {
     if (!exhausted) {
       const unsigned m = __ballot_sync(FULL, rid < 0);
-      if (m) {
+      if (m == FULL || __popc(m) >= REFILL) {
         const int leader = __ffs(m) - 1;
         int base = 0;
         if (lane == leader) base = atomicAdd(cursor, __popc(m));
