@@ -317,6 +317,34 @@ __device__ __forceinline__ StepResult leaf_step(const DevBVH& b, RayState& r, fl
   return kContinue;
 }
 
+// leaf_step that tests at most P triangles per call: the rest of the leaf stays
+// in r.ref (first + k, count - k), so a round of the persistent loop is not
+// held up by the warp's largest leaf (P = 2 measured best; 1, 3 and 4 close).
+// Each ray still tests its triangles in the same order, so results are those
+// of leaf_step.
+template <bool ANY, int P>
+__device__ __forceinline__ StepResult leaf_step_part(const DevBVH& b, RayState& r, float eps, int* stack, int stride) {
+  const uint32_t u = (uint32_t)r.ref;
+  const uint32_t first = u & b.first_mask;
+  const uint32_t cnt = (u >> b.leaf_shift) & b.count_mask;
+  const uint32_t m = cnt < (uint32_t)P ? cnt : (uint32_t)P;
+  const float4* tp = b.tris + 3 * (size_t)first;
+  for (uint32_t k = 0; k < m; k++) {
+    const float4 a = __ldg(tp + 3 * k), e1 = __ldg(tp + 3 * k + 1), e2 = __ldg(tp + 3 * k + 2);
+    if (tri_test(a, e1, e2, r.ox, r.oy, r.oz, r.dx, r.dy, r.dz, eps, r.t)) {
+      r.hit = __float_as_int(a.w);
+      if (ANY) return kDone;
+    }
+  }
+  if (cnt > m) {
+    r.ref = (int)(u + m - (m << b.leaf_shift));
+    return kContinue;
+  }
+  if (r.sp == 0) return kDone;
+  r.ref = stack[--r.sp * stride];
+  return kContinue;
+}
+
 // Whole traversal of one ray by one thread. ANY = stop at the first hit
 // (traverseMBVHShadow: nodes culled against maxDist, triangles accepted below
 // it). `stack` is this thread's column of a [entries][stride] shared array.
@@ -384,7 +412,7 @@ __device__ __forceinline__ void trace_persistent(const DevBVH& b, int n, int* cu
     const StepResult s = r.ref >= 0 ? (ANY ? inner_step_any<FASTMM>(b, r, stack, stride, limit)
                                            : (FASTMM ? inner_step_sorted(b, r, stack, stride, limit)
                                                      : inner_step<false>(b, r, stack, stride, limit)))
-                                    : leaf_step<ANY>(b, r, eps, stack, stride);
+                                    : leaf_step_part<ANY, 2>(b, r, eps, stack, stride);
     if (s != kContinue) {
       io.store(rid, r, s == kOverflow);
       rid = -1;
@@ -432,7 +460,7 @@ __device__ __forceinline__ void trace_persistent_batch(int n, int* cursor, IO& i
         r.ref >= 0 ? (ANY ? inner_step_any<FASTMM>(b, r, stack, stride, b.stack_entries)
                           : (FASTMM ? inner_step_sorted(b, r, stack, stride, b.stack_entries)
                                     : inner_step<false>(b, r, stack, stride, b.stack_entries)))
-                   : leaf_step<ANY>(b, r, eps, stack, stride);
+                   : leaf_step_part<ANY, 2>(b, r, eps, stack, stride);
     if (s != kContinue) {
       io.store(rid, r, s == kOverflow);
       rid = -1;
