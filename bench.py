@@ -649,7 +649,7 @@ def run_ours(args, world, rank, local):
     ctx.check(stream)
     st = job.stats(reset=True, stream=stream)
     # stage times: a separate pass with per-launch events, frames one after another
-    # (the timed frames overlap on six streams, where an interval is not one kernel)
+    # (the timed frames overlap on ten streams, where an interval is not one kernel)
     job.profile(True)
     job.profile_read(reset=True)
     prof_frames = max(4, args.steps // 4)

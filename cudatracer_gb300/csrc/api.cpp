@@ -137,9 +137,11 @@ struct ct_bvh {
 
 // Fast-math frames in flight at once, each in its own queue set and
 // accumulation buffer: the last, nearly empty bounces of one frame overlap
-// the first passes of the next ones (measured on the 1080p terrain frame:
-// 2 slots 600, 4 slots 710, 6 slots 736, 8 slots 744 Msamples/s).
-constexpr int kFrameSlots = 6;
+// the first passes of the next ones (measured on the 1080p terrain frame with
+// the first kernels: 2 slots 600, 4 slots 710, 6 slots 736, 8 slots 744
+// Msamples/s; with the current ones, 64-thread blocks: 6 slots 973, 8 slots
+// 991, 10 slots 997, 12 slots 995).
+constexpr int kFrameSlots = 10;
 
 struct ct_render {
   int32_t w = 0, h = 0;
