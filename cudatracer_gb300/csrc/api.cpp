@@ -863,18 +863,32 @@ ct_status ct_trace_any(ct_ctx* ctx, const ct_bvh* bvh, const float* org, const f
   return CT_OK;
 }
 
+// One queue set: a single zero-filled allocation carved into 256-byte aligned
+// buffers (one cudaMalloc, one fill and one wait per set, so the ten frame
+// slots of a small job cost a few calls, not a hundred).
 static ct_status alloc_queues(ct_ctx* ctx, Allocs& a, size_t n, DevQueues& q) {
-  ct_status s;
+  auto al = [](size_t b) { return (b + 255) & ~(size_t)255; };
+  const size_t f4 = al(n * sizeof(float4)), hb = al(n * sizeof(int2)), pb = al(n * sizeof(int32_t));
+  const size_t cb = al(16 * sizeof(int32_t)), sb = al(8 * sizeof(unsigned long long));
+  char* base = nullptr;
+  const ct_status s = upload(ctx, a, &base, nullptr, 10 * f4 + hb + pb + cb + sb);
+  if (s != CT_OK) return s;
+  char* p = base;
+  auto take = [&p](size_t bytes) {
+    char* r = p;
+    p += bytes;
+    return r;
+  };
   q.capacity = (int32_t)n;
-  auto alloc4 = [&](float4** p) { return upload(ctx, a, p, nullptr, n * sizeof(float4)); };
-  if ((s = alloc4(&q.org[0])) != CT_OK || (s = alloc4(&q.org[1])) != CT_OK || (s = alloc4(&q.dir[0])) != CT_OK ||
-      (s = alloc4(&q.dir[1])) != CT_OK || (s = alloc4(&q.thr[0])) != CT_OK || (s = alloc4(&q.thr[1])) != CT_OK ||
-      (s = alloc4(&q.sorg)) != CT_OK || (s = alloc4(&q.sdir)) != CT_OK || (s = alloc4(&q.scol)) != CT_OK ||
-      (s = alloc4(&q.accum)) != CT_OK || (s = upload(ctx, a, &q.hit, nullptr, n * sizeof(int2))) != CT_OK ||
-      (s = upload(ctx, a, &q.perm_buf, nullptr, n * sizeof(int32_t))) != CT_OK ||
-      (s = upload(ctx, a, &q.counts, nullptr, 16 * sizeof(int32_t))) != CT_OK ||
-      (s = upload(ctx, a, &q.stats, nullptr, 8 * sizeof(unsigned long long))) != CT_OK)
-    return s;
+  q.org[0] = (float4*)take(f4), q.org[1] = (float4*)take(f4);
+  q.dir[0] = (float4*)take(f4), q.dir[1] = (float4*)take(f4);
+  q.thr[0] = (float4*)take(f4), q.thr[1] = (float4*)take(f4);
+  q.sorg = (float4*)take(f4), q.sdir = (float4*)take(f4), q.scol = (float4*)take(f4);
+  q.accum = (float4*)take(f4);
+  q.hit = (int2*)take(hb);
+  q.perm_buf = (int32_t*)take(pb);
+  q.counts = (int32_t*)take(cb);
+  q.stats = (unsigned long long*)take(sb);
   q.error = ctx->d_error;
   q.perm = nullptr;  // queue order unless a stage sorted the queue
   return CT_OK;
