@@ -82,7 +82,7 @@ class ct_batch_job(Structure):
 
 class ct_batch_tuning(Structure):
     _fields_ = [("extend_block", c_int32), ("connect_block", c_int32), ("shade_waves", c_int32),
-                ("use_graph", c_int32), ("sort_key", c_int32)]
+                ("use_graph", c_int32), ("sort_key", c_int32), ("refill", c_int32)]
 
 
 class ct_server_config(Structure):

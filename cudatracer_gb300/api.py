@@ -702,8 +702,8 @@ class Batch:
         check(self.ctx.lib.ct_batch_get_tuning(self.h, ctypes.byref(t)))
         return {k: getattr(t, k) for k, _ in t._fields_}
 
-    def set_tuning(self, extend_block=128, connect_block=128, shade_waves=1, use_graph=1, sort_key=0):
-        t = _lib.ct_batch_tuning(extend_block, connect_block, shade_waves, use_graph, sort_key)
+    def set_tuning(self, extend_block=128, connect_block=128, shade_waves=1, use_graph=1, sort_key=0, refill=24):
+        t = _lib.ct_batch_tuning(extend_block, connect_block, shade_waves, use_graph, sort_key, refill)
         check(self.ctx.lib.ct_batch_set_tuning(self.ctx.h, self.h, ctypes.byref(t)), self.ctx.h)
 
     def autotune(self, stream=None) -> tuple[dict, float]:

@@ -1193,10 +1193,10 @@ struct ct_batch {
   Allocs allocs;
   std::vector<BatchJob> jobs0;  // job table at the first sample
   std::vector<int32_t> bases;
-  ct_batch_tuning tune{128, 128, 1, 1, CT_SORT_NONE};
+  ct_batch_tuning tune{128, 128, 1, 1, CT_SORT_NONE, 24};
   cudaStream_t cap = nullptr;  // capture stream
   cudaGraphExec_t exec = nullptr;
-  ct_batch_tuning exec_tune{0, 0, 0, 0, 0};
+  ct_batch_tuning exec_tune{0, 0, 0, 0, 0, 0};
   ~ct_batch() {
     if (exec) cudaGraphExecDestroy(exec);
     if (cap) cudaStreamDestroy(cap);
@@ -1255,7 +1255,7 @@ cudaError_t batch_iteration(ct_batch* b, const ct_batch_tuning& t, cudaStream_t 
     }
     if (e == cudaSuccess)
       e = b->dev.wide ? launch_batch_extend_wide(b->dev, qx, cur, st)
-                      : launch_batch_extend(b->dev, qx, cur, !b->exact, t.extend_block, st);
+                      : launch_batch_extend(b->dev, qx, cur, !b->exact, t.extend_block, t.refill, st);
     if (e == cudaSuccess) e = launch_batch_shade(b->dev, b->q, cur, path_length, pass, b->exact, t.shade_waves, st);
     if (e == cudaSuccess)
       e = b->dev.wide ? launch_batch_connect_wide(b->dev, b->q, st)
@@ -1311,7 +1311,8 @@ cudaError_t batch_iterations(ct_batch* b, uint32_t iters, cudaStream_t st) {
 bool tuning_ok(const ct_batch_tuning& t) {
   auto blk = [](int32_t v) { return v == 64 || v == 128 || v == 256; };
   return blk(t.extend_block) && blk(t.connect_block) && t.shade_waves >= 1 && t.shade_waves <= 8 &&
-         (t.use_graph == 0 || t.use_graph == 1) && t.sort_key >= CT_SORT_NONE && t.sort_key <= CT_SORT_FACE_CELLS;
+         (t.use_graph == 0 || t.use_graph == 1) && t.sort_key >= CT_SORT_NONE && t.sort_key <= CT_SORT_FACE_CELLS &&
+         (t.refill == 8 || t.refill == 16 || t.refill == 24);
 }
 
 }  // namespace
@@ -1475,14 +1476,15 @@ ct_status ct_batch_autotune(ct_ctx* ctx, ct_batch* b, void* stream, ct_batch_tun
     err = measure(t, ms);
     if (err == cudaSuccess && ms < best_ms) best_ms = ms, best = t;
   };
-  // coordinate search: traversal block sizes, then the ray-sort key, shade
-  // waves and graph replay
+  // coordinate search: traversal block sizes, then the refill (lane
+  // compaction) threshold, the ray-sort key, shade waves and graph replay
   for (int eb : {64, 128, 256})
-    for (int cb : {128, 256}) trial(ct_batch_tuning{eb, cb, 1, 1, CT_SORT_NONE});
+    for (int cb : {128, 256}) trial(ct_batch_tuning{eb, cb, 1, 1, CT_SORT_NONE, 24});
+  for (int rf : {8, 16}) trial(ct_batch_tuning{best.extend_block, best.connect_block, 1, 1, CT_SORT_NONE, rf});
   for (int key : {CT_SORT_OCTANT, CT_SORT_FACE_CELLS})
-    trial(ct_batch_tuning{best.extend_block, best.connect_block, 1, 1, key});
-  trial(ct_batch_tuning{best.extend_block, best.connect_block, 2, 1, best.sort_key});
-  trial(ct_batch_tuning{best.extend_block, best.connect_block, best.shade_waves, 0, best.sort_key});
+    trial(ct_batch_tuning{best.extend_block, best.connect_block, 1, 1, key, best.refill});
+  trial(ct_batch_tuning{best.extend_block, best.connect_block, 2, 1, best.sort_key, best.refill});
+  trial(ct_batch_tuning{best.extend_block, best.connect_block, best.shade_waves, 0, best.sort_key, best.refill});
   cudaEventDestroy(e0);
   cudaEventDestroy(e1);
   if (err != cudaSuccess) return cuda_fail(ctx, err, "batch autotune");

@@ -234,7 +234,9 @@ cudaError_t launch_trace_wide_any(const DevWBVH& b, const float4* org, const flo
 // capacity is the batch's total pixel count; counts[0] must be zero before
 // raygen (launch_batch_advance leaves it so).
 cudaError_t launch_batch_raygen(const DevBatch& b, const DevQueues& q, int exact, cudaStream_t s);
-cudaError_t launch_batch_extend(const DevBatch& b, const DevQueues& q, int queue, bool fast, int block, cudaStream_t s);
+// refill: idle lanes (8, 16 or 24 of 32) at which a traversal warp takes new rays
+cudaError_t launch_batch_extend(const DevBatch& b, const DevQueues& q, int queue, bool fast, int block, int refill,
+                                cudaStream_t s);
 cudaError_t launch_batch_shade(const DevBatch& b, const DevQueues& q, int queue, uint32_t path_length, int pass,
                                int exact, int grid_mult, cudaStream_t s);
 cudaError_t launch_batch_connect(const DevBatch& b, const DevQueues& q, bool fast, int block, cudaStream_t s);

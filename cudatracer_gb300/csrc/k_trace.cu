@@ -328,7 +328,7 @@ struct BatchExtendIO {
   }
 };
 
-template <bool FASTMM, int BLOCK>
+template <bool FASTMM, int BLOCK, int REFILL>
 __global__ void __launch_bounds__(BLOCK) k_batch_extend(DevBatch bt, DevQueues q, int qi) {
   extern __shared__ int s_stack[];
   const int n = q.counts[qi];
@@ -338,7 +338,7 @@ __global__ void __launch_bounds__(BLOCK) k_batch_extend(DevBatch bt, DevQueues q
     atomicAdd(&q.stats[0], (unsigned long long)n);
   }
   BatchExtendIO io{q.org_q(qi), q.dir_q(qi), q.hit, q.error, bt.jobs, bt.bases, bt.n_jobs, q.perm};
-  trace_persistent_batch<false, FASTMM, kExtendRefill>(n, q.counts + 4, io, s_stack + threadIdx.x, BLOCK);
+  trace_persistent_batch<false, FASTMM, REFILL>(n, q.counts + 4, io, s_stack + threadIdx.x, BLOCK);
 }
 
 template <bool FASTMM, int BLOCK>
@@ -371,10 +371,10 @@ __global__ void __launch_bounds__(BLOCK) k_batch_connect(DevBatch bt, DevQueues 
   }
 }
 
-template <bool FASTMM, int BLOCK>
+template <bool FASTMM, int BLOCK, int REFILL>
 cudaError_t batch_extend(const DevBatch& b, const DevQueues& q, int queue, cudaStream_t s) {
   const size_t smem = (size_t)b.max_stack * BLOCK * sizeof(int);
-  auto kernel = k_batch_extend<FASTMM, BLOCK>;
+  auto kernel = k_batch_extend<FASTMM, BLOCK, REFILL>;
   if (smem > 48 * 1024) {
     cudaError_t e = cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     if (e != cudaSuccess) return e;
@@ -405,10 +405,25 @@ cudaError_t batch_connect(const DevBatch& b, const DevQueues& q, cudaStream_t s)
 
 }  // namespace
 
-cudaError_t launch_batch_extend(const DevBatch& b, const DevQueues& q, int queue, bool fast, int block, cudaStream_t s) {
-  if (block == 64) return fast ? batch_extend<true, 64>(b, q, queue, s) : batch_extend<false, 64>(b, q, queue, s);
-  if (block == 256) return fast ? batch_extend<true, 256>(b, q, queue, s) : batch_extend<false, 256>(b, q, queue, s);
-  return fast ? batch_extend<true, 128>(b, q, queue, s) : batch_extend<false, 128>(b, q, queue, s);
+namespace {
+template <int BLOCK, int REFILL>
+cudaError_t batch_extend_math(const DevBatch& b, const DevQueues& q, int queue, bool fast, cudaStream_t s) {
+  return fast ? batch_extend<true, BLOCK, REFILL>(b, q, queue, s) : batch_extend<false, BLOCK, REFILL>(b, q, queue, s);
+}
+template <int BLOCK>
+cudaError_t batch_extend_refill(const DevBatch& b, const DevQueues& q, int queue, bool fast, int refill,
+                                cudaStream_t s) {
+  if (refill == 8) return batch_extend_math<BLOCK, 8>(b, q, queue, fast, s);
+  if (refill == 16) return batch_extend_math<BLOCK, 16>(b, q, queue, fast, s);
+  return batch_extend_math<BLOCK, 24>(b, q, queue, fast, s);
+}
+}  // namespace
+
+cudaError_t launch_batch_extend(const DevBatch& b, const DevQueues& q, int queue, bool fast, int block, int refill,
+                                cudaStream_t s) {
+  if (block == 64) return batch_extend_refill<64>(b, q, queue, fast, refill, s);
+  if (block == 256) return batch_extend_refill<256>(b, q, queue, fast, refill, s);
+  return batch_extend_refill<128>(b, q, queue, fast, refill, s);
 }
 
 cudaError_t launch_batch_connect(const DevBatch& b, const DevQueues& q, bool fast, int block, cudaStream_t s) {

@@ -257,7 +257,7 @@ cudaError_t ct_server::render_iteration(std::vector<Request*>& finished) {
   for (int pass = 0; pass < depth && e == cudaSuccess; pass++) {
     const int cur = pass & 1;
     const uint32_t path_length = pass == 0 ? 0u : (uint32_t)pass + 1u;  // Kernel.cu:306, 330
-    e = launch_batch_extend(b, q, cur, fast, 128, rs);
+    e = launch_batch_extend(b, q, cur, fast, 128, 24, rs);
     if (e == cudaSuccess) e = launch_batch_shade(b, q, cur, path_length, pass, cfg.exact_math, 1, rs);
     if (e == cudaSuccess) e = launch_batch_connect(b, q, fast, 128, rs);
   }

@@ -312,6 +312,9 @@ typedef struct ct_batch_tuning {
   int32_t shade_waves;
   int32_t use_graph;
   int32_t sort_key;      /* CT_SORT_*: ray-sort key of the bounce queues */
+  int32_t refill;        /* queue-compaction threshold: a closest-hit traversal warp replaces its
+                            finished rays with new ones from the queue once this many of its 32
+                            lanes are idle (8, 16 or 24) */
 } ct_batch_tuning;
 /* Copies the job table; allocates queues for every job's pixels at once and
  * one FP32 RGBA accumulation buffer holding all jobs' images back to back. */

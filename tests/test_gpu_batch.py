@@ -111,8 +111,8 @@ def test_graph_replay_and_tunings_do_not_change_results(gpu_ctx, scenes_):
     ref, _ = _run(gpu_ctx, jobs, tuning=dict(extend_block=128, connect_block=128, shade_waves=1, use_graph=0))
     for t in (dict(extend_block=64, connect_block=256, shade_waves=2, use_graph=1),
               dict(extend_block=256, connect_block=128, shade_waves=1, use_graph=1),
-              dict(extend_block=128, connect_block=128, shade_waves=1, use_graph=1, sort_key=1),
-              dict(extend_block=64, connect_block=128, shade_waves=2, use_graph=0, sort_key=2)):
+              dict(extend_block=128, connect_block=128, shade_waves=1, use_graph=1, sort_key=1, refill=8),
+              dict(extend_block=64, connect_block=128, shade_waves=2, use_graph=0, sort_key=2, refill=16)):
         out, _ = _run(gpu_ctx, jobs, tuning=t)
         for a, b in zip(ref, out):
             assert np.array_equal(a.view(np.int32), b.view(np.int32))
@@ -128,6 +128,7 @@ def test_autotune_picks_a_valid_shape(gpu_ctx, scenes_):
     t, ms = b.autotune()
     assert t["extend_block"] in (64, 128, 256) and t["connect_block"] in (64, 128, 256)
     assert t["shade_waves"] in (1, 2) and t["use_graph"] in (0, 1) and t["sort_key"] in (0, 1, 2) and ms > 0
+    assert t["refill"] in (8, 16, 24)
     assert b.tuning == t
     b.run()
     torch.cuda.synchronize()
