@@ -479,6 +479,26 @@ __global__ void __launch_bounds__(kBlock) k_shade(DevScene sc, DevQueues q, Fram
 
 // generatePrimaryRays + Ray::generate (Kernel.cu:208-234, Ray.cuh:85-95) with
 // start_position = 0: buffer index == pixel.
+// Pixel of primary-queue slot j: 8x4 tiles in row-major tile order over the
+// largest region whose sides are multiples of 8 and 4, then the right strip and
+// the bottom strip row by row. A bijection on [0, w*h): each warp's 32 rays
+// cover one compact tile, so they traverse alike; ray results are per pixel,
+// so the order changes no result.
+__device__ __forceinline__ int tile_pixel(int j, int w, int h) {
+  const int w8 = w & ~7, h4 = h & ~3;
+  const int main = w8 * h4;
+  if (j < main) {
+    const int t = j >> 5, k = j & 31, tiles_x = w8 >> 3;
+    const int x = ((t % tiles_x) << 3) + (k & 7), y = ((t / tiles_x) << 2) + (k >> 3);
+    return y * w + x;
+  }
+  j -= main;
+  const int rw = w - w8, right = rw * h4;
+  if (j < right) return (j / rw) * w + w8 + j % rw;
+  j -= right;
+  return (h4 + j / w) * w + j % w;
+}
+
 __global__ void __launch_bounds__(kBlock) k_raygen(DevQueues q, FrameConst f) {
   const int npix = f.width * f.height;
   if (blockIdx.x == 0 && threadIdx.x == 0) {
@@ -490,7 +510,8 @@ __global__ void __launch_bounds__(kBlock) k_raygen(DevQueues q, FrameConst f) {
   const float invw = 1.0f / (float)f.width, invh = 1.0f / (float)f.height;
   const V3 w = v3(f.cam_w.x, f.cam_w.y, f.cam_w.z), hor = v3(f.hor.x, f.hor.y, f.hor.z),
            ver = v3(f.ver.x, f.ver.y, f.ver.z);
-  for (int i = blockIdx.x * kBlock + threadIdx.x; i < npix; i += gridDim.x * kBlock) {
+  for (int j = blockIdx.x * kBlock + threadIdx.x; j < npix; j += gridDim.x * kBlock) {
+    const int i = tile_pixel(j, f.width, f.height);
     uint32_t seed = ((uint32_t)i + f.frame * 147565741u) * 720898027u;
     const int x = i % f.width, y = (i / f.width) % f.height;
     const float px = ((float)x + rnd_float(seed)) - 0.5f;
@@ -498,9 +519,9 @@ __global__ void __launch_bounds__(kBlock) k_raygen(DevQueues q, FrameConst f) {
     const float sx = 2.0f * (px * invw) - 1.0f;
     const float sy = 1.0f - 2.0f * (py * invh);
     const V3 p = (w + hor * sx) + ver * sy;
-    q.org_q(0)[i] = make_float4(f.cam_pos.x, f.cam_pos.y, f.cam_pos.z, __int_as_float(i));
-    q.dir_q(0)[i] = f4(normalize(p), __int_as_float(0));  // lastBounceType = SPECULAR
-    q.thr_q(0)[i] = make_float4(1.0f, 1.0f, 1.0f, 1.0f);  // throughput 1, lastBsdfPDF 1
+    q.org_q(0)[j] = make_float4(f.cam_pos.x, f.cam_pos.y, f.cam_pos.z, __int_as_float(i));
+    q.dir_q(0)[j] = f4(normalize(p), __int_as_float(0));  // lastBounceType = SPECULAR
+    q.thr_q(0)[j] = make_float4(1.0f, 1.0f, 1.0f, 1.0f);  // throughput 1, lastBsdfPDF 1
   }
 }
 
