@@ -538,7 +538,7 @@ __global__ void __launch_bounds__(kBlock) k_batch_raygen(DevBatch bt, DevQueues 
       const BatchJob& J = bt.jobs[batch_job_of(bt.bases, bt.n_jobs, g)];
       if (J.spp_left > 0) {
         const FrameConst& f = J.f;
-        const int i = g - J.pix_base;
+        const int i = tile_pixel(g - J.pix_base, f.width, f.height);  // the job's pixels in 8x4 tiles
         uint32_t seed = ((uint32_t)i + f.frame * 147565741u) * 720898027u;
         const int x = i % f.width, y = (i / f.width) % f.height;
         const float invw = 1.0f / (float)f.width, invh = 1.0f / (float)f.height;
@@ -549,7 +549,7 @@ __global__ void __launch_bounds__(kBlock) k_batch_raygen(DevBatch bt, DevQueues 
         const V3 w = v3(f.cam_w.x, f.cam_w.y, f.cam_w.z), hor = v3(f.hor.x, f.hor.y, f.hor.z),
                  ver = v3(f.ver.x, f.ver.y, f.ver.z);
         const V3 p = (w + hor * sx) + ver * sy;
-        o = make_float4(f.cam_pos.x, f.cam_pos.y, f.cam_pos.z, __int_as_float(g));
+        o = make_float4(f.cam_pos.x, f.cam_pos.y, f.cam_pos.z, __int_as_float(J.pix_base + i));
         d = f4(normalize(p), __int_as_float(0));
         want = true;
       }
