@@ -104,6 +104,12 @@ ct_status upload(ct_ctx* ctx, Allocs& a, T** dst, const void* src, size_t bytes)
 
 bool finite3(const float* p) { return std::isfinite(p[0]) && std::isfinite(p[1]) && std::isfinite(p[2]); }
 
+float bits_as_float(uint32_t u) {
+  float f;
+  std::memcpy(&f, &u, sizeof(f));
+  return f;
+}
+
 }  // namespace
 
 struct ct_scene {
@@ -403,12 +409,25 @@ ct_status ct_scene_create(ct_ctx* ctx, const ct_scene_desc* d, ct_scene** out) {
                           0.0f);
     }
   }
+  std::vector<float4> rec((size_t)nt * 8);
+  for (uint32_t i = 0; i < nt; i++) {
+    const uint4 t = i4[i];
+    float4* r = rec.data() + 8 * (size_t)i;
+    r[0] = make_float4(v4[t.x].x, v4[t.x].y, v4[t.x].z, bits_as_float(t.w));
+    r[1] = make_float4(v4[t.y].x, v4[t.y].y, v4[t.y].z, 0.0f);
+    r[2] = make_float4(v4[t.z].x, v4[t.z].y, v4[t.z].z, 0.0f);
+    r[3] = make_float4(n4[t.x].x, n4[t.x].y, n4[t.x].z, uv[t.x].x);
+    r[4] = make_float4(n4[t.y].x, n4[t.y].y, n4[t.y].z, uv[t.x].y);
+    r[5] = make_float4(n4[t.z].x, n4[t.z].y, n4[t.z].z, uv[t.y].x);
+    r[6] = make_float4(cn[i].x, cn[i].y, cn[i].z, uv[t.y].y);
+    r[7] = make_float4(uv[t.z].x, uv[t.z].y, 0.0f, 0.0f);
+  }
   std::vector<DevMaterial> dm(d->material_count);
   for (uint32_t i = 0; i < d->material_count; i++) dm[i] = to_dev(d->materials[i]);
   std::vector<uint2> dims(d->texture_count);
   for (uint32_t i = 0; i < d->texture_count; i++) dims[i] = make_uint2(d->texture_dims[2 * i], d->texture_dims[2 * i + 1]);
   DevScene& ds = sc->dev;
-  float4 *dv = nullptr, *dn = nullptr, *dc = nullptr, *dt = nullptr;
+  float4 *dv = nullptr, *dn = nullptr, *dc = nullptr, *dt = nullptr, *drec = nullptr;
   float2* duv = nullptr;
   uint4* di = nullptr;
   uint32_t *dl = nullptr, *doff = nullptr;
@@ -418,6 +437,7 @@ ct_status ct_scene_create(ct_ctx* ctx, const ct_scene_desc* d, ct_scene** out) {
       (s = upload(ctx, sc->allocs, &duv, uv.data(), uv.size() * sizeof(float2))) != CT_OK ||
       (s = upload(ctx, sc->allocs, &di, i4.data(), i4.size() * sizeof(uint4))) != CT_OK ||
       (s = upload(ctx, sc->allocs, &dc, cn.data(), cn.size() * sizeof(float4))) != CT_OK ||
+      (s = upload(ctx, sc->allocs, &drec, rec.data(), rec.size() * sizeof(float4))) != CT_OK ||
       (s = upload(ctx, sc->allocs, &sc->d_mats, dm.data(), dm.size() * sizeof(DevMaterial))) != CT_OK ||
       (s = upload(ctx, sc->allocs, &dl, d->light_indices, (size_t)d->light_count * 4)) != CT_OK ||
       (s = upload(ctx, sc->allocs, &dt, d->texels, (size_t)d->texel_count * sizeof(float4))) != CT_OK ||
@@ -432,6 +452,7 @@ ct_status ct_scene_create(ct_ctx* ctx, const ct_scene_desc* d, ct_scene** out) {
   ds.uvs = duv;
   ds.idx = di;
   ds.cnormals = dc;
+  ds.shade_rec = drec;
   ds.mats = sc->d_mats;
   ds.lights = dl;
   ds.light_count = d->light_count;

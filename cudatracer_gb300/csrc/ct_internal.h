@@ -85,6 +85,11 @@ struct DevScene {
   const float2* uvs;       // per vertex
   const uint4* idx;        // per triangle, w = material index
   const float4* cnormals;  // per triangle centre normal
+  // per triangle shading record, 8 float4 (one 128-byte line): {p0, material},
+  // {p1, 0}, {p2, 0}, {n0, uv0.x}, {n1, uv0.y}, {n2, uv1.x}, {centre normal,
+  // uv1.y}, {uv2, 0, 0}: the same values as the per-vertex arrays above, so a
+  // hit is shaded from one line instead of an index fetch and ten gathers
+  const float4* shade_rec;
   const DevMaterial* mats;
   const uint32_t* lights;
   uint32_t light_count;

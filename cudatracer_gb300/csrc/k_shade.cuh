@@ -138,6 +138,25 @@ struct Emit {
 // pix_base: first pixel of the job in a batch (0 for a single job); seeds use
 // the job's own pixel index so a job renders the same alone and in a batch.
 // acc: where the job's pixels accumulate (q.accum when null); indexed by pix - pix_base.
+// A hit triangle's shading inputs from its 128-byte record (DevScene::shade_rec):
+// eight independent 16-byte loads of one line.
+struct TriRec {
+  V3 p0, p1, p2, n0, n1, n2, cn;
+  float2 uv0, uv1, uv2;
+  uint32_t mat;
+};
+__device__ __forceinline__ TriRec load_tri(const DevScene& sc, int prim) {
+  const float4* r = sc.shade_rec + 8 * (size_t)prim;
+  const float4 a = __ldg(r), b = __ldg(r + 1), c = __ldg(r + 2), d = __ldg(r + 3);
+  const float4 e = __ldg(r + 4), g = __ldg(r + 5), k = __ldg(r + 6), m = __ldg(r + 7);
+  TriRec t;
+  t.p0 = v3(a), t.p1 = v3(b), t.p2 = v3(c);
+  t.n0 = v3(d), t.n1 = v3(e), t.n2 = v3(g), t.cn = v3(k);
+  t.uv0 = make_float2(d.w, e.w), t.uv1 = make_float2(g.w, k.w), t.uv2 = make_float2(m.x, m.y);
+  t.mat = __float_as_uint(a.w);
+  return t;
+}
+
 __device__ __forceinline__ void shade_compat(const DevScene& sc, const DevQueues& q, const FrameConst& f, int cur,
                                              int i, uint32_t path_length, Emit& e, int pix_base = 0,
                                              float4* acc = nullptr) {
@@ -158,19 +177,19 @@ __device__ __forceinline__ void shade_compat(const DevScene& sc, const DevQueues
     return;
   }
   const int prim = h.x;
-  const uint4 ti = __ldg(sc.idx + prim);
-  V3 N = v3(__ldg(sc.cnormals + prim));
-  const V3 p0 = v3(__ldg(sc.verts + ti.x)), p1 = v3(__ldg(sc.verts + ti.y)), p2 = v3(__ldg(sc.verts + ti.z));
+  const TriRec tri = load_tri(sc, prim);
+  V3 N = tri.cn;
+  const V3 p0 = tri.p0, p1 = tri.p1, p2 = tri.p2;
   // triangle::getBaryCoords at the ray ORIGIN, before it moves (Kernel.cu:107)
   const float aABC = dot(N, cross(p1 - p0, p2 - p0));
   const float aPBC = dot(N, cross(p1 - org, p2 - org));
   const float aPCA = dot(N, cross(p2 - org, p0 - org));
   const float ba = aPBC / aABC, bb = aPCA / aABC, bc = (1.f - ba) - bb;
-  V3 iN = (v3(__ldg(sc.normals + ti.x)) * ba + v3(__ldg(sc.normals + ti.y)) * bb) + v3(__ldg(sc.normals + ti.z)) * bc;
-  const float2 uv0 = __ldg(sc.uvs + ti.x), uv1 = __ldg(sc.uvs + ti.y), uv2 = __ldg(sc.uvs + ti.z);
+  V3 iN = (tri.n0 * ba + tri.n1 * bb) + tri.n2 * bc;
+  const float2 uv0 = tri.uv0, uv1 = tri.uv1, uv2 = tri.uv2;
   const float tu = (uv0.x * ba + uv1.x * bb) + uv2.x * bc;
   const float tv = (uv0.y * ba + uv1.y * bb) + uv2.y * bc;
-  const DevMaterial* mp = sc.mats + ti.w;
+  const DevMaterial* mp = sc.mats + tri.mat;
   const float4 alb = __ldg(&mp->albedo_ior);
   const int4 mtex = __ldg(&mp->tex);
   const float4 tr = __ldg(&mp->type_rough);
@@ -334,8 +353,8 @@ __device__ __forceinline__ void shade_full(const DevScene& sc, const DevQueues& 
     return;
   }
   const int prim = h.x;
-  const uint4 ti = __ldg(sc.idx + prim);
-  const V3 p0 = v3(__ldg(sc.verts + ti.x)), p1 = v3(__ldg(sc.verts + ti.y)), p2 = v3(__ldg(sc.verts + ti.z));
+  const TriRec tri = load_tri(sc, prim);
+  const V3 p0 = tri.p0, p1 = tri.p1, p2 = tri.p2;
   const V3 p = v3(o4) + dir * t;
   V3 Ngf = cross(p1 - p0, p2 - p0);
   const float area2 = sqrtf(dot(Ngf, Ngf));
@@ -343,12 +362,12 @@ __device__ __forceinline__ void shade_full(const DevScene& sc, const DevQueues& 
   // barycentrics of the hit point
   const float b1 = dot(Ngf, cross(p2 - p, p0 - p)) / area2, b2 = dot(Ngf, cross(p0 - p, p1 - p)) / area2;
   const float b0 = 1.0f - b1 - b2;
-  V3 Ns = v3(__ldg(sc.normals + ti.x)) * b0 + v3(__ldg(sc.normals + ti.y)) * b1 + v3(__ldg(sc.normals + ti.z)) * b2;
+  V3 Ns = tri.n0 * b0 + tri.n1 * b1 + tri.n2 * b2;
   const float nl = dot(Ns, Ns);
   Ns = nl > 0.0f ? Ns * (1.0f / sqrtf(nl)) : Ngf;
-  const float2 uv0 = __ldg(sc.uvs + ti.x), uv1 = __ldg(sc.uvs + ti.y), uv2 = __ldg(sc.uvs + ti.z);
+  const float2 uv0 = tri.uv0, uv1 = tri.uv1, uv2 = tri.uv2;
   const float tu = uv0.x * b0 + uv1.x * b1 + uv2.x * b2, tv = uv0.y * b0 + uv1.y * b1 + uv2.y * b2;
-  const DevMaterial* mp = sc.mats + ti.w;
+  const DevMaterial* mp = sc.mats + tri.mat;
   const float4 alb = __ldg(&mp->albedo_ior);
   const int4 mtex = __ldg(&mp->tex);
   const float4 tr = __ldg(&mp->type_rough);
@@ -357,7 +376,7 @@ __device__ __forceinline__ void shade_full(const DevScene& sc, const DevQueues& 
   if (mtype == full::kLight) {
     if (!f.indirect) return;
     // emitters radiate on the side their centre normal faces (as the reference's NEE assumes)
-    const V3 cn = normalize(v3(__ldg(sc.cnormals + prim)));
+    const V3 cn = normalize(tri.cn);
     const float cos_l = -dot(cn, dir);
     if (cos_l <= 0.0f) return;
     float w = 1.0f;
