@@ -5,19 +5,23 @@
 //      shared queue capacity allow (render: its accumulation buffer and its
 //      pixels of the queues; query: its ray and result buffers);
 //   2. starts admitted queries on the query stream (copy in, trace, copy out);
-//   3. runs one batched iteration of all admitted render jobs on the render
-//      stream (up to k samples each, the ct_batch kernels with a job table built
-//      for this iteration), at most two iterations ahead of the device;
+//   3. runs one batched iteration of all admitted render jobs (up to k samples
+//      each, the ct_batch kernels with a job table built for this iteration),
+//      alternating between two render streams with a queue set each, so one
+//      iteration's last, nearly empty bounces overlap the next iteration's
+//      first passes; at most two iterations ahead of the device;
 //   4. retires requests whose completion events have fired, freeing their
 //      device state and waking waiters.
 // Jobs arriving while others are on the GPU join at the next iteration; a
 // job's samples, seeds and per-pixel accumulation order do not depend on the
-// other jobs, so its result equals the job rendered alone. A job has
-// k = min(spp, I / pixels) slot buffers, I = min(iter_pixels,
-// max_inflight_pixels), at least one; it takes up to k samples per iteration,
-// sample i into slot i mod k, and its slots are added in slot order when it
-// finishes. Each slot sums its samples in sample order however many samples an
-// iteration takes, and k depends only on the job and the configuration.
+// other jobs, so its result equals the job rendered alone. A job takes up to
+// k = min(spp, I / pixels) samples per iteration, I = min(iter_pixels,
+// max_inflight_pixels), at least one, and has min(spp, 2k) slot buffers:
+// sample i goes to slot i mod 2k, so two consecutive iterations (on the two
+// streams) write disjoint slots and the iteration after next, on the same
+// stream, is ordered after. The slots are added in slot order when the job
+// finishes. Each slot sums its samples in sample order however the
+// iterations fall, and k depends only on the job and the configuration.
 #include <cuda_runtime.h>
 
 #include <algorithm>
@@ -51,7 +55,11 @@ struct Request {
   ct_batch_job job{};
   float* host_out = nullptr;
   uint32_t done_spp = 0;
-  uint32_t k = 1;  // samples per iteration (slot buffers)
+  uint32_t k = 1;      // samples per iteration
+  uint32_t slots = 1;  // slot buffers: min(spp, 2k)
+  int64_t last_iter = -2;  // the last iteration that took samples of this job
+  cudaEvent_t ready = nullptr;  // its slot buffers are zeroed
+  uint32_t waited = 0;          // render streams already ordered after `ready` (bit per stream)
   // query
   const ct_bvh* bvh = nullptr;
   const float* horg = nullptr;
@@ -70,7 +78,7 @@ struct Request {
 };
 
 size_t request_bytes(const Request& r) {
-  if (r.kind == kRender) return (size_t)r.k * r.pixels * sizeof(float4);
+  if (r.kind == kRender) return (size_t)r.slots * r.pixels * sizeof(float4);
   // org + dir + hit/occluded + t + cursor, each 256-byte aligned
   auto al = [](size_t b) { return (b + 255) & ~(size_t)255; };
   return al((size_t)r.n * 16) * 2 + al((size_t)r.n * 4) * 2 + 256;
@@ -97,8 +105,8 @@ struct ct_server {
   size_t used_bytes = 0;
   uint32_t inflight_pixels = 0;
   std::chrono::steady_clock::time_point t0;
-  DevQueues q{};
-  std::vector<std::pair<void*, size_t>> q_owned;
+  DevQueues q[2] = {};  // one queue set per render stream
+  std::vector<std::pair<void*, size_t>> q_owned[2];
   int32_t max_stack = 1;
   BatchJob* d_table[2] = {nullptr, nullptr};
   int32_t* d_bases[2] = {nullptr, nullptr};
@@ -106,8 +114,9 @@ struct ct_server {
   int32_t* h_bases[2] = {nullptr, nullptr};
   uint32_t table_cap = 0;
   cudaEvent_t table_ev[2] = {nullptr, nullptr};
-  int slot = 0;
-  cudaStream_t rs = nullptr, qs = nullptr;
+  int slot = 0;          // render stream, queue set and job table of the next iteration
+  int64_t iter = 0;      // iterations issued
+  cudaStream_t rs[2] = {nullptr, nullptr}, qs = nullptr, ms = nullptr;  // render, query, setup
 
   double now() const { return std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count(); }
   void loop();
@@ -121,7 +130,7 @@ struct ct_server {
 // Device state of an admitted request: stream-ordered allocation on the stream
 // that uses it, so freeing never waits for the whole device.
 void ct_server::start(Request* r) {
-  cudaStream_t st = r->kind == kRender ? rs : qs;
+  cudaStream_t st = r->kind == kRender ? ms : qs;
   cudaError_t e = cudaMallocAsync(&r->dmem, r->bytes, st);
   if (e != cudaSuccess) {
     cudaGetLastError();
@@ -136,9 +145,13 @@ void ct_server::start(Request* r) {
     return;
   }
   if (r->kind == kRender) {
-    if (cudaMemsetAsync(r->dmem, 0, r->bytes, rs) != cudaSuccess) {
+    // zeroed on the setup stream; each render stream waits for `ready` before its first use
+    if (cudaMemsetAsync(r->dmem, 0, r->bytes, ms) != cudaSuccess ||
+        cudaEventCreateWithFlags(&r->ready, cudaEventDisableTiming) != cudaSuccess ||
+        cudaEventRecord(r->ready, ms) != cudaSuccess) {
+      cudaGetLastError();
       r->status = CT_ERR_CUDA;
-      cudaFreeAsync(r->dmem, rs);
+      cudaFreeAsync(r->dmem, ms);
       r->dmem = nullptr;
     }
   } else {
@@ -207,7 +220,8 @@ cudaError_t ct_server::render_iteration(std::vector<Request*>& finished) {
   cudaError_t e = cudaEventSynchronize(table_ev[slot]);
   if (e != cudaSuccess) return e;
   if (n > table_cap) {
-    if ((e = cudaStreamSynchronize(rs)) != cudaSuccess) return e;  // the other slot may be in use
+    for (int k = 0; k < 2; k++)  // the other table may be in use
+      if ((e = cudaStreamSynchronize(rs[k])) != cudaSuccess) return e;
     free_tables();
     const uint32_t cap = std::max<uint32_t>(64, n * 2);
     for (int k = 0; k < 2; k++) {
@@ -219,12 +233,18 @@ cudaError_t ct_server::render_iteration(std::vector<Request*>& finished) {
     }
     table_cap = cap;
   }
+  cudaStream_t st = rs[slot];
+  const DevQueues& q = this->q[slot];
   BatchJob* ht = h_table[slot];
   int32_t* hb = h_bases[slot];
   int32_t base = 0, depth = 1;
   uint32_t j = 0;
   for (Request* r : render) {
     const uint32_t m = std::min(r->k, r->job.spp - r->done_spp);
+    if (!(r->waited & (1u << slot))) {  // each stream's first use waits for the zero fill
+      if ((e = cudaStreamWaitEvent(st, r->ready, 0)) != cudaSuccess) return e;
+      r->waited |= 1u << slot;
+    }
     BatchJob J;
     std::memset(&J, 0, sizeof(J));
     J.sc = rt_scene_dev(r->job.scene);
@@ -237,7 +257,7 @@ cudaError_t ct_server::render_iteration(std::vector<Request*>& finished) {
       const uint32_t i = r->done_spp + s;  // sample index
       ht[j] = J;
       ht[j].f.frame = r->job.params.frame_index + 2u * i;
-      ht[j].accum = (float4*)r->dmem + (size_t)(i % r->k) * r->pixels;
+      ht[j].accum = (float4*)r->dmem + (size_t)(i % r->slots) * r->pixels;
       ht[j].pix_base = base;
       hb[j] = base;
       base += (int32_t)r->pixels;
@@ -246,38 +266,44 @@ cudaError_t ct_server::render_iteration(std::vector<Request*>& finished) {
     max_stack = std::max(max_stack, J.bvh.stack_entries);
     r->done_spp += m;
   }
+  const int64_t this_iter = iter++;
   hb[n] = base;
-  if ((e = cudaMemcpyAsync(d_table[slot], ht, (size_t)n * sizeof(BatchJob), cudaMemcpyHostToDevice, rs)) != cudaSuccess)
+  if ((e = cudaMemcpyAsync(d_table[slot], ht, (size_t)n * sizeof(BatchJob), cudaMemcpyHostToDevice, st)) != cudaSuccess)
     return e;
-  if ((e = cudaMemcpyAsync(d_bases[slot], hb, (size_t)(n + 1) * 4, cudaMemcpyHostToDevice, rs)) != cudaSuccess) return e;
-  if ((e = cudaMemsetAsync(q.counts, 0, 16 * sizeof(int32_t), rs)) != cudaSuccess) return e;
+  if ((e = cudaMemcpyAsync(d_bases[slot], hb, (size_t)(n + 1) * 4, cudaMemcpyHostToDevice, st)) != cudaSuccess) return e;
+  if ((e = cudaMemsetAsync(q.counts, 0, 16 * sizeof(int32_t), st)) != cudaSuccess) return e;
   DevBatch b{d_table[slot], d_bases[slot], (int32_t)n, base, max_stack, 0};  // quad BVHs
   const bool fast = !cfg.exact_math;
-  e = launch_batch_raygen(b, q, cfg.exact_math, rs);
+  e = launch_batch_raygen(b, q, cfg.exact_math, st);
   for (int pass = 0; pass < depth && e == cudaSuccess; pass++) {
     const int cur = pass & 1;
     const uint32_t path_length = pass == 0 ? 0u : (uint32_t)pass + 1u;  // Kernel.cu:306, 330
-    e = launch_batch_extend(b, q, cur, fast, 128, 24, rs);
-    if (e == cudaSuccess) e = launch_batch_shade(b, q, cur, path_length, pass, cfg.exact_math, 1, rs);
-    if (e == cudaSuccess) e = launch_batch_connect(b, q, fast, 128, rs);
+    e = launch_batch_extend(b, q, cur, fast, 128, 24, st);
+    if (e == cudaSuccess) e = launch_batch_shade(b, q, cur, path_length, pass, cfg.exact_math, 1, st);
+    if (e == cudaSuccess) e = launch_batch_connect(b, q, fast, 128, st);
   }
-  if (e == cudaSuccess) e = cudaEventRecord(table_ev[slot], rs);
-  slot ^= 1;
+  if (e == cudaSuccess) e = cudaEventRecord(table_ev[slot], st);
+  const int other = slot ^ 1;
+  slot = other;
   std::vector<Request*> keep;
   for (Request* r : render) {
+    const int64_t prev = r->last_iter;
+    r->last_iter = this_iter;
     if (r->done_spp < r->job.spp) {
       keep.push_back(r);
       continue;
     }
+    // samples of the previous iteration ran on the other stream: wait for them
+    if (prev == this_iter - 1 && e == cudaSuccess) e = cudaStreamWaitEvent(st, table_ev[other], 0);
     // add the slot buffers in slot order, copy the image out, free in stream order
     float4* acc = (float4*)r->dmem;
-    for (uint32_t s = 1; s < r->k && e == cudaSuccess; s++)
-      e = launch_fold(acc, acc + (size_t)s * r->pixels, (int)r->pixels, rs);
+    for (uint32_t s = 1; s < r->slots && e == cudaSuccess; s++)
+      e = launch_fold(acc, acc + (size_t)s * r->pixels, (int)r->pixels, st);
     if (e == cudaSuccess)
-      e = cudaMemcpyAsync(r->host_out, r->dmem, (size_t)r->pixels * sizeof(float4), cudaMemcpyDeviceToHost, rs);
-    if (e == cudaSuccess) e = cudaFreeAsync(r->dmem, rs);
-    if (e == cudaSuccess) e = cudaEventRecord(r->ev, rs);
-    inflight_pixels -= r->k * r->pixels;  // later iterations are ordered after this one on the stream
+      e = cudaMemcpyAsync(r->host_out, r->dmem, (size_t)r->pixels * sizeof(float4), cudaMemcpyDeviceToHost, st);
+    if (e == cudaSuccess) e = cudaFreeAsync(r->dmem, st);
+    if (e == cudaSuccess) e = cudaEventRecord(r->ev, st);
+    inflight_pixels -= r->k * r->pixels;  // its queue space frees with this iteration's set
     finished.push_back(r);
   }
   render.swap(keep);
@@ -300,6 +326,7 @@ void ct_server::retire_locked() {
     }
     r->dmem = nullptr;
     if (r->ev) cudaEventDestroy(r->ev), r->ev = nullptr;
+    if (r->ready) cudaEventDestroy(r->ready), r->ready = nullptr;
     r->t_done = now();
     r->state = kDone;
     if (r->status == CT_OK) stats.completed++;
@@ -401,7 +428,8 @@ ct_status ct_server_create(ct_ctx* ctx, const ct_server_config* cfg, ct_server**
   s->cfg = *cfg;
   s->device = rt_ctx_device(ctx);
   s->t0 = std::chrono::steady_clock::now();
-  ct_status st = rt_alloc_queues(ctx, cfg->max_inflight_pixels, s->q, s->q_owned);
+  ct_status st = rt_alloc_queues(ctx, cfg->max_inflight_pixels, s->q[0], s->q_owned[0]);
+  if (st == CT_OK) st = rt_alloc_queues(ctx, cfg->max_inflight_pixels, s->q[1], s->q_owned[1]);
   cudaError_t e = cudaSuccess;
   // keep freed request memory in the device's pool between requests
   cudaMemPool_t pool = nullptr;
@@ -409,14 +437,18 @@ ct_status ct_server_create(ct_ctx* ctx, const ct_server_config* cfg, ct_server**
     uint64_t keep = ~0ull;
     cudaMemPoolSetAttribute(pool, cudaMemPoolAttrReleaseThreshold, &keep);
   }
-  if (st == CT_OK) e = cudaStreamCreateWithFlags(&s->rs, cudaStreamNonBlocking);
+  for (int k = 0; k < 2 && st == CT_OK && e == cudaSuccess; k++)
+    e = cudaStreamCreateWithFlags(&s->rs[k], cudaStreamNonBlocking);
   if (st == CT_OK && e == cudaSuccess) e = cudaStreamCreateWithFlags(&s->qs, cudaStreamNonBlocking);
+  if (st == CT_OK && e == cudaSuccess) e = cudaStreamCreateWithFlags(&s->ms, cudaStreamNonBlocking);
   for (int k = 0; k < 2 && st == CT_OK && e == cudaSuccess; k++) {
     e = cudaEventCreateWithFlags(&s->table_ev[k], cudaEventDisableTiming);
-    if (e == cudaSuccess) e = cudaEventRecord(s->table_ev[k], s->rs);
+    if (e == cudaSuccess) e = cudaEventRecord(s->table_ev[k], s->rs[k]);
   }
   if (st != CT_OK || e != cudaSuccess) {
-    rt_free_list(ctx, s->q_owned);
+    for (int k = 0; k < 2; k++) rt_free_list(ctx, s->q_owned[k]);
+    for (cudaStream_t x : {s->rs[0], s->rs[1], s->qs, s->ms})
+      if (x) cudaStreamDestroy(x);
     delete s;
     return st != CT_OK ? st : rt_fail(ctx, CT_ERR_CUDA, cudaGetErrorString(e));
   }
@@ -435,13 +467,18 @@ ct_status ct_server_destroy(ct_server* s) {
   s->th.join();
   cudaSetDevice(s->device);
   cudaDeviceSynchronize();
-  for (auto& kv : s->all) delete kv.second;
+  for (auto& kv : s->all) {
+    if (kv.second->ev) cudaEventDestroy(kv.second->ev);
+    if (kv.second->ready) cudaEventDestroy(kv.second->ready);
+    delete kv.second;
+  }
   s->free_tables();
-  for (int k = 0; k < 2; k++)
+  for (int k = 0; k < 2; k++) {
     if (s->table_ev[k]) cudaEventDestroy(s->table_ev[k]);
-  rt_free_list(s->ctx, s->q_owned);
-  if (s->rs) cudaStreamDestroy(s->rs);
-  if (s->qs) cudaStreamDestroy(s->qs);
+    rt_free_list(s->ctx, s->q_owned[k]);
+  }
+  for (cudaStream_t x : {s->rs[0], s->rs[1], s->qs, s->ms})
+    if (x) cudaStreamDestroy(x);
   delete s;
   return CT_OK;
 }
@@ -457,6 +494,7 @@ ct_status ct_server_submit_render(ct_server* s, const ct_batch_job* job, float* 
   r->pixels = (uint32_t)(job->params.width * job->params.height);
   const uint32_t per_iter = std::min(s->cfg.iter_pixels ? s->cfg.iter_pixels : kIterPixels, s->cfg.max_inflight_pixels);
   r->k = std::max<uint32_t>(1, std::min<uint32_t>(job->spp, per_iter / r->pixels));
+  r->slots = std::min<uint32_t>(job->spp, 2 * r->k);
   {
     std::lock_guard<std::mutex> g(s->mu);
     r->id = s->next_id++;
@@ -528,8 +566,12 @@ ct_status ct_server_get_stats(ct_server* s, ct_server_stats* out) {
   if (!s || !out) return CT_ERR_INVALID_ARGUMENT;
   unsigned long long h[8] = {0};
   cudaSetDevice(s->device);
-  // ray counters of the render iterations (current when no iteration is running)
-  if (cudaMemcpy(h, s->q.stats, sizeof(h), cudaMemcpyDeviceToHost) != cudaSuccess) return CT_ERR_CUDA;
+  // ray counters of the render iterations, both queue sets (current when no iteration is running)
+  for (int k = 0; k < 2; k++) {
+    unsigned long long hk[8] = {0};
+    if (cudaMemcpy(hk, s->q[k].stats, sizeof(hk), cudaMemcpyDeviceToHost) != cudaSuccess) return CT_ERR_CUDA;
+    for (int i = 0; i < 8; i++) h[i] += hk[i];
+  }
   std::lock_guard<std::mutex> g(s->mu);
   *out = s->stats;
   out->extension_rays = h[0];

@@ -340,15 +340,16 @@ ct_status ct_batch_stats(ct_ctx* ctx, ct_batch* b, ct_frame_stats* out, int32_t 
  * batched iterations at the next iteration boundary (a job of p pixels takes
  * up to k = min(spp, I / p) samples per iteration, at least one, where
  * I = min(iter_pixels, max_inflight_pixels); sample i goes to private slot
- * buffer i mod k and the k slots are added in order at the end) and leave
- * when their samples are done; ray queries
+ * buffer i mod 2k, min(spp, 2k) slots, added in order at the end, so that
+ * consecutive iterations, which overlap on two streams, never share a slot)
+ * and leave when their samples are done; ray queries
  * run on a second stream, overlapping the iterations. Requests are admitted
  * in arrival order; one that can never fit fails with CT_ERR_OUT_OF_MEMORY.
  * Results are the same as the request alone (a render job's pixels use their
  * own seeds and its samples' summation order depends on the job only;
  * queries are per ray; k depends on the job and the server's configuration
  * only). A render result equals ct_batch's for the same job up to that
- * summation order (the same bits when k = 1). Host buffers given to the server must stay
+ * summation order (the same bits when the job has one slot, spp = 1). Host buffers given to the server must stay
  * valid until the request is waited for; pinned buffers let copies overlap. */
 typedef struct ct_server ct_server;
 typedef struct ct_server_config {
@@ -357,7 +358,7 @@ typedef struct ct_server_config {
   int32_t exact_math;           /* math mode of every render job */
   uint32_t iter_pixels;         /* pixel-samples a render job may take per iteration (0 = 4,194,304):
                                    larger values finish big jobs in fewer, larger iterations and
-                                   cost k * p * 16 bytes of slot buffers per job */
+                                   cost min(spp, 2k) * p * 16 bytes of slot buffers per job */
 } ct_server_config;
 typedef struct ct_request_info {
   ct_status status;

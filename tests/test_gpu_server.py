@@ -142,7 +142,8 @@ def test_admission_respects_the_budget(gpu_ctx, world):
     reqs = _requests(world)
     def render_bytes(r):
         px = r["params"].width * r["params"].height
-        return max(1, min(r["spp"], 65536 // px)) * px * 16
+        k = max(1, min(r["spp"], 65536 // px))
+        return min(r["spp"], 2 * k) * px * 16  # slot buffers
 
     sizes = [render_bytes(r) if k == "render" else r["org"].shape[0] * 40 + 2048 for k, r in reqs]
     budget = max(sizes) + 4096
