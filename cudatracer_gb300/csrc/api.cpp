@@ -1209,18 +1209,32 @@ struct ct_batch {
   int32_t exact = 0;
   int32_t max_depth = 1;
   uint32_t max_spp = 0;
-  DevQueues q{};
-  DevBatch dev{};
+  // Fast-math batches run two lanes: lane 0 takes every job's even samples and
+  // lane 1 its odd ones, each with its own job table, queue set, accumulation
+  // and stream, so one lane's last bounces overlap the other lane's first
+  // passes; lane 1's accumulation is added to lane 0's when the run ends.
+  // Exact-math batches run one lane (bit-identical to ct_render_accumulate).
+  int lanes = 1;
+  DevQueues q{}, q2{};
+  DevBatch dev{}, dev2{};
   Allocs allocs;
-  std::vector<BatchJob> jobs0;  // job table at the first sample
+  std::vector<BatchJob> jobs0, jobs0b;  // job tables at the first sample (lane 0, lane 1)
   std::vector<int32_t> bases;
   ct_batch_tuning tune{128, 128, 1, 1, CT_SORT_NONE, 24};
   cudaStream_t cap = nullptr;  // capture stream
-  cudaGraphExec_t exec = nullptr;
+  cudaGraphExec_t exec[2] = {nullptr, nullptr};
   ct_batch_tuning exec_tune{0, 0, 0, 0, 0, 0};
+  cudaStream_t side[2] = {nullptr, nullptr};  // lane streams (two lanes)
+  cudaEvent_t fork_ev = nullptr, join_ev[2] = {nullptr, nullptr};
   ~ct_batch() {
-    if (exec) cudaGraphExecDestroy(exec);
+    for (auto& x : exec)
+      if (x) cudaGraphExecDestroy(x);
     if (cap) cudaStreamDestroy(cap);
+    for (auto& x : side)
+      if (x) cudaStreamDestroy(x);
+    if (fork_ev) cudaEventDestroy(fork_ev);
+    for (auto& x : join_ev)
+      if (x) cudaEventDestroy(x);
   }
 };
 
@@ -1264,45 +1278,46 @@ FrameConst batch_frame_const(const ct_camera* cam, const ct_render_params* p) {
 }
 
 // One iteration: every job that still takes samples traces one more.
-cudaError_t batch_iteration(ct_batch* b, const ct_batch_tuning& t, cudaStream_t st) {
-  cudaError_t e = launch_batch_raygen(b->dev, b->q, b->exact, st);
+cudaError_t batch_iteration(ct_batch* b, int lane, const ct_batch_tuning& t, cudaStream_t st) {
+  const DevBatch& dev = lane ? b->dev2 : b->dev;
+  const DevQueues& q = lane ? b->q2 : b->q;
+  cudaError_t e = launch_batch_raygen(dev, q, b->exact, st);
   for (int pass = 0; pass < b->max_depth && e == cudaSuccess; pass++) {
     const int cur = pass & 1;
     const uint32_t path_length = pass == 0 ? 0u : (uint32_t)pass + 1u;  // Kernel.cu:306, 330
-    DevQueues qx = b->q;
+    DevQueues qx = q;
     if (pass > 0 && t.sort_key != CT_SORT_NONE) {
-      e = launch_ray_sort(b->q, cur, t.sort_key, st);
-      qx.perm = b->q.perm_buf;
+      e = launch_ray_sort(q, cur, t.sort_key, st);
+      qx.perm = q.perm_buf;
     }
     if (e == cudaSuccess)
-      e = b->dev.wide ? launch_batch_extend_wide(b->dev, qx, cur, st)
-                      : launch_batch_extend(b->dev, qx, cur, !b->exact, t.extend_block, t.refill, st);
-    if (e == cudaSuccess) e = launch_batch_shade(b->dev, b->q, cur, path_length, pass, b->exact, t.shade_waves, st);
+      e = dev.wide ? launch_batch_extend_wide(dev, qx, cur, st)
+                   : launch_batch_extend(dev, qx, cur, !b->exact, t.extend_block, t.refill, st);
+    if (e == cudaSuccess) e = launch_batch_shade(dev, q, cur, path_length, pass, b->exact, t.shade_waves, st);
     if (e == cudaSuccess)
-      e = b->dev.wide ? launch_batch_connect_wide(b->dev, b->q, st)
-                      : launch_batch_connect(b->dev, b->q, !b->exact, t.connect_block, st);
+      e = dev.wide ? launch_batch_connect_wide(dev, q, st)
+                   : launch_batch_connect(dev, q, !b->exact, t.connect_block, st);
   }
-  if (e == cudaSuccess) e = launch_batch_advance(b->dev, b->q, st);
+  if (e == cudaSuccess) e = launch_batch_advance(dev, q, st);
   return e;
 }
 
 cudaError_t batch_graph(ct_batch* b) {
-  if (b->exec && std::memcmp(&b->exec_tune, &b->tune, sizeof(b->tune)) == 0) return cudaSuccess;
-  if (b->exec) {
-    cudaGraphExecDestroy(b->exec);
-    b->exec = nullptr;
-  }
+  if (b->exec[0] && std::memcmp(&b->exec_tune, &b->tune, sizeof(b->tune)) == 0) return cudaSuccess;
+  for (auto& x : b->exec)
+    if (x) cudaGraphExecDestroy(x), x = nullptr;
   cudaError_t e = cudaSuccess;
   if (!b->cap) e = cudaStreamCreateWithFlags(&b->cap, cudaStreamNonBlocking);
-  if (e != cudaSuccess) return e;
-  e = cudaStreamBeginCapture(b->cap, cudaStreamCaptureModeRelaxed);
-  if (e != cudaSuccess) return e;
-  const cudaError_t le = batch_iteration(b, b->tune, b->cap);
-  cudaGraph_t g = nullptr;
-  e = cudaStreamEndCapture(b->cap, &g);
-  if (le != cudaSuccess) e = le;
-  if (e == cudaSuccess) e = cudaGraphInstantiate(&b->exec, g, 0);
-  if (g) cudaGraphDestroy(g);
+  for (int lane = 0; lane < b->lanes && e == cudaSuccess; lane++) {
+    e = cudaStreamBeginCapture(b->cap, cudaStreamCaptureModeRelaxed);
+    if (e != cudaSuccess) return e;
+    const cudaError_t le = batch_iteration(b, lane, b->tune, b->cap);
+    cudaGraph_t g = nullptr;
+    e = cudaStreamEndCapture(b->cap, &g);
+    if (le != cudaSuccess) e = le;
+    if (e == cudaSuccess) e = cudaGraphInstantiate(&b->exec[lane], g, 0);
+    if (g) cudaGraphDestroy(g);
+  }
   if (e == cudaSuccess) b->exec_tune = b->tune;
   return e;
 }
@@ -1314,17 +1329,38 @@ cudaError_t batch_reset(ct_batch* b, cudaStream_t st, bool zero_accum) {
   if (e == cudaSuccess) e = cudaMemsetAsync(b->q.counts, 0, 16 * sizeof(int32_t), st);
   if (e == cudaSuccess && zero_accum)
     e = cudaMemsetAsync(b->q.accum, 0, (size_t)b->dev.total_pix * sizeof(float4), st);
-  if (e == cudaSuccess) e = cudaStreamSynchronize(st);  // jobs0 is pageable host memory
+  if (b->lanes == 2) {
+    if (e == cudaSuccess)
+      e = cudaMemcpyAsync(b->dev2.jobs, b->jobs0b.data(), b->jobs0b.size() * sizeof(BatchJob),
+                          cudaMemcpyHostToDevice, st);
+    if (e == cudaSuccess) e = cudaMemsetAsync(b->q2.counts, 0, 16 * sizeof(int32_t), st);
+    if (e == cudaSuccess && zero_accum)
+      e = cudaMemsetAsync(b->q2.accum, 0, (size_t)b->dev.total_pix * sizeof(float4), st);
+  }
+  if (e == cudaSuccess) e = cudaStreamSynchronize(st);  // the job tables are pageable host memory
   return e;
 }
 
+// `iters` iterations on `st`: one lane in order, or two lanes alternating on
+// their own streams (forked from and joined back into `st`).
 cudaError_t batch_iterations(ct_batch* b, uint32_t iters, cudaStream_t st) {
   cudaError_t e = cudaSuccess;
-  if (b->tune.use_graph) {
-    e = batch_graph(b);
-    for (uint32_t k = 0; k < iters && e == cudaSuccess; k++) e = cudaGraphLaunch(b->exec, st);
-  } else {
-    for (uint32_t k = 0; k < iters && e == cudaSuccess; k++) e = batch_iteration(b, b->tune, st);
+  if (b->tune.use_graph) e = batch_graph(b);
+  if (e != cudaSuccess) return e;
+  if (b->lanes == 1) {
+    for (uint32_t k = 0; k < iters && e == cudaSuccess; k++)
+      e = b->tune.use_graph ? cudaGraphLaunch(b->exec[0], st) : batch_iteration(b, 0, b->tune, st);
+    return e;
+  }
+  e = cudaEventRecord(b->fork_ev, st);
+  for (int l = 0; l < 2 && e == cudaSuccess; l++) e = cudaStreamWaitEvent(b->side[l], b->fork_ev, 0);
+  for (uint32_t k = 0; k < iters && e == cudaSuccess; k++) {
+    const int l = (int)(k & 1u);
+    e = b->tune.use_graph ? cudaGraphLaunch(b->exec[l], b->side[l]) : batch_iteration(b, l, b->tune, b->side[l]);
+  }
+  for (int l = 0; l < 2 && e == cudaSuccess; l++) {
+    e = cudaEventRecord(b->join_ev[l], b->side[l]);
+    if (e == cudaSuccess) e = cudaStreamWaitEvent(st, b->join_ev[l], 0);
   }
   return e;
 }
@@ -1393,7 +1429,7 @@ ct_status ct_batch_create(ct_ctx* ctx, const ct_batch_job* jobs, uint32_t n, int
     d.f = batch_frame_const(&J.camera, &J.params);
     d.pix_base = base;
     d.max_depth = J.params.max_depth;
-    d.spp_left = (int32_t)J.spp;
+    d.spp_left = (int32_t)(exact_math ? J.spp : (J.spp + 1) / 2);  // lane 0: even samples
     d.exact = b->exact;
     b->bases[j] = base;
     base += J.params.width * J.params.height;
@@ -1416,12 +1452,41 @@ ct_status ct_batch_create(ct_ctx* ctx, const ct_batch_job* jobs, uint32_t n, int
     delete b;
     return cuda_fail(ctx, e, "batch job table");
   }
+  b->lanes = exact_math ? 1 : 2;
   b->dev.jobs = djobs;
   b->dev.bases = dbases;
   b->dev.n_jobs = (int32_t)n;
   b->dev.total_pix = base;
   b->dev.max_stack = max_stack;
   b->dev.wide = jobs[0].bvh->wide ? 1 : 0;
+  b->dev.frame_step = 2 * b->lanes;
+  if (b->lanes == 2) {
+    // lane 1: the odd samples (frame + 2, + 6, ...) into its own queue set and accumulation
+    BatchJob* djobs2 = nullptr;
+    b->jobs0b = b->jobs0;
+    for (uint32_t j = 0; j < n; j++) {
+      BatchJob& d = b->jobs0b[j];
+      d.spp_left = (int32_t)(jobs[j].spp / 2);
+      d.f.frame += 2;
+    }
+    if ((s = alloc_queues(ctx, b->allocs, (size_t)base, b->q2)) == CT_OK) {
+      for (uint32_t j = 0; j < n; j++) b->jobs0b[j].accum = b->q2.accum + b->bases[j];
+      s = upload(ctx, b->allocs, &djobs2, b->jobs0b.data(), n * sizeof(BatchJob));
+    }
+    cudaError_t ce = cudaSuccess;
+    for (int l = 0; l < 2 && s == CT_OK && ce == cudaSuccess; l++) {
+      ce = cudaStreamCreateWithFlags(&b->side[l], cudaStreamNonBlocking);
+      if (ce == cudaSuccess) ce = cudaEventCreateWithFlags(&b->join_ev[l], cudaEventDisableTiming);
+    }
+    if (s == CT_OK && ce == cudaSuccess) ce = cudaEventCreateWithFlags(&b->fork_ev, cudaEventDisableTiming);
+    if (s != CT_OK || ce != cudaSuccess) {
+      free_all(ctx, b->allocs);
+      delete b;
+      return s != CT_OK ? s : cuda_fail(ctx, ce, "batch lanes");
+    }
+    b->dev2 = b->dev;
+    b->dev2.jobs = djobs2;
+  }
   *out = b;
   return CT_OK;
 }
@@ -1442,6 +1507,7 @@ ct_status ct_batch_run(ct_ctx* ctx, ct_batch* b, void* stream) {
   cudaStream_t st = (cudaStream_t)stream;
   CT_CUDA(ctx, batch_reset(b, st, true));
   CT_CUDA(ctx, batch_iterations(b, b->max_spp, st));
+  if (b->lanes == 2) CT_CUDA(ctx, launch_fold(b->q.accum, b->q2.accum, b->dev.total_pix, st));
   return CT_OK;
 }
 
@@ -1521,16 +1587,19 @@ ct_status ct_batch_stats(ct_ctx* ctx, ct_batch* b, ct_frame_stats* out, int32_t 
   if (s != CT_OK) return s;
   cudaStream_t st = (cudaStream_t)stream;
   unsigned long long h[8] = {0};
-  CT_CUDA(ctx, cudaMemcpyAsync(h, b->q.stats, sizeof(h), cudaMemcpyDeviceToHost, st));
+  for (int l = 0; l < b->lanes; l++) {
+    unsigned long long hl[8] = {0};
+    const DevQueues& q = l ? b->q2 : b->q;
+    CT_CUDA(ctx, cudaMemcpyAsync(hl, q.stats, sizeof(hl), cudaMemcpyDeviceToHost, st));
+    CT_CUDA(ctx, cudaStreamSynchronize(st));
+    for (int k = 0; k < 8; k++) h[k] += hl[k];
+    if (reset) CT_CUDA(ctx, cudaMemsetAsync(q.stats, 0, sizeof(hl), st));
+  }
   CT_CUDA(ctx, cudaStreamSynchronize(st));
   out->extension_rays = h[0];
   out->shadow_rays = h[1];
   out->samples = h[2];
   out->frames = (uint32_t)h[3];
-  if (reset) {
-    CT_CUDA(ctx, cudaMemsetAsync(b->q.stats, 0, sizeof(h), st));
-    CT_CUDA(ctx, cudaStreamSynchronize(st));
-  }
   return CT_OK;
 }
 

@@ -161,6 +161,8 @@ struct DevBatch {
   int32_t total_pix;
   int32_t max_stack;     // largest traversal stack among the jobs' BVHs
   int32_t wide;          // 1: every job traces its wide BVH (fast-math frames on the quantised tree)
+  int32_t frame_step;    // seed frames a job advances per iteration of this table (2, or 4 when
+                         // two tables take alternate samples)
 };
 #ifdef __CUDACC__
 __device__ __forceinline__ int batch_job_of(const int32_t* __restrict__ bases, int n, int pix) {

@@ -635,7 +635,7 @@ __global__ void k_batch_advance(DevBatch bt, DevQueues q) {
   if (J.spp_left > 0) {
     atomicAdd(&q.stats[2], (unsigned long long)(J.f.width * J.f.height));
     J.spp_left -= 1;
-    J.f.frame += 2;
+    J.f.frame += bt.frame_step;
   }
 }
 

@@ -272,7 +272,7 @@ cudaError_t ct_server::render_iteration(std::vector<Request*>& finished) {
     return e;
   if ((e = cudaMemcpyAsync(d_bases[slot], hb, (size_t)(n + 1) * 4, cudaMemcpyHostToDevice, st)) != cudaSuccess) return e;
   if ((e = cudaMemsetAsync(q.counts, 0, 16 * sizeof(int32_t), st)) != cudaSuccess) return e;
-  DevBatch b{d_table[slot], d_bases[slot], (int32_t)n, base, max_stack, 0};  // quad BVHs
+  DevBatch b{d_table[slot], d_bases[slot], (int32_t)n, base, max_stack, 0, 2};  // quad BVHs
   const bool fast = !cfg.exact_math;
   e = launch_batch_raygen(b, q, cfg.exact_math, st);
   for (int pass = 0; pass < depth && e == cudaSuccess; pass++) {

@@ -317,7 +317,13 @@ typedef struct ct_batch_tuning {
                             lanes are idle (8, 16 or 24) */
 } ct_batch_tuning;
 /* Copies the job table; allocates queues for every job's pixels at once and
- * one FP32 RGBA accumulation buffer holding all jobs' images back to back. */
+ * one FP32 RGBA accumulation buffer holding all jobs' images back to back.
+ * Fast-math batches run two lanes (even and odd samples of every job, each
+ * with its own queue set and accumulation, on two streams, so one lane's last
+ * bounces overlap the other's first passes; the odd lane's accumulation is
+ * added at the end of ct_batch_run): a job's result does not depend on the
+ * other jobs. Exact-math batches run one lane and equal ct_render_accumulate
+ * bit for bit. */
 ct_status ct_batch_create(ct_ctx* ctx, const ct_batch_job* jobs, uint32_t n, int32_t exact_math, ct_batch** out);
 ct_status ct_batch_destroy(ct_ctx* ctx, ct_batch* b);
 /* Zero the accumulation, reset every job to its first sample, and render all
