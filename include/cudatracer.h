@@ -318,12 +318,14 @@ typedef struct ct_batch_tuning {
 } ct_batch_tuning;
 /* Copies the job table; allocates queues for every job's pixels at once and
  * one FP32 RGBA accumulation buffer holding all jobs' images back to back.
- * Fast-math batches run two lanes (even and odd samples of every job, each
- * with its own queue set and accumulation, on two streams, so one lane's last
- * bounces overlap the other's first passes; the odd lane's accumulation is
- * added at the end of ct_batch_run): a job's result does not depend on the
- * other jobs. Exact-math batches run one lane and equal ct_render_accumulate
- * bit for bit. */
+ * Fast-math batches run four lanes (lane l takes samples l, l + 4, ... of
+ * every job, each lane with its own queue set and accumulation, on its own
+ * stream, so one lane's last bounces overlap the others' passes; the lanes'
+ * accumulations are added in lane order at the end of ct_batch_run): a job's
+ * result does not depend on the other jobs. Device memory: four queue sets of
+ * 172 bytes per pixel of the batch plus the accumulations; a batch that does
+ * not fit fails with CT_ERR_OUT_OF_MEMORY and can be split. Exact-math batches
+ * run one lane and equal ct_render_accumulate bit for bit. */
 ct_status ct_batch_create(ct_ctx* ctx, const ct_batch_job* jobs, uint32_t n, int32_t exact_math, ct_batch** out);
 ct_status ct_batch_destroy(ct_ctx* ctx, ct_batch* b);
 /* Zero the accumulation, reset every job to its first sample, and render all
