@@ -16,10 +16,10 @@
 // job's samples, seeds and per-pixel accumulation order do not depend on the
 // other jobs, so its result equals the job rendered alone. A job takes up to
 // k = min(spp, I / pixels) samples per iteration, I = min(iter_pixels,
-// max_inflight_pixels), at least one, and has min(spp, 2k) slot buffers:
-// sample i goes to slot i mod 2k, so two consecutive iterations (on the two
-// streams) write disjoint slots and the iteration after next, on the same
-// stream, is ordered after. The slots are added in slot order when the job
+// max_inflight_pixels), at least one, and has min(spp, S k) slot buffers, S =
+// kStreams: sample i goes to slot i mod S k, so S consecutive iterations (on
+// the S streams) write disjoint slots and the next one, on the same stream as
+// the first, is ordered after it. The slots are added in slot order when the job
 // finishes. Each slot sums its samples in sample order however the
 // iterations fall, and k depends only on the job and the configuration.
 #include <cuda_runtime.h>
@@ -42,6 +42,10 @@ using namespace ct;
 namespace {
 
 constexpr uint32_t kIterPixels = 1u << 22;  // default pixel-samples a job may take per iteration
+// Render streams, each with a queue set and a job table (measured at 100 and
+// 400 requests/s: 4 streams gave the same tails as 2 within noise, for two more
+// queue sets).
+constexpr int kStreams = 2;
 
 enum Kind { kRender = 0, kClosest = 1, kAny = 2 };
 enum State { kPending, kActive, kFinishing, kDone };
@@ -56,7 +60,7 @@ struct Request {
   float* host_out = nullptr;
   uint32_t done_spp = 0;
   uint32_t k = 1;      // samples per iteration
-  uint32_t slots = 1;  // slot buffers: min(spp, 2k)
+  uint32_t slots = 1;  // slot buffers: min(spp, kStreams * k)
   int64_t last_iter = -2;  // the last iteration that took samples of this job
   cudaEvent_t ready = nullptr;  // its slot buffers are zeroed
   uint32_t waited = 0;          // render streams already ordered after `ready` (bit per stream)
@@ -105,18 +109,18 @@ struct ct_server {
   size_t used_bytes = 0;
   uint32_t inflight_pixels = 0;
   std::chrono::steady_clock::time_point t0;
-  DevQueues q[2] = {};  // one queue set per render stream
-  std::vector<std::pair<void*, size_t>> q_owned[2];
+  DevQueues q[kStreams] = {};  // one queue set per render stream
+  std::vector<std::pair<void*, size_t>> q_owned[kStreams];
   int32_t max_stack = 1;
-  BatchJob* d_table[2] = {nullptr, nullptr};
-  int32_t* d_bases[2] = {nullptr, nullptr};
-  BatchJob* h_table[2] = {nullptr, nullptr};  // pinned staging
-  int32_t* h_bases[2] = {nullptr, nullptr};
+  BatchJob* d_table[kStreams] = {};
+  int32_t* d_bases[kStreams] = {};
+  BatchJob* h_table[kStreams] = {};  // pinned staging
+  int32_t* h_bases[kStreams] = {};
   uint32_t table_cap = 0;
-  cudaEvent_t table_ev[2] = {nullptr, nullptr};
+  cudaEvent_t table_ev[kStreams] = {};
   int slot = 0;          // render stream, queue set and job table of the next iteration
   int64_t iter = 0;      // iterations issued
-  cudaStream_t rs[2] = {nullptr, nullptr}, qs = nullptr, ms = nullptr;  // render, query, setup
+  cudaStream_t rs[kStreams] = {}, qs = nullptr, ms = nullptr;  // render, query, setup
 
   double now() const { return std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count(); }
   void loop();
@@ -200,7 +204,7 @@ void ct_server::start_query(Request* r) {
 }
 
 void ct_server::free_tables() {
-  for (int k = 0; k < 2; k++) {
+  for (int k = 0; k < kStreams; k++) {
     if (d_table[k]) rt_free(ctx, d_table[k], (size_t)table_cap * sizeof(BatchJob));
     if (d_bases[k]) rt_free(ctx, d_bases[k], (size_t)(table_cap + 1) * 4);
     if (h_table[k]) cudaFreeHost(h_table[k]);
@@ -220,11 +224,11 @@ cudaError_t ct_server::render_iteration(std::vector<Request*>& finished) {
   cudaError_t e = cudaEventSynchronize(table_ev[slot]);
   if (e != cudaSuccess) return e;
   if (n > table_cap) {
-    for (int k = 0; k < 2; k++)  // the other table may be in use
+    for (int k = 0; k < kStreams; k++)  // the other tables may be in use
       if ((e = cudaStreamSynchronize(rs[k])) != cudaSuccess) return e;
     free_tables();
     const uint32_t cap = std::max<uint32_t>(64, n * 2);
-    for (int k = 0; k < 2; k++) {
+    for (int k = 0; k < kStreams; k++) {
       if (rt_alloc(ctx, (size_t)cap * sizeof(BatchJob), (void**)&d_table[k]) != CT_OK ||
           rt_alloc(ctx, (size_t)(cap + 1) * 4, (void**)&d_bases[k]) != CT_OK)
         return cudaErrorMemoryAllocation;
@@ -283,8 +287,7 @@ cudaError_t ct_server::render_iteration(std::vector<Request*>& finished) {
     if (e == cudaSuccess) e = launch_batch_connect(b, q, fast, 128, st);
   }
   if (e == cudaSuccess) e = cudaEventRecord(table_ev[slot], st);
-  const int other = slot ^ 1;
-  slot = other;
+  slot = (slot + 1) % kStreams;
   std::vector<Request*> keep;
   for (Request* r : render) {
     const int64_t prev = r->last_iter;
@@ -293,8 +296,11 @@ cudaError_t ct_server::render_iteration(std::vector<Request*>& finished) {
       keep.push_back(r);
       continue;
     }
-    // samples of the previous iteration ran on the other stream: wait for them
-    if (prev == this_iter - 1 && e == cudaSuccess) e = cudaStreamWaitEvent(st, table_ev[other], 0);
+    // samples of earlier iterations may still run on the other streams: wait for
+    // their latest iterations (a job that took all its samples in this one skips it)
+    if (prev >= 0)
+      for (int k = 0; k < kStreams && e == cudaSuccess; k++)
+        if (rs[k] != st) e = cudaStreamWaitEvent(st, table_ev[k], 0);
     // add the slot buffers in slot order, copy the image out, free in stream order
     float4* acc = (float4*)r->dmem;
     for (uint32_t s = 1; s < r->slots && e == cudaSuccess; s++)
@@ -428,8 +434,9 @@ ct_status ct_server_create(ct_ctx* ctx, const ct_server_config* cfg, ct_server**
   s->cfg = *cfg;
   s->device = rt_ctx_device(ctx);
   s->t0 = std::chrono::steady_clock::now();
-  ct_status st = rt_alloc_queues(ctx, cfg->max_inflight_pixels, s->q[0], s->q_owned[0]);
-  if (st == CT_OK) st = rt_alloc_queues(ctx, cfg->max_inflight_pixels, s->q[1], s->q_owned[1]);
+  ct_status st = CT_OK;
+  for (int k = 0; k < kStreams && st == CT_OK; k++)
+    st = rt_alloc_queues(ctx, cfg->max_inflight_pixels, s->q[k], s->q_owned[k]);
   cudaError_t e = cudaSuccess;
   // keep freed request memory in the device's pool between requests
   cudaMemPool_t pool = nullptr;
@@ -437,17 +444,20 @@ ct_status ct_server_create(ct_ctx* ctx, const ct_server_config* cfg, ct_server**
     uint64_t keep = ~0ull;
     cudaMemPoolSetAttribute(pool, cudaMemPoolAttrReleaseThreshold, &keep);
   }
-  for (int k = 0; k < 2 && st == CT_OK && e == cudaSuccess; k++)
+  for (int k = 0; k < kStreams && st == CT_OK && e == cudaSuccess; k++)
     e = cudaStreamCreateWithFlags(&s->rs[k], cudaStreamNonBlocking);
   if (st == CT_OK && e == cudaSuccess) e = cudaStreamCreateWithFlags(&s->qs, cudaStreamNonBlocking);
   if (st == CT_OK && e == cudaSuccess) e = cudaStreamCreateWithFlags(&s->ms, cudaStreamNonBlocking);
-  for (int k = 0; k < 2 && st == CT_OK && e == cudaSuccess; k++) {
+  for (int k = 0; k < kStreams && st == CT_OK && e == cudaSuccess; k++) {
     e = cudaEventCreateWithFlags(&s->table_ev[k], cudaEventDisableTiming);
     if (e == cudaSuccess) e = cudaEventRecord(s->table_ev[k], s->rs[k]);
   }
   if (st != CT_OK || e != cudaSuccess) {
-    for (int k = 0; k < 2; k++) rt_free_list(ctx, s->q_owned[k]);
-    for (cudaStream_t x : {s->rs[0], s->rs[1], s->qs, s->ms})
+    for (int k = 0; k < kStreams; k++) {
+      rt_free_list(ctx, s->q_owned[k]);
+      if (s->rs[k]) cudaStreamDestroy(s->rs[k]);
+    }
+    for (cudaStream_t x : {s->qs, s->ms})
       if (x) cudaStreamDestroy(x);
     delete s;
     return st != CT_OK ? st : rt_fail(ctx, CT_ERR_CUDA, cudaGetErrorString(e));
@@ -473,11 +483,12 @@ ct_status ct_server_destroy(ct_server* s) {
     delete kv.second;
   }
   s->free_tables();
-  for (int k = 0; k < 2; k++) {
+  for (int k = 0; k < kStreams; k++) {
     if (s->table_ev[k]) cudaEventDestroy(s->table_ev[k]);
     rt_free_list(s->ctx, s->q_owned[k]);
+    if (s->rs[k]) cudaStreamDestroy(s->rs[k]);
   }
-  for (cudaStream_t x : {s->rs[0], s->rs[1], s->qs, s->ms})
+  for (cudaStream_t x : {s->qs, s->ms})
     if (x) cudaStreamDestroy(x);
   delete s;
   return CT_OK;
@@ -494,7 +505,7 @@ ct_status ct_server_submit_render(ct_server* s, const ct_batch_job* job, float* 
   r->pixels = (uint32_t)(job->params.width * job->params.height);
   const uint32_t per_iter = std::min(s->cfg.iter_pixels ? s->cfg.iter_pixels : kIterPixels, s->cfg.max_inflight_pixels);
   r->k = std::max<uint32_t>(1, std::min<uint32_t>(job->spp, per_iter / r->pixels));
-  r->slots = std::min<uint32_t>(job->spp, 2 * r->k);
+  r->slots = std::min<uint32_t>(job->spp, kStreams * r->k);
   {
     std::lock_guard<std::mutex> g(s->mu);
     r->id = s->next_id++;
@@ -567,7 +578,7 @@ ct_status ct_server_get_stats(ct_server* s, ct_server_stats* out) {
   unsigned long long h[8] = {0};
   cudaSetDevice(s->device);
   // ray counters of the render iterations, both queue sets (current when no iteration is running)
-  for (int k = 0; k < 2; k++) {
+  for (int k = 0; k < kStreams; k++) {
     unsigned long long hk[8] = {0};
     if (cudaMemcpy(hk, s->q[k].stats, sizeof(hk), cudaMemcpyDeviceToHost) != cudaSuccess) return CT_ERR_CUDA;
     for (int i = 0; i < 8; i++) h[i] += hk[i];
