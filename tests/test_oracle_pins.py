@@ -210,3 +210,30 @@ def test_frame_oracle_runs_and_is_deterministic(orc, w, h):
     assert np.array_equal(acc1, acc2)
     assert np.isfinite(acc1).all() and acc1[:, 3].min() >= 0
     assert acc1[:, :3].sum() > 0
+
+
+def test_full_sort_child_order_changes_work_not_results(orc):
+    """The roofline counts traversal work in the child order fast-math GPU frames
+    use (a full distance sort instead of the reference's partial network). The
+    order must not change a frame (the nearest hit does not depend on it here),
+    only the node-visit and triangle-test counts."""
+    from cudatracer_gb300 import scenes
+
+    ts, cam = scenes.terrain_scene(grid=96, spheres=12, sky_size=(64, 32))
+    a = scenes.scene_arrays(ts)
+    b = orc.bvh_build(ts.vertices, ts.indices)
+    mats = orc.pack_materials(ts.materials)
+    out = {}
+    try:
+        for full in (False, True):
+            orc.set_full_sort(full)
+            orc.work_read(reset=True)
+            acc = orc.render_frames(a, mats, b["quad"], b["prims"], cam, 48, 32, [0], 6, textures=ts.textures,
+                                    sky_tex=0)
+            out[full] = (acc, orc.work_read(reset=True))
+    finally:
+        orc.set_full_sort(False)
+    (a0, w0), (a1, w1) = out[False], out[True]
+    assert np.array_equal(a0.view(np.int32), a1.view(np.int32))
+    assert w0["ext_rays"] == w1["ext_rays"] > 0
+    assert (w0["ext_nodes"], w0["ext_tris"]) != (w1["ext_nodes"], w1["ext_tris"])
