@@ -560,7 +560,7 @@ def serving_poisson(ctx, rate: float = 100.0, duration_s: float = 5.0, seed: int
         "mrays_per_s": rays / wall / 1e6, "wall_s": wall, "completed": st["completed"], "failed": st["failed"],
         "peak_request_bytes": st["peak_bytes"], "iterations": st["iterations"],
         "serial_plain_latency_ms": pct(slat), "serial_plain_busy_s": float(sum(svc)),
-        "iter_pixels": iter_pixels or (1 << 22), "setup_s": setup_s,
+        "iter_pixels": iter_pixels or (1 << 24), "setup_s": setup_s,
     }
 
 
@@ -768,7 +768,7 @@ def run_ours(args, world, rank, local):
     c3 = precision_soup(ctx) if (rank == 0 and not args.skip_precision) else None
     c4 = batching_jobs(ctx) if (rank == 0 and not args.skip_serving) else None
     # the light end of the request-rate range and one where serial execution saturates
-    c5 = ([serving_poisson(ctx), serving_poisson(ctx, rate=400.0, duration_s=2.0)]
+    c5 = ([serving_poisson(ctx, duration_s=10.0), serving_poisson(ctx, rate=400.0, duration_s=2.0)]
           if (rank == 0 and not args.skip_serving) else None)
     # our kernels in the timed region: per frame raygen + depth x (extend, shade,
     # connect) + the fold of a fast-math frame slot (the launch counts of the

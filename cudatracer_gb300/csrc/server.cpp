@@ -41,7 +41,7 @@ using namespace ct;
 
 namespace {
 
-constexpr uint32_t kIterPixels = 1u << 22;  // default pixel-samples a job may take per iteration
+constexpr uint32_t kIterPixels = 1u << 24;  // default pixel-samples a job may take per iteration
 // Render streams, each with a queue set and a job table (measured at 100 and
 // 400 requests/s: 4 streams gave the same tails as 2 within noise, for two more
 // queue sets).

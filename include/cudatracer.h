@@ -364,7 +364,7 @@ typedef struct ct_server_config {
   uint64_t hbm_budget;          /* bytes of per-request device state admitted at once (0 = no limit) */
   uint32_t max_inflight_pixels; /* shared ray-queue capacity: pixels of all render jobs in flight */
   int32_t exact_math;           /* math mode of every render job */
-  uint32_t iter_pixels;         /* pixel-samples a render job may take per iteration (0 = 4,194,304):
+  uint32_t iter_pixels;         /* pixel-samples a render job may take per iteration (0 = 16,777,216):
                                    larger values finish big jobs in fewer, larger iterations and
                                    cost min(spp, 2k) * p * 16 bytes of slot buffers per job */
 } ct_server_config;
