@@ -217,13 +217,13 @@ __device__ __forceinline__ uint32_t meta_at(const WNode8& n, int i) {
   return ((i < 4 ? w[0] : w[1]) >> (8 * (i & 3))) & 0xffu;
 }
 
-// Whole traversal in FP64 triangle tests (boxes as above, culled with the FP64
-// best distance rounded up): the fallback for rays with too many candidates.
 // A warp refills its idle lanes from the cursor once this many are idle (or
 // all are): fewer cursor atomics and refill passes than refilling at the
 // first idle lane (measured best for queries and frames on the wide tree).
 constexpr int kWideRefill = 8;
 
+// Whole traversal in FP64 triangle tests (boxes as above, culled with the FP64
+// best distance rounded up): the fallback for rays with too many candidates.
 template <bool ANY>
 __device__ bool trace_fp64(const DevWBVH& b, const WRay& r, uint32_t* st_node, float* st_t, uint32_t* err, int& best,
                            double& tb) {
