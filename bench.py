@@ -161,15 +161,16 @@ def measured_peaks():
         return 6800.0, "fallback"
 
 
-def profiled_traffic():
-    """DRAM bytes per extension ray of the extend kernel, from the committed ncu
-    summary (profiles/extend_terrain_1080p.md), or None."""
+def profiled_traffic(key: str = "dram_bytes_per_extension_ray"):
+    """Bytes per extension ray of the extend kernel (DRAM, or with
+    key="l2_bytes_per_extension_ray" L2), from the committed ncu summary
+    (profiles/extend_terrain_1080p.md), or None."""
     path = os.path.join(ROOT, "profiles", "extend_terrain_1080p.md")
     try:
         txt = open(path).read()
     except OSError:
         return None
-    m = re.search(r"dram_bytes_per_extension_ray:\s*([0-9.eE+]+)", txt)
+    m = re.search(key + r":\s*([0-9.eE+]+)", txt)
     return float(m.group(1)) if m else None
 
 
@@ -701,6 +702,7 @@ def run_ours(args, world, rank, local):
     peak, peak_kind = measured_peaks()
     ext = prof["extend"]
     roofline = None
+    roofline_sample = None
     cpu_base = None
     work = None
     if rank == 0:
@@ -709,31 +711,58 @@ def run_ours(args, world, rank, local):
         oracle.build_oracle()
         quad, prims = bvh.export()
         omats = oracle.pack_materials(ts.materials)
-        # traversal work per extension ray on sampled rows: the reference's traverseMBVH
-        # counts, in the child order the GPU frames use (full distance order in fast math)
-        oracle.set_full_sort(not args.exact_math)
-        oracle.work_read(reset=True)
-        acc = np.zeros((W * H, 4), np.float32)
-        for r0 in range(0, H, 135):
-            oracle.render_frames(arrays, omats, quad, prims, cam, W, H, [0], DEPTH, accum=acc, exact_math=False,
-                                 textures=ts.textures, sky_tex=0, pixels=(r0 * W, (r0 + 2) * W),
-                                 nthreads=os.cpu_count() or 1)
-        work = oracle.work_read(reset=True)
-        oracle.set_full_sort(False)
+        # traversal work on sampled rows (16 rows of the frame), counted by the oracle
+        def oracle_work(full_sort):
+            oracle.set_full_sort(full_sort)
+            oracle.work_read(reset=True)
+            acc = np.zeros((W * H, 4), np.float32)
+            paths = 0
+            for r0 in range(0, H, 135):
+                oracle.render_frames(arrays, omats, quad, prims, cam, W, H, [0], DEPTH, accum=acc, exact_math=False,
+                                     textures=ts.textures, sky_tex=0, pixels=(r0 * W, (r0 + 2) * W),
+                                     nthreads=os.cpu_count() or 1)
+                paths += 2 * W
+            w = oracle.work_read(reset=True)
+            oracle.set_full_sort(False)
+            return w, paths
+
+        # the algorithmic bytes follow the reference's traverseMBVH order; the counts in
+        # the order fast-math frames visit children (full distance sort) are reported beside
+        work, paths = oracle_work(False)
+        work_fast = oracle_work(True)[0] if not args.exact_math else work
         v_node = work["ext_nodes"] / max(1, work["ext_rays"])
         v_tri = work["ext_tris"] / max(1, work["ext_rays"])
         b_ray = 32 + v_node * 128 + v_tri * 52
         ext_rays = prof_st["extension_rays"]  # rays of the profiling pass, whose launches ext["ms"] times
         achieved = ext_rays * b_ray / (ext["ms"] / 1e3) / 1e9 if ext["ms"] > 0 else None
         tpr = profiled_traffic()
+        l2pr = profiled_traffic("l2_bytes_per_extension_ray")
         roofline = {
             "kernel": "k_extend (closest-hit quad-BVH traversal)", "bound": "hbm",
             "achieved": achieved, "peak": peak, "unit": "GB/s",
             "frac": achieved / peak if achieved else None, "peak_source": peak_kind,
             "traffic": (tpr * ext_rays / max(1, ext["launches"])) if tpr else None,
+            "l2_traffic": (l2pr * ext_rays / max(1, ext["launches"])) if l2pr else None,
             "algorithmic_bytes_per_ray": b_ray, "mean_node_visits": v_node, "mean_tri_tests": v_tri,
+            "mean_node_visits_fast_order": work_fast["ext_nodes"] / max(1, work_fast["ext_rays"]),
+            "mean_tri_tests_fast_order": work_fast["ext_tris"] / max(1, work_fast["ext_rays"]),
             "rays_per_launch": ext_rays / max(1, ext["launches"]),
             "avg_launch_ms": ext["ms"] / max(1, ext["launches"]),
+        }
+        # the whole path per sample: extension and shadow traversals, the shading gathers
+        # of every extension ray (index 12 + positions 36 + normals 36 + uvs 24 + centre
+        # normal 12 + material index 4 + material 52 bytes) and the accumulation update
+        vs_node = work["shadow_nodes"] / max(1, work["shadow_rays"])
+        vs_tri = work["shadow_tris"] / max(1, work["shadow_rays"])
+        b_shadow = 28 + vs_node * 128 + vs_tri * 52
+        b_sample = (work["ext_rays"] * (b_ray + 176) + work["shadow_rays"] * b_shadow) / max(1, paths) + 32
+        ach_sample = b_sample * (value / world) * 1e6 / 1e9  # per GPU
+        roofline_sample = {
+            "model": "bytes per path-traced sample: extension rays x (B_ray + 176 shading) + shadow rays x "
+                     "B_shadow + 32 accumulation, counts from the oracle on 16 rows of the frame",
+            "bytes_per_sample": b_sample, "extension_rays_per_sample": work["ext_rays"] / max(1, paths),
+            "shadow_rays_per_sample": work["shadow_rays"] / max(1, paths), "shadow_bytes_per_ray": b_shadow,
+            "achieved": ach_sample, "peak": peak, "unit": "GB/s", "frac": ach_sample / peak,
         }
         if world == 1 and args.cpu_seconds > 0:
             cpu_base = cpu_baseline_port(arrays, ts.textures, omats, quad, prims, cam, args.cpu_seconds)
@@ -788,7 +817,7 @@ def run_ours(args, world, rank, local):
         "stage_ms": {k: v["ms"] for k, v in prof.items()}, "stage_frames": prof_frames,
         "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": h2d_bytes, "d2h_bytes_per_step": d2h_bytes},
         "gpu_launches": launches,
-        "roofline": roofline, "cpu_baseline": cpu_base, "closest_hit": c1, "precision": c3, "batching": c4, "serving": c5, "full_materials": full, "clocks": clk,
+        "roofline": roofline, "roofline_sample": roofline_sample, "cpu_baseline": cpu_base, "closest_hit": c1, "precision": c3, "batching": c4, "serving": c5, "full_materials": full, "clocks": clk,
         "setup": {"scene_and_bvh_s": setup_s, "quad_nodes": info["quad_node_count"],
                   "bvh_device_build_ms": min(dev_build),
                   "bvh_host_build_ms": (hinfo["build_ms"] + hinfo["collapse_ms"] + hinfo["upload_ms"]) if hinfo else None,
