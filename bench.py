@@ -46,6 +46,8 @@ def parse_args():
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
     ap.add_argument("--cpu-seconds", type=float, default=12.0, help="CPU-baseline sample budget")
     ap.add_argument("--exact-math", action="store_true")
+    ap.add_argument("--tree", choices=["fast", "reference"], default="fast",
+                    help="tree traced by fast-math frames (exact-math frames always trace the reference's)")
     ap.add_argument("--width", type=int, default=1920, help="smaller frames for profiler captures")
     ap.add_argument("--height", type=int, default=1080)
     ap.add_argument("--skip-extras", action="store_true",
@@ -163,14 +165,15 @@ def measured_peaks():
 
 def profiled_traffic(key: str = "dram_bytes_per_extension_ray"):
     """Bytes per extension ray of the extend kernel (DRAM, or with
-    key="l2_bytes_per_extension_ray" L2), from the committed ncu summary
+    key="l2_bytes_per_extension_ray" L2; keys prefixed "reference_tree_" for
+    frames on the reference's tree), from the committed ncu summary
     (profiles/extend_terrain_1080p.md), or None."""
     path = os.path.join(ROOT, "profiles", "extend_terrain_1080p.md")
     try:
         txt = open(path).read()
     except OSError:
         return None
-    m = re.search(key + r":\s*([0-9.eE+]+)", txt)
+    m = re.search(r"(?m)^" + key + r":\s*([0-9.eE+]+)", txt)
     return float(m.group(1)) if m else None
 
 
@@ -610,8 +613,8 @@ def run_ours(args, world, rank, local):
     t_setup = time.perf_counter()
     ts, cam, arrays = build_scene()
     sc = ctx.scene(arrays, [api.Material(**m) for m in ts.materials], ts.textures, ts.skybox_texture)
-    bvh = sc.build_bvh_device()  # bit-identical quad nodes to the host SAH build
-    info = bvh.info()
+    ref_bvh = sc.build_bvh_device()  # the reference's tree: quad nodes bit-identical to the host SAH build
+    info = ref_bvh.info()
     setup_s = time.perf_counter() - t_setup
     dev_build = []
     for _ in range(3):
@@ -619,6 +622,12 @@ def run_ours(args, world, rank, local):
         t0 = time.perf_counter()
         sc.build_bvh_device().close()
         dev_build.append((time.perf_counter() - t0) * 1e3)
+    # fast-math frames trace the tree built for traversal speed (equal hits up to
+    # exact t ties); exact-math frames keep the reference's tree
+    t0 = time.perf_counter()
+    fast_bvh = None if (args.exact_math or args.tree == "reference") else sc.build_bvh_fast()
+    fast_build_ms = (time.perf_counter() - t0) * 1e3
+    bvh = ref_bvh if fast_bvh is None else fast_bvh
     hinfo = None
     if rank == 0:
         hb = sc.build_bvh(0)
@@ -661,6 +670,35 @@ def run_ours(args, world, rank, local):
     job.profile(False)
     prof_st = job.stats(reset=True, stream=stream)
     ms_max = max_over_ranks(ms, world)
+    # the same frames on the reference's tree, timed the same way
+    ref_tree = None
+    if fast_bvh is not None and not args.skip_extras:
+        pr_ = api.Params(W, H, camera=camera, max_depth=DEPTH, exact_math=False)
+        pr_.reset(job, stream)
+        for _ in range(args.warmup):
+            api.launch_kernels(job, sc, ref_bvh, pr_, stream=stream)
+        stream.synchronize()
+        barrier(world)
+        torch.cuda.synchronize()
+        e0.record(stream)
+        for _ in range(args.steps):
+            api.launch_kernels(job, sc, ref_bvh, pr_, stream=stream)
+        e1.record(stream)
+        stream.synchronize()
+        barrier(world)
+        ms_ref = max_over_ranks(e0.elapsed_time(e1), world)
+        job.profile(True)
+        job.profile_read(reset=True)
+        for _ in range(prof_frames):
+            api.launch_kernels(job, sc, ref_bvh, pr_, stream=stream)
+        stream.synchronize()
+        prof_ref = job.profile_read(reset=True)
+        job.profile(False)
+        job.stats(reset=True, stream=stream)
+        ref_tree = {"value": world * W * H * args.steps / (ms_ref / 1e3) / 1e6, "unit": UNIT,
+                    "ms_per_step": ms_ref / args.steps, "stage_ms": {k: v["ms"] for k, v in prof_ref.items()},
+                    "tree": "the reference's SAH + MergeNodes quad tree (device build)",
+                    "quad_nodes": info["quad_node_count"]}
     samples = W * H * args.steps
     value = world * samples / (ms_max / 1e3) / 1e6
     mrays = world * (st["extension_rays"] + st["shadow_rays"]) / (ms_max / 1e3) / 1e6
@@ -709,10 +747,10 @@ def run_ours(args, world, rank, local):
         import oracle
 
         oracle.build_oracle()
-        quad, prims = bvh.export()
+        quad, prims = ref_bvh.export()
         omats = oracle.pack_materials(ts.materials)
         # traversal work on sampled rows (16 rows of the frame), counted by the oracle
-        def oracle_work(full_sort):
+        def oracle_work(quad, prims, full_sort):
             oracle.set_full_sort(full_sort)
             oracle.work_read(reset=True)
             acc = np.zeros((W * H, 4), np.float32)
@@ -726,17 +764,19 @@ def run_ours(args, world, rank, local):
             oracle.set_full_sort(False)
             return w, paths
 
-        # the algorithmic bytes follow the reference's traverseMBVH order; the counts in
-        # the order fast-math frames visit children (full distance sort) are reported beside
-        work, paths = oracle_work(False)
-        work_fast = oracle_work(True)[0] if not args.exact_math else work
+        # the algorithmic bytes follow the reference's traverseMBVH order on the
+        # reference's tree; the counts of the traced tree in the order fast-math
+        # frames visit children (full distance sort) are reported beside
+        work, paths = oracle_work(quad, prims, False)
+        work_fast = oracle_work(*bvh.export(), True)[0] if not args.exact_math else work
         v_node = work["ext_nodes"] / max(1, work["ext_rays"])
         v_tri = work["ext_tris"] / max(1, work["ext_rays"])
         b_ray = 32 + v_node * 128 + v_tri * 52
         ext_rays = prof_st["extension_rays"]  # rays of the profiling pass, whose launches ext["ms"] times
         achieved = ext_rays * b_ray / (ext["ms"] / 1e3) / 1e9 if ext["ms"] > 0 else None
-        tpr = profiled_traffic()
-        l2pr = profiled_traffic("l2_bytes_per_extension_ray")
+        pre = "" if fast_bvh is not None else "reference_tree_"
+        tpr = profiled_traffic(pre + "dram_bytes_per_extension_ray")
+        l2pr = profiled_traffic(pre + "l2_bytes_per_extension_ray")
         roofline = {
             "kernel": "k_extend (closest-hit quad-BVH traversal)", "bound": "hbm",
             "achieved": achieved, "peak": peak, "unit": "GB/s",
@@ -744,8 +784,13 @@ def run_ours(args, world, rank, local):
             "traffic": (tpr * ext_rays / max(1, ext["launches"])) if tpr else None,
             "l2_traffic": (l2pr * ext_rays / max(1, ext["launches"])) if l2pr else None,
             "algorithmic_bytes_per_ray": b_ray, "mean_node_visits": v_node, "mean_tri_tests": v_tri,
-            "mean_node_visits_fast_order": work_fast["ext_nodes"] / max(1, work_fast["ext_rays"]),
-            "mean_tri_tests_fast_order": work_fast["ext_tris"] / max(1, work_fast["ext_rays"]),
+            "traced_tree": {
+                "tree": "reference" if fast_bvh is None else "ct_bvh_build_fast",
+                "mean_node_visits": work_fast["ext_nodes"] / max(1, work_fast["ext_rays"]),
+                "mean_tri_tests": work_fast["ext_tris"] / max(1, work_fast["ext_rays"]),
+                "bytes_per_ray": 32 + 128 * work_fast["ext_nodes"] / max(1, work_fast["ext_rays"])
+                + 52 * work_fast["ext_tris"] / max(1, work_fast["ext_rays"]),
+                "order": "full distance sort" if fast_bvh is not None else "traverseMBVH"},
             "rays_per_launch": ext_rays / max(1, ext["launches"]),
             "avg_launch_ms": ext["ms"] / max(1, ext["launches"]),
         }
@@ -811,17 +856,21 @@ def run_ours(args, world, rank, local):
         "config": {"workload": WORKLOAD, "width": W, "height": H, "max_depth": DEPTH, "triangles": int(ts.ntri),
                    "frames_per_step": 1, "shading": "compat (reference shade)",
                    "math": "exact" if args.exact_math else "fast",
-                   "l2": "inputs larger than L2: 94 MB nodes + 150 MB triangles + 150 MB scene arrays + 300 MB queues",
+                   "l2": "inputs larger than L2: 85-94 MB nodes + 150 MB triangles + 150 MB scene arrays + 300 MB queues",
                    "parallelism": f"replicas x{world}"},
         "mrays_per_s": mrays, "rays_per_step": (st["extension_rays"] + st["shadow_rays"]) / args.steps,
         "stage_ms": {k: v["ms"] for k, v in prof.items()}, "stage_frames": prof_frames,
         "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": h2d_bytes, "d2h_bytes_per_step": d2h_bytes},
         "gpu_launches": launches,
+        "reference_tree": ref_tree,
         "roofline": roofline, "roofline_sample": roofline_sample, "cpu_baseline": cpu_base, "closest_hit": c1, "precision": c3, "batching": c4, "serving": c5, "full_materials": full, "clocks": clk,
-        "setup": {"scene_and_bvh_s": setup_s, "quad_nodes": info["quad_node_count"],
+        "setup": {"scene_and_bvh_s": setup_s, "quad_nodes": bvh.info()["quad_node_count"],
                   "bvh_device_build_ms": min(dev_build),
+                  "bvh_fast_build_ms": fast_build_ms if fast_bvh is not None else None,
                   "bvh_host_build_ms": (hinfo["build_ms"] + hinfo["collapse_ms"] + hinfo["upload_ms"]) if hinfo else None,
-                  "bvh": "device SAH build (quad nodes bit-identical to the host build)"},
+                  "bvh": ("reference SAH tree, device build (quad nodes bit-identical to the host build)"
+                          if fast_bvh is None else "ct_bvh_build_fast (host, all cores); the reference's tree "
+                          "is timed beside it in reference_tree")},
     }
     if rank == 0:
         print(json.dumps(line), flush=True)

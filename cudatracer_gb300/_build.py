@@ -25,6 +25,7 @@ LIB = os.path.join(PKG, "libcudatracer.so")
 SOURCES = {
     "api.cpp": [],
     "bvh_build.cpp": [],
+    "bvh_fast.cpp": [],
     "mesh_io.cpp": [],
     "server.cpp": [],
     "k_trace.cu": [],

@@ -121,12 +121,14 @@ SIGNATURES = {
     "ct_scene_destroy": (c_int32, [P, P]),
     "ct_scene_set_material": (c_int32, [P, P, c_uint32, POINTER(ct_material)]),
     "ct_bvh_build": (c_int32, [P, P, c_int32, PP]),
+    "ct_bvh_build_fast": (c_int32, [P, P, c_int32, PP]),
     "ct_bvh_import_quad": (c_int32, [P, P, P, c_uint32, P, c_uint32, PP]),
     "ct_bvh_import_binary": (c_int32, [P, P, P, c_uint32, P, c_uint32, PP]),
     "ct_bvh_info_get": (c_int32, [P, POINTER(ct_bvh_info)]),
     "ct_bvh_export": (c_int32, [P, c_int32, P, P]),
     "ct_bvh_destroy": (c_int32, [P, P]),
     "ct_host_bvh_build": (c_int32, [P, c_uint32, P, c_uint32, c_int32, PP]),
+    "ct_host_bvh_build_fast": (c_int32, [P, c_uint32, P, c_uint32, c_int32, PP]),
     "ct_host_bvh_counts": (c_int32, [P, POINTER(c_uint32), POINTER(c_uint32), POINTER(c_uint32),
                                      POINTER(c_double), POINTER(c_double)]),
     "ct_host_bvh_export": (c_int32, [P, c_int32, P, P]),

@@ -391,6 +391,13 @@ class Scene:
         check(self.ctx.lib.ct_bvh_build(self.ctx.h, self.h, nthreads, ctypes.byref(h)), self.ctx.h)
         return BVH(self, h)
 
+    def build_bvh_fast(self, nthreads: int = 0) -> "BVH":
+        """Quad tree built for traversal speed (ct_bvh_build_fast): hits equal the
+        reference tree's up to exact t ties; use it for fast-math frames and queries."""
+        h = ctypes.c_void_p()
+        check(self.ctx.lib.ct_bvh_build_fast(self.ctx.h, self.h, nthreads, ctypes.byref(h)), self.ctx.h)
+        return BVH(self, h)
+
     def build_bvh_device(self, stream=None) -> "BVH":
         """The same SAH tree built on the GPU (ct_bvh_build_device): quad nodes
         equal build_bvh's bit for bit, primitives within a leaf may be reordered."""
@@ -480,14 +487,16 @@ class BVH:
         return occluded
 
 
-def host_bvh_build(vertices: np.ndarray, indices: np.ndarray, nthreads: int = 0) -> dict:
+def host_bvh_build(vertices: np.ndarray, indices: np.ndarray, nthreads: int = 0, fast: bool = False) -> dict:
     """BVHTree + MBVHTree construction on the host only (no device): returns the
-    reference-layout binary nodes (n,8 int32 view), quad nodes (n,32) and prims."""
+    reference-layout binary nodes (n,8 int32 view), quad nodes (n,32) and prims.
+    fast=True builds ct_bvh_build_fast's tree instead (no binary nodes: 0 rows)."""
     lib = _lib.load()
     v = np.ascontiguousarray(vertices, np.float32)
     ix = np.ascontiguousarray(indices, np.uint32)
     h = ctypes.c_void_p()
-    check(lib.ct_host_bvh_build(ptr(v), v.shape[0], ptr(ix), ix.shape[0], nthreads, ctypes.byref(h)))
+    fn = lib.ct_host_bvh_build_fast if fast else lib.ct_host_bvh_build
+    check(fn(ptr(v), v.shape[0], ptr(ix), ix.shape[0], nthreads, ctypes.byref(h)))
     try:
         nb, nq, npr = ctypes.c_uint32(), ctypes.c_uint32(), ctypes.c_uint32()
         bms, cms = ctypes.c_double(), ctypes.c_double()
@@ -496,7 +505,8 @@ def host_bvh_build(vertices: np.ndarray, indices: np.ndarray, nthreads: int = 0)
         bin_nodes = np.zeros((nb.value, 8), np.int32)
         quad = np.zeros((nq.value, 32), np.int32)
         prims = np.zeros(npr.value, np.uint32)
-        check(lib.ct_host_bvh_export(h, _lib.CT_BVH_BINARY, ptr(bin_nodes), None))
+        if nb.value:
+            check(lib.ct_host_bvh_export(h, _lib.CT_BVH_BINARY, ptr(bin_nodes), None))
         check(lib.ct_host_bvh_export(h, _lib.CT_BVH_QUAD, ptr(quad), ptr(prims)))
         return {"binary": bin_nodes, "quad": quad, "prims": prims, "build_ms": bms.value, "collapse_ms": cms.value}
     finally:

@@ -506,6 +506,22 @@ ct_status ct_bvh_build(ct_ctx* ctx, const ct_scene* scene, int32_t nthreads, ct_
   return CT_OK;
 }
 
+ct_status ct_bvh_build_fast(ct_ctx* ctx, const ct_scene* scene, int32_t nthreads, ct_bvh** out) {
+  if (!ctx || !scene || !out) return fail(ctx, CT_ERR_INVALID_ARGUMENT, "null argument");
+  *out = nullptr;
+  ct_status s = set_device(ctx);
+  if (s != CT_OK) return s;
+  auto* b = new ct_bvh();
+  build_fast_quad(scene->verts.data(), scene->idx.data(), scene->nt, nthreads, b->host);
+  if ((s = finish_bvh(ctx, scene, b)) != CT_OK) {
+    free_all(ctx, b->allocs);
+    delete b;
+    return s;
+  }
+  *out = b;
+  return CT_OK;
+}
+
 ct_status ct_bvh_build_device(ct_ctx* ctx, const ct_scene* scene, void* stream, ct_bvh** out) {
   if (!ctx || !scene || !out) return fail(ctx, CT_ERR_INVALID_ARGUMENT, "null argument");
   *out = nullptr;
@@ -817,6 +833,20 @@ ct_status ct_host_bvh_build(const float* vertices, uint32_t vertex_count, const 
   return CT_OK;
 }
 
+ct_status ct_host_bvh_build_fast(const float* vertices, uint32_t vertex_count, const uint32_t* indices,
+                                 uint32_t triangle_count, int32_t nthreads, ct_host_bvh** out) {
+  if (!vertices || !indices || !out || triangle_count == 0 || vertex_count == 0) return CT_ERR_INVALID_ARGUMENT;
+  *out = nullptr;
+  for (uint32_t i = 0; i < vertex_count; i++)
+    if (!finite3(vertices + 3 * (size_t)i)) return CT_ERR_INVALID_ARGUMENT;
+  for (uint64_t i = 0; i < 3ull * triangle_count; i++)
+    if (indices[i] >= vertex_count) return CT_ERR_INVALID_ARGUMENT;
+  auto* h = new ct_host_bvh();
+  build_fast_quad(vertices, indices, triangle_count, nthreads, h->host);
+  *out = h;
+  return CT_OK;
+}
+
 ct_status ct_host_bvh_counts(const ct_host_bvh* h, uint32_t* binary_nodes, uint32_t* quad_nodes, uint32_t* prims,
                              double* build_ms, double* collapse_ms) {
   if (!h) return CT_ERR_INVALID_ARGUMENT;
@@ -831,6 +861,7 @@ ct_status ct_host_bvh_counts(const ct_host_bvh* h, uint32_t* binary_nodes, uint3
 ct_status ct_host_bvh_export(const ct_host_bvh* h, ct_bvh_layout layout, void* nodes, uint32_t* prim_indices) {
   if (!h) return CT_ERR_INVALID_ARGUMENT;
   if (layout == CT_BVH_BINARY) {
+    if (h->host.bin.empty() && nodes) return CT_ERR_UNSUPPORTED;
     if (nodes) std::memcpy(nodes, h->host.bin.data(), h->host.bin.size() * sizeof(BinNode));
   } else if (layout == CT_BVH_QUAD) {
     if (nodes) std::memcpy(nodes, h->host.quad.data(), h->host.quad.size() * sizeof(QuadNode));

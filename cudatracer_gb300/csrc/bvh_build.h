@@ -35,6 +35,11 @@ struct HostBVH {
 void build_binary(const float* verts, const uint32_t* idx, uint32_t ntri, int nthreads, HostBVH& out);
 // MBVHNode::MergeNodes collapse of out.bin into out.quad (deterministic numbering).
 void collapse_quad(HostBVH& out);
+// Quad tree built for traversal speed (bvh_fast.cpp): padded-relative triangle
+// boxes, 16-bin SAH to single triangles, cost-optimal four-wide collapse with
+// leaves of at most four triangles. Fills out.quad and out.prims; out.bin stays
+// empty.
+void build_fast_quad(const float* verts, const uint32_t* idx, uint32_t ntri, int nthreads, HostBVH& out);
 // Structural validation of an imported tree; returns "" when valid.
 std::string validate_quad(const std::vector<QuadNode>& q, uint32_t prim_count);
 std::string validate_binary(const std::vector<BinNode>& b, uint32_t prim_count);

@@ -202,6 +202,21 @@ ct_status ct_bvh_import_binary(ct_ctx* ctx, const ct_scene* scene, const void* n
  * the SAH cost reach 1e34 (coordinates beyond ~1e14). Exports the QUAD layout
  * only (ct_bvh_export with CT_BVH_BINARY and non-NULL nodes fails). */
 ct_status ct_bvh_build_device(ct_ctx* ctx, const ct_scene* scene, void* stream, ct_bvh** out);
+/* Quad tree built for traversal speed (no reference counterpart; same node and
+ * leaf formats, so every trace and frame entry point takes it). Triangle boxes
+ * are padded by 1e-5 x max(1, |coordinate|) per side instead of the
+ * reference's -0.001/+0.01; a binary SAH over 16 centroid bins per axis is
+ * split to single triangles and collapsed to four-wide nodes by dynamic
+ * programming over the surface-area cost, with leaves of at most four
+ * triangles. Closest and any hits equal the reference tree's up to the winner
+ * of an exact t tie; fast-math frames on it are the fast-math frames on the
+ * reference tree up to those ties (about 10 % fewer node and triangle tests
+ * per ray on a terrain view). Exact-math frames run but follow this tree's
+ * child order, so they are not bit-identical to the reference's: keep
+ * ct_bvh_build / ct_bvh_build_device for those. Host build with nthreads
+ * threads (<= 0: every hardware thread); the tree does not depend on the
+ * thread count. Exports the QUAD layout only. */
+ct_status ct_bvh_build_fast(ct_ctx* ctx, const ct_scene* scene, int32_t nthreads, ct_bvh** out);
 /* 8-wide BVH with 8-bit quantised child bounds (no reference counterpart: the
  * precision extension of the ray-query path). 80-byte nodes {quantisation
  * origin p, three exponents, inner-child mask, first inner child, first
@@ -234,6 +249,9 @@ ct_status ct_bvh_destroy(ct_ctx* ctx, ct_bvh* bvh);
 typedef struct ct_host_bvh ct_host_bvh;
 ct_status ct_host_bvh_build(const float* vertices, uint32_t vertex_count, const uint32_t* indices,
                             uint32_t triangle_count, int32_t nthreads, ct_host_bvh** out);
+/* Host-only ct_bvh_build_fast tree (binary_nodes reads 0; QUAD export only). */
+ct_status ct_host_bvh_build_fast(const float* vertices, uint32_t vertex_count, const uint32_t* indices,
+                                 uint32_t triangle_count, int32_t nthreads, ct_host_bvh** out);
 ct_status ct_host_bvh_counts(const ct_host_bvh* h, uint32_t* binary_nodes, uint32_t* quad_nodes, uint32_t* prims,
                              double* build_ms, double* collapse_ms);
 ct_status ct_host_bvh_export(const ct_host_bvh* h, ct_bvh_layout layout, void* nodes, uint32_t* prim_indices);

@@ -1,0 +1,209 @@
+"""The traversal-speed quad tree (ct_host_bvh_build_fast / ct_bvh_build_fast)
+on the host, no GPU: structure, thread-count independence, and the oracle's
+closest and any hits on it against the oracle on the reference's tree (equal
+t bit for bit; another primitive only where two triangles tie at that t)."""
+import numpy as np
+import pytest
+
+
+def _fast(v, ix, nthreads=4):
+    from cudatracer_gb300 import api
+
+    return api.host_bvh_build(v, ix, nthreads, fast=True)
+
+
+def _check_structure(q, pr, v, ix, max_leaf=4):
+    """Every primitive in exactly one leaf of at most max_leaf, every inner
+    node reached once, every slot box holding its triangles / child slots."""
+    nq = q.shape[0]
+    f = q.view(np.float32)
+    lo = np.stack([f[:, 0:4], f[:, 8:12], f[:, 16:20]], 2)   # (n, 4, 3) slot minima
+    hi = np.stack([f[:, 4:8], f[:, 12:16], f[:, 20:24]], 2)
+    ch, cnt = q[:, 24:28], q[:, 28:32]
+    assert np.array_equal(np.sort(pr), np.arange(pr.size))
+    inner = cnt == -1
+    kids = ch[inner]
+    assert (kids > 0).all() and (kids < nq).all()
+    assert np.array_equal(np.sort(kids), np.arange(1, nq))  # each non-root node reached once
+    assert ((cnt == -1) | (cnt > 0)).sum(1).min() >= 1      # no node without children
+    leaf = cnt > 0
+    assert cnt[leaf].max() <= max_leaf
+    cover = np.zeros(pr.size, np.int32)
+    tri = v[ix.astype(np.int64)]  # (ntri, 3, 3)
+    for (n, s) in zip(*np.nonzero(leaf)):
+        first, c = ch[n, s], cnt[n, s]
+        cover[first:first + c] += 1
+        pts = tri[pr[first:first + c]].reshape(-1, 3)
+        assert (pts >= lo[n, s]).all() and (pts <= hi[n, s]).all()
+    assert (cover == 1).all()
+    for (n, s) in zip(*np.nonzero(inner)):
+        c = ch[n, s]
+        used = cnt[c] != 0
+        assert (lo[c][used] >= lo[n, s]).all() and (hi[c][used] <= hi[n, s]).all()
+
+
+def _tie_ok(orc, v, ix, o, d, prim, t, eps):
+    """The oracle's triangle test alone on `prim` gives exactly t."""
+    tri = v[ix[prim].astype(np.int64)].astype(np.float32)
+    q1 = orc.bvh_build(tri, np.array([[0, 1, 2]], np.uint32))
+    h, t1 = orc.trace_closest(q1["quad"], q1["prims"], tri, np.array([[0, 1, 2]], np.uint32), o[None], d[None],
+                              eps=eps)
+    return h[0] == 0 and t1.view(np.int32)[0] == np.float32(t).view(np.int32)
+
+
+def _compare_hits(orc, v, ix, o, d, eps=1e-3, any_hit=True):
+    from cudatracer_gb300 import api
+
+    # the reference's tree (ct_host_bvh_build: equal to the oracle's build except
+    # that a root leaf stays traceable where the reference's collapse empties it)
+    ref = api.host_bvh_build(v, ix, 4)
+    fast = _fast(v, ix)
+    rh, rt = orc.trace_closest(ref["quad"], ref["prims"], v, ix, o, d, eps=eps)
+    fh, ft = orc.trace_closest(fast["quad"], fast["prims"], v, ix, o, d, eps=eps)
+    assert np.array_equal(rt.view(np.int32), ft.view(np.int32))
+    diff = np.nonzero(rh != fh)[0]
+    assert diff.size <= max(8, rh.size // 100)
+    for i in diff[:64]:
+        assert rh[i] >= 0 and fh[i] >= 0 and _tie_ok(orc, v, ix, o[i, :3], d[i, :3], fh[i], ft[i], eps)
+    if any_hit:
+        rng = np.random.default_rng(11)
+        tmax = np.where(rt < 1e30, rt * rng.uniform(0.5, 1.5, size=rt.size), 50.0).astype(np.float32)
+        ra = orc.trace_any(ref["quad"], ref["prims"], v, ix, o, d, tmax, eps=eps)
+        fa = orc.trace_any(fast["quad"], fast["prims"], v, ix, o, d, tmax, eps=eps)
+        assert np.array_equal(ra, fa)
+    return (rh >= 0).sum()
+
+
+@pytest.fixture(scope="module")
+def small_terrain():
+    from cudatracer_gb300 import scenes
+
+    return scenes.terrain_scene(grid=128, spheres=12, sky_size=(64, 32))
+
+
+def _view_rays(cam, n, seed):
+    rng = np.random.default_rng(seed)
+    fw = np.asarray(cam["forward"], np.float64)
+    fw /= np.linalg.norm(fw)
+    d = fw[None] + rng.uniform(-0.6, 0.6, size=(n, 3))
+    d /= np.linalg.norm(d, axis=1, keepdims=True)
+    o = np.tile(np.asarray(cam["position"], np.float32), (n, 1))
+    return o.astype(np.float32), d.astype(np.float32)
+
+
+def test_fast_tree_structure_and_thread_independence(lib, small_terrain):
+    from cudatracer_gb300 import scenes
+
+    ts, _ = small_terrain
+    for v, ix in ((ts.vertices, ts.indices), (scenes.soup_scene(5000, seed=2).vertices,
+                                               scenes.soup_scene(5000, seed=2).indices)):
+        a = _fast(v, ix, 1)
+        b = _fast(v, ix, 8)
+        assert np.array_equal(a["quad"], b["quad"]) and np.array_equal(a["prims"], b["prims"])
+        assert a["binary"].shape[0] == 0
+        _check_structure(a["quad"], a["prims"], v, ix)
+        ref = _fast(v, ix)  # same tree again: the build is deterministic
+        assert np.array_equal(ref["quad"], a["quad"])
+
+
+def test_fast_tree_hits_equal_reference_tree_terrain(lib, orc, small_terrain):
+    from cudatracer_gb300 import scenes
+
+    ts, cam = small_terrain
+    o, d = _view_rays(cam, 20000, 3)
+    assert _compare_hits(orc, ts.vertices, ts.indices, o, d) > 10000
+    # incoherent rays from inside the scene's bounds
+    rng = np.random.default_rng(4)
+    lo, hi = ts.vertices.min(0), ts.vertices.max(0)
+    o2 = rng.uniform(lo, hi, size=(20000, 3)).astype(np.float32)
+    d2 = rng.normal(size=(20000, 3))
+    d2 = (d2 / np.linalg.norm(d2, axis=1, keepdims=True)).astype(np.float32)
+    assert _compare_hits(orc, ts.vertices, ts.indices, o2, d2) > 5000
+
+
+@pytest.mark.parametrize("seed,ntri", [(1, 7), (2, 300), (3, 5000), (4, 40000)])
+def test_fast_tree_hits_equal_reference_tree_soups(lib, orc, seed, ntri):
+    from cudatracer_gb300 import scenes
+
+    s = scenes.soup_scene(ntri, seed=seed)
+    o, d = scenes.incoherent_rays(4096, seed=seed + 10)
+    o, d = o[:, :3].copy(), d[:, :3].copy()
+    n = _compare_hits(orc, s.vertices, s.indices, o, d, eps=1e-12)
+    assert n > 0 or ntri < 100
+
+
+def test_fast_tree_degenerate_inputs(lib, orc):
+    """One triangle (one leaf slot under the root), coincident triangles (every
+    hit a tie), and axis-aligned flat quads hit by axis-parallel rays from
+    origins on the quads' planes."""
+    v1 = np.array([[0, 0, 0], [1, 0, 0], [0, 1, 0]], np.float32)
+    i1 = np.array([[0, 1, 2]], np.uint32)
+    h1 = _fast(v1, i1, 1)
+    assert h1["quad"].shape[0] == 1 and h1["quad"][0, 28] == 1 and (h1["quad"][0, 29:32] == 0).all()
+    o = np.array([[0.2, 0.2, 1.0], [2.0, 2.0, 1.0]], np.float32)
+    d = np.array([[0, 0, -1.0], [0, 0, -1.0]], np.float32)
+    # the reference's collapse empties a root leaf (nothing to compare with)
+    h, t = orc.trace_closest(h1["quad"], h1["prims"], v1, i1, o, d)
+    assert h.tolist() == [0, -1] and t[0] == np.float32(1.0)
+    v = np.tile(v1, (192, 1))
+    ix = np.arange(v.shape[0], dtype=np.uint32).reshape(-1, 3)
+    f = _fast(v, ix, 2)
+    _check_structure(f["quad"], f["prims"], v, ix)
+    rng = np.random.default_rng(0)
+    o2 = np.concatenate([rng.uniform(0, 0.5, size=(256, 2)), np.ones((256, 1))], 1).astype(np.float32)
+    d2 = np.tile(np.array([[0, 0, -1.0]], np.float32), (256, 1))
+    _compare_hits(orc, v, ix, o2, d2, any_hit=False)
+    # a stack of flat axis-aligned quads, 2 triangles each, at y = k
+    quads = []
+    for k in range(40):
+        x0, z0 = rng.uniform(-5, 5, size=2)
+        quads.append([[x0, k, z0], [x0 + 1, k, z0], [x0 + 1, k, z0 + 1], [x0, k, z0 + 1]])
+    vq = np.asarray(quads, np.float32).reshape(-1, 3)
+    iq = np.concatenate([[[4 * k, 4 * k + 1, 4 * k + 2], [4 * k, 4 * k + 2, 4 * k + 3]] for k in range(40)]).astype(np.uint32)
+    n = 4096
+    oq = rng.uniform(-5, 6, size=(n, 3)).astype(np.float32)
+    oq[:, 1] = rng.integers(0, 40, size=n).astype(np.float32) + np.where(rng.random(n) < 0.5, 0.0, 0.5)
+    dq = np.zeros((n, 3), np.float32)
+    dq[np.arange(n), rng.integers(0, 3, size=n)] = rng.choice([-1.0, 1.0], size=n)
+    dq[: n // 4] = rng.normal(size=(n // 4, 3))
+    dq /= np.linalg.norm(dq, axis=1, keepdims=True)
+    _compare_hits(orc, vq, iq, oq, dq)
+
+
+def test_fast_tree_tests_fewer_triangles_per_ray(lib, orc, small_terrain):
+    """Fast-math frames on the small terrain: fewer node visits plus triangle
+    tests per extension ray on the fast tree, and the same accumulation (the
+    hits are equal)."""
+    from cudatracer_gb300 import scenes
+
+    ts, cam = small_terrain
+    arr = scenes.scene_arrays(ts)
+    mats = orc.pack_materials(ts.materials)
+    W, H = 160, 96
+    out = {}
+    for name, tree in (("ref", orc.bvh_build(ts.vertices, ts.indices)), ("fast", _fast(ts.vertices, ts.indices))):
+        orc.set_full_sort(True)
+        orc.work_read(reset=True)
+        acc = orc.render_frames(arr, mats, tree["quad"], tree["prims"], cam, W, H, [0], 5, exact_math=False,
+                                textures=ts.textures, sky_tex=0)
+        w = orc.work_read(reset=True)
+        orc.set_full_sort(False)
+        out[name] = (w["ext_nodes"] / w["ext_rays"], w["ext_tris"] / w["ext_rays"], acc)
+    # 1.6-unit triangles here, so the reference's fixed box padding costs little;
+    # on the 0.2-unit triangles of a 1024-grid terrain the fast tree tests 22 % fewer
+    assert out["fast"][1] <= out["ref"][1]
+    assert out["fast"][0] + out["fast"][1] < 0.98 * (out["ref"][0] + out["ref"][1])
+    a, b = out["ref"][2], out["fast"][2]
+    rel = np.abs(a - b) / np.maximum(np.abs(a), 1e-6)
+    assert (rel > 1e-4).any(axis=1).mean() < 1e-3
+
+
+def test_fast_build_rejects_bad_input(lib):
+    from cudatracer_gb300 import _lib
+
+    v = np.array([[0, 0, 0], [1, 0, 0], [0, np.nan, 0]], np.float32)
+    with pytest.raises(_lib.CTError):
+        _fast(v, np.array([[0, 1, 2]], np.uint32))
+    v[2, 1] = 1.0
+    with pytest.raises(_lib.CTError):
+        _fast(v, np.array([[0, 1, 3]], np.uint32))
