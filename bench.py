@@ -267,20 +267,28 @@ def sphere_closest_hit(ctx):
     D = torch.from_numpy(np.tile(D, (64, 1))).cuda()
     hit = torch.empty(O.shape[0], dtype=torch.int32, device="cuda")
     t = torch.empty(O.shape[0], device="cuda")
-    for _ in range(3):
-        bvh.trace_closest(O, D, hit, t)
-    torch.cuda.synchronize()
-    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-    e0.record()
-    for _ in range(10):
-        bvh.trace_closest(O, D, hit, t)
-    e1.record()
-    torch.cuda.synchronize()
-    ms = e0.elapsed_time(e1) / 10
+
+    def rate(tree):
+        for _ in range(3):
+            tree.trace_closest(O, D, hit, t)
+        torch.cuda.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record()
+        for _ in range(10):
+            tree.trace_closest(O, D, hit, t)
+        e1.record()
+        torch.cuda.synchronize()
+        return O.shape[0] / (e0.elapsed_time(e1) / 10) / 1e3
+
+    mrays = rate(bvh)
+    fb = sc.build_bvh_fast()
+    mrays_fast = rate(fb)
+    fb.close()
     sc.close()
     bvh.close()
-    return {"mrays_per_s": O.shape[0] / ms / 1e3, "rays": int(O.shape[0]),
-            "workload": "81,920-tri sphere, 256x256 pinhole rays x64, ct_trace_closest"}
+    return {"mrays_per_s": mrays, "fast_tree_mrays_per_s": mrays_fast, "rays": int(O.shape[0]),
+            "workload": "81,920-tri sphere, 256x256 pinhole rays x64, ct_trace_closest (reference's tree; "
+                        "fast_tree_mrays_per_s: ct_bvh_build_fast's)"}
 
 
 def precision_soup(ctx, ntri: int = 10_000_000, nray: int = 16_000_000, sample_every: int = 8) -> dict:
@@ -386,7 +394,7 @@ def batching_jobs(ctx, n_jobs: int = 256, seed: int = 2024) -> dict:
                        ts.skybox_texture)
         p = api.default_params(side, side)
         p.max_depth = depth
-        jobs.append(dict(scene=sc, bvh=sc.build_bvh_device(), params=p, spp=spp,
+        jobs.append(dict(scene=sc, bvh=sc.build_bvh_fast(), params=p, spp=spp,
                          camera=api.Camera(side, side, cam["fov"], cam["position"], cam["forward"], cam["up"])))
         tris += ts.indices.shape[0]
     setup_s = time.perf_counter() - t0
@@ -431,6 +439,7 @@ def batching_jobs(ctx, n_jobs: int = 256, seed: int = 2024) -> dict:
         "ms": ms, "iterations": st["frames"], "tuning": tuning, "autotune_ms_per_iteration": tune_ms,
         "serial_plain_ms": serial_ms, "serial_plain_msamples_per_s": samples / serial_ms / 1e3,
         "speedup_vs_serial": serial_ms / ms, "setup_s": setup_s,
+        "tree": "ct_bvh_build_fast (host, all cores; in setup_s)",
     }
 
 
@@ -459,7 +468,7 @@ def serving_poisson(ctx, rate: float = 100.0, duration_s: float = 5.0, seed: int
         ts, cam = scenes.terrain_scene(grid=grid, spheres=sph, seed=100 + k, extent=200.0, sky_size=(256, 128))
         sc = ctx.scene(scenes.scene_arrays(ts), [api.Material(**m) for m in ts.materials], ts.textures,
                        ts.skybox_texture)
-        rscenes.append((sc, sc.build_bvh_device(), cam))
+        rscenes.append((sc, sc.build_bvh_fast(), cam))
     qbvhs = []
     for k, ntri in enumerate([10_000, 100_000, 1_000_000, 10_000_000]):
         s = scenes.soup_scene(ntri, seed=200 + k)
@@ -564,7 +573,7 @@ def serving_poisson(ctx, rate: float = 100.0, duration_s: float = 5.0, seed: int
         "mrays_per_s": rays / wall / 1e6, "wall_s": wall, "completed": st["completed"], "failed": st["failed"],
         "peak_request_bytes": st["peak_bytes"], "iterations": st["iterations"],
         "serial_plain_latency_ms": pct(slat), "serial_plain_busy_s": float(sum(svc)),
-        "iter_pixels": iter_pixels or (1 << 24), "setup_s": setup_s,
+        "iter_pixels": iter_pixels or (1 << 24), "setup_s": setup_s, "render_tree": "ct_bvh_build_fast",
     }
 
 

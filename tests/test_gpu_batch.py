@@ -169,3 +169,20 @@ def test_wide_batch_job_alone_equals_job_in_mix(gpu_ctx, scenes_):
                                              sort_key=2))
     for a, b in zip(mixed, srt):
         assert np.array_equal(a.view(np.int32), b.view(np.int32))
+
+
+def test_fast_tree_batch(gpu_ctx, scenes_):
+    """Batches on ct_bvh_build_fast's trees: independent of the mix, and equal
+    to the same batch on the reference's trees up to exact t ties."""
+    jobs = _mix(scenes_)
+    ref, _ = _run(gpu_ctx, jobs)
+    fast = {id(S["sc"]): S["sc"].build_bvh_fast() for S in scenes_}
+    for j in jobs:
+        j["bvh"] = fast[id(j["scene"])]
+    mixed, _ = _run(gpu_ctx, jobs)
+    for k in (0, 3, 5):
+        alone, _ = _run(gpu_ctx, [jobs[k]])
+        assert np.array_equal(alone[0].view(np.int32), mixed[k].view(np.int32)), k
+    for a, b in zip(mixed, ref):
+        rel = np.abs(a - b) / np.maximum(np.abs(b), 1e-6)
+        assert (rel > 1e-4).any(axis=-1).mean() < 2e-3
