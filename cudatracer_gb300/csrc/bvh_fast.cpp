@@ -18,7 +18,8 @@
 //    C(n, i) is the least cost of subtree n spread over i slots of its parent;
 //    a subtree of at most four primitives may become one leaf slot, charged
 //    area x 2 x ceil(count / 2) because the traversal tests a leaf's
-//    triangles two per round; an inner node is charged its area once.
+//    triangles two per round; an inner node is charged its area once;
+//  * the slots of a node in descending box area.
 //
 // The primitive order is the binary tree's leaf order (each subtree covers one
 // contiguous range), so every leaf slot is a contiguous range. The result does
@@ -273,6 +274,11 @@ void collapse(const std::vector<FNode>& nodes, const std::vector<Cost>& d, std::
     }
     emit(nodes, d, (uint32_t)n.l, bk, ch);
     emit(nodes, d, (uint32_t)n.r, 4 - bk, ch);
+    // largest box first: the any-hit step takes the lowest hit slot next, and a
+    // larger child is the likelier occluder (closest-hit frames sort by distance)
+    std::stable_sort(ch.begin(), ch.end(), [&](const Slot& a, const Slot& b) {
+      return farea(nodes[a.n].box) > farea(nodes[b.n].box);
+    });
     Item kids[4];
     int nk = 0;
     for (int i = 0; i < 4; i++) {

@@ -208,7 +208,7 @@ ct_status ct_bvh_build_device(ct_ctx* ctx, const ct_scene* scene, void* stream, 
  * reference's -0.001/+0.01; a binary SAH over 16 centroid bins per axis is
  * split to single triangles and collapsed to four-wide nodes by dynamic
  * programming over the surface-area cost, with leaves of at most four
- * triangles. Closest and any hits equal the reference tree's up to the winner
+ * triangles and each node's slots in descending box area. Closest and any hits equal the reference tree's up to the winner
  * of an exact t tie; fast-math frames on it are the fast-math frames on the
  * reference tree up to those ties (about 10 % fewer node and triangle tests
  * per ray on a terrain view). Exact-math frames run but follow this tree's
