@@ -295,7 +295,8 @@ def precision_soup(ctx, ntri: int = 10_000_000, nray: int = 16_000_000, sample_e
     """The precision workload: a 10M-triangle seeded soup (centroids U[0,1]^3,
     edges log-uniform 1e-4..1e-2) and 16M incoherent rays. Closest-hit Mrays/s
     of the plain quad BVH (reference Moller-Trumbore, epsilon 1e-12 since the
-    reference's 1e-3 culls every soup triangle) and of the 8-wide quantised BVH
+    reference's 1e-3 culls every soup triangle) on the reference's tree and on
+    ct_bvh_build_fast's, and of the 8-wide quantised BVH
     (watertight FP32 + FP64 settlement); ids, lost hits and t error of both
     against the FP64 watertight oracle on every 8th ray."""
     import numpy as np
@@ -334,6 +335,12 @@ def precision_soup(ctx, ntri: int = 10_000_000, nray: int = 16_000_000, sample_e
 
     q_trace = timed(lambda: qb.trace_closest(org, dirs, hit, t, tri_eps=1e-12))
     hq, tq = hit.cpu().numpy().copy(), t.cpu().numpy().copy()
+    t0 = time.perf_counter()
+    fb = sc.build_bvh_fast()
+    f_ms = (time.perf_counter() - t0) * 1e3
+    f_trace = timed(lambda: fb.trace_closest(org, dirs, hit, t, tri_eps=1e-12))
+    hf, tf = hit.cpu().numpy().copy(), t.cpu().numpy().copy()
+    fb.close()
     wb.wide_stats(reset=True)
     w_trace = timed(lambda: wb.trace_closest(org, dirs, hit, t))
     st = wb.wide_stats(reset=True)
@@ -354,6 +361,7 @@ def precision_soup(ctx, ntri: int = 10_000_000, nray: int = 16_000_000, sample_e
     out = {
         "workload": f"{ntri:,}-triangle soup, {nray:,} incoherent rays (origins U[0,1]^3, directions uniform)",
         "plain_quad_fp32": {"mrays_per_s": nray / q_trace / 1e3, "build_ms": q_ms, **against(hq, tq)},
+        "plain_quad_fp32_fast_tree": {"mrays_per_s": nray / f_trace / 1e3, "build_ms": f_ms, **against(hf, tf)},
         "wide8_q8": {"mrays_per_s": nray / w_trace / 1e3, "build_ms": w_ms, "nodes": wb.info()["quad_node_count"],
                      "node_bytes": 80, "fp64_retest_frac": st["fp64_retests"] / max(1, st["rays"]),
                      "fp64_full_traversals": st["fp64_full"], **against(hw, tw)},
@@ -361,6 +369,8 @@ def precision_soup(ctx, ntri: int = 10_000_000, nray: int = 16_000_000, sample_e
                          f"{int((ho >= 0).sum()):,} hits)",
     }
     out["speedup_wide_vs_plain"] = out["wide8_q8"]["mrays_per_s"] / out["plain_quad_fp32"]["mrays_per_s"]
+    out["speedup_wide_vs_plain_fast_tree"] = (out["wide8_q8"]["mrays_per_s"]
+                                              / out["plain_quad_fp32_fast_tree"]["mrays_per_s"])
     qb.close()
     wb.close()
     sc.close()
@@ -850,8 +860,10 @@ def run_ours(args, world, rank, local):
     c1 = sphere_closest_hit(ctx) if rank == 0 else None
     c3 = precision_soup(ctx) if (rank == 0 and not args.skip_precision) else None
     c4 = batching_jobs(ctx) if (rank == 0 and not args.skip_serving) else None
-    # the light end of the request-rate range and one where serial execution saturates
-    c5 = ([serving_poisson(ctx, duration_s=10.0), serving_poisson(ctx, rate=400.0, duration_s=2.0)]
+    # the light end of the request-rate range, one where serial execution saturates, and the
+    # top of the range (2,000 req/s), where the server saturates too
+    c5 = ([serving_poisson(ctx, duration_s=10.0), serving_poisson(ctx, rate=400.0, duration_s=2.0),
+           serving_poisson(ctx, rate=2000.0, duration_s=1.0)]
           if (rank == 0 and not args.skip_serving) else None)
     # our kernels in the timed region: per frame raygen + depth x (extend, shade,
     # connect) + the fold of a fast-math frame slot (the launch counts of the
