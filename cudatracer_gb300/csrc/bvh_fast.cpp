@@ -10,8 +10,9 @@
 //  * triangle boxes padded by 1e-5 x max(1, |coordinate|) per side (about 80
 //    float ulps), enough for the fast-math slab test never to lose a hit that
 //    a box touches, instead of the absolute padding;
-//  * a binary tree over centroid bins (16 per axis, all three axes) split down
-//    to one primitive per leaf;
+//  * a binary tree over centroid bins (16 per axis, all three axes; ranges of
+//    at most 16 primitives sweep every split of the centroid order exactly)
+//    split down to one primitive per leaf;
 //  * binary-to-quad conversion by dynamic programming over the surface-area
 //    cost (the optimal n-wide collapse of Ylitie, Karras and Laine, "Efficient
 //    Incoherent Ray Traversal on GPUs Through Compressed Wide BVHs", HPG 2017):
@@ -44,6 +45,7 @@ constexpr int kBins = 16;
 constexpr uint32_t kLeafMax = 4;   // largest leaf the collapse may make
 constexpr int kDepthLimit = 60;    // binary depth at which a node stays a leaf
 constexpr float kPad = 1e-5f;      // relative box padding per side
+constexpr uint32_t kSweepMax = 16; // ranges up to this size take the exact SAH sweep
 
 struct FBox {
   float mn[3], mx[3];
@@ -105,10 +107,9 @@ void bin_range(const FCtx& C, const float lo[3], const float scale[3], uint32_t 
   }
 }
 
-void build_node(const FCtx& C, uint32_t ni, int depth) {
-  FNode& n = C.nodes[ni];
-  const uint32_t first = n.first, count = n.count;
-  if (count <= 1 || depth >= kDepthLimit) return;
+// Binned SAH split of [first, first + count): partitions the range, returns
+// the left count.
+uint32_t binned_split(const FCtx& C, uint32_t first, uint32_t count) {
   FBox cb = fempty();
   for (uint32_t k = first; k < first + count; k++) {
     const float* c = C.cent + 3 * (size_t)C.prims[k];
@@ -169,6 +170,52 @@ void build_node(const FCtx& C, uint32_t ni, int depth) {
     mid = (uint32_t)(m - b);
     if (mid == 0 || mid == count) mid = count / 2;
   }
+  return mid;
+}
+
+// Exact SAH split of a small range: every split of the centroid order on
+// each axis (ties by primitive id). Reorders the range, returns the left count.
+uint32_t sweep_split(const FCtx& C, uint32_t first, uint32_t count) {
+  uint32_t ord[3][kSweepMax];
+  float best = 3e38f;
+  int bax = 0;
+  uint32_t bmid = count / 2;
+  for (int a = 0; a < 3; a++) {
+    uint32_t* o = ord[a];
+    for (uint32_t k = 0; k < count; k++) {
+      const uint32_t p = C.prims[first + k];
+      const float c = C.cent[3 * (size_t)p + a];
+      uint32_t j = k;
+      for (; j > 0; j--) {
+        const uint32_t q = o[j - 1];
+        const float cq = C.cent[3 * (size_t)q + a];
+        if (cq < c || (cq == c && q < p)) break;
+        o[j] = q;
+      }
+      o[j] = p;
+    }
+    float ra[kSweepMax];
+    FBox r = fempty();
+    for (uint32_t i = count - 1; i > 0; i--) {
+      fgrow(r, C.pb[o[i]]);
+      ra[i] = farea(r);
+    }
+    FBox l = fempty();
+    for (uint32_t i = 1; i < count; i++) {
+      fgrow(l, C.pb[o[i - 1]]);
+      const float cost = farea(l) * (float)i + ra[i] * (float)(count - i);
+      if (cost < best) best = cost, bax = a, bmid = i;
+    }
+  }
+  memcpy(C.prims + first, ord[bax], count * sizeof(uint32_t));
+  return bmid;
+}
+
+void build_node(const FCtx& C, uint32_t ni, int depth) {
+  FNode& n = C.nodes[ni];
+  const uint32_t first = n.first, count = n.count;
+  if (count <= 1 || depth >= kDepthLimit) return;
+  const uint32_t mid = count <= kSweepMax ? sweep_split(C, first, count) : binned_split(C, first, count);
   FBox lb = fempty(), rb = fempty();
   for (uint32_t k = first; k < first + mid; k++) fgrow(lb, C.pb[C.prims[k]]);
   for (uint32_t k = first + mid; k < first + count; k++) fgrow(rb, C.pb[C.prims[k]]);

@@ -43,15 +43,18 @@ def _check_structure(q, pr, v, ix, max_leaf=4):
 
 
 def _tie_ok(orc, v, ix, o, d, prim, t, eps):
-    """The oracle's triangle test alone on `prim` gives exactly t."""
+    """The oracle's triangle test alone on `prim` gives exactly t (one-triangle
+    tree from ct_host_bvh_build, whose root leaf stays traceable)."""
+    from cudatracer_gb300 import api
+
     tri = v[ix[prim].astype(np.int64)].astype(np.float32)
-    q1 = orc.bvh_build(tri, np.array([[0, 1, 2]], np.uint32))
+    q1 = api.host_bvh_build(tri, np.array([[0, 1, 2]], np.uint32), 1)
     h, t1 = orc.trace_closest(q1["quad"], q1["prims"], tri, np.array([[0, 1, 2]], np.uint32), o[None], d[None],
                               eps=eps)
     return h[0] == 0 and t1.view(np.int32)[0] == np.float32(t).view(np.int32)
 
 
-def _compare_hits(orc, v, ix, o, d, eps=1e-3, any_hit=True):
+def _compare_hits(orc, v, ix, o, d, eps=1e-3, any_hit=True, all_ties=False):
     from cudatracer_gb300 import api
 
     # the reference's tree (ct_host_bvh_build: equal to the oracle's build except
@@ -62,7 +65,8 @@ def _compare_hits(orc, v, ix, o, d, eps=1e-3, any_hit=True):
     fh, ft = orc.trace_closest(fast["quad"], fast["prims"], v, ix, o, d, eps=eps)
     assert np.array_equal(rt.view(np.int32), ft.view(np.int32))
     diff = np.nonzero(rh != fh)[0]
-    assert diff.size <= max(8, rh.size // 100)
+    if not all_ties:  # in a scene of coincident triangles every hit is a tie
+        assert diff.size <= max(8, rh.size // 100)
     for i in diff[:64]:
         assert rh[i] >= 0 and fh[i] >= 0 and _tie_ok(orc, v, ix, o[i, :3], d[i, :3], fh[i], ft[i], eps)
     if any_hit:
@@ -152,7 +156,7 @@ def test_fast_tree_degenerate_inputs(lib, orc):
     rng = np.random.default_rng(0)
     o2 = np.concatenate([rng.uniform(0, 0.5, size=(256, 2)), np.ones((256, 1))], 1).astype(np.float32)
     d2 = np.tile(np.array([[0, 0, -1.0]], np.float32), (256, 1))
-    _compare_hits(orc, v, ix, o2, d2, any_hit=False)
+    _compare_hits(orc, v, ix, o2, d2, any_hit=False, all_ties=True)
     # a stack of flat axis-aligned quads, 2 triangles each, at y = k
     quads = []
     for k in range(40):
