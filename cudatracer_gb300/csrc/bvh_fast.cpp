@@ -107,9 +107,21 @@ void bin_range(const FCtx& C, const float lo[3], const float scale[3], uint32_t 
   }
 }
 
-// Binned SAH split of [first, first + count): partitions the range, returns
-// the left count.
-uint32_t binned_split(const FCtx& C, uint32_t first, uint32_t count) {
+struct Cut {
+  uint32_t mid;  // primitives in the left child
+  FBox lb, rb;   // child boxes
+};
+
+// Boxes of the two halves of a range, by a pass over its primitives.
+void cut_boxes(const FCtx& C, uint32_t first, uint32_t count, Cut& c) {
+  c.lb = fempty(), c.rb = fempty();
+  for (uint32_t k = first; k < first + c.mid; k++) fgrow(c.lb, C.pb[C.prims[k]]);
+  for (uint32_t k = first + c.mid; k < first + count; k++) fgrow(c.rb, C.pb[C.prims[k]]);
+}
+
+// Binned SAH split of [first, first + count): partitions the range; the child
+// boxes are the unions of their bins (exact: a bin box is a min/max union).
+Cut binned_split(const FCtx& C, uint32_t first, uint32_t count) {
   FBox cb = fempty();
   for (uint32_t k = first; k < first + count; k++) {
     const float* c = C.cent + 3 * (size_t)C.prims[k];
@@ -161,21 +173,27 @@ uint32_t binned_split(const FCtx& C, uint32_t first, uint32_t count) {
       if (cost < best) best = cost, bax = a, bsp = i;
     }
   }
-  uint32_t mid = count / 2;  // all centroids in one bin: split the range in half
+  Cut c;
   if (bax >= 0) {
     uint32_t* b = C.prims + first;
     uint32_t* m = std::partition(b, b + count, [&](uint32_t p) {
       return bin_of(C.cent[3 * (size_t)p + bax], lo[bax], scale[bax]) < bsp;
     });
-    mid = (uint32_t)(m - b);
-    if (mid == 0 || mid == count) mid = count / 2;
+    c.mid = (uint32_t)(m - b);
+    if (c.mid > 0 && c.mid < count) {
+      c.lb = fempty(), c.rb = fempty();
+      for (int i = 0; i < kBins; i++) fgrow(i < bsp ? c.lb : c.rb, bins.box[bax][i]);
+      return c;
+    }
   }
-  return mid;
+  c.mid = count / 2;  // all centroids in one bin: split the range in half
+  cut_boxes(C, first, count, c);
+  return c;
 }
 
 // Exact SAH split of a small range: every split of the centroid order on
 // each axis (ties by primitive id). Reorders the range, returns the left count.
-uint32_t sweep_split(const FCtx& C, uint32_t first, uint32_t count) {
+Cut sweep_split(const FCtx& C, uint32_t first, uint32_t count) {
   uint32_t ord[3][kSweepMax];
   float best = 3e38f;
   int bax = 0;
@@ -208,17 +226,20 @@ uint32_t sweep_split(const FCtx& C, uint32_t first, uint32_t count) {
     }
   }
   memcpy(C.prims + first, ord[bax], count * sizeof(uint32_t));
-  return bmid;
+  Cut c;
+  c.mid = bmid;
+  cut_boxes(C, first, count, c);
+  return c;
 }
 
 void build_node(const FCtx& C, uint32_t ni, int depth) {
   FNode& n = C.nodes[ni];
   const uint32_t first = n.first, count = n.count;
   if (count <= 1 || depth >= kDepthLimit) return;
-  const uint32_t mid = count <= kSweepMax ? sweep_split(C, first, count) : binned_split(C, first, count);
-  FBox lb = fempty(), rb = fempty();
-  for (uint32_t k = first; k < first + mid; k++) fgrow(lb, C.pb[C.prims[k]]);
-  for (uint32_t k = first + mid; k < first + count; k++) fgrow(rb, C.pb[C.prims[k]]);
+  const Cut cut = count <= kSweepMax ? sweep_split(C, first, count) : binned_split(C, first, count);
+  const uint32_t mid = cut.mid;
+  const FBox& lb = cut.lb;
+  const FBox& rb = cut.rb;
   const uint32_t li = C.next->fetch_add(2), ri = li + 1;
   C.nodes[li] = FNode{lb, first, mid, -1, -1};
   C.nodes[ri] = FNode{rb, first + mid, count - mid, -1, -1};
