@@ -7,9 +7,12 @@
 // children are leaves keeps empty slots (one per node on average). This
 // builder keeps the reference's node and leaf formats and changes the tree:
 //
-//  * triangle boxes padded by 1e-5 x max(1, |coordinate|) per side (about 80
-//    float ulps), enough for the fast-math slab test never to lose a hit that
-//    a box touches, instead of the absolute padding;
+//  * triangle boxes padded per side by 1e-5 x max(|coordinate|, M / 4), M the
+//    largest vertex coordinate magnitude, instead of the absolute padding. The
+//    fast-math slab plane fma(b, 1/d, -o/d) errs by about 1.2e-7 |o| + 6e-8 |b|
+//    in distance, so a ray whose origin lies within about 10 M of the scene's
+//    centre of coordinates (every secondary ray, and cameras in that range)
+//    never loses a box that holds its hit;
 //  * a binary tree over centroid bins (16 per axis, all three axes; ranges of
 //    at most 16 primitives sweep every split of the centroid order exactly)
 //    split down to one primitive per leaf;
@@ -54,8 +57,11 @@ inline FBox fempty() { return {{1e34f, 1e34f, 1e34f}, {-1e34f, -1e34f, -1e34f}};
 inline void fgrow(FBox& b, const FBox& o) {
   for (int k = 0; k < 3; k++) b.mn[k] = std::min(b.mn[k], o.mn[k]), b.mx[k] = std::max(b.mx[k], o.mx[k]);
 }
-inline float farea(const FBox& b) {
-  const float dx = b.mx[0] - b.mn[0], dy = b.mx[1] - b.mn[1], dz = b.mx[2] - b.mn[2];
+// Surface area with the extents scaled by s, a power of two chosen from the
+// scene's extent: exact scaling, so the cost comparisons are those of the
+// unscaled areas wherever those are finite, and finite for any float scene.
+inline float farea(const FBox& b, float s) {
+  const float dx = (b.mx[0] - b.mn[0]) * s, dy = (b.mx[1] - b.mn[1]) * s, dz = (b.mx[2] - b.mn[2]) * s;
   if (dx < 0.0f) return 0.0f;
   return 2.0f * (dx * dy + dy * dz + dz * dx);
 }
@@ -87,6 +93,7 @@ struct FCtx {
   std::atomic<uint32_t>* next;
   std::atomic<int>* busy;
   int nthreads;
+  float scale;  // area scale (farea)
 };
 
 inline int bin_of(float c, float lo, float scale) {
@@ -161,7 +168,7 @@ Cut binned_split(const FCtx& C, uint32_t first, uint32_t count) {
     for (int i = kBins - 1; i > 0; i--) {
       fgrow(r, bins.box[a][i]);
       rc += bins.cnt[a][i];
-      ra[i] = farea(r), rn[i] = rc;
+      ra[i] = farea(r, C.scale), rn[i] = rc;
     }
     FBox l = fempty();
     uint32_t lc = 0;
@@ -169,7 +176,7 @@ Cut binned_split(const FCtx& C, uint32_t first, uint32_t count) {
       fgrow(l, bins.box[a][i - 1]);
       lc += bins.cnt[a][i - 1];
       if (lc == 0 || rn[i] == 0) continue;
-      const float cost = farea(l) * (float)lc + ra[i] * (float)rn[i];
+      const float cost = farea(l, C.scale) * (float)lc + ra[i] * (float)rn[i];
       if (cost < best) best = cost, bax = a, bsp = i;
     }
   }
@@ -216,12 +223,12 @@ Cut sweep_split(const FCtx& C, uint32_t first, uint32_t count) {
     FBox r = fempty();
     for (uint32_t i = count - 1; i > 0; i--) {
       fgrow(r, C.pb[o[i]]);
-      ra[i] = farea(r);
+      ra[i] = farea(r, C.scale);
     }
     FBox l = fempty();
     for (uint32_t i = 1; i < count; i++) {
       fgrow(l, C.pb[o[i - 1]]);
-      const float cost = farea(l) * (float)i + ra[i] * (float)(count - i);
+      const float cost = farea(l, C.scale) * (float)i + ra[i] * (float)(count - i);
       if (cost < best) best = cost, bax = a, bmid = i;
     }
   }
@@ -270,11 +277,11 @@ struct Cost {
   int8_t split[5];  // with i slots: 0 = as with i - 1, else slots given to the left subtree
 };
 
-void solve(const std::vector<FNode>& nodes, uint32_t used, std::vector<Cost>& d) {
+void solve(const std::vector<FNode>& nodes, uint32_t used, float scale, std::vector<Cost>& d) {
   d.assign(used, Cost{});
   for (uint32_t x = used; x-- > 0;) {  // children are numbered after their parent
     const FNode& n = nodes[x];
-    const float A = farea(n.box);
+    const float A = farea(n.box, scale);
     Cost& e = d[x];
     float leaf = 3e38f;
     if (n.count <= kLeafMax || n.l < 0) leaf = A * (float)(2 * ((n.count + 1) / 2));
@@ -322,7 +329,7 @@ void set_slot(QuadNode& q, int i, const FBox& b) {
 }
 
 // quad nodes in pre-order from node qi (binary inner node bn); iterative
-void collapse(const std::vector<FNode>& nodes, const std::vector<Cost>& d, std::vector<QuadNode>& quad) {
+void collapse(const std::vector<FNode>& nodes, const std::vector<Cost>& d, float scale, std::vector<QuadNode>& quad) {
   struct Item {
     uint32_t qi, bn;
   };
@@ -345,7 +352,7 @@ void collapse(const std::vector<FNode>& nodes, const std::vector<Cost>& d, std::
     // largest box first: the any-hit step takes the lowest hit slot next, and a
     // larger child is the likelier occluder (closest-hit frames sort by distance)
     std::stable_sort(ch.begin(), ch.end(), [&](const Slot& a, const Slot& b) {
-      return farea(nodes[a.n].box) > farea(nodes[b.n].box);
+      return farea(nodes[a.n].box, scale) > farea(nodes[b.n].box, scale);
     });
     Item kids[4];
     int nk = 0;
@@ -380,6 +387,12 @@ void build_fast_quad(const float* verts, const uint32_t* idx, uint32_t ntri, int
   out.quad.clear();
   out.prims.assign(ntri, 0);
   if (ntri == 0) return;
+  float M = 0.0f;  // largest coordinate magnitude of the triangles' vertices
+  for (uint64_t i = 0; i < 3ull * ntri; i++) {
+    const float* p = verts + 3 * (size_t)idx[i];
+    M = std::max(M, std::max(std::fabs(p[0]), std::max(std::fabs(p[1]), std::fabs(p[2]))));
+  }
+  const float floor_mag = 0.25f * M;
   std::vector<FBox> pb(ntri);
   std::vector<float> cent(3 * (size_t)ntri);
   auto prep = [&](uint32_t b, uint32_t e) {
@@ -390,7 +403,7 @@ void build_fast_quad(const float* verts, const uint32_t* idx, uint32_t ntri, int
       FBox& t = pb[i];
       for (int k = 0; k < 3; k++) {
         float mn = std::min(p0[k], std::min(p1[k], p2[k])), mx = std::max(p0[k], std::max(p1[k], p2[k]));
-        const float pad = kPad * std::max(1.0f, std::max(std::fabs(mn), std::fabs(mx)));
+        const float pad = kPad * std::max(floor_mag, std::max(std::fabs(mn), std::fabs(mx)));
         mn -= pad, mx += pad;
         t.mn[k] = mn, t.mx[k] = mx;
         cent[3 * (size_t)i + k] = 0.5f * (mn + mx);
@@ -414,7 +427,17 @@ void build_fast_quad(const float* verts, const uint32_t* idx, uint32_t ntri, int
   nodes[0] = FNode{root, 0, ntri, -1, -1};
   std::atomic<uint32_t> next{1};
   std::atomic<int> busy{0};
-  const FCtx C{pb.data(), cent.data(), out.prims.data(), nodes.data(), &next, &busy, nthreads};
+  // 2^-e with the largest root extent in [2^(e-1), 2^e): scaled extents below 1
+  float scale = 1.0f;
+  {
+    const float ext = std::max(root.mx[0] - root.mn[0], std::max(root.mx[1] - root.mn[1], root.mx[2] - root.mn[2]));
+    if (ext > 0.0f && std::isfinite(ext)) {
+      int e = 0;
+      std::frexp(ext, &e);
+      scale = std::ldexp(1.0f, -e);
+    }
+  }
+  const FCtx C{pb.data(), cent.data(), out.prims.data(), nodes.data(), &next, &busy, nthreads, scale};
   build_node(C, 0, 0);
   const auto t1 = std::chrono::high_resolution_clock::now();
   out.build_ms = std::chrono::duration<double, std::milli>(t1 - t0).count();
@@ -430,8 +453,8 @@ void build_fast_quad(const float* verts, const uint32_t* idx, uint32_t ntri, int
     for (int i = 1; i < 4; i++) set_slot(q, i, none), q.childs[i] = -1, q.counts[i] = 0;
   } else {
     std::vector<Cost> d;
-    solve(nodes, used, d);
-    collapse(nodes, d, out.quad);
+    solve(nodes, used, scale, d);
+    collapse(nodes, d, scale, out.quad);
   }
   const auto t2 = std::chrono::high_resolution_clock::now();
   out.collapse_ms = std::chrono::duration<double, std::milli>(t2 - t1).count();

@@ -204,8 +204,11 @@ ct_status ct_bvh_import_binary(ct_ctx* ctx, const ct_scene* scene, const void* n
 ct_status ct_bvh_build_device(ct_ctx* ctx, const ct_scene* scene, void* stream, ct_bvh** out);
 /* Quad tree built for traversal speed (no reference counterpart; same node and
  * leaf formats, so every trace and frame entry point takes it). Triangle boxes
- * are padded by 1e-5 x max(1, |coordinate|) per side instead of the
- * reference's -0.001/+0.01; a binary SAH over 16 centroid bins per axis is
+ * are padded by 1e-5 x max(|coordinate|, M / 4) per side, M the largest vertex
+ * coordinate magnitude, instead of the reference's -0.001/+0.01: the
+ * fast-math slab test keeps every box holding a hit for ray origins within
+ * about 10 M in magnitude (every secondary ray; cameras in that range); a
+ * binary SAH over 16 centroid bins per axis is
  * split to single triangles and collapsed to four-wide nodes by dynamic
  * programming over the surface-area cost, with leaves of at most four
  * triangles and each node's slots in descending box area. Closest and any hits equal the reference tree's up to the winner

@@ -211,3 +211,62 @@ def test_fast_build_rejects_bad_input(lib):
     v[2, 1] = 1.0
     with pytest.raises(_lib.CTError):
         _fast(v, np.array([[0, 1, 3]], np.uint32))
+
+
+def _fma_slab_hits(lo, hi, o, d):
+    """The fast-math slab test of the traversal kernels for one box per ray:
+    inv = 1/d and nox = -o * inv in float32, each plane fmaf(b, inv, nox)
+    (emulated: the float64 product is exact, the sum is rounded to float64 and
+    then to float32), hit when tmax > 0 and tmin <= tmax."""
+    inv = (np.float32(1.0) / d.astype(np.float32)).astype(np.float32)
+    nox = (-o.astype(np.float32) * inv).astype(np.float32)
+    t1 = (lo.astype(np.float64) * inv + nox).astype(np.float32)
+    t2 = (hi.astype(np.float64) * inv + nox).astype(np.float32)
+    tmin = np.minimum(t1, t2).max(axis=1)
+    tmax = np.maximum(t1, t2).min(axis=1)
+    return (tmax > 0) & (tmin <= tmax)
+
+
+@pytest.mark.parametrize("which", ["terrain", "soup"])
+def test_fast_padding_keeps_grazing_hits(lib, small_terrain, which):
+    """Rays from origins up to 10 M away (M: largest coordinate magnitude) aimed
+    just inside a triangle next to the vertex that defines a face of its box:
+    the leaf slot box that holds the triangle passes the kernels' fast-math
+    slab test for every ray; without padding the same rays lose boxes."""
+    from cudatracer_gb300 import scenes
+
+    if which == "terrain":
+        v, ix = small_terrain[0].vertices, small_terrain[0].indices
+    else:
+        s = scenes.soup_scene(20000, seed=6)
+        v, ix = s.vertices, s.indices
+    f = _fast(v, ix)
+    q, pr = f["quad"], f["prims"]
+    qf = q.view(np.float32)
+    box_of = np.zeros((pr.size, 2, 3), np.float32)
+    for n, sl in zip(*np.nonzero(q[:, 28:32] > 0)):
+        first, c = q[n, 24 + sl], q[n, 28 + sl]
+        box_of[pr[first:first + c], 0] = qf[n, [sl, 8 + sl, 16 + sl]]
+        box_of[pr[first:first + c], 1] = qf[n, [4 + sl, 12 + sl, 20 + sl]]
+    M = float(np.abs(v).max())
+    rng = np.random.default_rng(8)
+    n = 40000
+    tri = rng.integers(0, ix.shape[0], size=n)
+    P = v[ix[tri].astype(np.int64)].astype(np.float64)  # (n, 3 vertices, 3)
+    axis = rng.integers(0, 3, size=n)
+    side = rng.integers(0, 2, size=n)
+    key = np.where(side[:, None] == 0, P[np.arange(n), :, axis], -P[np.arange(n), :, axis])
+    k = key.argmin(axis=1)  # the vertex that defines the box face on (axis, side)
+    e = 1e-4
+    target = (1 - 2 * e) * P[np.arange(n), k] + e * P[np.arange(n), (k + 1) % 3] + e * P[np.arange(n), (k + 2) % 3]
+    for R in (0.5 * M, 2.0 * M, 10.0 * M):
+        u = rng.normal(size=(n, 3))
+        u /= np.linalg.norm(u, axis=1, keepdims=True)
+        o = (target + R * u).astype(np.float32)
+        d = target - o.astype(np.float64)
+        d = (d / np.linalg.norm(d, axis=1, keepdims=True)).astype(np.float32)
+        ok = _fma_slab_hits(box_of[tri, 0], box_of[tri, 1], o, d)
+        assert ok.all(), (R / M, int((~ok).sum()))
+    # the check has teeth: exact (unpadded) triangle boxes lose some of these rays
+    lo, hi = P.min(axis=1).astype(np.float32), P.max(axis=1).astype(np.float32)
+    assert (~_fma_slab_hits(lo, hi, o, d)).sum() > 0
