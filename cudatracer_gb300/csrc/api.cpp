@@ -12,6 +12,7 @@
 #include <mutex>
 #include <string>
 #include <thread>
+#include <new>
 #include <vector>
 
 #include "bvh_build.h"
@@ -495,8 +496,13 @@ ct_status ct_bvh_build(ct_ctx* ctx, const ct_scene* scene, int32_t nthreads, ct_
   ct_status s = set_device(ctx);
   if (s != CT_OK) return s;
   auto* b = new ct_bvh();
-  build_binary(scene->verts.data(), scene->idx.data(), scene->nt, nthreads, b->host);
-  collapse_quad(b->host);
+  try {
+    build_binary(scene->verts.data(), scene->idx.data(), scene->nt, nthreads, b->host);
+    collapse_quad(b->host);
+  } catch (const std::bad_alloc&) {
+    delete b;
+    return fail(ctx, CT_ERR_OUT_OF_MEMORY, "host allocation failed while building the BVH");
+  }
   if ((s = finish_bvh(ctx, scene, b)) != CT_OK) {
     free_all(ctx, b->allocs);
     delete b;
@@ -512,7 +518,12 @@ ct_status ct_bvh_build_fast(ct_ctx* ctx, const ct_scene* scene, int32_t nthreads
   ct_status s = set_device(ctx);
   if (s != CT_OK) return s;
   auto* b = new ct_bvh();
-  build_fast_quad(scene->verts.data(), scene->idx.data(), scene->nt, nthreads, b->host);
+  try {
+    build_fast_quad(scene->verts.data(), scene->idx.data(), scene->nt, nthreads, b->host);
+  } catch (const std::bad_alloc&) {
+    delete b;
+    return fail(ctx, CT_ERR_OUT_OF_MEMORY, "host allocation failed while building the BVH");
+  }
   if ((s = finish_bvh(ctx, scene, b)) != CT_OK) {
     free_all(ctx, b->allocs);
     delete b;
@@ -827,8 +838,13 @@ ct_status ct_host_bvh_build(const float* vertices, uint32_t vertex_count, const 
   for (uint64_t i = 0; i < 3ull * triangle_count; i++)
     if (indices[i] >= vertex_count) return CT_ERR_INVALID_ARGUMENT;
   auto* h = new ct_host_bvh();
-  build_binary(vertices, indices, triangle_count, nthreads, h->host);
-  collapse_quad(h->host);
+  try {
+    build_binary(vertices, indices, triangle_count, nthreads, h->host);
+    collapse_quad(h->host);
+  } catch (const std::bad_alloc&) {
+    delete h;
+    return CT_ERR_OUT_OF_MEMORY;
+  }
   *out = h;
   return CT_OK;
 }
@@ -842,7 +858,12 @@ ct_status ct_host_bvh_build_fast(const float* vertices, uint32_t vertex_count, c
   for (uint64_t i = 0; i < 3ull * triangle_count; i++)
     if (indices[i] >= vertex_count) return CT_ERR_INVALID_ARGUMENT;
   auto* h = new ct_host_bvh();
-  build_fast_quad(vertices, indices, triangle_count, nthreads, h->host);
+  try {
+    build_fast_quad(vertices, indices, triangle_count, nthreads, h->host);
+  } catch (const std::bad_alloc&) {
+    delete h;
+    return CT_ERR_OUT_OF_MEMORY;
+  }
   *out = h;
   return CT_OK;
 }

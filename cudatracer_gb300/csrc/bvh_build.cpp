@@ -20,6 +20,7 @@
 #include <chrono>
 #include <cmath>
 #include <cstring>
+#include <system_error>
 #include <thread>
 
 #include "ct_internal.h"
@@ -119,7 +120,11 @@ void build_node(const Ctx& C, uint32_t ni, unsigned depth) {
     const uint32_t chunk = (count + want - 1) / want;
     for (int t = 0; t < want; t++) {
       const uint32_t b = first + t * chunk, e = std::min(first + count, b + chunk);
-      ts.emplace_back([&, t, b, e] { bin_range(C, planes, b, e, part[t]); });
+      try {
+        ts.emplace_back([&, t, b, e] { bin_range(C, planes, b, e, part[t]); });
+      } catch (const std::system_error&) {
+        bin_range(C, planes, b, e, part[t]);
+      }
     }
     for (auto& th : ts) th.join();
     bins = part[0];
@@ -187,8 +192,12 @@ void build_node(const Ctx& C, uint32_t ni, unsigned depth) {
   std::thread th;
   if (lc > 16384 && count - lc > 16384) {
     if (C.busy->fetch_add(1) < C.nthreads - 1) {
-      th = std::thread([&C, li, depth] { build_node(C, li, depth); });
-      spawned = true;
+      try {
+        th = std::thread([&C, li, depth] { build_node(C, li, depth); });
+        spawned = true;
+      } catch (const std::system_error&) {  // no thread to be had: build it here
+        C.busy->fetch_sub(1);
+      }
     } else {
       C.busy->fetch_sub(1);
     }
@@ -260,7 +269,11 @@ void build_binary(const float* verts, const uint32_t* idx, uint32_t ntri, int nt
     for (int t = 0; t < nthreads; t++) {
       const uint32_t b = t * chunk, e = std::min(ntri, b + chunk);
       if (b >= e) break;
-      ts.emplace_back(prep, b, e);
+      try {
+        ts.emplace_back(prep, b, e);
+      } catch (const std::system_error&) {
+        prep(b, e);
+      }
     }
     for (auto& th : ts) th.join();
   }

@@ -36,6 +36,7 @@
 #include <atomic>
 #include <chrono>
 #include <cmath>
+#include <system_error>
 #include <thread>
 #include <vector>
 
@@ -149,7 +150,11 @@ Cut binned_split(const FCtx& C, uint32_t first, uint32_t count) {
     const uint32_t chunk = (count + want - 1) / want;
     for (int t = 0; t < want; t++) {
       const uint32_t b = first + t * chunk, e = std::min(first + count, b + chunk);
-      ts.emplace_back([&, t, b, e] { bin_range(C, lo, scale, b, e, part[t]); });
+      try {
+        ts.emplace_back([&, t, b, e] { bin_range(C, lo, scale, b, e, part[t]); });
+      } catch (const std::system_error&) {
+        bin_range(C, lo, scale, b, e, part[t]);
+      }
     }
     for (auto& th : ts) th.join();
     bins = part[0];
@@ -256,8 +261,12 @@ void build_node(const FCtx& C, uint32_t ni, int depth) {
   std::thread th;
   if (mid > 16384 && count - mid > 16384) {
     if (C.busy->fetch_add(1) < C.nthreads - 1) {
-      th = std::thread([&C, li, depth] { build_node(C, li, depth + 1); });
-      spawned = true;
+      try {
+        th = std::thread([&C, li, depth] { build_node(C, li, depth + 1); });
+        spawned = true;
+      } catch (const std::system_error&) {  // no thread to be had: build it here
+        C.busy->fetch_sub(1);
+      }
     } else {
       C.busy->fetch_sub(1);
     }
@@ -417,7 +426,11 @@ void build_fast_quad(const float* verts, const uint32_t* idx, uint32_t ntri, int
     for (int t = 0; t < nthreads; t++) {
       const uint32_t b = t * chunk, e = std::min(ntri, b + chunk);
       if (b >= e) break;
-      ts.emplace_back(prep, b, e);
+      try {
+        ts.emplace_back(prep, b, e);
+      } catch (const std::system_error&) {
+        prep(b, e);
+      }
     }
     for (auto& th : ts) th.join();
   }

@@ -25,7 +25,7 @@ extern "C" {
 typedef enum ct_status {
   CT_OK = 0,
   CT_ERR_INVALID_ARGUMENT = 1, /* NULL pointer, bad size, index out of range, non-finite vertex */
-  CT_ERR_OUT_OF_MEMORY = 2,    /* device allocation refused (or the context's HBM budget exceeded) */
+  CT_ERR_OUT_OF_MEMORY = 2,    /* device allocation refused, the context's HBM budget exceeded, or a host BVH build's allocation failed */
   CT_ERR_CUDA = 3,             /* a CUDA runtime call failed; see ct_last_error */
   CT_ERR_UNSUPPORTED = 4,      /* e.g. a BVH whose leaves cannot be encoded */
   CT_ERR_TIMEOUT = 5,          /* a bounded device-side wait ran out */
