@@ -56,3 +56,18 @@ def test_two_replica_ranks_time_the_slowest_and_rank0_reports():
     assert res[1][4] < 1.0  # the reference arm's rank 1 returns at once
     assert all(p.exitcode == 0 for p in procs)
 
+
+
+def test_profiled_traffic_keys():
+    """The bench's traffic figures come from the committed extend summary: one
+    pair of keys for frames on the fast tree and one for the reference's tree,
+    each read from its own line (one key is a suffix of the other)."""
+    import bench
+
+    fast = bench.profiled_traffic("dram_bytes_per_extension_ray")
+    ref = bench.profiled_traffic("reference_tree_dram_bytes_per_extension_ray")
+    l2_fast = bench.profiled_traffic("l2_bytes_per_extension_ray")
+    l2_ref = bench.profiled_traffic("reference_tree_l2_bytes_per_extension_ray")
+    assert None not in (fast, ref, l2_fast, l2_ref)
+    assert 0 < fast < ref and 0 < l2_fast < l2_ref
+    assert fast < l2_fast and ref < l2_ref
