@@ -1,20 +1,24 @@
 #!/usr/bin/env python
 """Benchmark: path-traced Msamples/s of the wavefront tracer on one GB300.
 
-Workload (one step = one 1-spp frame, the reference's launchKernels):
+Workload (one step = one 64-frame accumulation: Params::reset, then 64 calls
+of the reference's launchKernels, each a 1-spp frame):
   1920x1080, max depth 8, quad BVH, FP32 RGBA accumulation, over a seeded
   fBm-displaced 1024x1024-vertex terrain (2,093,058 triangles) + 200
   icospheres of 5,120 triangles (radii U[0.5,3]) + 4 emissive quads, with a
   2048x1024 FP32 equirect sky (3,117,066 triangles). Synthetic, seeded data.
-  Reference shading (compat mode), CUDA float transcendentals.
+  Reference shading (compat mode). Math mode (--math): exact-shade (default:
+  bit-reproducible ray generation and shading with the fast traversal; whole
+  1080p frames within 1e-4 of the oracle per pixel), fast (CUDA float
+  transcendentals) or exact (bit-identical to the oracle, frames in sequence).
 
-    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl reference]
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl reference] [--math M]
 
 Prints one JSON line (rank 0). `value` is device-resident throughput; `e2e`
-is the same through the C ABI with the presented frame read back to pinned
-host memory every step. Under torchrun each rank renders its own replica
-(the tracer does not shard), and value sums all ranks' samples over the
-slowest rank's time.
+is the same through the C ABI with every frame presented and read back to
+pinned host memory. Under torchrun each rank renders its own replica (the
+tracer does not shard), and value sums all ranks' samples over the slowest
+rank's time.
 """
 from __future__ import annotations
 
@@ -33,21 +37,28 @@ sys.path.insert(0, ROOT)
 sys.path.insert(0, os.path.join(ROOT, "oracle"))
 
 W, H, DEPTH = 1920, 1080, 8
+FRAMES_PER_STEP = 64  # 1 spp per frame for 64 frames
+MATH = {"fast": 0, "exact": 1, "exact-shade": 2}  # CT_MATH_*
 METRIC = "Msamples/s path-traced"
 UNIT = "Msamples/s"
-WORKLOAD = "wavefront path tracing 1920x1080 1spp/frame depth 8, 3.12M-tri fBm terrain + 200 spheres, quad BVH"
+WORKLOAD = ("wavefront path tracing 1920x1080, 64 frames of 1 spp per step, depth 8, 3.12M-tri fBm terrain + "
+            "200 spheres, quad BVH")
 
 
 def parse_args():
+    global W, H, FRAMES_PER_STEP
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=64)
+    ap.add_argument("--steps", type=int, default=10, help="timed steps (64-frame accumulations)")
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
     ap.add_argument("--cpu-seconds", type=float, default=12.0, help="CPU-baseline sample budget")
-    ap.add_argument("--exact-math", action="store_true")
+    ap.add_argument("--math", choices=sorted(MATH), default="exact-shade",
+                    help="math mode of the headline frames (CT_MATH_*)")
+    ap.add_argument("--frames-per-step", type=int, default=FRAMES_PER_STEP,
+                    help="frames accumulated per step (smaller for profiler captures)")
     ap.add_argument("--tree", choices=["fast", "reference"], default="fast",
-                    help="tree traced by fast-math frames (exact-math frames always trace the reference's)")
+                    help="tree traced by frames with the fast traversal (exact frames always trace the reference's)")
     ap.add_argument("--width", type=int, default=1920, help="smaller frames for profiler captures")
     ap.add_argument("--height", type=int, default=1080)
     ap.add_argument("--skip-extras", action="store_true",
@@ -62,8 +73,8 @@ def parse_args():
     ap.add_argument("--skip-precision", action="store_true",
                     help="leave out the 10M-triangle precision workload (wide vs quad BVH against FP64)")
     args = ap.parse_args()
-    global W, H
-    W, H = args.width, args.height
+    W, H, FRAMES_PER_STEP = args.width, args.height, args.frames_per_step
+    args.math_mode = MATH[args.math]
     return args
 
 
@@ -641,10 +652,11 @@ def run_ours(args, world, rank, local):
         t0 = time.perf_counter()
         sc.build_bvh_device().close()
         dev_build.append((time.perf_counter() - t0) * 1e3)
-    # fast-math frames trace the tree built for traversal speed (equal hits up to
-    # exact t ties); exact-math frames keep the reference's tree
+    # frames with the fast traversal trace the tree built for traversal speed
+    # (equal hits up to exact t ties); exact frames keep the reference's tree
+    math = args.math_mode
     t0 = time.perf_counter()
-    fast_bvh = None if (args.exact_math or args.tree == "reference") else sc.build_bvh_fast()
+    fast_bvh = None if (math == MATH["exact"] or args.tree == "reference") else sc.build_bvh_fast()
     fast_build_ms = (time.perf_counter() - t0) * 1e3
     bvh = ref_bvh if fast_bvh is None else fast_bvh
     hinfo = None
@@ -654,106 +666,116 @@ def run_ours(args, world, rank, local):
         hb.close()
     job = api.RenderJob(ctx, W, H)
     camera = api.Camera(W, H, cam["fov"], cam["position"], cam["forward"], cam["up"])
-    params = api.Params(W, H, camera=camera, max_depth=DEPTH, exact_math=args.exact_math)
     stream = torch.cuda.Stream()
-    params.reset(job, stream)
-    for _ in range(args.warmup):
-        api.launch_kernels(job, sc, bvh, params, stream=stream)
-    stream.synchronize()
-    job.stats(reset=True, stream=stream)
-    clocks = Clocks(local)
-    barrier(world)
-    torch.cuda.synchronize()
-    clocks.start()
     e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-    e0.record(stream)
-    for _ in range(args.steps):
-        api.launch_kernels(job, sc, bvh, params, stream=stream)
-    e1.record(stream)
-    stream.synchronize()
-    torch.cuda.synchronize()
-    barrier(world)
-    clk = clocks.stop()
-    ms = e0.elapsed_time(e1)
-    ctx.check(stream)
-    st = job.stats(reset=True, stream=stream)
+
+    def accumulation(tree, mode, frames=None, present=None, host=None):
+        """One step: Params::reset, then `frames` launchKernels calls (1-spp
+        frames, seeds advancing by 2); with `present`, every frame is presented
+        (draw_framebuffer) and read back to pinned host memory."""
+        p = api.Params(W, H, camera=camera, max_depth=DEPTH, exact_math=mode)
+        p.reset(job, stream)
+        for _ in range(FRAMES_PER_STEP if frames is None else frames):
+            api.launch_kernels(job, sc, tree, p, present_out=present, stream=stream)
+            if host is not None:
+                with torch.cuda.stream(stream):
+                    host.copy_(present, non_blocking=True)
+
+    def timed(tree, mode, steps, warmup, clocks=None, **kw):
+        """CUDA-event time (and host wall time) of `steps` accumulations after
+        `warmup` untimed ones, bracketed by barriers and synchronisation."""
+        for _ in range(warmup):
+            accumulation(tree, mode, **kw)
+        stream.synchronize()
+        job.stats(reset=True, stream=stream)
+        barrier(world)
+        torch.cuda.synchronize()
+        if clocks is not None:
+            clocks.start()
+        w0 = time.perf_counter()
+        e0.record(stream)
+        for _ in range(steps):
+            accumulation(tree, mode, **kw)
+        e1.record(stream)
+        stream.synchronize()
+        wall = (time.perf_counter() - w0) * 1e3
+        torch.cuda.synchronize()
+        barrier(world)
+        clk = clocks.stop() if clocks is not None else None
+        ctx.check(stream)
+        return e0.elapsed_time(e1), wall, clk, job.stats(reset=True, stream=stream)
+
+    clocks = Clocks(local)
+    ms, _, clk, st = timed(bvh, math, args.steps, args.warmup, clocks=clocks)
+    ms_max = max_over_ranks(ms, world)
+    frames = FRAMES_PER_STEP * args.steps
     # stage times: a separate pass with per-launch events, frames one after another
     # (the timed frames overlap on ten streams, where an interval is not one kernel)
     job.profile(True)
     job.profile_read(reset=True)
-    prof_frames = max(4, args.steps // 4)
-    for _ in range(prof_frames):
-        api.launch_kernels(job, sc, bvh, params, stream=stream)
+    prof_frames = 16
+    accumulation(bvh, math, frames=prof_frames)
     stream.synchronize()
     prof = job.profile_read(reset=True)
     job.profile(False)
     prof_st = job.stats(reset=True, stream=stream)
-    ms_max = max_over_ranks(ms, world)
-    # the same frames on the reference's tree, timed the same way
+
+    def rate(ms_, steps_):
+        return world * W * H * FRAMES_PER_STEP * steps_ / (max_over_ranks(ms_, world) / 1e3) / 1e6
+
+    # every math mode, and the headline mode on the reference's tree, timed the same way
+    modes = None
     ref_tree = None
-    if fast_bvh is not None and not args.skip_extras:
-        pr_ = api.Params(W, H, camera=camera, max_depth=DEPTH, exact_math=False)
-        pr_.reset(job, stream)
-        for _ in range(args.warmup):
-            api.launch_kernels(job, sc, ref_bvh, pr_, stream=stream)
-        stream.synchronize()
-        barrier(world)
-        torch.cuda.synchronize()
-        e0.record(stream)
-        for _ in range(args.steps):
-            api.launch_kernels(job, sc, ref_bvh, pr_, stream=stream)
-        e1.record(stream)
-        stream.synchronize()
-        barrier(world)
-        ms_ref = max_over_ranks(e0.elapsed_time(e1), world)
-        job.profile(True)
-        job.profile_read(reset=True)
-        for _ in range(prof_frames):
-            api.launch_kernels(job, sc, ref_bvh, pr_, stream=stream)
-        stream.synchronize()
-        prof_ref = job.profile_read(reset=True)
-        job.profile(False)
-        job.stats(reset=True, stream=stream)
-        ref_tree = {"value": world * W * H * args.steps / (ms_ref / 1e3) / 1e6, "unit": UNIT,
-                    "ms_per_step": ms_ref / args.steps, "stage_ms": {k: v["ms"] for k, v in prof_ref.items()},
-                    "tree": "the reference's SAH + MergeNodes quad tree (device build)",
-                    "quad_nodes": info["quad_node_count"]}
-    samples = W * H * args.steps
+    if not args.skip_extras:
+        modes = {}
+        for name, mode in MATH.items():
+            if mode == math:
+                modes[name] = {"value": world * W * H * frames / (ms_max / 1e3) / 1e6, "steps": args.steps}
+                continue
+            tree = ref_bvh if (mode == MATH["exact"] or fast_bvh is None) else fast_bvh
+            m_ms = timed(tree, mode, 2, 1)[0]
+            modes[name] = {"value": rate(m_ms, 2), "steps": 2}
+        for name, mode in MATH.items():
+            modes[name].update({
+                "unit": UNIT, "tree": "reference" if (mode == MATH["exact"] or fast_bvh is None) else "ct_bvh_build_fast",
+                "parity": {"fast": "statistical: a measured fraction of pixels leaves 1e-4 of the oracle "
+                                   "(tests/test_gpu_render.py)",
+                           "exact": "accumulation bit-identical to the oracle, whole 1080p frames",
+                           "exact-shade": "whole 1080p frames within 1e-4 of the oracle per pixel (0 out of band)"}[name]})
+        if fast_bvh is not None:
+            r_ms = timed(ref_bvh, math, 2, 1)[0]
+            job.profile(True)
+            job.profile_read(reset=True)
+            accumulation(ref_bvh, math, frames=prof_frames)
+            stream.synchronize()
+            prof_ref = job.profile_read(reset=True)
+            job.profile(False)
+            job.stats(reset=True, stream=stream)
+            ref_tree = {"value": rate(r_ms, 2), "unit": UNIT, "steps": 2, "math": args.math,
+                        "stage_ms": {k: v["ms"] for k, v in prof_ref.items()}, "stage_frames": prof_frames,
+                        "tree": "the reference's SAH + MergeNodes quad tree (device build)",
+                        "quad_nodes": info["quad_node_count"]}
+    samples = W * H * frames
     value = world * samples / (ms_max / 1e3) / 1e6
     mrays = world * (st["extension_rays"] + st["shadow_rays"]) / (ms_max / 1e3) / 1e6
 
     if args.skip_extras:
         if rank == 0:
             print(json.dumps({"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
-                              "ms_per_step": ms_max / args.steps, "mrays_per_s": mrays,
+                              "ms_per_step": ms_max / args.steps, "mrays_per_s": mrays, "math": args.math,
+                              "frames_per_step": FRAMES_PER_STEP,
                               "stage_ms": {k: v["ms"] for k, v in prof.items()}, "stage_frames": prof_frames,
                               "config": {"width": W, "height": H, "max_depth": DEPTH}}), flush=True)
         return
 
-    # ---- e2e: C ABI with the presented frame copied to pinned host memory each step
+    # ---- e2e: C ABI, every frame presented and copied to pinned host memory
     out_dev = torch.empty((W * H, 4), device="cuda")
     out_host = torch.empty((W * H, 4), pin_memory=True)
-    params_e2e = api.Params(W, H, camera=camera, max_depth=DEPTH, exact_math=args.exact_math)
-    params_e2e.reset(job, stream)
-    for _ in range(args.warmup):
-        api.launch_kernels(job, sc, bvh, params_e2e, present_out=out_dev, stream=stream)
-        with torch.cuda.stream(stream):
-            out_host.copy_(out_dev, non_blocking=True)
-    stream.synchronize()
-    barrier(world)
-    w0 = time.perf_counter()
-    e0.record(stream)
-    for _ in range(args.steps):
-        api.launch_kernels(job, sc, bvh, params_e2e, present_out=out_dev, stream=stream)
-        with torch.cuda.stream(stream):
-            out_host.copy_(out_dev, non_blocking=True)
-    e1.record(stream)
-    stream.synchronize()
-    wall_ms = (time.perf_counter() - w0) * 1e3
-    e2e_ms = max_over_ranks(max(e0.elapsed_time(e1), wall_ms), world)
+    e_ms, e_wall, _, _ = timed(bvh, math, args.steps, args.warmup, present=out_dev, host=out_host)
+    e2e_ms = max_over_ranks(max(e_ms, e_wall), world)
     e2e_value = world * samples / (e2e_ms / 1e3) / 1e6
-    h2d_bytes = 40 + 48  # ct_camera + ct_render_params passed from host memory per frame
-    d2h_bytes = W * H * 16
+    h2d_bytes = FRAMES_PER_STEP * (40 + 48)  # ct_camera + ct_render_params passed from host memory per frame
+    d2h_bytes = FRAMES_PER_STEP * W * H * 16  # every presented frame
 
     # ---- roofline of the dominant kernel (extend: closest-hit traversal)
     peak, peak_kind = measured_peaks()
@@ -787,7 +809,7 @@ def run_ours(args, world, rank, local):
         # reference's tree; the counts of the traced tree in the order fast-math
         # frames visit children (full distance sort) are reported beside
         work, paths = oracle_work(quad, prims, False)
-        work_fast = oracle_work(*bvh.export(), True)[0] if not args.exact_math else work
+        work_fast = oracle_work(*bvh.export(), True)[0] if math != MATH["exact"] else work
         v_node = work["ext_nodes"] / max(1, work["ext_rays"])
         v_tri = work["ext_tris"] / max(1, work["ext_rays"])
         b_ray = 32 + v_node * 128 + v_tri * 52
@@ -809,7 +831,7 @@ def run_ours(args, world, rank, local):
                 "mean_tri_tests": work_fast["ext_tris"] / max(1, work_fast["ext_rays"]),
                 "bytes_per_ray": 32 + 128 * work_fast["ext_nodes"] / max(1, work_fast["ext_rays"])
                 + 52 * work_fast["ext_tris"] / max(1, work_fast["ext_rays"]),
-                "order": "full distance sort" if fast_bvh is not None else "traverseMBVH"},
+                "order": "traverseMBVH" if math == MATH["exact"] else "full distance sort"},
             "rays_per_launch": ext_rays / max(1, ext["launches"]),
             "avg_launch_ms": ext["ms"] / max(1, ext["launches"]),
         }
@@ -836,27 +858,26 @@ def run_ours(args, world, rank, local):
     # ---- the same workload with every material shaded (CT_SHADE_FULL), for context
     from cudatracer_gb300 import _lib
 
-    pf = api.Params(W, H, camera=camera, max_depth=DEPTH, exact_math=False)
-    pf.reset(job, stream)
-    full_frames = max(8, args.steps // 4)
+    full_frames = FRAMES_PER_STEP
 
-    def full_frame():
-        c = pf.to_ct()
-        c.shading_mode = _lib.CT_SHADE_FULL
-        job.accumulate(sc, bvh, camera, c, stream)
-        pf.samples += 2
+    def full_accumulation():
+        pf = api.Params(W, H, camera=camera, max_depth=DEPTH, exact_math=math)
+        pf.reset(job, stream)
+        for _ in range(full_frames):
+            c = pf.to_ct()
+            c.shading_mode = _lib.CT_SHADE_FULL
+            job.accumulate(sc, bvh, camera, c, stream)
+            pf.samples += 2
 
-    for _ in range(args.warmup):
-        full_frame()
+    full_accumulation()
     stream.synchronize()
     e0.record(stream)
-    for _ in range(full_frames):
-        full_frame()
+    full_accumulation()
     e1.record(stream)
     stream.synchronize()
     full_ms = e0.elapsed_time(e1) / full_frames
     full = {"msamples_per_s": W * H / full_ms / 1e3, "ms_per_frame": full_ms, "frames": full_frames,
-            "shading": "full materials (Lambert, mirror, dielectric IOR 1.5, GGX) with MIS"}
+            "math": args.math, "shading": "full materials (Lambert, mirror, dielectric IOR 1.5, GGX) with MIS"}
     c1 = sphere_closest_hit(ctx) if rank == 0 else None
     c3 = precision_soup(ctx) if (rank == 0 and not args.skip_precision) else None
     c4 = batching_jobs(ctx) if (rank == 0 and not args.skip_serving) else None
@@ -868,22 +889,22 @@ def run_ours(args, world, rank, local):
     # our kernels in the timed region: per frame raygen + depth x (extend, shade,
     # connect) + the fold of a fast-math frame slot (the launch counts of the
     # stage-timing pass, which has no fold, confirm the per-frame stage count)
-    per_frame = sum(v["launches"] for v in prof.values()) / prof_frames + (0 if args.exact_math else 1)
-    launches = int(round(per_frame * args.steps))
+    per_frame = sum(v["launches"] for v in prof.values()) / prof_frames + (0 if math == MATH["exact"] else 1)
+    launches = int(round(per_frame * frames))
     line = {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": ms_max / args.steps, "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded procedural scene)",
         "config": {"workload": WORKLOAD, "width": W, "height": H, "max_depth": DEPTH, "triangles": int(ts.ntri),
-                   "frames_per_step": 1, "shading": "compat (reference shade)",
-                   "math": "exact" if args.exact_math else "fast",
+                   "frames_per_step": FRAMES_PER_STEP, "spp_per_frame": 1, "shading": "compat (reference shade)",
+                   "math": args.math,
                    "l2": "inputs larger than L2: 85-94 MB nodes + 150 MB triangles + 150 MB scene arrays + 300 MB queues",
                    "parallelism": f"replicas x{world}"},
         "mrays_per_s": mrays, "rays_per_step": (st["extension_rays"] + st["shadow_rays"]) / args.steps,
         "stage_ms": {k: v["ms"] for k, v in prof.items()}, "stage_frames": prof_frames,
         "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": h2d_bytes, "d2h_bytes_per_step": d2h_bytes},
         "gpu_launches": launches,
-        "reference_tree": ref_tree,
+        "reference_tree": ref_tree, "math_modes": modes,
         "roofline": roofline, "roofline_sample": roofline_sample, "cpu_baseline": cpu_base, "closest_hit": c1, "precision": c3, "batching": c4, "serving": c5, "full_materials": full, "clocks": clk,
         "setup": {"scene_and_bvh_s": setup_s, "quad_nodes": bvh.info()["quad_node_count"],
                   "bvh_device_build_ms": min(dev_build),
@@ -933,27 +954,35 @@ def run_reference(args, world, rank):
         bvh_src = "oracle restatement of the reference SAH build"
     omats = oracle.pack_materials(ts.materials)
     acc = np.zeros((W * H, 4), np.float32)
+    # each step: a band of rows of the 64-frame accumulation, every frame of it
+    # (seeds 0, 2, ..., 126), so a step is about 2 M paths of the workload
     rows_per_step = 16
+
+    def step(s):
+        r0 = (s * rows_per_step * 7) % (H - rows_per_step)
+        acc[r0 * W:(r0 + rows_per_step) * W] = 0.0  # Params::reset of the band
+        oracle.render_frames(arrays, omats, quad, prims, cam, W, H, [2 * f for f in range(FRAMES_PER_STEP)], DEPTH,
+                             accum=acc, exact_math=False, textures=ts.textures, sky_tex=0,
+                             pixels=(r0 * W, (r0 + rows_per_step) * W), nthreads=threads)
+
     for s in range(args.warmup):
-        oracle.render_frames(arrays, omats, quad, prims, cam, W, H, [0], DEPTH, accum=acc, exact_math=False,
-                             textures=ts.textures, sky_tex=0, pixels=(0, rows_per_step * W), nthreads=threads)
+        step(s)
     t0 = time.perf_counter()
     for s in range(args.steps):
-        r0 = (s * rows_per_step * 7) % (H - rows_per_step)
-        oracle.render_frames(arrays, omats, quad, prims, cam, W, H, [2 * s], DEPTH, accum=acc, exact_math=False,
-                             textures=ts.textures, sky_tex=0, pixels=(r0 * W, (r0 + rows_per_step) * W),
-                             nthreads=threads)
+        step(args.warmup + s)
     dt = time.perf_counter() - t0
-    samples = args.steps * rows_per_step * W
+    samples = args.steps * rows_per_step * W * FRAMES_PER_STEP
     value = samples / dt / 1e6
     line = {
         "impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": dt * 1e3 / args.steps, "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded procedural scene)",
         "config": {"workload": WORKLOAD, "width": W, "height": H, "max_depth": DEPTH, "triangles": int(ts.ntri),
-                   "step_sample": f"{rows_per_step} rows x {W} px of one frame per step"},
+                   "frames_per_step": FRAMES_PER_STEP,
+                   "step_sample": f"{rows_per_step} rows x {W} px x {FRAMES_PER_STEP} frames per step"},
         "cpu_baseline": {"value": value, "unit": UNIT, "cores": threads, "kind": kind,
-                         "sample": f"{rows_per_step * W} paths per step; BVH from the {bvh_src} "
+                         "sample": f"{rows_per_step * W * FRAMES_PER_STEP} paths per step ({rows_per_step} rows "
+                                   f"x {FRAMES_PER_STEP} frames); BVH from the {bvh_src} "
                                    f"({build_ms:.0f} ms)"},
         "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }

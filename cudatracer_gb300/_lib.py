@@ -23,6 +23,7 @@ CT_BVH_BINARY, CT_BVH_QUAD, CT_BVH_WIDE8_Q8 = 0, 1, 2
 CT_SHADE_COMPAT, CT_SHADE_FULL = 0, 1
 CT_TEX_NEAREST, CT_TEX_BILINEAR = 0, 1
 CT_SORT_NONE, CT_SORT_OCTANT, CT_SORT_FACE_CELLS = 0, 1, 2
+CT_MATH_FAST, CT_MATH_EXACT, CT_MATH_EXACT_SHADE = 0, 1, 2
 
 
 class CTError(RuntimeError):

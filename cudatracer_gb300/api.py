@@ -627,7 +627,7 @@ class Params:
     shadow: bool = True
     indirect: bool = True
     sky: bool = True
-    exact_math: bool = False
+    exact_math: int = _lib.CT_MATH_FAST  # CT_MATH_*: False/0 fast, True/1 exact, 2 exact shading + fast traversal
     normal_eps: float = 1e-5
     dist_eps: float = 1e-5
     tri_eps: float = 1e-3

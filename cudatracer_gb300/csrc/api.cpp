@@ -214,6 +214,49 @@ DevMaterial to_dev(const ct_material& m) {
   return d;
 }
 
+// Frame constants of one job: core::Camera's basis and plane distance
+// (Camera constructor, m_PlaneDistance = tanf(radians(fov * 0.5f)),
+// src/Core/Camera.cpp:11-16) and sample()'s u = normalize(cross(w, up)),
+// v = normalize(cross(u, w)) with the aspect ratio on the longer axis
+// (src/CUDA/Kernel.cu:274-290), plus the flags and epsilons of Params. Every
+// frame entry point (frames, the allocation-free frame, batches, serving)
+// derives its constants here, so they agree bit for bit.
+FrameConst frame_const(const ct_camera* cam, const ct_render_params* p) {
+  const float dist = tanf((cam->fov_deg * 0.5f) * 0.01745329251994329576923690768489f);
+  const float* w = cam->forward;
+  const float* up = cam->up;
+  float u[3] = {w[1] * up[2] - up[1] * w[2], w[2] * up[0] - up[2] * w[0], w[0] * up[1] - up[0] * w[1]};
+  float inv = 1.0f / std::sqrt((u[0] * u[0] + u[1] * u[1]) + u[2] * u[2]);
+  u[0] *= inv, u[1] *= inv, u[2] *= inv;
+  float v[3] = {u[1] * w[2] - w[1] * u[2], u[2] * w[0] - w[2] * u[0], u[0] * w[1] - w[0] * u[1]};
+  inv = 1.0f / std::sqrt((v[0] * v[0] + v[1] * v[1]) + v[2] * v[2]);
+  v[0] *= inv, v[1] *= inv, v[2] *= inv;
+  float hor[3] = {u[0] * dist, u[1] * dist, u[2] * dist};
+  float ver[3] = {v[0] * dist, v[1] * dist, v[2] * dist};
+  const float aspect = (float)p->width / (float)p->height;
+  if (p->width > p->height)
+    hor[0] *= aspect, hor[1] *= aspect, hor[2] *= aspect;
+  else
+    ver[0] *= aspect, ver[1] *= aspect, ver[2] *= aspect;
+  FrameConst f;
+  f.cam_pos = make_float3(cam->position[0], cam->position[1], cam->position[2]);
+  f.cam_w = make_float3(w[0], w[1], w[2]);
+  f.hor = make_float3(hor[0], hor[1], hor[2]);
+  f.ver = make_float3(ver[0], ver[1], ver[2]);
+  f.width = p->width;
+  f.height = p->height;
+  f.frame = p->frame_index;
+  f.normal_eps = p->normal_eps;
+  f.dist_eps = p->dist_eps;
+  f.tri_eps = p->tri_eps;
+  f.shadow = p->shadow;
+  f.indirect = p->indirect;
+  f.sky = p->sky;
+  f.shading_mode = p->shading_mode;
+  f.tex_filter = p->texture_filter;
+  return f;
+}
+
 ct_status set_device(ct_ctx* ctx) {
   cudaError_t e = cudaSetDevice(ctx->device);
   if (e != cudaSuccess) return cuda_fail(ctx, e, "cudaSetDevice");
@@ -1019,8 +1062,9 @@ static ct_status ensure_slots(ct_ctx* ctx, ct_render* r) {
 // Issue one frame's stages on stream st into queues q.
 static ct_status emit_frame(ct_ctx* ctx, ct_render* r, const DevQueues& q, const ct_scene* scene, const ct_bvh* bvh,
                             const FrameConst& f, const ct_render_params* p, cudaStream_t st) {
-  const bool fast = !p->exact_math;
-  CT_CUDA(ctx, staged(r, 0, st, [&] { return launch_raygen(q, f, p->exact_math, st); }));
+  const bool fast = math_fast_traversal(p->exact_math);
+  const int exact_shade = math_exact_shading(p->exact_math);
+  CT_CUDA(ctx, staged(r, 0, st, [&] { return launch_raygen(q, f, exact_shade, st); }));
   for (int pass = 0; pass < p->max_depth; pass++) {
     const int cur = pass & 1;
     const int path_length = pass == 0 ? 0 : pass + 1;  // Kernel.cu:306, 330
@@ -1033,7 +1077,7 @@ static ct_status emit_frame(ct_ctx* ctx, ct_render* r, const DevQueues& q, const
       CT_CUDA(ctx, staged(r, 1, st, [&] { return launch_extend_wide(bvh->wdev, qx, cur, p->tri_eps, st); }));
     else
       CT_CUDA(ctx, staged(r, 1, st, [&] { return launch_extend(bvh->dev, qx, cur, p->tri_eps, fast, st); }));
-    CT_CUDA(ctx, staged(r, 2, st, [&] { return launch_shade(scene->dev, q, f, cur, path_length, p->exact_math, st); }));
+    CT_CUDA(ctx, staged(r, 2, st, [&] { return launch_shade(scene->dev, q, f, cur, path_length, exact_shade, st); }));
     if (p->shadow) {
       if (bvh->wide)
         CT_CUDA(ctx, staged(r, 3, st, [&] { return launch_connect_wide(bvh->wdev, q, p->tri_eps, st); }));
@@ -1060,6 +1104,7 @@ ct_status ct_render_accumulate(ct_ctx* ctx, const ct_scene* scene, const ct_bvh*
   if (bvh->nt != scene->nt) return fail(ctx, CT_ERR_INVALID_ARGUMENT, "BVH was built for another scene");
   if (p->shading_mode != CT_SHADE_COMPAT && p->shading_mode != CT_SHADE_FULL)
     return fail(ctx, CT_ERR_INVALID_ARGUMENT, "unknown shading mode");
+  if (!math_mode_valid(p->exact_math)) return fail(ctx, CT_ERR_INVALID_ARGUMENT, "unknown math mode");
   if (p->texture_filter != CT_TEX_NEAREST && p->texture_filter != CT_TEX_BILINEAR)
     return fail(ctx, CT_ERR_INVALID_ARGUMENT, "unknown texture filter");
   if (p->ray_sort < CT_SORT_NONE || p->ray_sort > CT_SORT_FACE_CELLS)
@@ -1069,51 +1114,9 @@ ct_status ct_render_accumulate(ct_ctx* ctx, const ct_scene* scene, const ct_bvh*
   ct_status s = set_device(ctx);
   if (s != CT_OK) return s;
   cudaStream_t st = (cudaStream_t)stream;
-  // Camera constructor: m_PlaneDistance = tanf(radians(fov * 0.5f)) (Camera.cpp:16);
-  // sample(): u = normalize(cross(w, up)), v = normalize(cross(u, w)), aspect on the longer axis.
-  const float dist = tanf((cam->fov_deg * 0.5f) * 0.01745329251994329576923690768489f);
-  const float w[3] = {cam->forward[0], cam->forward[1], cam->forward[2]};
-  const float* up = cam->up;
-  auto cross = [](const float* a, const float* b, float* o) {
-    o[0] = a[1] * b[2] - b[1] * a[2];
-    o[1] = a[2] * b[0] - b[2] * a[0];
-    o[2] = a[0] * b[1] - b[0] * a[1];
-  };
-  auto normalize = [](float* v) {
-    const float d = (v[0] * v[0] + v[1] * v[1]) + v[2] * v[2];
-    const float inv = 1.0f / std::sqrt(d);
-    v[0] *= inv, v[1] *= inv, v[2] *= inv;
-  };
-  float u[3], v[3];
-  cross(w, up, u);
-  normalize(u);
-  cross(u, w, v);
-  normalize(v);
-  float hor[3] = {u[0] * dist, u[1] * dist, u[2] * dist};
-  float ver[3] = {v[0] * dist, v[1] * dist, v[2] * dist};
-  const float aspect = (float)p->width / (float)p->height;
-  if (p->width > p->height)
-    hor[0] *= aspect, hor[1] *= aspect, hor[2] *= aspect;
-  else
-    ver[0] *= aspect, ver[1] *= aspect, ver[2] *= aspect;
-  FrameConst f;
-  f.cam_pos = make_float3(cam->position[0], cam->position[1], cam->position[2]);
-  f.cam_w = make_float3(w[0], w[1], w[2]);
-  f.hor = make_float3(hor[0], hor[1], hor[2]);
-  f.ver = make_float3(ver[0], ver[1], ver[2]);
-  f.width = p->width;
-  f.height = p->height;
-  f.frame = p->frame_index;
-  f.normal_eps = p->normal_eps;
-  f.dist_eps = p->dist_eps;
-  f.tri_eps = p->tri_eps;
-  f.shadow = p->shadow;
-  f.indirect = p->indirect;
-  f.sky = p->sky;
-  f.shading_mode = p->shading_mode;
-  f.tex_filter = p->texture_filter;
+  const FrameConst f = frame_const(cam, p);
   // exact math accumulates strictly in sequence; profiling times kernels alone
-  if (p->exact_math || r->profile) return emit_frame(ctx, r, r->q, scene, bvh, f, p, st);
+  if (p->exact_math == CT_MATH_EXACT || r->profile) return emit_frame(ctx, r, r->q, scene, bvh, f, p, st);
   // Fast-math frames overlap: the frame renders into one of kFrameSlots
   // private slots (queues + accumulation) on the slot's own stream, so its
   // first passes can run while earlier frames' last bounces are still
@@ -1145,45 +1148,14 @@ ct_status ct_render_accumulate_noalloc(ct_ctx* ctx, const ct_scene* scene, const
   if (bvh->wide) return fail(ctx, CT_ERR_UNSUPPORTED, "frames trace quad BVHs; the wide BVH serves ray queries");
   if (p->shading_mode != CT_SHADE_COMPAT && p->shading_mode != CT_SHADE_FULL)
     return fail(ctx, CT_ERR_INVALID_ARGUMENT, "unknown shading mode");
+  if (!math_mode_valid(p->exact_math)) return fail(ctx, CT_ERR_INVALID_ARGUMENT, "unknown math mode");
   if (p->texture_filter != CT_TEX_NEAREST && p->texture_filter != CT_TEX_BILINEAR)
     return fail(ctx, CT_ERR_INVALID_ARGUMENT, "unknown texture filter");
   if (!finite3(cam->position) || !finite3(cam->forward) || !finite3(cam->up) || !std::isfinite(cam->fov_deg))
     return fail(ctx, CT_ERR_INVALID_ARGUMENT, "non-finite camera");
   ct_status s = set_device(ctx);
   if (s != CT_OK) return s;
-  // camera basis exactly as ct_render_accumulate derives it
-  const float dist = tanf((cam->fov_deg * 0.5f) * 0.01745329251994329576923690768489f);
-  const float* w = cam->forward;
-  const float* up = cam->up;
-  float u[3] = {w[1] * up[2] - up[1] * w[2], w[2] * up[0] - up[2] * w[0], w[0] * up[1] - up[0] * w[1]};
-  float inv = 1.0f / std::sqrt((u[0] * u[0] + u[1] * u[1]) + u[2] * u[2]);
-  u[0] *= inv, u[1] *= inv, u[2] *= inv;
-  float v[3] = {u[1] * w[2] - w[1] * u[2], u[2] * w[0] - w[2] * u[0], u[0] * w[1] - w[0] * u[1]};
-  inv = 1.0f / std::sqrt((v[0] * v[0] + v[1] * v[1]) + v[2] * v[2]);
-  v[0] *= inv, v[1] *= inv, v[2] *= inv;
-  float hor[3] = {u[0] * dist, u[1] * dist, u[2] * dist};
-  float ver[3] = {v[0] * dist, v[1] * dist, v[2] * dist};
-  const float aspect = (float)p->width / (float)p->height;
-  if (p->width > p->height)
-    hor[0] *= aspect, hor[1] *= aspect, hor[2] *= aspect;
-  else
-    ver[0] *= aspect, ver[1] *= aspect, ver[2] *= aspect;
-  FrameConst f;
-  f.cam_pos = make_float3(cam->position[0], cam->position[1], cam->position[2]);
-  f.cam_w = make_float3(w[0], w[1], w[2]);
-  f.hor = make_float3(hor[0], hor[1], hor[2]);
-  f.ver = make_float3(ver[0], ver[1], ver[2]);
-  f.width = p->width;
-  f.height = p->height;
-  f.frame = p->frame_index;
-  f.normal_eps = p->normal_eps;
-  f.dist_eps = p->dist_eps;
-  f.tri_eps = p->tri_eps;
-  f.shadow = p->shadow;
-  f.indirect = p->indirect;
-  f.sky = p->sky;
-  f.shading_mode = p->shading_mode;
-  f.tex_filter = p->texture_filter;
+  const FrameConst f = frame_const(cam, p);
   CT_CUDA(ctx, noalloc_render(ctx->device, scene->dev, bvh->dev, f, p->max_depth, p->exact_math,
                               (float4*)accum_device, ctx->d_error, (cudaStream_t)stream));
   return CT_OK;
@@ -1304,48 +1276,12 @@ struct ct_batch {
 
 namespace {
 
-// core::Camera + sample() basis (Camera.cpp:11-16, Kernel.cu:274-290), as ct_render_accumulate derives it.
-FrameConst batch_frame_const(const ct_camera* cam, const ct_render_params* p) {
-  const float dist = tanf((cam->fov_deg * 0.5f) * 0.01745329251994329576923690768489f);
-  const float* w = cam->forward;
-  const float* up = cam->up;
-  float u[3] = {w[1] * up[2] - up[1] * w[2], w[2] * up[0] - up[2] * w[0], w[0] * up[1] - up[0] * w[1]};
-  float inv = 1.0f / std::sqrt((u[0] * u[0] + u[1] * u[1]) + u[2] * u[2]);
-  u[0] *= inv, u[1] *= inv, u[2] *= inv;
-  float v[3] = {u[1] * w[2] - w[1] * u[2], u[2] * w[0] - w[2] * u[0], u[0] * w[1] - w[0] * u[1]};
-  inv = 1.0f / std::sqrt((v[0] * v[0] + v[1] * v[1]) + v[2] * v[2]);
-  v[0] *= inv, v[1] *= inv, v[2] *= inv;
-  float hor[3] = {u[0] * dist, u[1] * dist, u[2] * dist};
-  float ver[3] = {v[0] * dist, v[1] * dist, v[2] * dist};
-  const float aspect = (float)p->width / (float)p->height;
-  if (p->width > p->height)
-    hor[0] *= aspect, hor[1] *= aspect, hor[2] *= aspect;
-  else
-    ver[0] *= aspect, ver[1] *= aspect, ver[2] *= aspect;
-  FrameConst f;
-  f.cam_pos = make_float3(cam->position[0], cam->position[1], cam->position[2]);
-  f.cam_w = make_float3(w[0], w[1], w[2]);
-  f.hor = make_float3(hor[0], hor[1], hor[2]);
-  f.ver = make_float3(ver[0], ver[1], ver[2]);
-  f.width = p->width;
-  f.height = p->height;
-  f.frame = p->frame_index;
-  f.normal_eps = p->normal_eps;
-  f.dist_eps = p->dist_eps;
-  f.tri_eps = p->tri_eps;
-  f.shadow = p->shadow;
-  f.indirect = p->indirect;
-  f.sky = p->sky;
-  f.shading_mode = p->shading_mode;
-  f.tex_filter = p->texture_filter;
-  return f;
-}
 
 // One iteration: every job that still takes samples traces one more.
 cudaError_t batch_iteration(ct_batch* b, int lane, const ct_batch_tuning& t, cudaStream_t st) {
   const DevBatch& dev = b->lane_dev(lane);
   const DevQueues& q = b->lane_q(lane);
-  cudaError_t e = launch_batch_raygen(dev, q, b->exact, st);
+  cudaError_t e = launch_batch_raygen(dev, q, math_exact_shading(b->exact), st);
   for (int pass = 0; pass < b->max_depth && e == cudaSuccess; pass++) {
     const int cur = pass & 1;
     const uint32_t path_length = pass == 0 ? 0u : (uint32_t)pass + 1u;  // Kernel.cu:306, 330
@@ -1356,11 +1292,11 @@ cudaError_t batch_iteration(ct_batch* b, int lane, const ct_batch_tuning& t, cud
     }
     if (e == cudaSuccess)
       e = dev.wide ? launch_batch_extend_wide(dev, qx, cur, st)
-                   : launch_batch_extend(dev, qx, cur, !b->exact, t.extend_block, t.refill, st);
-    if (e == cudaSuccess) e = launch_batch_shade(dev, q, cur, path_length, pass, b->exact, t.shade_waves, st);
+                   : launch_batch_extend(dev, qx, cur, math_fast_traversal(b->exact), t.extend_block, t.refill, st);
+    if (e == cudaSuccess) e = launch_batch_shade(dev, q, cur, path_length, pass, math_exact_shading(b->exact), t.shade_waves, st);
     if (e == cudaSuccess)
       e = dev.wide ? launch_batch_connect_wide(dev, q, st)
-                   : launch_batch_connect(dev, q, !b->exact, t.connect_block, st);
+                   : launch_batch_connect(dev, q, math_fast_traversal(b->exact), t.connect_block, st);
   }
   if (e == cudaSuccess) e = launch_batch_advance(dev, q, st);
   return e;
@@ -1443,6 +1379,7 @@ extern "C" {
 ct_status ct_batch_create(ct_ctx* ctx, const ct_batch_job* jobs, uint32_t n, int32_t exact_math, ct_batch** out) {
   if (!ctx || !jobs || !out || n == 0) return fail(ctx, CT_ERR_INVALID_ARGUMENT, "null argument or empty batch");
   *out = nullptr;
+  if (!math_mode_valid(exact_math)) return fail(ctx, CT_ERR_INVALID_ARGUMENT, "unknown math mode");
   int64_t total = 0;
   int32_t max_stack = 1, max_depth = 1;
   uint32_t max_spp = 0;
@@ -1477,10 +1414,10 @@ ct_status ct_batch_create(ct_ctx* ctx, const ct_batch_job* jobs, uint32_t n, int
   if (s != CT_OK) return s;
   auto* b = new ct_batch();
   b->n = (int32_t)n;
-  b->exact = exact_math ? 1 : 0;
+  b->exact = exact_math;
   b->max_depth = max_depth;
   b->max_spp = max_spp;
-  b->lanes = exact_math ? 1 : kBatchLanes;
+  b->lanes = exact_math == CT_MATH_EXACT ? 1 : kBatchLanes;
   b->jobs0.resize(n);
   b->bases.resize(n + 1);
   int32_t base = 0;
@@ -1491,7 +1428,7 @@ ct_status ct_batch_create(ct_ctx* ctx, const ct_batch_job* jobs, uint32_t n, int
     d.sc = J.scene->dev;
     d.bvh = J.bvh->dev;
     d.wbvh = J.bvh->wdev;
-    d.f = batch_frame_const(&J.camera, &J.params);
+    d.f = frame_const(&J.camera, &J.params);
     d.pix_base = base;
     d.max_depth = J.params.max_depth;
     d.spp_left = (int32_t)((J.spp + b->lanes - 1) / b->lanes);  // lane 0: samples 0, L, 2L, ...
@@ -1709,7 +1646,7 @@ void rt_free_list(ct_ctx* c, std::vector<std::pair<void*, size_t>>& owned) {
   free_all(c, a);
   owned.clear();
 }
-FrameConst rt_frame_const(const ct_camera* cam, const ct_render_params* p) { return batch_frame_const(cam, p); }
+FrameConst rt_frame_const(const ct_camera* cam, const ct_render_params* p) { return frame_const(cam, p); }
 const DevWBVH& rt_bvh_wdev(const ct_bvh* b) { return b->wdev; }
 bool rt_account(ct_ctx* c, int64_t delta) {
   if (delta > 0 && c->budget && c->bytes.load() + (uint64_t)delta > c->budget) return false;

@@ -138,6 +138,14 @@ struct FrameConst {
 
 enum : uint32_t { kErrStackOverflow = 1u };
 
+// Math modes (CT_MATH_FAST 0, CT_MATH_EXACT 1, CT_MATH_EXACT_SHADE 2): which
+// build each stage runs. Only CT_MATH_EXACT traverses with the reference's
+// arithmetic and child order (and runs frames strictly in sequence); ray
+// generation and shading are the bit-reproducible build in both exact modes.
+inline bool math_fast_traversal(int mode) { return mode != 1; }
+inline int math_exact_shading(int mode) { return mode != 0 ? 1 : 0; }
+inline bool math_mode_valid(int mode) { return mode >= 0 && mode <= 2; }
+
 // ---------------------------------------------------------------------------
 // Batches: many render jobs share one queue set and one launch per stage.
 // A ray's pixel index (origin.w) is global to the batch; the job owning it is

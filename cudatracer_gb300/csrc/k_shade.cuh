@@ -1,9 +1,9 @@
 // Ray generation, shading and presentation kernels of the wavefront loop.
 //
 // This file is compiled twice: k_shade_exact.cu (-fmad=false, sin/cos/atan2/
-// acos evaluated in double and rounded once: reproducible bit for bit by the
-// CPU oracle) and k_shade_fast.cu (FMA contraction and CUDA's float
-// transcendentals). CT_SHADE_NS names the namespace, CT_EXACT selects the math.
+// acos from portable_math.h: reproducible bit for bit by the CPU oracle) and
+// k_shade_fast.cu (FMA contraction and CUDA's float transcendentals).
+// CT_SHADE_NS names the namespace, CT_EXACT selects the math.
 //
 // Compat shading restates the reference's `shade` kernel
 // (src/CUDA/Kernel.cu:88-206) with its BSDF (src/Core/BSDF.h:26-63): every
@@ -16,6 +16,7 @@
 
 #include "bsdf_full.cuh"
 #include "ct_internal.h"
+#include "portable_math.h"
 #include "vmath.cuh"
 
 #ifndef CT_MODE_FULL
@@ -36,10 +37,12 @@ constexpr float kTwoPi = 6.28318530717958647692528676655900576f;
 constexpr int kBlock = 128;
 
 #if CT_EXACT
-__device__ __forceinline__ float xsin(float x) { return (float)sin((double)x); }
-__device__ __forceinline__ float xcos(float x) { return (float)cos((double)x); }
-__device__ __forceinline__ float xatan2(float y, float x) { return (float)atan2((double)y, (double)x); }
-__device__ __forceinline__ float xacos(float x) { return (float)acos((double)x); }
+// reproducible binary32 functions (portable_math.h): the oracle evaluates the
+// same operations on the host, so exact frames agree bit for bit
+__device__ __forceinline__ float xsin(float x) { return pm::sin(x); }
+__device__ __forceinline__ float xcos(float x) { return pm::cos(x); }
+__device__ __forceinline__ float xatan2(float y, float x) { return pm::atan2(y, x); }
+__device__ __forceinline__ float xacos(float x) { return pm::acos(x); }
 #else
 __device__ __forceinline__ float xsin(float x) { return sinf(x); }
 __device__ __forceinline__ float xcos(float x) { return cosf(x); }

@@ -16,7 +16,10 @@
 //     contexts on one device) race with each other and must be serialised;
 //   * the first call on each device looks up the array's device address
 //     with cudaGetSymbolAddress; make that first call before any stream
-//     capture begins.
+//     capture begins. The address is kept for the life of the process and
+//     belongs to the device's context as it was then: after a cudaDeviceReset
+//     of that device it is stale, so the entry point must not be used on a
+//     device this process has reset since its first call there.
 #include <mutex>
 
 #include "ct_internal.h"
@@ -80,13 +83,15 @@ cudaError_t noalloc_render(int device, const DevScene& sc, const DevBVH& bvh, co
   q.capacity = f.width * f.height;
   // counters and statistics start at zero on every call (the array keeps the last call's values)
   if ((e = cudaMemsetAsync(base + kCountsOffset, 0, kScratchBytes - kCountsOffset, s)) != cudaSuccess) return e;
-  if ((e = launch_raygen(q, f, exact_math, s)) != cudaSuccess) return e;
+  const bool fast = math_fast_traversal(exact_math);
+  const int exact_shade = math_exact_shading(exact_math);
+  if ((e = launch_raygen(q, f, exact_shade, s)) != cudaSuccess) return e;
   for (int pass = 0; pass < max_depth; pass++) {
     const int cur = pass & 1;
     const int path_length = pass == 0 ? 0 : pass + 1;
-    if ((e = launch_extend(bvh, q, cur, f.tri_eps, !exact_math, s)) != cudaSuccess) return e;
-    if ((e = launch_shade(sc, q, f, cur, path_length, exact_math, s)) != cudaSuccess) return e;
-    if (f.shadow && (e = launch_connect(bvh, q, f.tri_eps, !exact_math, s)) != cudaSuccess) return e;
+    if ((e = launch_extend(bvh, q, cur, f.tri_eps, fast, s)) != cudaSuccess) return e;
+    if ((e = launch_shade(sc, q, f, cur, path_length, exact_shade, s)) != cudaSuccess) return e;
+    if (f.shadow && (e = launch_connect(bvh, q, f.tri_eps, fast, s)) != cudaSuccess) return e;
   }
   return cudaSuccess;
 }

@@ -121,6 +121,10 @@ struct ct_server {
   int slot = 0;          // render stream, queue set and job table of the next iteration
   int64_t iter = 0;      // iterations issued
   cudaStream_t rs[kStreams] = {}, qs = nullptr, ms = nullptr;  // render, query, setup
+  // the server's own memory pool for request state: freed request memory stays
+  // reserved in it between requests (release threshold at its maximum) without
+  // changing the device's default pool, which the host application may use
+  cudaMemPool_t pool = nullptr;
 
   double now() const { return std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count(); }
   void loop();
@@ -135,7 +139,7 @@ struct ct_server {
 // that uses it, so freeing never waits for the whole device.
 void ct_server::start(Request* r) {
   cudaStream_t st = r->kind == kRender ? ms : qs;
-  cudaError_t e = cudaMallocAsync(&r->dmem, r->bytes, st);
+  cudaError_t e = cudaMallocFromPoolAsync(&r->dmem, r->bytes, pool, st);
   if (e != cudaSuccess) {
     cudaGetLastError();
     r->dmem = nullptr;
@@ -277,13 +281,14 @@ cudaError_t ct_server::render_iteration(std::vector<Request*>& finished) {
   if ((e = cudaMemcpyAsync(d_bases[slot], hb, (size_t)(n + 1) * 4, cudaMemcpyHostToDevice, st)) != cudaSuccess) return e;
   if ((e = cudaMemsetAsync(q.counts, 0, 16 * sizeof(int32_t), st)) != cudaSuccess) return e;
   DevBatch b{d_table[slot], d_bases[slot], (int32_t)n, base, max_stack, 0, 2};  // quad BVHs
-  const bool fast = !cfg.exact_math;
-  e = launch_batch_raygen(b, q, cfg.exact_math, st);
+  const bool fast = math_fast_traversal(cfg.exact_math);
+  const int exact_shade = math_exact_shading(cfg.exact_math);
+  e = launch_batch_raygen(b, q, exact_shade, st);
   for (int pass = 0; pass < depth && e == cudaSuccess; pass++) {
     const int cur = pass & 1;
     const uint32_t path_length = pass == 0 ? 0u : (uint32_t)pass + 1u;  // Kernel.cu:306, 330
     e = launch_batch_extend(b, q, cur, fast, 128, 24, st);
-    if (e == cudaSuccess) e = launch_batch_shade(b, q, cur, path_length, pass, cfg.exact_math, 1, st);
+    if (e == cudaSuccess) e = launch_batch_shade(b, q, cur, path_length, pass, exact_shade, 1, st);
     if (e == cudaSuccess) e = launch_batch_connect(b, q, fast, 128, st);
   }
   if (e == cudaSuccess) e = cudaEventRecord(table_ev[slot], st);
@@ -406,7 +411,12 @@ void ct_server::loop() {
       iterated = true;
       if (e != cudaSuccess) {
         cudaGetLastError();
-        for (Request* r : render) r->status = CT_ERR_CUDA, finished.push_back(r);
+        // jobs still in flight give their queue space back with their failure
+        for (Request* r : render) {
+          r->status = CT_ERR_CUDA;
+          inflight_pixels -= r->k * r->pixels;
+          finished.push_back(r);
+        }
         render.clear();
       }
     }
@@ -438,11 +448,18 @@ ct_status ct_server_create(ct_ctx* ctx, const ct_server_config* cfg, ct_server**
   for (int k = 0; k < kStreams && st == CT_OK; k++)
     st = rt_alloc_queues(ctx, cfg->max_inflight_pixels, s->q[k], s->q_owned[k]);
   cudaError_t e = cudaSuccess;
-  // keep freed request memory in the device's pool between requests
-  cudaMemPool_t pool = nullptr;
-  if (cudaDeviceGetDefaultMemPool(&pool, s->device) == cudaSuccess) {
-    uint64_t keep = ~0ull;
-    cudaMemPoolSetAttribute(pool, cudaMemPoolAttrReleaseThreshold, &keep);
+  // a private pool that keeps freed request memory between requests
+  if (st == CT_OK) {
+    cudaMemPoolProps props;
+    std::memset(&props, 0, sizeof(props));
+    props.allocType = cudaMemAllocationTypePinned;
+    props.location.type = cudaMemLocationTypeDevice;
+    props.location.id = s->device;
+    e = cudaMemPoolCreate(&s->pool, &props);
+    if (e == cudaSuccess) {
+      uint64_t keep = ~0ull;
+      e = cudaMemPoolSetAttribute(s->pool, cudaMemPoolAttrReleaseThreshold, &keep);
+    }
   }
   for (int k = 0; k < kStreams && st == CT_OK && e == cudaSuccess; k++)
     e = cudaStreamCreateWithFlags(&s->rs[k], cudaStreamNonBlocking);
@@ -459,6 +476,7 @@ ct_status ct_server_create(ct_ctx* ctx, const ct_server_config* cfg, ct_server**
     }
     for (cudaStream_t x : {s->qs, s->ms})
       if (x) cudaStreamDestroy(x);
+    if (s->pool) cudaMemPoolDestroy(s->pool);
     delete s;
     return st != CT_OK ? st : rt_fail(ctx, CT_ERR_CUDA, cudaGetErrorString(e));
   }
@@ -490,6 +508,7 @@ ct_status ct_server_destroy(ct_server* s) {
   }
   for (cudaStream_t x : {s->qs, s->ms})
     if (x) cudaStreamDestroy(x);
+  if (s->pool) cudaMemPoolDestroy(s->pool);  // every request's memory was freed in stream order above
   delete s;
   return CT_OK;
 }

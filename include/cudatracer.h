@@ -120,6 +120,23 @@ typedef struct ct_camera {
 } ct_camera;
 
 enum { CT_SHADE_COMPAT = 0, CT_SHADE_FULL = 1 };
+/* Math modes of a frame (ct_render_params.exact_math, the batch and server
+ * exact_math arguments; no reference counterpart: the reference has one build).
+ *   CT_MATH_FAST        CUDA float transcendentals and FMA contraction in ray
+ *                       generation and shading; traversal with fused slab
+ *                       planes and children in full distance order.
+ *   CT_MATH_EXACT       ray generation and shading bit-reproducible (no FMA,
+ *                       sin/cos/atan2/acos in double rounded once) and the
+ *                       reference's traversal arithmetic and child order:
+ *                       accumulation bit-identical to the oracle; frames run
+ *                       one after another.
+ *   CT_MATH_EXACT_SHADE ray generation and shading as CT_MATH_EXACT, traversal
+ *                       as CT_MATH_FAST. The traversal returns the same closest
+ *                       hit (t bit-equal; only the winner of an exact t tie can
+ *                       differ) and the same occlusion, so frames equal
+ *                       CT_MATH_EXACT's up to such ties and the rounding of
+ *                       adding each overlapped frame into the accumulation. */
+enum { CT_MATH_FAST = 0, CT_MATH_EXACT = 1, CT_MATH_EXACT_SHADE = 2 };
 /* Texture filtering: the reference's nearest texel (SceneData::getTextureColor,
  * src/Core/SceneData.cuh:81-116), or bilinear over the same texel grid
  * (texel centres at u*(width-1), v*(height-1), clamped at the edges). */
@@ -141,7 +158,7 @@ typedef struct ct_render_params {
   int32_t max_depth;     /* extend+shade+connect passes per path (reference: 5) */
   uint32_t frame_index;  /* RNG frame; the reference's launchKernels advances it by 2 per frame */
   int32_t shading_mode;  /* CT_SHADE_COMPAT (reference shade) or CT_SHADE_FULL (all materials, MIS) */
-  int32_t exact_math;    /* 1: sin/cos/atan2/acos evaluated in double and rounded once (bit-reproducible) */
+  int32_t exact_math;    /* CT_MATH_*: 0 fast, 1 exact (bit-reproducible), 2 exact shading + fast traversal */
   int32_t shadow;        /* SceneData::shadow */
   int32_t indirect;      /* SceneData::indirect */
   int32_t sky;           /* SceneData::skyboxEnabled (needs a skybox texture) */
@@ -471,7 +488,13 @@ ct_status ct_render_profile_read(ct_ctx* ctx, ct_render* r, ct_stage_times* out,
  *     (other streams, threads or contexts on the same device) race and must
  *     be serialised by the caller;
  *   - the first call on each device looks up the array's device address
- *     (cudaGetSymbolAddress); make that first call before any stream capture. */
+ *     (cudaGetSymbolAddress); make that first call before any stream capture;
+ *   - that address is kept for the life of the process. A cudaDeviceReset
+ *     destroys the context it belongs to, so after a reset of a device the
+ *     kept address is stale: do not call this entry point on a device that
+ *     this process has reset since its first call there.
+ * With exact_math = CT_MATH_EXACT it adds exactly the bits that
+ * ct_render_accumulate adds for the same frame. */
 #define CT_NOALLOC_MAX_PIXELS 65536
 ct_status ct_render_accumulate_noalloc(ct_ctx* ctx, const ct_scene* scene, const ct_bvh* bvh, const ct_camera* cam,
                                        const ct_render_params* params, float* accum_device, void* stream);

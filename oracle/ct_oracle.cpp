@@ -26,9 +26,12 @@
  *   SceneData::getTextureColor        src/Core/SceneData.cuh:81-97
  *
  * Transcendentals: with exact_math=1 the oracle (and the GPU's matching mode)
- * evaluate sin/cos/atan2/acos in double and round once to float, which makes
- * CPU and GPU agree bit for bit; exact_math=0 calls the C library's float
- * functions, which differ from CUDA's by an ulp now and then.
+ * evaluate sin/cos/atan2/acos with the binary32 functions of
+ * cudatracer_gb300/csrc/portable_math.h, fixed sequences of correctly rounded
+ * IEEE operations, which makes CPU and GPU agree bit for bit (that header's
+ * accuracy against correctly rounded values is tested on its own);
+ * exact_math=0 calls the C library's float functions, which differ from
+ * CUDA's by an ulp now and then.
  */
 #include <algorithm>
 #include <atomic>
@@ -39,6 +42,8 @@
 #include <memory>
 #include <thread>
 #include <vector>
+
+#include "../cudatracer_gb300/csrc/portable_math.h"
 
 namespace {
 
@@ -582,10 +587,10 @@ struct SceneView {
   int tex_filter;
 };
 
-inline float xsin(float x, int exact) { return exact ? (float)std::sin((double)x) : sinf(x); }
-inline float xcos(float x, int exact) { return exact ? (float)std::cos((double)x) : cosf(x); }
-inline float xatan2(float y, float x, int exact) { return exact ? (float)std::atan2((double)y, (double)x) : atan2f(y, x); }
-inline float xacos(float x, int exact) { return exact ? (float)std::acos((double)x) : acosf(x); }
+inline float xsin(float x, int exact) { return exact ? ct::pm::sin(x) : sinf(x); }
+inline float xcos(float x, int exact) { return exact ? ct::pm::cos(x) : cosf(x); }
+inline float xatan2(float y, float x, int exact) { return exact ? ct::pm::atan2(y, x) : atan2f(y, x); }
+inline float xacos(float x, int exact) { return exact ? ct::pm::acos(x) : acosf(x); }
 
 // Texel addressing of SceneData::getTextureColor/getTextureNormal
 // (src/Core/SceneData.cuh:81-116): grid coordinate u*(width-1); NaN or
@@ -709,7 +714,7 @@ inline void accum_add(float* acc, V3 c) {
  * in the order the wavefront kernels do. */
 void render_path(const SceneView& s, const Geo& g, int pixel, int px, int py, int W, int H, uint32_t frame, int depth,
                  V3 cam_o, V3 cam_w, V3 hor, V3 ver, int exact, float* acc, Work* wext = nullptr,
-                 Work* wshd = nullptr) {
+                 Work* wshd = nullptr, int32_t* hit_log = nullptr, float* t_log = nullptr) {
   // generatePrimaryRays (Kernel.cu:208-234) with start_position = 0.
   uint32_t seed = ((uint32_t)pixel + frame * 147565741u) * 720898027u;
   const float fx = ((float)px + rnd_float(seed)) - 0.5f;
@@ -726,6 +731,7 @@ void render_path(const SceneView& s, const Geo& g, int pixel, int px, int py, in
     float t = kMaxDistance;
     int hit = -1;
     trace_closest(g, r.org, r.dir, &t, &hit, nullptr, wext);
+    if (hit_log) hit_log[pass] = hit, t_log[pass] = t;
     // ---- shade (Kernel.cu:88-206) ----
     if (!(t < kMaxDistance)) {
       if (s.sky_enabled) {
@@ -1007,6 +1013,24 @@ void or_render_frame(const OrSceneDesc* sd, const float* cam_pos, const float* c
   });
 }
 
+/* The closest hit of every extension pass of one pixel's path in one frame:
+ * primitive id (-1: miss) and t per pass, -2 and 0 for passes the path does
+ * not reach. Comparing the logs of two trees shows at which bounce their
+ * answers part, and whether at an equal t (an exact tie, where the winner
+ * depends on the order in which the tree presents the two triangles). */
+void or_path_hits(const OrSceneDesc* sd, const float* cam_pos, const float* cam_w, const float* hor, const float* ver,
+                  int W, int H, uint32_t frame, int depth, int exact_math, int pixel, int32_t* hits, float* ts) {
+  SceneView s{sd->verts, sd->normals, sd->center_normals, sd->uvs, sd->idx, sd->mat_idx, (const Material*)sd->materials,
+              sd->lights, sd->light_count, sd->tex, sd->tex_dims, sd->tex_offsets, sd->sky_tex, sd->sky_enabled,
+              sd->shadow, sd->indirect, sd->normal_eps, sd->dist_eps, sd->tri_eps, (const QNode*)sd->qnodes,
+              sd->prims, sd->tex_filter};
+  Geo g{sd->verts, sd->idx, sd->prims, (const QNode*)sd->qnodes, nullptr, sd->tri_eps};
+  for (int k = 0; k < depth; k++) hits[k] = -2, ts[k] = 0.0f;
+  float acc[4] = {0, 0, 0, 0};
+  render_path(s, g, pixel, pixel % W, (pixel / W) % H, W, H, frame, depth, load3(cam_pos, 0), load3(cam_w, 0),
+              load3(hor, 0), load3(ver, 0), exact_math, acc, nullptr, nullptr, hits, ts);
+}
+
 /* Traversal work of the frames rendered since the last reset:
  * [ext rays, ext quad-node visits, ext triangle tests, shadow rays, shadow
  * node visits, shadow triangle tests]. */
@@ -1099,6 +1123,21 @@ void or_cos_weighted(float r3, float r4, int exact, float* out) {
   const float term1 = kTwoPi * r3;
   const float term2 = (float)std::sqrt(1.0 - (double)r4);
   out[0] = xcos(term1, exact) * term2, out[1] = xsin(term1, exact) * term2, out[2] = std::sqrt(r4);
+}
+
+/* The reproducible binary32 functions of portable_math.h over arrays (their
+ * accuracy tests): sin, cos, atan2(y, x) and acos. */
+void or_pm_eval(const float* x, const float* y, int n, float* s, float* c, float* at2, float* ac) {
+  for (int i = 0; i < n; i++) {
+    if (s || c) {
+      float a, b;
+      ct::pm::sincos(x[i], &a, &b);
+      if (s) s[i] = a;
+      if (c) c[i] = b;
+    }
+    if (at2) at2[i] = ct::pm::atan2(y[i], x[i]);
+    if (ac) ac[i] = ct::pm::acos(x[i]);
+  }
 }
 
 /* draw_framebuffer (Kernel.cu:258-270): pow(sum.rgb / samples, 1/2.2), alpha 1. */

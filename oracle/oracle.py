@@ -18,6 +18,8 @@ import numpy as np
 
 HERE = os.path.dirname(os.path.abspath(__file__))
 ORACLE_SRC = os.path.join(HERE, "ct_oracle.cpp")
+# the reproducible binary32 functions exact-math frames use on both sides
+PORTABLE_MATH = os.path.join(os.path.dirname(HERE), "cudatracer_gb300", "csrc", "portable_math.h")
 ORACLE_LIB = os.path.join(HERE, "liboracle.so")
 REF_LIB = os.path.join(HERE, "_ref", "libctref.so")
 P = ctypes.c_void_p
@@ -42,6 +44,7 @@ def _native_machine() -> int:
 
 def build_oracle(force: bool = False) -> str:
     fresh = (os.path.exists(ORACLE_LIB) and os.path.getmtime(ORACLE_LIB) >= os.path.getmtime(ORACLE_SRC)
+             and os.path.getmtime(ORACLE_LIB) >= os.path.getmtime(PORTABLE_MATH)
              and _elf_machine(ORACLE_LIB) == _native_machine())
     if fresh and not force:
         return ORACLE_LIB
@@ -349,15 +352,12 @@ def camera_basis(forward, up, fov_deg, width, height):
     return hor, ver
 
 
-def render_frames(arrays: dict, materials: np.ndarray, quad, prims, camera: dict, width: int, height: int,
-                  frames, depth: int, accum: np.ndarray | None = None, exact_math: bool = True,
-                  textures=(), sky_tex: int = -1, sky: bool = True, shadow: bool = True, indirect: bool = True,
-                  eps=(1e-5, 1e-5, 1e-3), pixels=None, nthreads: int = 8, tex_filter: int = 0) -> np.ndarray:
-    """Accumulate 1-spp frames (seed frame indices `frames`) into accum (h*w,4)."""
-    L = lib()
+def _frame_scene(arrays: dict, materials: np.ndarray, quad, prims, camera: dict, width: int, height: int,
+                 textures=(), sky_tex: int = -1, sky: bool = True, shadow: bool = True, indirect: bool = True,
+                 eps=(1e-5, 1e-5, 1e-3), tex_filter: int = 0):
+    """The OrSceneDesc of a frame and the camera vectors, with the arrays they
+    point into (keep the returned tuple alive while the pointers are used)."""
     a = {k: np.ascontiguousarray(v) for k, v in arrays.items()}
-    if accum is None:
-        accum = np.zeros((width * height, 4), np.float32)
     texels = dims = offs = None
     if textures:
         flat, dl, ol, o = [], [], [], 0
@@ -383,8 +383,39 @@ def render_frames(arrays: dict, materials: np.ndarray, quad, prims, camera: dict
     hor, ver = camera_basis(camera["forward"], camera["up"], camera["fov"], width, height)
     pos = np.asarray(camera["position"], np.float32)
     fw = np.asarray(camera["forward"], np.float32)
+    keep = (a, texels, dims, offs, mats, q, pr)
+    return d, pos, fw, hor, ver, keep
+
+
+def render_frames(arrays: dict, materials: np.ndarray, quad, prims, camera: dict, width: int, height: int,
+                  frames, depth: int, accum: np.ndarray | None = None, exact_math: bool = True,
+                  textures=(), sky_tex: int = -1, sky: bool = True, shadow: bool = True, indirect: bool = True,
+                  eps=(1e-5, 1e-5, 1e-3), pixels=None, nthreads: int = 8, tex_filter: int = 0) -> np.ndarray:
+    """Accumulate 1-spp frames (seed frame indices `frames`) into accum (h*w,4)."""
+    L = lib()
+    if accum is None:
+        accum = np.zeros((width * height, 4), np.float32)
+    d, pos, fw, hor, ver, _keep = _frame_scene(arrays, materials, quad, prims, camera, width, height, textures,
+                                               sky_tex, sky, shadow, indirect, eps, tex_filter)
     p0, p1 = (0, width * height) if pixels is None else pixels
     for fr in frames:
         L.or_render_frame(ctypes.byref(d), _p(pos), _p(fw), _p(hor), _p(ver), width, height, int(fr), depth,
                           int(exact_math), _p(accum), p0, p1, nthreads)
     return accum
+
+
+def path_hits(arrays: dict, materials: np.ndarray, quad, prims, camera: dict, width: int, height: int, frame: int,
+              depth: int, pixel: int, exact_math: bool = True, textures=(), sky_tex: int = -1, **kw):
+    """Closest hit of each extension pass of one pixel's path: (primitive ids,
+    t values), -2 / 0 for passes the path does not reach (or_path_hits)."""
+    L = lib()
+    d, pos, fw, hor, ver, _keep = _frame_scene(arrays, materials, quad, prims, camera, width, height, textures,
+                                               sky_tex, **kw)
+    hits = np.zeros(depth, np.int32)
+    ts = np.zeros(depth, np.float32)
+    P = ctypes.c_void_p
+    L.or_path_hits.argtypes = [P, P, P, P, P, ctypes.c_int, ctypes.c_int, ctypes.c_uint32, ctypes.c_int, ctypes.c_int,
+                               ctypes.c_int, P, P]
+    L.or_path_hits(ctypes.byref(d), _p(pos), _p(fw), _p(hor), _p(ver), width, height, int(frame), depth,
+                   int(exact_math), int(pixel), _p(hits), _p(ts))
+    return hits, ts

@@ -31,6 +31,8 @@ import sys
 HERE = os.path.dirname(os.path.abspath(__file__))
 REF_OUT = os.path.join(HERE, "_ref")
 LIB = os.path.join(REF_OUT, "libctref.so")
+# where the reference checkout is looked for: build(reference=...), then
+# `--reference PATH` on the command line, then $CT_REFERENCE_DIR, then this
 DEFAULT_REFERENCE = "/root/reference"
 
 SRC_FILES = [
@@ -158,4 +160,11 @@ def build(reference: str | None = None, verbose: bool = False) -> str | None:
 
 
 if __name__ == "__main__":
-    print(build(verbose="-v" in sys.argv))
+    import argparse
+
+    ap = argparse.ArgumentParser(description="stage and compile the reference's host BVH/camera code")
+    ap.add_argument("--reference", default=None, help="reference checkout (default: $CT_REFERENCE_DIR or "
+                                                      f"{DEFAULT_REFERENCE})")
+    ap.add_argument("-v", action="store_true", help="print the compiler commands")
+    a = ap.parse_args()
+    print(build(reference=a.reference, verbose=a.v))

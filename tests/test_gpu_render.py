@@ -89,13 +89,56 @@ def test_ray_sort_keys_do_not_change_frames(gpu_ctx, orc, small, exact):
         api.launch_kernels(job, small["sc"], small["bvh"], p)
 
 
+def _fold_oracle(orc, S, W, H, frames, depth, **kw):
+    """The oracle's exact frames, each accumulated into a zeroed buffer and then
+    added to the running sum in float32 (round to nearest): the grouping of the
+    overlapped GPU frames, whose private buffers k_fold adds into the job's
+    buffer in frame order."""
+    acc = np.zeros((W * H, 4), np.float32)
+    for f in range(frames):
+        acc = acc + _oracle_frames(orc, S, W, H, [2 * f], depth, **kw)
+    return acc
+
+
+def _oracle_frames(orc, S, W, H, seeds, depth, **kw):
+    return orc.render_frames(S["arr"], S["omats"], S["ob"]["quad"], S["ob"]["prims"], S["cam"], W, H, seeds, depth,
+                             exact_math=True, textures=S["ts"].textures, sky_tex=0, **kw)
+
+
+@pytest.mark.parametrize("tree", ["reference", "fast"])
+def test_exact_shade_frames_match_oracle(gpu_ctx, orc, small, tree):
+    """CT_MATH_EXACT_SHADE: the bit-reproducible ray generation and shading with
+    the fast traversal (fused slab planes, children in full distance order), in
+    overlapped frame slots. That traversal returns the reference traversal's
+    closest hit (t bit-equal, only an exact tie's winner can differ) and its
+    occlusion, on the reference's tree and on the traversal-speed tree, so no
+    pixel leaves the 1e-4 band of the oracle's exact frames (the oracle traces
+    the reference's tree) and the accumulation equals those frames summed in
+    the GPU's grouping bit for bit (ties aside)."""
+    from cudatracer_gb300 import _lib
+
+    W, H = 96, 64
+    S = dict(small)
+    if tree == "fast":
+        S["bvh"] = small["sc"].build_bvh_fast()
+    _, p, acc = _render(gpu_ctx, S, W, H, 4, 5, _lib.CT_MATH_EXACT_SHADE)
+    assert p.samples == 8
+    oacc = _fold_oracle(orc, small, W, H, 4, 5)
+    assert _bad(acc, oacc).sum() == 0
+    bit = (acc.view(np.int32) == oacc.view(np.int32)).all(axis=1).mean()
+    assert bit >= 0.999
+    assert acc[:, 3].max() > 0
+
+
 def test_fast_math_frames_close_to_oracle(gpu_ctx, orc, small):
+    """CT_MATH_FAST: CUDA's float sin/cos/atan2/acos and contracted multiply-adds
+    differ from the exact build by an ulp or so; a path that grazes an edge then
+    diverges, so a few pixels leave the 1e-4 band (the fraction at full size is
+    measured in test_full_size_frames_against_oracle). The image total stays
+    close."""
     W, H = 96, 64
     _, _, acc = _render(gpu_ctx, small, W, H, 4, 5, False)
     oacc = _oracle(orc, small, W, H, 4, 5, True)
-    # CUDA's float sin/cos/atan2/acos differ from the double-rounded ones by an
-    # ulp; a path that grazes an edge then diverges. Most pixels stay within
-    # tolerance and the image total stays close.
     assert _bad(acc, oacc).mean() < 0.10
     assert abs(acc[:, :3].sum() - oacc[:, :3].sum()) / oacc[:, :3].sum() < 0.02
 
@@ -201,33 +244,98 @@ def test_memory_budget_refuses_allocation(gpu_ctx):
         gpu_ctx.set_memory_budget(0)
 
 
-def test_full_size_frame_properties(gpu_ctx, orc):
-    """The 1920x1080, depth-8 workload on the 3.1M-triangle terrain scene:
-    two runs give bit-identical accumulation (compaction order does not leak
-    into results), the exact build matches the oracle on sampled rows, and
-    the image is finite and non-negative."""
+# CT_MATH_FAST on the 1920x1080, depth-8 terrain frame (seed frame 0) against
+# the oracle's whole frame: 52,687 of 2,073,600 pixels (2.54 %) measured
+# outside 1e-4 relative on a GB300; the bound leaves headroom.
+FULL_FAST_OUT_OF_BAND_MAX = 0.03
+
+
+@pytest.fixture(scope="module")
+def full(gpu_ctx, orc):
+    """The benchmark workload: 3,117,066-triangle terrain scene, its reference
+    tree (host build: the same leaves, primitive order included, as the
+    oracle's), its traversal-speed tree, and the oracle's build of the
+    reference tree."""
+    import os
+
     from cudatracer_gb300 import api, scenes
 
     ts, cam = scenes.terrain_scene()
     arr = scenes.scene_arrays(ts)
     sc = gpu_ctx.scene(arr, [api.Material(**m) for m in ts.materials], ts.textures, ts.skybox_texture)
-    bvh = sc.build_bvh()
-    S = dict(ts=ts, cam=cam, arr=arr, sc=sc, bvh=bvh)
+    ob = orc.bvh_build(ts.vertices, ts.indices, nthreads=os.cpu_count() or 8)
+    return dict(ts=ts, cam=cam, arr=arr, sc=sc, bvh=sc.build_bvh(), fast=sc.build_bvh_fast(), ob=ob,
+                omats=orc.pack_materials(ts.materials), threads=os.cpu_count() or 8)
+
+
+def test_full_size_frames_against_oracle(gpu_ctx, orc, full):
+    """The 1920x1080, depth-8 workload, whole frames against the oracle's whole
+    frame (reference tree, reference traversal order, exact math):
+      * CT_MATH_EXACT on the reference's tree: every channel bit-identical, and
+        a second run gives the same bits (compaction order never leaks in);
+      * CT_MATH_EXACT_SHADE on the traversal-speed tree (the benchmark's
+        headline mode): no pixel outside 1e-4 relative;
+      * CT_MATH_FAST on the traversal-speed tree: at most
+        FULL_FAST_OUT_OF_BAND_MAX of the pixels outside 1e-4, image total
+        within 0.5 %, finite and non-negative.
+    Every exact-shade pixel that differs from the oracle's frame must be an
+    exact tie: the oracle's own path for that pixel, traced through the
+    reference's tree and through the traversal-speed tree, parts at a bounce
+    where both trees report the same t bit for bit and another primitive (a
+    ray through the edge two triangles share: the first one tested wins, and
+    the trees present them in another order). Against the oracle tracing the
+    traversal-speed tree itself, no pixel may leave the band. Two frames of the
+    exact-shade mode are also compared with the oracle's two frames summed in
+    the GPU's grouping."""
+    from cudatracer_gb300 import _lib
+
     W, H = 1920, 1080
-    _, _, a1 = _render(gpu_ctx, S, W, H, 1, 8, True)
-    _, _, a2 = _render(gpu_ctx, S, W, H, 1, 8, True)
+    S = dict(full)
+    oacc = _oracle_frames(orc, S, W, H, [0], 8, nthreads=S["threads"])
+    fq, fp = full["fast"].export()
+    S_fast = dict(S, ob={"quad": fq, "prims": fp})
+    orc.set_full_sort(True)  # the child order of the fast traversal
+    try:
+        ofast = _oracle_frames(orc, S_fast, W, H, [0], 8, nthreads=S["threads"])
+    finally:
+        orc.set_full_sort(False)
+    _, _, a1 = _render(gpu_ctx, S, W, H, 1, 8, _lib.CT_MATH_EXACT)
+    _, _, a2 = _render(gpu_ctx, S, W, H, 1, 8, _lib.CT_MATH_EXACT)
     assert np.array_equal(a1.view(np.int32), a2.view(np.int32))
     assert np.isfinite(a1).all() and (a1 >= 0).all()
-    _, _, f1 = _render(gpu_ctx, S, W, H, 1, 8, False)
+    exact_bits = int((a1.view(np.int32) != oacc.view(np.int32)).any(axis=1).sum())
+    S["bvh"] = full["fast"]
+    _, _, h1 = _render(gpu_ctx, S, W, H, 1, 8, _lib.CT_MATH_EXACT_SHADE)
+    _, _, f1 = _render(gpu_ctx, S, W, H, 1, 8, _lib.CT_MATH_FAST)
+    hybrid_diff = np.nonzero((h1.view(np.int32) != oacc.view(np.int32)).any(axis=1))[0]
+    hybrid_bad = int(_bad(h1, oacc).sum())
+    hybrid_bad_same_tree = int(_bad(h1, ofast).sum())
+    fast_bad = float(_bad(f1, oacc).mean())
+    print(f"\nfull frame vs oracle: exact differing pixels {exact_bits}; exact-shade out of band {hybrid_bad} "
+          f"(not bit-equal {hybrid_diff.size}; against the oracle on the same tree {hybrid_bad_same_tree}); "
+          f"fast out of band {fast_bad:.5f} ({int(_bad(f1, oacc).sum())} of {W * H})")
+    assert exact_bits == 0
+    assert hybrid_bad_same_tree == 0
+    assert hybrid_diff.size <= 64
+    kw = dict(textures=S["ts"].textures, sky_tex=0)
+    for pix in hybrid_diff:
+        ha, ta = orc.path_hits(S["arr"], S["omats"], S["ob"]["quad"], S["ob"]["prims"], S["cam"], W, H, 0, 8,
+                               int(pix), **kw)
+        hb, tb = orc.path_hits(S["arr"], S["omats"], fq, fp, S["cam"], W, H, 0, 8, int(pix), **kw)
+        part = int(np.argmax(ha != hb)) if (ha != hb).any() else -1
+        assert part >= 0, f"pixel {pix}: the same path on both trees, yet the GPU frame differs"
+        assert ta.view(np.int32)[part] == tb.view(np.int32)[part], f"pixel {pix}: trees part at unequal t"
+    assert fast_bad <= FULL_FAST_OUT_OF_BAND_MAX
     assert np.isfinite(f1).all() and (f1 >= 0).all()
-    ob = orc.bvh_build(ts.vertices, ts.indices)
-    S.update(ob=ob, omats=orc.pack_materials(ts.materials))
-    rows = [(0, 1), (400, 401), (700, 701), (1079, 1080)]
-    for r0, r1 in rows:
-        oacc = orc.render_frames(arr, S["omats"], ob["quad"], ob["prims"], cam, W, H, [0], 8, exact_math=True,
-                                 textures=ts.textures, sky_tex=0, pixels=(r0 * W, r1 * W))
-        sl = slice(r0 * W, r1 * W)
-        assert _bad(a1[sl], oacc[sl]).sum() == 0
+    assert abs(f1[:, :3].sum() - oacc[:, :3].sum()) / oacc[:, :3].sum() < 0.005
+    # two accumulated frames: the second frame's buffer is added into the first
+    _, _, h2 = _render(gpu_ctx, S, W, H, 2, 8, _lib.CT_MATH_EXACT_SHADE)
+    orc.set_full_sort(True)
+    try:
+        o2 = ofast + _oracle_frames(orc, S_fast, W, H, [2], 8, nthreads=S["threads"])
+    finally:
+        orc.set_full_sort(False)
+    assert _bad(h2, o2).sum() == 0
 
 
 def test_loaded_model_frames_match_oracle(gpu_ctx, orc, tmp_path):

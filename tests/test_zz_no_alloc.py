@@ -9,8 +9,11 @@ frame may hold at most CT_NOALLOC_MAX_PIXELS (65,536) paths.
 
 The test calls it through the C ABI and compares what it adds to the caller's
 accumulation buffer with what ct_render_accumulate adds to a ct_render's
-buffer, for two calls in a row, at the 1e-4 relative tolerance the frame
-tests use. The file is named to be collected last."""
+buffer, for two calls in a row: bit for bit in exact math (both run the same
+kernels in the same order on the caller's stream), and at the 1e-4 relative
+tolerance the frame tests use in fast math (ct_render_accumulate adds each
+overlapped frame's private buffer into the job's, a different summation
+grouping). The file is named to be collected last."""
 import ctypes
 
 import numpy as np
@@ -52,6 +55,9 @@ def test_noalloc_matches_allocating_path_twice(gpu_ctx):
             gpu_ctx.check()
             got = accum.cpu().numpy()
             want = ref_job.accum_tensor().cpu().numpy()
+            if exact:
+                assert np.array_equal(got.view(np.int32), want.view(np.int32)), (
+                    f"{(got.view(np.int32) != want.view(np.int32)).any(axis=1).sum()} pixels differ in exact math")
             rel = np.abs(got - want) / np.maximum(np.abs(want), 1e-6)
             assert (rel <= RTOL).all(), f"{(rel > RTOL).any(axis=1).sum()} pixels differ (exact={exact})"
             assert want[:, 3].sum() > 0
