@@ -388,7 +388,7 @@ def precision_soup(ctx, ntri: int = 10_000_000, nray: int = 16_000_000, sample_e
     return out
 
 
-def batching_jobs(ctx, n_jobs: int = 256, seed: int = 2024) -> dict:
+def batching_jobs(ctx, n_jobs: int = 256, seed: int = 2024, math: int = MATH["exact-shade"]) -> dict:
     """The batching workload: n_jobs render jobs of the terrain-plus-spheres
     kind, triangle counts log-uniform 10k..2M, square resolutions log-uniform
     64..1024, spp log-uniform 1..64, depth uniform 4..12, all in one batch
@@ -420,7 +420,7 @@ def batching_jobs(ctx, n_jobs: int = 256, seed: int = 2024) -> dict:
         tris += ts.indices.shape[0]
     setup_s = time.perf_counter() - t0
     samples = sum(j["spp"] * j["params"].width * j["params"].height for j in jobs)
-    b = api.Batch(ctx, jobs)
+    b = api.Batch(ctx, jobs, exact_math=math)
     tuning, tune_ms = b.autotune()
     b.run()
     torch.cuda.synchronize()
@@ -441,7 +441,7 @@ def batching_jobs(ctx, n_jobs: int = 256, seed: int = 2024) -> dict:
     for j in jobs:
         W, H = j["params"].width, j["params"].height
         rj = api.RenderJob(ctx, W, H)
-        pp = api.Params(W, H, camera=j["camera"], max_depth=j["params"].max_depth)
+        pp = api.Params(W, H, camera=j["camera"], max_depth=j["params"].max_depth, exact_math=math)
         pp.reset(rj)
         for _ in range(j["spp"]):
             api.launch_kernels(rj, j["scene"], j["bvh"], pp)
@@ -461,10 +461,12 @@ def batching_jobs(ctx, n_jobs: int = 256, seed: int = 2024) -> dict:
         "serial_plain_ms": serial_ms, "serial_plain_msamples_per_s": samples / serial_ms / 1e3,
         "speedup_vs_serial": serial_ms / ms, "setup_s": setup_s,
         "tree": "ct_bvh_build_fast (host, all cores; in setup_s)",
+        "math": [k for k, v in MATH.items() if v == math][0],
     }
 
 
-def serving_poisson(ctx, rate: float = 100.0, duration_s: float = 5.0, seed: int = 77, iter_pixels: int = 0) -> dict:
+def serving_poisson(ctx, rate: float = 100.0, duration_s: float = 5.0, seed: int = 77, iter_pixels: int = 0,
+                    math: int = MATH["exact-shade"]) -> dict:
     """The serving workload: a Poisson request stream (rate req/s for
     duration_s) mixing render jobs (the batching workload's job distribution over 16
     resident terrain scenes) and ray queries (10k..4M incoherent rays against resident
@@ -522,7 +524,8 @@ def serving_poisson(ctx, rate: float = 100.0, duration_s: float = 5.0, seed: int
             return srv.submit_render(r)
         return srv.submit_query(r["bvh"], ray_o[r["off"]:r["off"] + r["n"]], ray_d[r["off"]:r["off"] + r["n"]])
 
-    srv = api.Server(ctx, hbm_budget=150 << 30, max_inflight_pixels=1 << 24, iter_pixels=iter_pixels)
+    srv = api.Server(ctx, hbm_budget=150 << 30, max_inflight_pixels=1 << 24, iter_pixels=iter_pixels,
+                     exact_math=math)
     ids = [None] * n_req
 
     def client():
@@ -555,7 +558,7 @@ def serving_poisson(ctx, rate: float = 100.0, duration_s: float = 5.0, seed: int
         if kind == "render":
             W, H = r["params"].width, r["params"].height
             rj = api.RenderJob(ctx, W, H)
-            pp = api.Params(W, H, camera=r["camera"], max_depth=r["params"].max_depth)
+            pp = api.Params(W, H, camera=r["camera"], max_depth=r["params"].max_depth, exact_math=math)
             pp.reset(rj)
             for _ in range(r["spp"]):
                 api.launch_kernels(rj, r["scene"], r["bvh"], pp)
@@ -614,12 +617,15 @@ def soup_case(args) -> None:
     arr = {"vertices": s.vertices, "normals": np.tile(np.array([[0, 0, 1]], np.float32), (s.vertices.shape[0], 1)),
            "indices": s.indices}
     sc = ctx.scene(arr, [api.Material()])
-    wb, qb = sc.build_bvh_wide(), sc.build_bvh_device()
+    wb, qb, fb = sc.build_bvh_wide(), sc.build_bvh_device(), sc.build_bvh_fast()
     org, dirs = torch.from_numpy(o).cuda(), torch.from_numpy(d).cuda()
     out = {}
     for name, fn in (("wide", lambda: wb.trace_closest(org, dirs)),
-                     ("quad", lambda: qb.trace_closest(org, dirs, tri_eps=1e-12))):
-        for _ in range(2):
+                     ("quad", lambda: qb.trace_closest(org, dirs, tri_eps=1e-12)),
+                     ("quad_fast_tree", lambda: fb.trace_closest(org, dirs, tri_eps=1e-12)),
+                     ("wide_any", lambda: wb.trace_any(org, dirs)),
+                     ("quad_fast_tree_any", lambda: fb.trace_any(org, dirs, tri_eps=1e-12))):
+        for _ in range(2):  # the second launch of each is the one a profiler captures
             torch.cuda.synchronize()
             e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
             e0.record()
@@ -880,11 +886,12 @@ def run_ours(args, world, rank, local):
             "math": args.math, "shading": "full materials (Lambert, mirror, dielectric IOR 1.5, GGX) with MIS"}
     c1 = sphere_closest_hit(ctx) if rank == 0 else None
     c3 = precision_soup(ctx) if (rank == 0 and not args.skip_precision) else None
-    c4 = batching_jobs(ctx) if (rank == 0 and not args.skip_serving) else None
+    c4 = batching_jobs(ctx, math=math) if (rank == 0 and not args.skip_serving) else None
     # the light end of the request-rate range, one where serial execution saturates, and the
     # top of the range (2,000 req/s), where the server saturates too
-    c5 = ([serving_poisson(ctx, duration_s=10.0), serving_poisson(ctx, rate=400.0, duration_s=2.0),
-           serving_poisson(ctx, rate=2000.0, duration_s=1.0)]
+    c5 = ([serving_poisson(ctx, duration_s=10.0, math=math),
+           serving_poisson(ctx, rate=400.0, duration_s=2.0, math=math),
+           serving_poisson(ctx, rate=2000.0, duration_s=1.0, math=math)]
           if (rank == 0 and not args.skip_serving) else None)
     # our kernels in the timed region: per frame raygen + depth x (extend, shade,
     # connect) + the fold of a fast-math frame slot (the launch counts of the

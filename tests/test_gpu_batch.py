@@ -106,6 +106,36 @@ def test_exact_batch_equals_render_and_oracle(gpu_ctx, orc, scenes_):
     assert not (rel > 1e-4).any()
 
 
+def test_exact_shade_batch_matches_oracle_and_is_independent_of_the_mix(gpu_ctx, orc, scenes_):
+    """CT_MATH_EXACT_SHADE batches (four lanes, fast traversal, reproducible
+    shading): a job in the mix equals the job alone bit for bit, and every
+    pixel of the accumulated samples stays within 1e-4 of the oracle's exact
+    frames traced in the same child order on the same tree."""
+    from cudatracer_gb300 import _lib
+
+    jobs = _mix(scenes_)
+    for j in jobs:
+        j["params"].shading_mode = 0
+        j["params"].texture_filter = 0
+    out, _ = _run(gpu_ctx, jobs, exact=_lib.CT_MATH_EXACT_SHADE)
+    alone, _ = _run(gpu_ctx, [jobs[3]], exact=_lib.CT_MATH_EXACT_SHADE)
+    assert np.array_equal(alone[0].view(np.int32), out[3].view(np.int32))
+    orc.set_full_sort(True)
+    try:
+        for k, si in ((0, 0), (2, 2), (3, 3)):
+            S, j = scenes_[si], jobs[k]
+            q, pr = S["bvh"].export()
+            W, H = j["params"].width, j["params"].height
+            frames = [j["params"].frame_index + 2 * s for s in range(j["spp"])]
+            oacc = orc.render_frames(S["arr"], orc.pack_materials(S["ts"].materials), q, pr, S["cam"], W, H, frames,
+                                     j["params"].max_depth, exact_math=True, textures=S["ts"].textures, sky_tex=0)
+            rel = np.abs(out[k] - oacc) / np.maximum(np.abs(oacc), 1e-6)
+            assert not (rel > 1e-4).any(), k
+            assert out[k][:, 3].sum() > 0
+    finally:
+        orc.set_full_sort(False)
+
+
 def test_graph_replay_and_tunings_do_not_change_results(gpu_ctx, scenes_):
     jobs = _mix(scenes_)
     ref, _ = _run(gpu_ctx, jobs, tuning=dict(extend_block=128, connect_block=128, shade_waves=1, use_graph=0))

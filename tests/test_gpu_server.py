@@ -73,18 +73,19 @@ def _same(a, b):
     return np.array_equal(np.ascontiguousarray(a).view(np.uint8), np.ascontiguousarray(b).view(np.uint8))
 
 
-def test_each_result_same_alone_and_in_mix(gpu_ctx, world):
+@pytest.mark.parametrize("math", [0, 2])  # CT_MATH_FAST, CT_MATH_EXACT_SHADE
+def test_each_result_same_alone_and_in_mix(gpu_ctx, world, math):
     from cudatracer_gb300 import api
 
     reqs = _requests(world)
-    srv = api.Server(gpu_ctx, max_inflight_pixels=1 << 16)
+    srv = api.Server(gpu_ctx, max_inflight_pixels=1 << 16, exact_math=math)
     alone = []
     for kind, r in reqs:
         rid = _submit(srv, kind, r)
         alone.append(srv.wait(rid)[1])
     srv.close()
     # all at once, in a shuffled order, some arriving while others run
-    srv = api.Server(gpu_ctx, max_inflight_pixels=1 << 16)
+    srv = api.Server(gpu_ctx, max_inflight_pixels=1 << 16, exact_math=math)
     order = np.random.default_rng(5).permutation(len(reqs))
     ids = {}
     for k, i in enumerate(order):
