@@ -27,7 +27,10 @@ struct ct_ctx {
   uint64_t budget = 0;
   std::atomic<uint64_t> bytes{0};
   uint32_t* d_error = nullptr;  // device error word
-  int* d_cursor = nullptr;      // ray-query fetch cursor (inside the same allocation)
+  int* d_cursor = nullptr;      // ray-query fetch cursor and record count (inside the same allocation)
+  // settlement records of wide-tree queries (kWideRecordBytes per ray), grown on demand
+  void* d_recs = nullptr;
+  size_t recs_bytes = 0;
 };
 
 namespace {
@@ -349,6 +352,7 @@ ct_status ct_ctx_destroy(ct_ctx* ctx) {
   if (!ctx) return CT_ERR_INVALID_ARGUMENT;
   cudaSetDevice(ctx->device);
   cudaFree(ctx->d_error);
+  if (ctx->d_recs) cudaFree(ctx->d_recs);
   delete ctx;
   return CT_OK;
 }
@@ -949,14 +953,41 @@ static ct_status check_rays(ct_ctx* ctx, const ct_bvh* bvh, const float* org, co
   return set_device(ctx);
 }
 
+// Settlement records for a wide-tree query of n rays: the context keeps one
+// buffer and grows it (after the device has finished with the old one) when a
+// query needs more; the bytes count against the context's budget.
+static ct_status ensure_wide_records(ct_ctx* ctx, uint32_t n) {
+  const size_t need = ((size_t)std::max<uint32_t>(n, 1) * kWideRecordBytes + 255) & ~(size_t)255;
+  if (ctx->recs_bytes >= need) return CT_OK;
+  if (ctx->budget && ctx->bytes.load() - ctx->recs_bytes + need > ctx->budget)
+    return fail(ctx, CT_ERR_OUT_OF_MEMORY, "device memory budget exceeded by the wide-query records of " +
+                                               std::to_string(n) + " rays");
+  if (ctx->d_recs) {
+    CT_CUDA(ctx, cudaDeviceSynchronize());
+    cudaFree(ctx->d_recs);
+    ctx->bytes -= ctx->recs_bytes;
+    ctx->d_recs = nullptr, ctx->recs_bytes = 0;
+  }
+  cudaError_t e = cudaMalloc(&ctx->d_recs, need);
+  if (e != cudaSuccess) {
+    cudaGetLastError();
+    ctx->d_recs = nullptr;
+    return cuda_fail(ctx, e, "cudaMalloc (wide-query records)");
+  }
+  ctx->recs_bytes = need;
+  ctx->bytes += need;
+  return CT_OK;
+}
+
 ct_status ct_trace_closest(ct_ctx* ctx, const ct_bvh* bvh, const float* org, const float* dir, int32_t* hit, float* t,
                            uint32_t n, float tri_eps, void* stream) {
   ct_status s = check_rays(ctx, bvh, org, dir, n);
   if (s != CT_OK) return s;
   if (n && (!hit || !t)) return fail(ctx, CT_ERR_INVALID_ARGUMENT, "null output buffer");
   if (bvh->wide) {
+    if ((s = ensure_wide_records(ctx, n)) != CT_OK) return s;
     CT_CUDA(ctx, launch_trace_wide_closest(bvh->wdev, (const float4*)org, (const float4*)dir, hit, t, n, ctx->d_error,
-                                           ctx->d_cursor, bvh->d_wstats, (cudaStream_t)stream));
+                                           ctx->d_cursor, ctx->d_recs, bvh->d_wstats, (cudaStream_t)stream));
     return CT_OK;
   }
   CT_CUDA(ctx, launch_trace_closest(bvh->dev, (const float4*)org, (const float4*)dir, hit, t, n, tri_eps, ctx->d_error,
@@ -970,8 +1001,9 @@ ct_status ct_trace_any(ct_ctx* ctx, const ct_bvh* bvh, const float* org, const f
   if (s != CT_OK) return s;
   if (n && !occluded) return fail(ctx, CT_ERR_INVALID_ARGUMENT, "null output buffer");
   if (bvh->wide) {
+    if ((s = ensure_wide_records(ctx, n)) != CT_OK) return s;
     CT_CUDA(ctx, launch_trace_wide_any(bvh->wdev, (const float4*)org, (const float4*)dir, occluded, n, ctx->d_error,
-                                       ctx->d_cursor, bvh->d_wstats, (cudaStream_t)stream));
+                                       ctx->d_cursor, ctx->d_recs, bvh->d_wstats, (cudaStream_t)stream));
     return CT_OK;
   }
   CT_CUDA(ctx, launch_trace_any(bvh->dev, (const float4*)org, (const float4*)dir, occluded, n, tri_eps, ctx->d_error,

@@ -236,14 +236,19 @@ cudaError_t gpu_wbvh_collapse(const DevScene& sc, void* scratch, void* scratch2,
 cudaError_t gpu_wbvh_copy_nodes(void* scratch2, uint32_t binary_nodes, WNode8* out, uint32_t count, cudaStream_t s);
 
 // Wide-tree queries: FP32 watertight tests; hits within the FP32 error bound
-// of an edge or of another hit's t are settled by FP64 tests. stats (may be
-// null): [0] rays, [1] rays re-tested in FP64, [2] rays traced fully in FP64,
-// [3] of [1], rays re-tested only because the best hit's t bound was loose.
+// of an edge or of another hit's t are settled by FP64 tests in a second
+// kernel. counters: 2 device ints the launch zeroes (fetch cursor, record
+// count); recs: kWideRecordBytes per ray, 16-byte aligned (settlement
+// records). stats (may be null): [0] rays, [1] rays re-tested in FP64, [2]
+// rays traced fully in FP64, [3] of [1], rays re-tested only because the best
+// hit's t bound was loose.
+constexpr size_t kWideRecordBytes = 32;
 cudaError_t launch_trace_wide_closest(const DevWBVH& b, const float4* org, const float4* dir, int32_t* hit, float* t,
-                                      uint32_t n, uint32_t* err, int* cursor, unsigned long long* stats,
-                                      cudaStream_t s);
+                                      uint32_t n, uint32_t* err, int* counters, void* recs,
+                                      unsigned long long* stats, cudaStream_t s);
 cudaError_t launch_trace_wide_any(const DevWBVH& b, const float4* org, const float4* dir, uint8_t* occ, uint32_t n,
-                                  uint32_t* err, int* cursor, unsigned long long* stats, cudaStream_t s);
+                                  uint32_t* err, int* counters, void* recs, unsigned long long* stats,
+                                  cudaStream_t s);
 
 // Batch stages (one launch each for every job of the batch). The queue
 // capacity is the batch's total pixel count; counts[0] must be zero before

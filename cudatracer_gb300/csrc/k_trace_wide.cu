@@ -1,9 +1,11 @@
 // Ray queries on the 8-wide quantised BVH (WNode8).
 //
-// Boxes: child bounds decoded as fma(2^e, q, p), which the builder rounded
-// outward, and a slab test whose far distance is scaled by 1 + 2*gamma(3)
-// (Ize 2013, "Robust BVH ray traversal"), so no box that the ray touches in
-// exact arithmetic is rejected.
+// Boxes: the builder rounds child bounds outward so that fl(p + 2^e q)
+// contains the child; the slab test evaluates each plane as one fused
+// multiply-add t = q A + B with per-node constants and widens every interval
+// by a bound of its rounding error (SlabSetup), so no box that the ray
+// touches in exact arithmetic is rejected. Culling against the best hit keeps
+// the margin 1 + 2 gamma(3) of Ize ("Robust BVH ray traversal", JCGT 2013).
 //
 // Triangles: the watertight test of Woop, Benthin and Wald (JCGT 2013) in FP32:
 // shear to ray space, edge functions U, V, W, no epsilon. Each edge function
@@ -30,7 +32,6 @@ namespace ct {
 namespace {
 
 constexpr int kWStack = 128;  // local-memory stack entries per thread
-constexpr int kCand = 8;
 constexpr float kU = 5.9604645e-08f;          // 2^-24
 constexpr float kFarScale = 1.00000036f;      // 1 + 2 * gamma(3), gamma(n) = n u / (1 - n u)
 constexpr float kTRel = 9e-6f;                // a best hit whose t bound exceeds this (relative) is re-tested in FP64
@@ -184,32 +185,70 @@ __device__ __forceinline__ bool tri64(const Ray64& q, const float4* tris, uint32
          t < q.tmax;
 }
 
-struct NodeBoxes {
-  float px, py, pz, sx, sy, sz;
+// Slab distances of a node's eight slots, set up once per node and ray.
+// Per axis a, with s = 2^(e - 127) the quantisation step and inv = 1/d:
+//   A = s * inv (exact: a power of two times a float),  B = (p - o) * inv,
+// so a plane q (0..255) lies at t = q * A + B, one fused multiply-add. Only the
+// ray's near plane (lo for inv >= 0, hi otherwise) and far plane of each axis
+// are evaluated, so no min/max per axis is needed. Every computed t differs
+// from the exact distance (L - o) / d of the builder's outward-rounded plane
+// L = fl(p + s q) by at most
+//   E = 5u (255 |A| + |B| + |p inv|) + 1e-30      (u = 2^-24)
+// (the rounding of inv, of p - o, of the product and of the FMA, and the
+// half-ulp by which p + s q may lie inside L; the last term covers underflow).
+// E is folded into the offsets: near planes use Bn = B - E, far planes
+// Bf = B + E (E is raised by the rounding of those two sums), so a slot's
+// [max near, min far] interval contains the exact one and no box the ray
+// touches is rejected.
+struct SlabSetup {
+  uint32_t nq[3][2], fq[3][2];  // near / far plane bytes of slots 0-3 and 4-7, per axis
+  float A[3], Bn[3], Bf[3];
 };
 
-// Slab test of slot i; returns the entry distance or +inf when missed.
-__device__ __forceinline__ float slot_box(const WRay& r, const WNode8& n, const NodeBoxes& nb, int i, float tfar) {
-  const float lx = __fmaf_rn(nb.sx, (float)n.qlo[0][i], nb.px), hx = __fmaf_rn(nb.sx, (float)n.qhi[0][i], nb.px);
-  const float ly = __fmaf_rn(nb.sy, (float)n.qlo[1][i], nb.py), hy = __fmaf_rn(nb.sy, (float)n.qhi[1][i], nb.py);
-  const float lz = __fmaf_rn(nb.sz, (float)n.qlo[2][i], nb.pz), hz = __fmaf_rn(nb.sz, (float)n.qhi[2][i], nb.pz);
-  const float t0x = (lx - r.ox) * r.ix, t1x = (hx - r.ox) * r.ix;
-  const float t0y = (ly - r.oy) * r.iy, t1y = (hy - r.oy) * r.iy;
-  const float t0z = (lz - r.oz) * r.iz, t1z = (hz - r.oz) * r.iz;
-  const float tn = fmaxf(fmaxf(fminf(t0x, t1x), fminf(t0y, t1y)), fmaxf(fminf(t0z, t1z), 0.0f));
-  const float tf = fminf(fminf(fmaxf(t0x, t1x), fmaxf(t0y, t1y)), fminf(fmaxf(t0z, t1z), tfar)) * kFarScale;
+__device__ __forceinline__ void slab_axis(float p, float e_scale, float o, float inv, uint2 lo, uint2 hi,
+                                          uint32_t* nq, uint32_t* fq, float& A, float& Bn, float& Bf) {
+  A = __fmul_rn(e_scale, inv);
+  const float B = __fmul_rn(__fsub_rn(p, o), inv);
+  const float u = 5.9604645e-08f;
+  float E = (5.0f * u) * (255.0f * fabsf(A) + fabsf(B) + fabsf(__fmul_rn(p, inv))) + 1e-30f;
+  E = E + (2.0f * u) * (fabsf(B) + E);  // the rounding of B -/+ E below
+  Bn = __fsub_rn(B, E);
+  Bf = __fadd_rn(B, E);
+  const bool pos = inv >= 0.0f;
+  nq[0] = pos ? lo.x : hi.x, nq[1] = pos ? lo.y : hi.y;
+  fq[0] = pos ? hi.x : lo.x, fq[1] = pos ? hi.y : lo.y;
+}
+
+__device__ __forceinline__ void slab_setup(const WNode8& n, float ox, float oy, float oz, float ix, float iy, float iz,
+                                           SlabSetup& S) {
+  const uint2* qlo = reinterpret_cast<const uint2*>(&n.qlo[0][0]);
+  const uint2* qhi = reinterpret_cast<const uint2*>(&n.qhi[0][0]);
+  slab_axis(n.px, __int_as_float((int)n.e[0] << 23), ox, ix, qlo[0], qhi[0], S.nq[0], S.fq[0], S.A[0], S.Bn[0],
+            S.Bf[0]);
+  slab_axis(n.py, __int_as_float((int)n.e[1] << 23), oy, iy, qlo[1], qhi[1], S.nq[1], S.fq[1], S.A[1], S.Bn[1],
+            S.Bf[1]);
+  slab_axis(n.pz, __int_as_float((int)n.e[2] << 23), oz, iz, qlo[2], qhi[2], S.nq[2], S.fq[2], S.A[2], S.Bn[2],
+            S.Bf[2]);
+}
+
+__device__ __forceinline__ float qbyte(const uint32_t* w, int i) { return (float)((w[i >> 2] >> (8 * (i & 3))) & 0xffu); }
+
+// Entry distance of slot i (clamped at 0), or +inf when the slot's box is
+// missed or begins beyond tfar.
+__device__ __forceinline__ float slot_test(const SlabSetup& S, int i, float tfar) {
+  const float nx = __fmaf_rn(qbyte(S.nq[0], i), S.A[0], S.Bn[0]), fx = __fmaf_rn(qbyte(S.fq[0], i), S.A[0], S.Bf[0]);
+  const float ny = __fmaf_rn(qbyte(S.nq[1], i), S.A[1], S.Bn[1]), fy = __fmaf_rn(qbyte(S.fq[1], i), S.A[1], S.Bf[1]);
+  const float nz = __fmaf_rn(qbyte(S.nq[2], i), S.A[2], S.Bn[2]), fz = __fmaf_rn(qbyte(S.fq[2], i), S.A[2], S.Bf[2]);
+  const float tn = fmaxf(fmaxf(nx, ny), fmaxf(nz, 0.0f));
+  const float tf = fminf(fminf(fx, fy), fminf(fz, tfar));
   return tn <= tf ? tn : __int_as_float(0x7f800000);
 }
 
-__device__ __forceinline__ void load_node(const WNode8* nodes, uint32_t i, WNode8& n, NodeBoxes& nb) {
+__device__ __forceinline__ void load_node(const WNode8* nodes, uint32_t i, WNode8& n) {
   const float4* s = reinterpret_cast<const float4*>(nodes + i);
   float4* d = reinterpret_cast<float4*>(&n);
 #pragma unroll
   for (int k = 0; k < 5; k++) d[k] = __ldg(s + k);
-  nb.px = n.px, nb.py = n.py, nb.pz = n.pz;
-  nb.sx = __int_as_float((int)n.e[0] << 23);
-  nb.sy = __int_as_float((int)n.e[1] << 23);
-  nb.sz = __int_as_float((int)n.e[2] << 23);
 }
 
 __device__ __forceinline__ uint32_t meta_at(const WNode8& n, int i) {
@@ -238,12 +277,13 @@ __device__ bool trace_fp64(const DevWBVH& b, const WRay& r, uint32_t* st_node, f
     const float far = __double2float_ru(tb) * kFarScale;
     if (st_t[sp] > far) continue;
     WNode8 n;
-    NodeBoxes nb;
-    load_node(b.nodes, ni, n, nb);
+    SlabSetup S;
+    load_node(b.nodes, ni, n);
+    slab_setup(n, r.ox, r.oy, r.oz, r.ix, r.iy, r.iz, S);
     for (int i = 0; i < 8; i++) {
       const uint32_t m = meta_at(n, i);
       if (!m) continue;
-      const float tn = slot_box(r, n, nb, i, far);
+      const float tn = slot_test(S, i, far);
       if (!(tn <= far)) continue;
       if (m & 0x80u) {
         if (sp >= kWStack) {
@@ -273,41 +313,55 @@ __device__ bool trace_fp64(const DevWBVH& b, const WRay& r, uint32_t* st_node, f
 
 constexpr uint32_t kLeafEntry = 0x80000000u;  // stack entry: bit 31 leaf, bits 29-30 count, 0-28 first triangle
 
+// Settlement records: a ray whose closest hit (or occlusion) FP32 could not
+// decide is not settled in the traversal kernel, where the few lanes doing
+// FP64 work would hold their warp's other lanes idle (binary64 runs at a small
+// fraction of the binary32 rate on this GPU). Instead the traversal appends a
+// 32-byte record and k_wide_settle re-tests the records' triangles in FP64,
+// one record per thread, so its warps run full.
+//   word 0  ray index
+//   word 1  the best FP32 hit's triangle slot, or -1
+//   word 2  candidate count (<= kRecCand), bit 31: trace the ray entirely in FP64
+//   words 3-7  candidate triangle slots
+constexpr int kRecCand = 5;
+constexpr uint32_t kRecFull = 0x80000000u;
+
 // Persistent traversal: each lane owns a ray and takes one step per round —
 // an inner node (eight slab tests; inner children and leaf groups pushed,
 // the nearest on top) or one leaf group (up to three triangle tests) — so
 // the warp's lanes do similar work each round; a lane whose ray is done takes
 // the next ray from the device cursor (one atomicAdd per warp). A ray that
-// would overflow the stack is traced again entirely in FP64.
+// would overflow the stack or keep more than kRecCand candidates is recorded
+// for a traversal entirely in FP64.
+//   counters[0]  ray fetch cursor;  counters[1]  records written
 template <bool ANY>
-// At least 6 resident blocks per SM: 80 registers with a few spills beat 90
-// registers and 5 blocks (290 vs 266 Mrays/s on a 4M-triangle soup).
-__global__ void __launch_bounds__(128, 6) k_trace_wide(const DevWBVH b, const float4* __restrict__ org,
+// 8 resident blocks of 128 threads per SM (64 registers): measured ahead of 6 (80 registers)
+__global__ void __launch_bounds__(128, 8) k_trace_wide(const DevWBVH b, const float4* __restrict__ org,
                                                     const float4* __restrict__ dir, int32_t* __restrict__ hit_out,
                                                     float* __restrict__ t_out, uint8_t* __restrict__ occ_out,
-                                                    uint32_t n, uint32_t* err, int* cursor,
+                                                    uint32_t n, int* counters, uint4* recs,
                                                     unsigned long long* stats) {
   uint32_t st_node[kWStack];
   float st_t[kWStack];
   const unsigned FULL = 0xffffffffu;
   const int lane = threadIdx.x & 31;
   const unsigned below = (1u << lane) - 1u;
-  unsigned long long n_rays = 0, n_retest = 0, n_full = 0, n_tbound = 0;
+  unsigned long long n_rays = 0;
   int rid = -1;
   bool exhausted = false;
   WRay r;
   int best = -1, nc = 0, sp = 0;
   float tb = 0.0f, tberr = 0.0f;
   bool overflow = false, occluded = false;
-  uint32_t cand[kCand];
-  float cand_lo[kCand];
+  uint32_t cand[kRecCand];
+  float cand_lo[kRecCand];
   while (true) {
     if (!exhausted) {
       const unsigned m = __ballot_sync(FULL, rid < 0);
       if (m == FULL || __popc(m) >= kWideRefill) {  // refill once 8 lanes are idle
         const int leader = __ffs(m) - 1;
         int base = 0;
-        if (lane == leader) base = atomicAdd(cursor, __popc(m));
+        if (lane == leader) base = atomicAdd(counters, __popc(m));
         base = __shfl_sync(FULL, base, leader);
         if ((uint32_t)(base + __popc(m)) >= n) exhausted = true;
         if (rid < 0) {
@@ -323,95 +377,150 @@ __global__ void __launch_bounds__(128, 6) k_trace_wide(const DevWBVH b, const fl
       }
     }
     if (__ballot_sync(FULL, rid >= 0) == 0) break;
-    if (rid < 0) continue;
-    // ---- one step
-    const float far = (tb + tberr) * kFarScale;
-    while (sp > 0 && st_t[sp - 1] > far) sp--;  // culled entries
-    bool finished = sp == 0 || overflow || (ANY && occluded);
-    if (!finished) {
-      const uint32_t ent = st_node[--sp];
-      if (ent & kLeafEntry) {
-        const uint32_t cnt = (ent >> 29) & 3u, first = ent & 0x1fffffffu;
-        for (uint32_t k = 0; k < cnt; k++) {
-          const uint32_t slot = first + k;
-          const float4* tr = b.tris + 3 * (size_t)slot;
-          float t, terr;
-          const int res = tri32(r, __ldg(tr), __ldg(tr + 1), __ldg(tr + 2), t, terr);
-          if (res == 0) continue;
-          if (res == 1 && t - terr > 0.0f && t + terr < tb - tberr) {
-            // certainly in range and certainly nearer than the best so far
-            best = (int)slot, tb = t, tberr = terr;
-            if (ANY) {
-              occluded = true;
-              break;
+    bool record = false;
+    if (rid >= 0) {
+      // ---- one step
+      const float far = (tb + tberr) * kFarScale;
+      while (sp > 0 && st_t[sp - 1] > far) sp--;  // culled entries
+      bool finished = sp == 0 || overflow || (ANY && occluded);
+      if (!finished) {
+        const uint32_t ent = st_node[--sp];
+        if (ent & kLeafEntry) {
+          const uint32_t cnt = (ent >> 29) & 3u, first = ent & 0x1fffffffu;
+          for (uint32_t k = 0; k < cnt; k++) {
+            const uint32_t slot = first + k;
+            const float4* tr = b.tris + 3 * (size_t)slot;
+            float t, terr;
+            const int res = tri32(r, __ldg(tr), __ldg(tr + 1), __ldg(tr + 2), t, terr);
+            if (res == 0) continue;
+            if (res == 1 && t - terr > 0.0f && t + terr < tb - tberr) {
+              // certainly in range and certainly nearer than the best so far
+              best = (int)slot, tb = t, tberr = terr;
+              if (ANY) {
+                occluded = true;
+                break;
+              }
+              continue;
             }
-            continue;
-          }
-          if (!(t - terr < tb + tberr)) continue;  // certainly beyond the best (or the ray's end)
-          if (res == 1 && t - terr > 0.0f && t < tb && t + terr < tb + tberr) {
-            // a certain hit nearer than the best within their errors: FP64 orders them
-            if (best >= 0) {
-              if (nc < kCand) cand[nc] = (uint32_t)best, cand_lo[nc] = tb - tberr, nc++;
-              else overflow = true;
+            if (!(t - terr < tb + tberr)) continue;  // certainly beyond the best (or the ray's end)
+            if (res == 1 && t - terr > 0.0f && t < tb && t + terr < tb + tberr) {
+              // a certain hit nearer than the best within their errors: FP64 orders them
+              if (best >= 0) {
+                if (nc < kRecCand) cand[nc] = (uint32_t)best, cand_lo[nc] = tb - tberr, nc++;
+                else overflow = true;
+              }
+              best = (int)slot, tb = t, tberr = terr;
+              continue;
             }
-            best = (int)slot, tb = t, tberr = terr;
-            continue;
+            if (nc < kRecCand) cand[nc] = slot, cand_lo[nc] = t - terr, nc++;
+            else overflow = true;
           }
-          if (nc < kCand) cand[nc] = slot, cand_lo[nc] = t - terr, nc++;
-          else overflow = true;
-        }
-      } else {
-        WNode8 nd;
-        NodeBoxes nb;
-        load_node(b.nodes, ent, nd, nb);
-        const int sp0 = sp;
+        } else {
+          WNode8 nd;
+          SlabSetup S;
+          load_node(b.nodes, ent, nd);
+          slab_setup(nd, r.ox, r.oy, r.oz, r.ix, r.iy, r.iz, S);
+          const int sp0 = sp;
 #pragma unroll
-        for (int i = 0; i < 8; i++) {
-          const uint32_t m = meta_at(nd, i);
-          if (!m) continue;
-          const float tn = slot_box(r, nd, nb, i, far);
-          if (!(tn <= far)) continue;
-          if (sp >= kWStack) {
-            overflow = true;  // settled by the full FP64 traversal
-            continue;
+          for (int i = 0; i < 8; i++) {
+            const uint32_t m = meta_at(nd, i);
+            if (!m) continue;
+            const float tn = slot_test(S, i, far);
+            if (!(tn <= far)) continue;
+            if (sp >= kWStack) {
+              overflow = true;  // settled by the full FP64 traversal
+              continue;
+            }
+            st_node[sp] = (m & 0x80u) ? nd.child_base + (m & 7u)
+                                      : (kLeafEntry | ((m >> 5) << 29) | (nd.prim_base + (m & 31u)));
+            st_t[sp] = tn;
+            sp++;
           }
-          st_node[sp] = (m & 0x80u) ? nd.child_base + (m & 7u)
-                                    : (kLeafEntry | ((m >> 5) << 29) | (nd.prim_base + (m & 31u)));
-          st_t[sp] = tn;
-          sp++;
+          if (sp - sp0 > 1) {
+            int bi = sp0;
+            for (int k = sp0 + 1; k < sp; k++)
+              if (st_t[k] < st_t[bi]) bi = k;
+            const uint32_t tnode = st_node[bi];
+            const float tt = st_t[bi];
+            st_node[bi] = st_node[sp - 1], st_t[bi] = st_t[sp - 1];
+            st_node[sp - 1] = tnode, st_t[sp - 1] = tt;
+          }
         }
-        if (sp - sp0 > 1) {
-          int bi = sp0;
-          for (int k = sp0 + 1; k < sp; k++)
-            if (st_t[k] < st_t[bi]) bi = k;
-          const uint32_t tnode = st_node[bi];
-          const float tt = st_t[bi];
-          st_node[bi] = st_node[sp - 1], st_t[bi] = st_t[sp - 1];
-          st_node[sp - 1] = tnode, st_t[sp - 1] = tt;
+        finished = sp == 0 || overflow || (ANY && occluded);
+      }
+      if (finished) {
+        if (!overflow) {
+          int k2 = 0;
+          for (int k = 0; k < nc; k++)
+            if (cand_lo[k] < tb + tberr) cand[k2] = cand[k], cand_lo[k2] = cand_lo[k], k2++;
+          nc = k2;
+        }
+        if (ANY && !occluded && best >= 0) occluded = true;
+        record = !(ANY && occluded) && (overflow || nc > 0 || (!ANY && best >= 0 && tberr > kTRel * tb));
+        if (!record) {
+          if (ANY) {
+            occ_out[rid] = occluded ? 1 : 0;
+          } else {
+            hit_out[rid] = best >= 0 ? __float_as_int(__ldg(b.tris + 3 * (size_t)best).w) : -1;
+            t_out[rid] = best >= 0 ? tb : r.tmax;
+          }
+          rid = -1;
         }
       }
-      finished = sp == 0 || overflow || (ANY && occluded);
     }
-    if (!finished) continue;
-    // ---- the ray is done: settle what FP32 could not
-    if (!overflow) {
-      int k2 = 0;
-      for (int k = 0; k < nc; k++)
-        if (cand_lo[k] < tb + tberr) cand[k2] = cand[k], cand_lo[k2] = cand_lo[k], k2++;
-      nc = k2;
+    // ---- records of the rays FP32 could not settle (one atomic per warp)
+    const unsigned rm = __ballot_sync(FULL, record);
+    if (rm) {
+      const int leader = __ffs(rm) - 1;
+      int base = 0;
+      if (lane == leader) base = atomicAdd(counters + 1, __popc(rm));
+      base = __shfl_sync(FULL, base, leader);
+      if (record) {
+        uint4* rec = recs + 2 * (size_t)(base + __popc(rm & below));
+        uint32_t c[kRecCand];
+#pragma unroll
+        for (int k = 0; k < kRecCand; k++) c[k] = k < nc ? cand[k] : 0u;
+        rec[0] = make_uint4((uint32_t)rid, (uint32_t)best, (uint32_t)nc | (overflow ? kRecFull : 0u), c[0]);
+        rec[1] = make_uint4(c[1], c[2], c[3], c[4]);
+        rid = -1;
+      }
     }
-    int out_prim = best >= 0 ? __float_as_int(__ldg(b.tris + 3 * (size_t)best).w) : -1;
-    float out_t = best >= 0 ? tb : r.tmax;
-    if (ANY && !occluded && best >= 0) occluded = true;
-    if (!(ANY && occluded) && overflow) {
+  }
+  if (stats) atomicAdd(stats + 0, n_rays);
+}
+
+// FP64 settlement of the records: the best FP32 hit and the candidates are
+// re-tested with the watertight test in FP64 and the nearest FP64 hit wins
+// (equal t: lower primitive id); a record flagged kRecFull is traced again
+// entirely in FP64 (trace_fp64). One record per thread, grid-stride over the
+// count the traversal left in counters[1].
+template <bool ANY>
+__global__ void __launch_bounds__(128) k_wide_settle(const DevWBVH b, const float4* __restrict__ org,
+                                                     const float4* __restrict__ dir, int32_t* __restrict__ hit_out,
+                                                     float* __restrict__ t_out, uint8_t* __restrict__ occ_out,
+                                                     const int* counters, const uint4* __restrict__ recs, uint32_t* err,
+                                                     unsigned long long* stats) {
+  uint32_t st_node[kWStack];
+  float st_t[kWStack];
+  const int nrec = counters[1];
+  unsigned long long n_retest = 0, n_full = 0, n_tbound = 0;
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < nrec; i += gridDim.x * blockDim.x) {
+    const uint4 r0 = recs[2 * (size_t)i], r1 = recs[2 * (size_t)i + 1];
+    const int rid = (int)r0.x, best = (int)r0.y;
+    const uint32_t nc = r0.z & 0xffu;
+    const uint32_t cand[kRecCand] = {r0.w, r1.x, r1.y, r1.z, r1.w};
+    WRay r;
+    setup(__ldg(org + rid), __ldg(dir + rid), r);
+    int out_prim = -1;
+    float out_t = r.tmax;
+    if (r0.z & kRecFull) {
       n_full++;
       double t64;
       int prim;
       const bool h = trace_fp64<ANY>(b, r, st_node, st_t, err, prim, t64);
       out_prim = h ? prim : -1;
       out_t = h ? (float)t64 : r.tmax;
-      occluded = h;
-    } else if (!(ANY && occluded) && (nc > 0 || (!ANY && best >= 0 && tberr > kTRel * tb))) {
+    } else {
       n_retest++;
       n_tbound += nc == 0;
       const Ray64 q = ray64(r);
@@ -424,21 +533,18 @@ __global__ void __launch_bounds__(128, 6) k_trace_wide(const DevWBVH b, const fl
         if (t < bt || (t == bt && prim < bp)) bt = t, bp = prim;
       };
       if (best >= 0) consider((uint32_t)best);
-      for (int k = 0; k < nc; k++) consider(cand[k]);
+      for (uint32_t k = 0; k < nc && k < (uint32_t)kRecCand; k++) consider(cand[k]);
       out_prim = bp;
       out_t = bp >= 0 ? (float)bt : r.tmax;
-      occluded = bp >= 0;
     }
     if (ANY) {
-      occ_out[rid] = occluded ? 1 : 0;
+      occ_out[rid] = out_prim >= 0 ? 1 : 0;
     } else {
       hit_out[rid] = out_prim;
       t_out[rid] = out_t;
     }
-    rid = -1;
   }
   if (stats) {
-    atomicAdd(stats + 0, n_rays);
     if (n_retest) atomicAdd(stats + 1, n_retest);
     if (n_full) atomicAdd(stats + 2, n_full);
     if (n_tbound) atomicAdd(stats + 3, n_tbound);
@@ -455,18 +561,6 @@ __global__ void __launch_bounds__(128, 6) k_trace_wide(const DevWBVH b, const fl
 struct MRay {
   float ox, oy, oz, dx, dy, dz, ix, iy, iz;
 };
-
-__device__ __forceinline__ float mslot_box(const MRay& r, const WNode8& n, const NodeBoxes& nb, int i, float tfar) {
-  const float lx = __fmaf_rn(nb.sx, (float)n.qlo[0][i], nb.px), hx = __fmaf_rn(nb.sx, (float)n.qhi[0][i], nb.px);
-  const float ly = __fmaf_rn(nb.sy, (float)n.qlo[1][i], nb.py), hy = __fmaf_rn(nb.sy, (float)n.qhi[1][i], nb.py);
-  const float lz = __fmaf_rn(nb.sz, (float)n.qlo[2][i], nb.pz), hz = __fmaf_rn(nb.sz, (float)n.qhi[2][i], nb.pz);
-  const float t0x = (lx - r.ox) * r.ix, t1x = (hx - r.ox) * r.ix;
-  const float t0y = (ly - r.oy) * r.iy, t1y = (hy - r.oy) * r.iy;
-  const float t0z = (lz - r.oz) * r.iz, t1z = (hz - r.oz) * r.iz;
-  const float tn = fmaxf(fmaxf(fminf(t0x, t1x), fminf(t0y, t1y)), fmaxf(fminf(t0z, t1z), 0.0f));
-  const float tf = fminf(fminf(fmaxf(t0x, t1x), fmaxf(t0y, t1y)), fminf(fmaxf(t0z, t1z), tfar)) * kFarScale;
-  return tn <= tf ? tn : __int_as_float(0x7f800000);
-}
 
 // Persistent, one step per round (as k_trace_wide). IO::load(i, o, d, t0, bvh, eps),
 // IO::store(i, hit, t, overflow).
@@ -527,14 +621,15 @@ __device__ __forceinline__ void trace_wide_mt(int n, int* cursor, IO& io, uint32
         finished = ANY && hit >= 0;
       } else {
         WNode8 nd;
-        NodeBoxes nb;
-        load_node(b.nodes, ent, nd, nb);
+        SlabSetup S;
+        load_node(b.nodes, ent, nd);
+        slab_setup(nd, r.ox, r.oy, r.oz, r.ix, r.iy, r.iz, S);
         const int sp0 = sp;
 #pragma unroll
         for (int i = 0; i < 8; i++) {
           const uint32_t m = meta_at(nd, i);
           if (!m) continue;
-          const float tn = mslot_box(r, nd, nb, i, far);
+          const float tn = slot_test(S, i, far);
           if (!(tn <= far)) continue;
           if (sp >= kWStack) {
             overflow = true;
@@ -740,37 +835,42 @@ int mt_grid(K kernel, int capacity) {
   return std::max(1, std::min(cap_blocks, std::max(1, per) * sm_count()));
 }
 
-int wide_grid() {
-  static int g = 0;
-  if (!g) {
-    int per = 0;
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k_trace_wide<false>, 128, 0);
-    g = std::max(1, per) * sm_count();
-  }
-  return g;
+template <typename K>
+int resident_blocks(K kernel) {
+  int per = 0;
+  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, kernel, 128, 0);
+  return std::max(1, per) * sm_count();
+}
+
+template <bool ANY>
+cudaError_t launch_wide_query(const DevWBVH& b, const float4* org, const float4* dir, int32_t* hit, float* t,
+                              uint8_t* occ, uint32_t n, uint32_t* err, int* counters, uint4* recs,
+                              unsigned long long* stats, cudaStream_t s) {
+  if (n == 0) return cudaSuccess;
+  cudaError_t e = cudaMemsetAsync(counters, 0, 2 * sizeof(int), s);
+  if (e != cudaSuccess) return e;
+  static int g_trace = 0, g_settle = 0;
+  if (!g_trace) g_trace = resident_blocks(k_trace_wide<ANY>), g_settle = resident_blocks(k_wide_settle<ANY>);
+  const int g = std::min<int>(g_trace, (int)((n + 127) / 128));
+  k_trace_wide<ANY><<<g, 128, 0, s>>>(b, org, dir, hit, t, occ, n, counters, recs, stats);
+  if ((e = cudaGetLastError()) != cudaSuccess) return e;
+  // the record count stays on the device: a grid of resident blocks strides over it
+  k_wide_settle<ANY><<<std::min<int>(g_settle, g), 128, 0, s>>>(b, org, dir, hit, t, occ, counters, recs, err, stats);
+  return cudaGetLastError();
 }
 
 }  // namespace
 
 cudaError_t launch_trace_wide_closest(const DevWBVH& b, const float4* org, const float4* dir, int32_t* hit, float* t,
-                                      uint32_t n, uint32_t* err, int* cursor, unsigned long long* stats,
-                                      cudaStream_t s) {
-  if (n == 0) return cudaSuccess;
-  cudaError_t e = cudaMemsetAsync(cursor, 0, sizeof(int), s);
-  if (e != cudaSuccess) return e;
-  const int g = std::min<int>(wide_grid(), (int)((n + 127) / 128));
-  k_trace_wide<false><<<g, 128, 0, s>>>(b, org, dir, hit, t, nullptr, n, err, cursor, stats);
-  return cudaGetLastError();
+                                      uint32_t n, uint32_t* err, int* counters, void* recs,
+                                      unsigned long long* stats, cudaStream_t s) {
+  return launch_wide_query<false>(b, org, dir, hit, t, nullptr, n, err, counters, (uint4*)recs, stats, s);
 }
 
 cudaError_t launch_trace_wide_any(const DevWBVH& b, const float4* org, const float4* dir, uint8_t* occ, uint32_t n,
-                                  uint32_t* err, int* cursor, unsigned long long* stats, cudaStream_t s) {
-  if (n == 0) return cudaSuccess;
-  cudaError_t e = cudaMemsetAsync(cursor, 0, sizeof(int), s);
-  if (e != cudaSuccess) return e;
-  const int g = std::min<int>(wide_grid(), (int)((n + 127) / 128));
-  k_trace_wide<true><<<g, 128, 0, s>>>(b, org, dir, nullptr, nullptr, occ, n, err, cursor, stats);
-  return cudaGetLastError();
+                                  uint32_t* err, int* counters, void* recs, unsigned long long* stats,
+                                  cudaStream_t s) {
+  return launch_wide_query<true>(b, org, dir, nullptr, nullptr, occ, n, err, counters, (uint4*)recs, stats, s);
 }
 
 

@@ -83,9 +83,10 @@ struct Request {
 
 size_t request_bytes(const Request& r) {
   if (r.kind == kRender) return (size_t)r.slots * r.pixels * sizeof(float4);
-  // org + dir + hit/occluded + t + cursor, each 256-byte aligned
+  // org + dir + hit/occluded + t + counters (+ settlement records on a wide BVH), each 256-byte aligned
   auto al = [](size_t b) { return (b + 255) & ~(size_t)255; };
-  return al((size_t)r.n * 16) * 2 + al((size_t)r.n * 4) * 2 + 256;
+  return al((size_t)r.n * 16) * 2 + al((size_t)r.n * 4) * 2 + 256 +
+         (rt_bvh_wide(r.bvh) ? al((size_t)r.n * kWideRecordBytes) : 0);
 }
 
 }  // namespace
@@ -175,14 +176,16 @@ void ct_server::start_query(Request* r) {
   int32_t* hit = (int32_t*)(m + 2 * al((size_t)r->n * 16));
   float* t = (float*)(m + 2 * al((size_t)r->n * 16) + al((size_t)r->n * 4));
   int* cursor = (int*)(m + 2 * al((size_t)r->n * 16) + 2 * al((size_t)r->n * 4));
+  void* recs = m + 2 * al((size_t)r->n * 16) + 2 * al((size_t)r->n * 4) + 256;
   cudaError_t e = cudaMemcpyAsync(org, r->horg, (size_t)r->n * 16, cudaMemcpyHostToDevice, qs);
   if (e == cudaSuccess) e = cudaMemcpyAsync(dir, r->hdir, (size_t)r->n * 16, cudaMemcpyHostToDevice, qs);
   if (e == cudaSuccess) {
     uint32_t* err = rt_ctx_error(ctx);
     if (rt_bvh_wide(r->bvh)) {
       e = r->kind == kClosest
-              ? launch_trace_wide_closest(rt_bvh_wdev(r->bvh), org, dir, hit, t, r->n, err, cursor, nullptr, qs)
-              : launch_trace_wide_any(rt_bvh_wdev(r->bvh), org, dir, (uint8_t*)hit, r->n, err, cursor, nullptr, qs);
+              ? launch_trace_wide_closest(rt_bvh_wdev(r->bvh), org, dir, hit, t, r->n, err, cursor, recs, nullptr, qs)
+              : launch_trace_wide_any(rt_bvh_wdev(r->bvh), org, dir, (uint8_t*)hit, r->n, err, cursor, recs, nullptr,
+                                      qs);
     } else {
       e = r->kind == kClosest
               ? launch_trace_closest(rt_bvh_dev(r->bvh), org, dir, hit, t, r->n, r->tri_eps, err, cursor, qs)

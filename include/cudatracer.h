@@ -125,8 +125,9 @@ enum { CT_SHADE_COMPAT = 0, CT_SHADE_FULL = 1 };
  *   CT_MATH_FAST        CUDA float transcendentals and FMA contraction in ray
  *                       generation and shading; traversal with fused slab
  *                       planes and children in full distance order.
- *   CT_MATH_EXACT       ray generation and shading bit-reproducible (no FMA,
- *                       sin/cos/atan2/acos in double rounded once) and the
+ *   CT_MATH_EXACT       ray generation and shading bit-reproducible (no FMA
+ *                       contraction; sin/cos/atan2/acos as fixed sequences of
+ *                       correctly rounded binary32 operations) and the
  *                       reference's traversal arithmetic and child order:
  *                       accumulation bit-identical to the oracle; frames run
  *                       one after another.
@@ -250,7 +251,11 @@ ct_status ct_bvh_build_fast(ct_ctx* ctx, const ct_scene* scene, int32_t nthreads
  * is the reference's Moller-Trumbore with tri_eps, so the hits are the quad
  * tree's up to the winner of an exact t tie. Export with CT_BVH_WIDE8_Q8
  * (80-byte nodes; prim_indices in leaf order). info.quad_node_count and
- * info.quad_depth describe the wide tree. */
+ * info.quad_depth describe the wide tree. Queries on it write a 32-byte
+ * settlement record per ray whose FP32 result needs FP64 re-tests; the
+ * context keeps a buffer of 32 bytes per ray of its largest wide query,
+ * allocated by the first query that needs more (counted against the
+ * context's memory budget). */
 ct_status ct_bvh_build_wide(ct_ctx* ctx, const ct_scene* scene, void* stream, ct_bvh** out);
 /* Counters of the wide tree's queries since the last reset: rays traced, rays
  * whose result needed FP64 re-tests, of those the ones re-tested only to

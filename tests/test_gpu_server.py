@@ -146,7 +146,10 @@ def test_admission_respects_the_budget(gpu_ctx, world):
         k = max(1, min(r["spp"], 65536 // px))
         return min(r["spp"], 2 * k) * px * 16  # slot buffers
 
-    sizes = [render_bytes(r) if k == "render" else r["org"].shape[0] * 40 + 2048 for k, r in reqs]
+    def query_bytes(r):  # rays, results, counters; queries on the wide tree add 32 B of records per ray
+        return r["org"].shape[0] * (72 if r["bvh"] is world["query"][1] else 40) + 2048
+
+    sizes = [render_bytes(r) if k == "render" else query_bytes(r) for k, r in reqs]
     budget = max(sizes) + 4096
     srv = api.Server(gpu_ctx, hbm_budget=budget, max_inflight_pixels=1 << 16)
     ids = [_submit(srv, *r) for r in reqs]
