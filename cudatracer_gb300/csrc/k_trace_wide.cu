@@ -258,8 +258,10 @@ __device__ __forceinline__ uint32_t meta_at(const WNode8& n, int i) {
 
 // A warp refills its idle lanes from the cursor once this many are idle (or
 // all are): fewer cursor atomics and refill passes than refilling at the
-// first idle lane (measured best for queries and frames on the wide tree).
-constexpr int kWideRefill = 8;
+// first idle lane. Queries (10M-triangle soup, incoherent rays): 4 ahead of 8
+// and 16; frames on the wide tree: 8.
+constexpr int kWideRefill = 4;
+constexpr int kWideFrameRefill = 8;
 
 // Whole traversal in FP64 triangle tests (boxes as above, culled with the FP64
 // best distance rounded up): the fallback for rays with too many candidates.
@@ -353,12 +355,14 @@ __global__ void __launch_bounds__(128, 8) k_trace_wide(const DevWBVH b, const fl
   int best = -1, nc = 0, sp = 0;
   float tb = 0.0f, tberr = 0.0f;
   bool overflow = false, occluded = false;
+  uint32_t cur = 0;        // the entry visited next, when have_cur (a node's nearest hit slot)
+  bool have_cur = false;
   uint32_t cand[kRecCand];
   float cand_lo[kRecCand];
   while (true) {
     if (!exhausted) {
       const unsigned m = __ballot_sync(FULL, rid < 0);
-      if (m == FULL || __popc(m) >= kWideRefill) {  // refill once 8 lanes are idle
+      if (m == FULL || __popc(m) >= kWideRefill) {  // refill once kWideRefill lanes are idle
         const int leader = __ffs(m) - 1;
         int base = 0;
         if (lane == leader) base = atomicAdd(counters, __popc(m));
@@ -371,7 +375,7 @@ __global__ void __launch_bounds__(128, 8) k_trace_wide(const DevWBVH b, const fl
             rid = my;
             n_rays++;
             best = -1, nc = 0, tb = r.tmax, tberr = 0.0f, overflow = false, occluded = false;
-            st_node[0] = 0, st_t[0] = 0.0f, sp = 1;
+            sp = 0, cur = 0, have_cur = true;  // the root
           }
         }
       }
@@ -381,10 +385,12 @@ __global__ void __launch_bounds__(128, 8) k_trace_wide(const DevWBVH b, const fl
     if (rid >= 0) {
       // ---- one step
       const float far = (tb + tberr) * kFarScale;
-      while (sp > 0 && st_t[sp - 1] > far) sp--;  // culled entries
-      bool finished = sp == 0 || overflow || (ANY && occluded);
+      if (!have_cur)
+        while (sp > 0 && st_t[sp - 1] > far) sp--;  // culled entries
+      bool finished = (!have_cur && sp == 0) || overflow || (ANY && occluded);
       if (!finished) {
-        const uint32_t ent = st_node[--sp];
+        const uint32_t ent = have_cur ? cur : st_node[--sp];
+        have_cur = false;
         if (ent & kLeafEntry) {
           const uint32_t cnt = (ent >> 29) & 3u, first = ent & 0x1fffffffu;
           for (uint32_t k = 0; k < cnt; k++) {
@@ -420,33 +426,35 @@ __global__ void __launch_bounds__(128, 8) k_trace_wide(const DevWBVH b, const fl
           SlabSetup S;
           load_node(b.nodes, ent, nd);
           slab_setup(nd, r.ox, r.oy, r.oz, r.ix, r.iy, r.iz, S);
-          const int sp0 = sp;
+          // the nearest hit slot is visited next without a stack round trip; the
+          // others are pushed (a slot displaced as nearest is pushed when replaced)
+          float tcur = __int_as_float(0x7f800000);
 #pragma unroll
           for (int i = 0; i < 8; i++) {
             const uint32_t m = meta_at(nd, i);
             if (!m) continue;
             const float tn = slot_test(S, i, far);
             if (!(tn <= far)) continue;
+            const uint32_t ce = (m & 0x80u) ? nd.child_base + (m & 7u)
+                                            : (kLeafEntry | ((m >> 5) << 29) | (nd.prim_base + (m & 31u)));
+            uint32_t pe = ce;
+            float pt = tn;
+            if (tn < tcur) {
+              pe = cur, pt = tcur;
+              cur = ce, tcur = tn;
+              if (!have_cur) {
+                have_cur = true;
+                continue;
+              }
+            }
             if (sp >= kWStack) {
               overflow = true;  // settled by the full FP64 traversal
               continue;
             }
-            st_node[sp] = (m & 0x80u) ? nd.child_base + (m & 7u)
-                                      : (kLeafEntry | ((m >> 5) << 29) | (nd.prim_base + (m & 31u)));
-            st_t[sp] = tn;
-            sp++;
-          }
-          if (sp - sp0 > 1) {
-            int bi = sp0;
-            for (int k = sp0 + 1; k < sp; k++)
-              if (st_t[k] < st_t[bi]) bi = k;
-            const uint32_t tnode = st_node[bi];
-            const float tt = st_t[bi];
-            st_node[bi] = st_node[sp - 1], st_t[bi] = st_t[sp - 1];
-            st_node[sp - 1] = tnode, st_t[sp - 1] = tt;
+            st_node[sp] = pe, st_t[sp] = pt, sp++;
           }
         }
-        finished = sp == 0 || overflow || (ANY && occluded);
+        finished = (!have_cur && sp == 0) || overflow || (ANY && occluded);
       }
       if (finished) {
         if (!overflow) {
@@ -579,7 +587,7 @@ __device__ __forceinline__ void trace_wide_mt(int n, int* cursor, IO& io, uint32
   while (true) {
     if (!exhausted) {
       const unsigned m = __ballot_sync(FULL, rid < 0);
-      if (m == FULL || __popc(m) >= kWideRefill) {  // refill once 8 lanes are idle
+      if (m == FULL || __popc(m) >= kWideFrameRefill) {  // refill once 8 lanes are idle
         const int leader = __ffs(m) - 1;
         int base = 0;
         if (lane == leader) base = atomicAdd(cursor, __popc(m));
