@@ -1013,6 +1013,42 @@ void or_render_frame(const OrSceneDesc* sd, const float* cam_pos, const float* c
   });
 }
 
+/* 1-spp frames frames[0..nframes) (seed frame indices, in that order) over the
+ * pixels listed in `pixels` of a W x H image, adding into accum (float4 per
+ * pixel, full image size). Each pixel accumulates its frames in frame order,
+ * exactly as or_render_frame called once per frame would; the threads are
+ * started once for all frames and take the listed pixels interleaved, so
+ * scattered rows of a frame are rendered in one balanced pass. */
+void or_render_pixels(const OrSceneDesc* sd, const float* cam_pos, const float* cam_w, const float* hor,
+                      const float* ver, int W, int H, const uint32_t* frames, int nframes, int depth, int exact_math,
+                      float* accum, const int32_t* pixels, int npix, int nthreads) {
+  SceneView s{sd->verts, sd->normals, sd->center_normals, sd->uvs, sd->idx, sd->mat_idx, (const Material*)sd->materials,
+              sd->lights, sd->light_count, sd->tex, sd->tex_dims, sd->tex_offsets, sd->sky_tex, sd->sky_enabled,
+              sd->shadow, sd->indirect, sd->normal_eps, sd->dist_eps, sd->tri_eps, (const QNode*)sd->qnodes,
+              sd->prims, sd->tex_filter};
+  Geo g{sd->verts, sd->idx, sd->prims, (const QNode*)sd->qnodes, nullptr, sd->tri_eps};
+  const V3 co = load3(cam_pos, 0), cw = load3(cam_w, 0), h = load3(hor, 0), v = load3(ver, 0);
+  const int nt = std::max(1, std::min(nthreads, npix));
+  auto work = [&](int t) {
+    Work we, ws;
+    for (int i = t; i < npix; i += nt) {
+      const int pix = pixels[i];
+      for (int f = 0; f < nframes; f++)
+        render_path(s, g, pix, pix % W, (pix / W) % H, W, H, frames[f], depth, co, cw, h, v, exact_math,
+                    accum + 4 * (size_t)pix, &we, &ws);
+    }
+    g_work[0] += we.rays, g_work[1] += we.nodes, g_work[2] += we.tris;
+    g_work[3] += ws.rays, g_work[4] += ws.nodes, g_work[5] += ws.tris;
+  };
+  if (nt == 1) {
+    work(0);
+    return;
+  }
+  std::vector<std::thread> ts;
+  for (int t = 0; t < nt; t++) ts.emplace_back(work, t);
+  for (auto& th : ts) th.join();
+}
+
 /* The closest hit of every extension pass of one pixel's path in one frame:
  * primitive id (-1: miss) and t per pass, -2 and 0 for passes the path does
  * not reach. Comparing the logs of two trees shows at which bounce their

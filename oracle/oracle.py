@@ -404,6 +404,26 @@ def render_frames(arrays: dict, materials: np.ndarray, quad, prims, camera: dict
     return accum
 
 
+def render_pixels(arrays: dict, materials: np.ndarray, quad, prims, camera: dict, width: int, height: int,
+                  frames, depth: int, pixels, accum: np.ndarray | None = None, exact_math: bool = True,
+                  textures=(), sky_tex: int = -1, nthreads: int = 8, **kw) -> np.ndarray:
+    """Accumulate 1-spp frames (seed frame indices `frames`, in order) over the
+    listed pixel indices into accum (h*w, 4), in one parallel pass."""
+    L = lib()
+    if accum is None:
+        accum = np.zeros((width * height, 4), np.float32)
+    d, pos, fw, hor, ver, _keep = _frame_scene(arrays, materials, quad, prims, camera, width, height, textures,
+                                               sky_tex, **kw)
+    px = np.ascontiguousarray(pixels, np.int32)
+    fr = np.ascontiguousarray(frames, np.uint32)
+    P = ctypes.c_void_p
+    L.or_render_pixels.argtypes = [P, P, P, P, P, ctypes.c_int, ctypes.c_int, P, ctypes.c_int, ctypes.c_int,
+                                   ctypes.c_int, P, P, ctypes.c_int, ctypes.c_int]
+    L.or_render_pixels(ctypes.byref(d), _p(pos), _p(fw), _p(hor), _p(ver), width, height, _p(fr), int(fr.size), depth,
+                       int(exact_math), _p(accum), _p(px), int(px.size), int(nthreads))
+    return accum
+
+
 def path_hits(arrays: dict, materials: np.ndarray, quad, prims, camera: dict, width: int, height: int, frame: int,
               depth: int, pixel: int, exact_math: bool = True, textures=(), sky_tex: int = -1, **kw):
     """Closest hit of each extension pass of one pixel's path: (primitive ids,
