@@ -465,19 +465,11 @@ def batching_jobs(ctx, n_jobs: int = 256, seed: int = 2024, math: int = MATH["ex
     }
 
 
-def serving_poisson(ctx, rate: float = 100.0, duration_s: float = 5.0, seed: int = 77, iter_pixels: int = 0,
-                    math: int = MATH["exact-shade"]) -> dict:
-    """The serving workload: a Poisson request stream (rate req/s for
-    duration_s) mixing render jobs (the batching workload's job distribution over 16
-    resident terrain scenes) and ray queries (10k..4M incoherent rays against resident
-    wide BVHs of 10k..10M-triangle soups), through ct_server with a 150 GB
-    HBM budget. Latency = completion - submission. Serial plain execution: the
-    same requests' service times measured one at a time through the plain
-    per-request path, queued FIFO at the same arrival times."""
-    import threading
-
+def serving_world(ctx, seed: int = 77) -> dict:
+    """The serving workload's resident state: 16 terrain scenes of the batching
+    workload's kind (10k..2M triangles) on fast trees, wide BVHs of 10k..10M-
+    triangle soups, and a pool of 4M incoherent rays."""
     import numpy as np
-    import torch
 
     from cudatracer_gb300 import api, scenes
 
@@ -501,6 +493,37 @@ def serving_poisson(ctx, rate: float = 100.0, duration_s: float = 5.0, seed: int
         qbvhs.append((sq, sq.build_bvh_wide()))
     ray_o, ray_d = scenes.incoherent_rays(4_000_000, seed=seed)
     setup_s = time.perf_counter() - t0
+    return dict(rscenes=rscenes, qbvhs=qbvhs, ray_o=ray_o, ray_d=ray_d, setup_s=setup_s)
+
+
+def serving_close(world: dict) -> None:
+    for sc, bvh, _ in world["rscenes"]:
+        bvh.close()
+        sc.close()
+    for sq, b in world["qbvhs"]:
+        b.close()
+        sq.close()
+
+
+def serving_poisson(ctx, world: dict, rate: float = 100.0, duration_s: float = 5.0, seed: int = 77,
+                    iter_pixels: int = 0, math: int = MATH["exact-shade"]) -> dict:
+    """The serving workload: a Poisson request stream (rate req/s for
+    duration_s) mixing render jobs (the batching workload's job distribution over 16
+    resident terrain scenes) and ray queries (10k..4M incoherent rays against resident
+    wide BVHs of 10k..10M-triangle soups), through ct_server with a 150 GB
+    HBM budget. Latency = completion - submission. Serial plain execution: the
+    same requests' service times measured one at a time through the plain
+    per-request path, queued FIFO at the same arrival times."""
+    import threading
+
+    import numpy as np
+    import torch
+
+    from cudatracer_gb300 import api, scenes
+
+    rng = np.random.default_rng(seed)
+    rscenes, qbvhs, ray_o, ray_d = world["rscenes"], world["qbvhs"], world["ray_o"], world["ray_d"]
+    setup_s = world["setup_s"]
     # the request list
     n_req = int(rate * duration_s)
     arrivals = np.cumsum(rng.exponential(1.0 / rate, n_req))
@@ -582,12 +605,6 @@ def serving_poisson(ctx, rate: float = 100.0, duration_s: float = 5.0, seed: int
         return {"p50": float(np.percentile(x, 50)), "p95": float(np.percentile(x, 95)),
                 "p99": float(np.percentile(x, 99))}
 
-    for sc, bvh, _ in rscenes:
-        bvh.close()
-        sc.close()
-    for sq, b in qbvhs:
-        b.close()
-        sq.close()
     return {
         "workload": f"Poisson {rate:g} req/s for {duration_s:g} s: {n_req} requests, {int(kinds.sum())} renders "
                     f"(res 64..1024, spp 1..64, depth 4..12 over 16 resident scenes of 10k..2M triangles), "
@@ -597,7 +614,8 @@ def serving_poisson(ctx, rate: float = 100.0, duration_s: float = 5.0, seed: int
         "mrays_per_s": rays / wall / 1e6, "wall_s": wall, "completed": st["completed"], "failed": st["failed"],
         "peak_request_bytes": st["peak_bytes"], "iterations": st["iterations"],
         "serial_plain_latency_ms": pct(slat), "serial_plain_busy_s": float(sum(svc)),
-        "iter_pixels": iter_pixels or (1 << 24), "setup_s": setup_s, "render_tree": "ct_bvh_build_fast",
+        "iter_pixels": iter_pixels or (1 << 22), "setup_s": setup_s, "render_tree": "ct_bvh_build_fast",
+        "rate_req_per_s": rate, "seed": seed,
     }
 
 
@@ -889,10 +907,14 @@ def run_ours(args, world, rank, local):
     c4 = batching_jobs(ctx, math=math) if (rank == 0 and not args.skip_serving) else None
     # the light end of the request-rate range, one where serial execution saturates, and the
     # top of the range (2,000 req/s), where the server saturates too
-    c5 = ([serving_poisson(ctx, duration_s=10.0, math=math),
-           serving_poisson(ctx, rate=400.0, duration_s=2.0, math=math),
-           serving_poisson(ctx, rate=2000.0, duration_s=1.0, math=math)]
-          if (rank == 0 and not args.skip_serving) else None)
+    c5 = None
+    if rank == 0 and not args.skip_serving:
+        sw = serving_world(ctx)
+        # three 10-s runs at the light end (100 req/s, other arrival seeds), and the two heavy rates
+        c5 = [serving_poisson(ctx, sw, duration_s=10.0, seed=sd, math=math) for sd in (77, 78, 79)]
+        c5 += [serving_poisson(ctx, sw, rate=400.0, duration_s=2.0, math=math),
+               serving_poisson(ctx, sw, rate=2000.0, duration_s=1.0, math=math)]
+        serving_close(sw)
     # our kernels in the timed region: per frame raygen + depth x (extend, shade,
     # connect) + the fold of a fast-math frame slot (the launch counts of the
     # stage-timing pass, which has no fold, confirm the per-frame stage count)

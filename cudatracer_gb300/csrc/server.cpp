@@ -3,13 +3,17 @@
 // One scheduler thread owns the device work. Each turn it
 //   1. admits pending requests in arrival order while the HBM budget and the
 //      shared queue capacity allow (render: its accumulation buffer and its
-//      pixels of the queues; query: its ray and result buffers);
+//      pixels of the queues; query: its ray and result buffers); a query may
+//      pass a render job that waits only for queue space;
 //   2. starts admitted queries on the query stream (copy in, trace, copy out);
 //   3. runs one batched iteration of all admitted render jobs (up to k samples
 //      each, the ct_batch kernels with a job table built for this iteration),
 //      alternating between two render streams with a queue set each, so one
 //      iteration's last, nearly empty bounces overlap the next iteration's
-//      first passes; at most two iterations ahead of the device;
+//      first passes; an iteration is issued once its stream's previous one has
+//      finished (at most two in flight), and the thread never blocks on one, so
+//      queries that arrive meanwhile start at once on their own stream, which
+//      runs at the device's highest priority;
 //   4. retires requests whose completion events have fired, freeing their
 //      device state and waking waiters.
 // Jobs arriving while others are on the GPU join at the next iteration; a
@@ -41,7 +45,7 @@ using namespace ct;
 
 namespace {
 
-constexpr uint32_t kIterPixels = 1u << 24;  // default pixel-samples a job may take per iteration
+constexpr uint32_t kIterPixels = 1u << 22;  // default pixel-samples a job may take per iteration
 // Render streams, each with a queue set and a job table (measured at 100 and
 // 400 requests/s: 4 streams gave the same tails as 2 within noise, for two more
 // queue sets).
@@ -360,34 +364,45 @@ void ct_server::loop() {
       cv.wait(lk, [&] { return stop || !pending.empty(); });
       continue;
     }
-    // admissions in arrival order (accounting under the lock, device work outside)
+    // admissions in arrival order (accounting under the lock, device work outside);
+    // a query may pass a render job that waits for queue space (renders keep their
+    // order among themselves, and the HBM budget is taken in arrival order)
     std::vector<Request*> admitted;
-    while (!pending.empty()) {
-      Request* r = pending.front();
+    bool render_waits = false;
+    for (size_t i = 0; i < pending.size();) {
+      Request* r = pending[i];
+      if (r->kind == kRender && render_waits) {
+        i++;
+        continue;
+      }
       r->bytes = request_bytes(*r);
       const bool fits_budget = cfg.hbm_budget == 0 || used_bytes + r->bytes <= cfg.hbm_budget;
       const bool fits_queue = r->kind != kRender || inflight_pixels + r->k * r->pixels <= cfg.max_inflight_pixels;
       if (!fits_budget || !fits_queue) {
-        if (render.empty() && finishing.empty() && admitted.empty()) {
+        if (i == 0 && render.empty() && finishing.empty() && admitted.empty()) {
           // cannot fit even with nothing else admitted
-          pending.pop_front();
+          pending.erase(pending.begin());
           r->status = CT_ERR_OUT_OF_MEMORY;
           r->bytes = 0;
           r->state = kFinishing;
           finishing.push_back(r);
           continue;
         }
+        if (fits_budget && r->kind == kRender) {  // waits for queue space only
+          render_waits = true;
+          i++;
+          continue;
+        }
         break;
       }
+      pending.erase(pending.begin() + (std::ptrdiff_t)i);
       if (!rt_account(ctx, (int64_t)r->bytes)) {
-        pending.pop_front();
         r->status = CT_ERR_OUT_OF_MEMORY;
         r->bytes = 0;
         r->state = kFinishing;
         finishing.push_back(r);
         continue;
       }
-      pending.pop_front();
       used_bytes += r->bytes;
       stats.peak_bytes = std::max<uint64_t>(stats.peak_bytes, used_bytes);
       if (r->kind == kRender) inflight_pixels += r->k * r->pixels;
@@ -408,8 +423,15 @@ void ct_server::loop() {
         finished.push_back(r);  // completion event recorded on the query stream
       }
     }
-    bool iterated = false;
+    bool iterated = false, stream_busy = false;
     if (!render.empty()) {
+      // issue the next iteration only once its stream's previous one has finished,
+      // so the thread keeps admitting and starting queries in the meantime
+      const cudaError_t q = cudaEventQuery(table_ev[slot]);
+      stream_busy = q == cudaErrorNotReady;
+      if (stream_busy) cudaGetLastError();
+    }
+    if (!render.empty() && !stream_busy) {
       const cudaError_t e = render_iteration(finished);
       iterated = true;
       if (e != cudaSuccess) {
@@ -427,11 +449,11 @@ void ct_server::loop() {
     if (iterated) stats.iterations++;
     for (Request* r : finished) r->state = kFinishing, finishing.push_back(r);
     retire_locked();
-    if (render.empty() && !finishing.empty() && pending.empty()) {
-      // only completions outstanding: wait briefly instead of spinning
-      lk.unlock();
-      std::this_thread::sleep_for(std::chrono::microseconds(50));
-      lk.lock();
+    if ((render.empty() && !finishing.empty() && pending.empty()) || stream_busy) {
+      // only completions outstanding, or the render streams busy: wait briefly
+      // instead of spinning (a new arrival ends the wait at once)
+      const uint64_t seen = next_id;  // advances with every submission
+      cv.wait_for(lk, std::chrono::microseconds(50), [&] { return stop || next_id != seen; });
     }
   }
 }
@@ -466,8 +488,14 @@ ct_status ct_server_create(ct_ctx* ctx, const ct_server_config* cfg, ct_server**
   }
   for (int k = 0; k < kStreams && st == CT_OK && e == cudaSuccess; k++)
     e = cudaStreamCreateWithFlags(&s->rs[k], cudaStreamNonBlocking);
-  if (st == CT_OK && e == cudaSuccess) e = cudaStreamCreateWithFlags(&s->qs, cudaStreamNonBlocking);
-  if (st == CT_OK && e == cudaSuccess) e = cudaStreamCreateWithFlags(&s->ms, cudaStreamNonBlocking);
+  // ray queries and the request set-up (zero fills) run at the device's highest stream
+  // priority: their kernels are short and a query should not wait behind a render iteration
+  int prio_least = 0, prio_greatest = 0;
+  if (st == CT_OK && e == cudaSuccess) e = cudaDeviceGetStreamPriorityRange(&prio_least, &prio_greatest);
+  if (st == CT_OK && e == cudaSuccess)
+    e = cudaStreamCreateWithPriority(&s->qs, cudaStreamNonBlocking, prio_greatest);
+  if (st == CT_OK && e == cudaSuccess)
+    e = cudaStreamCreateWithPriority(&s->ms, cudaStreamNonBlocking, prio_greatest);
   for (int k = 0; k < kStreams && st == CT_OK && e == cudaSuccess; k++) {
     e = cudaEventCreateWithFlags(&s->table_ev[k], cudaEventDisableTiming);
     if (e == cudaSuccess) e = cudaEventRecord(s->table_ev[k], s->rs[k]);

@@ -394,8 +394,10 @@ ct_status ct_batch_stats(ct_ctx* ctx, ct_batch* b, ct_frame_stats* out, int32_t 
  * buffer i mod 2k, min(spp, 2k) slots, added in order at the end, so that
  * consecutive iterations, which overlap on two streams, never share a slot)
  * and leave when their samples are done; ray queries
- * run on a second stream, overlapping the iterations. Requests are admitted
- * in arrival order; one that can never fit fails with CT_ERR_OUT_OF_MEMORY.
+ * run on a second stream (at the device's highest stream priority),
+ * overlapping the iterations. Requests are admitted in arrival order, except
+ * that a query may pass a render job that waits only for queue space; one
+ * that can never fit fails with CT_ERR_OUT_OF_MEMORY.
  * Results are the same as the request alone (a render job's pixels use their
  * own seeds and its samples' summation order depends on the job only;
  * queries are per ray; k depends on the job and the server's configuration
@@ -407,7 +409,7 @@ typedef struct ct_server_config {
   uint64_t hbm_budget;          /* bytes of per-request device state admitted at once (0 = no limit) */
   uint32_t max_inflight_pixels; /* shared ray-queue capacity: pixels of all render jobs in flight */
   int32_t exact_math;           /* math mode of every render job */
-  uint32_t iter_pixels;         /* pixel-samples a render job may take per iteration (0 = 16,777,216):
+  uint32_t iter_pixels;         /* pixel-samples a render job may take per iteration (0 = 4,194,304):
                                    larger values finish big jobs in fewer, larger iterations and
                                    cost min(spp, 2k) * p * 16 bytes of slot buffers per job */
 } ct_server_config;
