@@ -223,16 +223,17 @@ __device__ __forceinline__ void shade_compat(const DevScene& sc, const DevQueues
   const float r3 = rnd_float(seed), r4 = rnd_float(seed);
   V3 wo, fval;
   float pdf;
-  bool diffuse;  // the reference leaves the type unset when pdf = 0; NEE still runs then
+  // diffuse: the reference's reflectedType == DIFFUSE. A failed sample (pdf = 0) leaves the
+  // type unset; the reference's GPU build then runs no NEE, and the path ends here either way.
+  bool diffuse;
   if (tr.y < 0.1f) {
     wo = dir - (iN * dot(iN, dir)) * 2.0f;  // reflect(-wi, iN)
+    diffuse = false;
     if (dot(N, wo) <= 0.0f) {
       pdf = 0.0f;
       fval = v3(0, 0, 0);
-      diffuse = true;
     } else {
       pdf = 1.0f;
-      diffuse = false;
       fval = color * (1.0f / fabsf(dot(iN, wo)));
     }
   } else {
@@ -256,14 +257,14 @@ __device__ __forceinline__ void shade_compat(const DevScene& sc, const DevQueues
       Tt = v3(b, 1.0f - (n.y * n.y) * a, -n.y);
     }
     wo = normalize((Tt * vl.x + B * vl.y) + n * vl.z);
-    if (dot(N, wo) <= 0.0f) {
+    diffuse = dot(N, wo) > 0.0f;
+    if (!diffuse) {
       pdf = 0.0f;
       fval = v3(0, 0, 0);
     } else {
       pdf = gmax(0.0f, dot(wo, iN)) * kOneOverPi;
       fval = color * kOneOverPi;
     }
-    diffuse = true;
   }
   bool specular_next = !diffuse;
   dir = wo;

@@ -794,11 +794,16 @@ void render_path(const SceneView& s, const Geo& g, int pixel, int px, int py, in
     const float r3 = rnd_float(sd), r4 = rnd_float(sd);
     V3 wo, f;
     float pdf;
-    int type;  // 0 specular, 1 diffuse, -1 unset by the reference (treated as diffuse)
+    // type: 0 specular, 1 diffuse, -1 left unset by the reference (a failed
+    // sample). The reference then compares an uninitialised value with
+    // DIFFUSE (Kernel.cu:153,156); its own GPU build of Kernel.cu takes it as
+    // not diffuse (no NEE), which is what is done here. The path ends at this
+    // vertex either way (pdf = 0).
+    int type;
     sample_bsdf(color, mat.roughness, iN, N, r.dir, r3, r4, exact, wo, f, pdf, type);
-    r.specular = (type == 1 || type == -1) ? 0 : 1;
+    r.specular = type == 1 ? 0 : 1;
     r.dir = wo;
-    if ((type == 1 || type == -1) && s.shadow && s.light_count > 0) {
+    if (type == 1 && s.shadow && s.light_count > 0) {
       const int light = std::min(rnd_int_max(sd, (int)s.light_count - 1), (int)s.light_count - 1);
       const uint32_t lprim = s.lights[light];
       const uint32_t* li = s.idx + 3 * (size_t)lprim;

@@ -42,18 +42,28 @@ def _native_machine() -> int:
     return 62 if platform.machine().lower() in ("x86_64", "amd64") else 183
 
 
-def build_oracle(force: bool = False) -> str:
-    fresh = (os.path.exists(ORACLE_LIB) and os.path.getmtime(ORACLE_LIB) >= os.path.getmtime(ORACLE_SRC)
-             and os.path.getmtime(ORACLE_LIB) >= os.path.getmtime(PORTABLE_MATH)
-             and _elf_machine(ORACLE_LIB) == _native_machine())
+# The same source built with floating-point contraction (a*b+c fused where the
+# compiler finds it, as nvcc does by default): used only to compare with frames
+# the reference's own GPU build rendered, whose rounding it follows more closely.
+ORACLE_FMA_LIB = os.path.join(HERE, "liboracle_fma.so")
+
+
+def build_oracle(force: bool = False, contracted: bool = False) -> str:
+    out = ORACLE_FMA_LIB if contracted else ORACLE_LIB
+    fresh = (os.path.exists(out) and os.path.getmtime(out) >= os.path.getmtime(ORACLE_SRC)
+             and os.path.getmtime(out) >= os.path.getmtime(PORTABLE_MATH)
+             and _elf_machine(out) == _native_machine())
     if fresh and not force:
-        return ORACLE_LIB
-    tmp = ORACLE_LIB + ".tmp"
-    cmd = ["g++", "-std=c++17", "-O2", "-fPIC", "-shared", "-pthread", "-ffp-contract=off", "-fno-fast-math",
-           "-o", tmp, ORACLE_SRC]
+        return out
+    tmp = out + ".tmp"
+    if contracted:
+        fp = ["-ffp-contract=fast"] + (["-mfma"] if _native_machine() == 62 else [])
+    else:
+        fp = ["-ffp-contract=off"]
+    cmd = ["g++", "-std=c++17", "-O2", "-fPIC", "-shared", "-pthread", *fp, "-fno-fast-math", "-o", tmp, ORACLE_SRC]
     subprocess.run(cmd, check=True)
-    os.replace(tmp, ORACLE_LIB)
-    return ORACLE_LIB
+    os.replace(tmp, out)
+    return out
 
 
 FP64_SRC = os.path.join(HERE, "ct_fp64.cpp")
@@ -163,31 +173,39 @@ def build(force: bool = False) -> None:
 
 
 _orc = None
+_orc_fma = None
 _ref = None
 
 
-def lib() -> ctypes.CDLL:
-    global _orc
+def lib(contracted: bool = False) -> ctypes.CDLL:
+    """The oracle library; contracted=True the build with FMA contraction."""
+    global _orc, _orc_fma
+    if contracted:
+        if _orc_fma is None:
+            _orc_fma = _bind(ctypes.CDLL(build_oracle(contracted=True)))
+        return _orc_fma
     if _orc is None:
-        build_oracle()
-        L = ctypes.CDLL(ORACLE_LIB)
-        L.or_build.restype = P
-        L.or_build.argtypes = [P, P, ctypes.c_int, ctypes.c_int]
-        for n in ("or_bvh_count", "or_mbvh_count"):
-            getattr(L, n).argtypes = [P]
-        L.or_export.argtypes = [P, P, P, P]
-        L.or_free.argtypes = [P]
-        L.or_trace_closest.argtypes = [P, P, P, P, ctypes.c_float, P, P, ctypes.c_int, P, P, P, ctypes.c_int]
-        L.or_trace_any.argtypes = [P, P, P, P, ctypes.c_float, P, P, P, ctypes.c_int, P, ctypes.c_int]
-        L.or_trace_closest_binary.argtypes = [P, P, P, P, ctypes.c_float, P, P, ctypes.c_int, P, P, ctypes.c_int]
-        L.or_camera_basis.argtypes = [P, P, ctypes.c_float, ctypes.c_int, ctypes.c_int, P, P]
-        L.or_render_frame.argtypes = [P, P, P, P, P, ctypes.c_int, ctypes.c_int, ctypes.c_uint32, ctypes.c_int,
-                                      ctypes.c_int, P, ctypes.c_int, ctypes.c_int, ctypes.c_int]
-        L.or_present.argtypes = [P, ctypes.c_int, ctypes.c_float, P]
-        L.or_plane_distance.restype = ctypes.c_float
-        L.or_plane_distance.argtypes = [ctypes.c_float]
-        _orc = L
+        _orc = _bind(ctypes.CDLL(build_oracle()))
     return _orc
+
+
+def _bind(L: ctypes.CDLL) -> ctypes.CDLL:
+    L.or_build.restype = P
+    L.or_build.argtypes = [P, P, ctypes.c_int, ctypes.c_int]
+    for n in ("or_bvh_count", "or_mbvh_count"):
+        getattr(L, n).argtypes = [P]
+    L.or_export.argtypes = [P, P, P, P]
+    L.or_free.argtypes = [P]
+    L.or_trace_closest.argtypes = [P, P, P, P, ctypes.c_float, P, P, ctypes.c_int, P, P, P, ctypes.c_int]
+    L.or_trace_any.argtypes = [P, P, P, P, ctypes.c_float, P, P, P, ctypes.c_int, P, ctypes.c_int]
+    L.or_trace_closest_binary.argtypes = [P, P, P, P, ctypes.c_float, P, P, ctypes.c_int, P, P, ctypes.c_int]
+    L.or_camera_basis.argtypes = [P, P, ctypes.c_float, ctypes.c_int, ctypes.c_int, P, P]
+    L.or_render_frame.argtypes = [P, P, P, P, P, ctypes.c_int, ctypes.c_int, ctypes.c_uint32, ctypes.c_int,
+                                  ctypes.c_int, P, ctypes.c_int, ctypes.c_int, ctypes.c_int]
+    L.or_present.argtypes = [P, ctypes.c_int, ctypes.c_float, P]
+    L.or_plane_distance.restype = ctypes.c_float
+    L.or_plane_distance.argtypes = [ctypes.c_float]
+    return L
 
 
 def ref_available() -> bool:
@@ -390,9 +408,11 @@ def _frame_scene(arrays: dict, materials: np.ndarray, quad, prims, camera: dict,
 def render_frames(arrays: dict, materials: np.ndarray, quad, prims, camera: dict, width: int, height: int,
                   frames, depth: int, accum: np.ndarray | None = None, exact_math: bool = True,
                   textures=(), sky_tex: int = -1, sky: bool = True, shadow: bool = True, indirect: bool = True,
-                  eps=(1e-5, 1e-5, 1e-3), pixels=None, nthreads: int = 8, tex_filter: int = 0) -> np.ndarray:
-    """Accumulate 1-spp frames (seed frame indices `frames`) into accum (h*w,4)."""
-    L = lib()
+                  eps=(1e-5, 1e-5, 1e-3), pixels=None, nthreads: int = 8, tex_filter: int = 0,
+                  contracted: bool = False) -> np.ndarray:
+    """Accumulate 1-spp frames (seed frame indices `frames`) into accum (h*w,4);
+    contracted=True renders with the FMA-contracted build of the oracle."""
+    L = lib(contracted)
     if accum is None:
         accum = np.zeros((width * height, 4), np.float32)
     d, pos, fw, hor, ver, _keep = _frame_scene(arrays, materials, quad, prims, camera, width, height, textures,

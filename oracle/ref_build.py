@@ -68,6 +68,94 @@ PATCHES = {
 }
 
 
+# ---- the reference's own GPU frame (for the frame fixture, tests/golden/make_ref_frame.py)
+#
+# src/CUDA/Kernel.cu is built with nvcc from a patched copy of the whole src/
+# tree under oracle/_ref/gpu/src. The patches are mechanical: they remove the
+# OpenGL interop and the surface the viewer presents to (no graphics stack), let
+# Camera-free device code see triangle::getBounds as host-only (its __m128 box
+# type is host code), and replace the grid sizes n / 128 and n + n % 128 by
+# ceil(n / 128): as written, the last n % 128 rays of a pass are dropped, and a
+# bounce pass can read up to 127 rays past the end of its ray buffer.
+GPU_PATCHES = {
+    "CUDA/Kernel.cuh": [
+        ("#include <GL/glew.h>\n", "", 1),
+        ("#include <cuda_gl_interop.h>\n", "", 1),
+        ("\t\tint glDeviceId;\n\t\tunsigned int glDeviceCount;\n"
+         "\t\tcudaGLGetDevices(&glDeviceCount, &glDeviceId, 1u, cudaGLDeviceListAll);\n",
+         "\t\tint glDeviceId = 0;\n\t\tcudaGetDevice(&glDeviceId);\n", 1),
+    ],
+    "CUDA/Kernel.cu": [
+        ("#include <surface_functions.h>\n", "", 1),
+        ("#include <cuda_surface_types.h>\n", "", 1),
+        ("surface<void, cudaSurfaceType2D> framebuffer;\n", "", 1),
+        ("\tsurf2Dwrite(color, framebuffer, x * sizeof(vec4), y);\n", "", 1),
+        ("\tsurf2Dwrite(color, framebuffer, x * sizeof(vec4), y, cudaBoundaryModeZero);\n", "", 1),
+        ("\terr = cuda(BindSurfaceToArray(framebuffer, array));\n", "\terr = cudaSuccess;\n", 1),
+        ("\tint groups = activePaths / 128;\n", "\tint groups = (activePaths + 127) / 128;\n", 1),
+        ("const int shadowGroups = (connectCount + (connectCount % 128)) / 128;",
+         "const int shadowGroups = (connectCount + 127) / 128;", 2),
+        ("\t\tactivePaths = activePaths + (activePaths % 128);\n", "", 1),
+        ("\t\tgroups = activePaths / 128;\n", "\t\tgroups = (activePaths + 127) / 128;\n", 1),
+    ],
+    "Core/Triangle.cuh": [
+        ("\t__device__ __host__ inline static AABB getBounds(", "\t__host__ inline static AABB getBounds(", 1),
+    ],
+    "BVH/BVHNode.cuh": PATCHES["BVH/BVHNode.cuh"],
+    "BVH/BVHNode.cu": PATCHES["BVH/BVHNode.cu"],
+}
+GPU_DIR = os.path.join(REF_OUT, "gpu")
+GPU_LIB = os.path.join(REF_OUT, "libctref_gpu.so")
+
+
+def stage_gpu_sources(reference: str) -> None:
+    """Copy the reference's src/ tree to oracle/_ref/gpu/src and apply GPU_PATCHES."""
+    dst = os.path.join(GPU_DIR, "src")
+    if os.path.isdir(dst):
+        shutil.rmtree(dst)
+    shutil.copytree(os.path.join(reference, "src"), dst)
+    for rel, patches in GPU_PATCHES.items():
+        path = os.path.join(dst, rel)
+        with open(path, "r", encoding="utf-8-sig", errors="replace") as f:
+            text = _normalise(f.read())
+        for old, new, count in patches:
+            found = text.count(old)
+            if found != count:
+                raise RuntimeError(f"reference GPU patch for {rel}: expected {count} match(es), found {found}")
+            text = text.replace(old, new)
+        with open(path, "w", encoding="utf-8") as f:
+            f.write(text)
+
+
+def compile_gpu_lib(verbose: bool = False) -> str:
+    """nvcc build of the patched Kernel.cu + Camera.cpp + oracle/ref_gpu_harness.cu into
+    oracle/_ref/libctref_gpu.so (sm_103a). Needs oracle/_ref/gpu/src (staged from the
+    reference checkout) and the staged headers in oracle/_ref/include."""
+    src = os.path.join(GPU_DIR, "src")
+    if not os.path.isdir(src):
+        raise FileNotFoundError("oracle/_ref/gpu/src is missing: the reference checkout was never staged")
+    nvcc = os.path.join(os.environ.get("CUDA_HOME", "/usr/local/cuda"), "bin", "nvcc")
+    shim = os.path.join(HERE, "ref_shim")
+    flags = ["-gencode", "arch=compute_103a,code=sm_103a", "-std=c++17", "-O2", "-w", "-Xcompiler", "-fPIC",
+             "-DGLM_FORCE_PURE", "-DGLEW_NO_GLU", "-DGLFW_INCLUDE_NONE",
+             "-include", os.path.join(shim, "ct_ref_cuda_shim.h"), "-I", os.path.join(shim, "stub")]
+    if not _is_x86():  # the box-type AABB's SSE intrinsics from the portable header
+        flags += ["-I", os.path.join(shim, "portable")]
+    flags += ["-I", src, "-I", os.path.join(REF_OUT, "include")]
+    objs = []
+    for p in (os.path.join(src, "CUDA", "Kernel.cu"), os.path.join(src, "Core", "Camera.cpp"),
+              os.path.join(HERE, "ref_gpu_harness.cu")):
+        obj = os.path.join(GPU_DIR, os.path.basename(p).replace(".", "_") + ".o")
+        cmd = [nvcc] + flags + ["-x", "cu", "-c", p, "-o", obj]
+        if verbose:
+            print(" ".join(cmd))
+        subprocess.run(cmd, check=True)
+        objs.append(obj)
+    cmd = [nvcc, "-shared", "-gencode", "arch=compute_103a,code=sm_103a", "-o", GPU_LIB] + objs
+    subprocess.run(cmd, check=True)
+    return GPU_LIB
+
+
 def _normalise(text: str) -> str:
     return text.replace("\r\n", "\n")
 
@@ -154,6 +242,7 @@ def build(reference: str | None = None, verbose: bool = False) -> str | None:
     reference = reference or os.environ.get("CT_REFERENCE_DIR", DEFAULT_REFERENCE)
     if os.path.isdir(os.path.join(reference, "src", "BVH")):
         stage_sources(reference)
+        stage_gpu_sources(reference)
     if not os.path.isdir(os.path.join(REF_OUT, "src")):
         return None
     return compile_lib(verbose=verbose)
