@@ -3,10 +3,12 @@ GPU kernels (tests/golden/ref_frame_gpu.npz: the reference's Kernel.cu built for
 sm_103a and its launchKernels, on its own quad BVH; 64x48, depth 5, compat
 shading, no sky, first frame; made by tests/golden/make_ref_frame.py).
 
-CT_MATH_FAST rounds as the reference's build does (nvcc's FMA contraction,
-CUDA's sinf/cosf) but not operation for operation, so a few paths that graze
-an edge diverge; the reproducible modes round like the uncontracted oracle.
-Bounds are about twice what was measured; the per-pixel band is 1e-4."""
+CT_MATH_FAST uses nvcc's FMA contraction and CUDA's sinf/cosf like the
+reference's build, but its source contracts into other FMAs, so some paths that
+graze an edge diverge (45 of 3,072 pixels measured on the reference's tree).
+CT_MATH_EXACT is the uncontracted oracle bit for bit (67 pixels, the oracle's
+own count); CT_MATH_EXACT_SHADE the same up to exact-t ties. Bounds are about
+twice what was measured; the per-pixel band is 1e-4."""
 import numpy as np
 import pytest
 
@@ -43,7 +45,7 @@ def _frame(gpu_ctx, R, bvh, math):
     return job.accum_tensor().cpu().numpy().copy()
 
 
-@pytest.mark.parametrize("math,tree,max_bad", [(0, "reference", 24), (0, "fast", 24), (1, "reference", 120),
+@pytest.mark.parametrize("math,tree,max_bad", [(0, "reference", 90), (0, "fast", 90), (1, "reference", 120),
                                                (2, "fast", 120)])
 def test_frame_matches_reference_gpu_frame(gpu_ctx, ref_scene, math, tree, max_bad):
     sc = ref_scene["sc"]
