@@ -30,6 +30,7 @@ SOURCES = {
     "server.cpp": [],
     "k_trace.cu": [],
     "bvh_gpu.cu": [],
+    "bvh_gpu_fast.cu": ["-fmad=false"],
     "k_trace_wide.cu": [],
     "k_shade_exact.cu": ["-fmad=false"],
     "k_shade_fast.cu": [],

@@ -135,6 +135,7 @@ SIGNATURES = {
     "ct_host_bvh_export": (c_int32, [P, c_int32, P, P]),
     "ct_host_bvh_destroy": (c_int32, [P]),
     "ct_bvh_build_device": (c_int32, [P, P, P, PP]),
+    "ct_bvh_build_fast_device": (c_int32, [P, P, P, PP]),
     "ct_bvh_build_wide": (c_int32, [P, P, P, PP]),
     "ct_bvh_wide_stats": (c_int32, [P, P, POINTER(c_uint64), POINTER(c_uint64), POINTER(c_uint64), POINTER(c_uint64),
                                     c_int32]),

@@ -406,6 +406,14 @@ class Scene:
         check(self.ctx.lib.ct_bvh_build_device(self.ctx.h, self.h, s, ctypes.byref(h)), self.ctx.h)
         return BVH(self, h)
 
+    def build_bvh_fast_device(self, stream=None) -> "BVH":
+        """build_bvh_fast's tree built on the GPU (ct_bvh_build_fast_device): the
+        same quad nodes and primitive order, byte for byte."""
+        h = ctypes.c_void_p()
+        s = None if stream is None else getattr(stream, "cuda_stream", stream)
+        check(self.ctx.lib.ct_bvh_build_fast_device(self.ctx.h, self.h, s, ctypes.byref(h)), self.ctx.h)
+        return BVH(self, h)
+
     def build_bvh_wide(self, stream=None) -> "BVH":
         """8-wide BVH with 8-bit quantised child bounds for ray queries
         (ct_bvh_build_wide): FP32 watertight tests settled in FP64 where FP32

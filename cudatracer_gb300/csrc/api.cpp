@@ -580,7 +580,13 @@ ct_status ct_bvh_build_fast(ct_ctx* ctx, const ct_scene* scene, int32_t nthreads
   return CT_OK;
 }
 
-ct_status ct_bvh_build_device(ct_ctx* ctx, const ct_scene* scene, void* stream, ct_bvh** out) {
+}  // extern "C"
+
+namespace {
+
+// Device quad builds: the reference's SAH tree (fast = false, bvh_gpu.cu) or
+// ct_bvh_build_fast's tree (fast = true, bvh_gpu_fast.cu).
+ct_status build_device_quad(ct_ctx* ctx, const ct_scene* scene, void* stream, ct_bvh** out, bool fast) {
   if (!ctx || !scene || !out) return fail(ctx, CT_ERR_INVALID_ARGUMENT, "null argument");
   *out = nullptr;
   const uint32_t n = scene->nt;
@@ -604,12 +610,17 @@ ct_status ct_bvh_build_device(ct_ctx* ctx, const ct_scene* scene, void* stream, 
     }
     return r;
   };
-  if ((s = dev_alloc(ctx, scratch_allocs, &scratch, gpu_bvh_scratch_bytes(n))) != CT_OK) return cleanup(s);
+  const size_t scratch_bytes = fast ? gpu_fbvh_scratch_bytes(n) : gpu_bvh_scratch_bytes(n);
+  if ((s = dev_alloc(ctx, scratch_allocs, &scratch, scratch_bytes)) != CT_OK) return cleanup(s);
   cudaError_t e = cudaMallocHost((void**)&hc, 64);
   if (e != cudaSuccess) return cleanup(cuda_fail(ctx, e, "cudaMallocHost"));
   GpuBvhResult r;
-  e = gpu_bvh_build(scene->dev, scratch, hc, st, r);
+  e = fast ? gpu_fbvh_build(scene->dev, scratch, hc, st, r) : gpu_bvh_build(scene->dev, scratch, hc, st, r);
   if (e != cudaSuccess) return cleanup(cuda_fail(ctx, e, "device BVH build"));
+  if ((r.error & 1u) && fast)
+    return cleanup(fail(ctx, CT_ERR_UNSUPPORTED,
+                        "device BVH build: a padded triangle box is not finite (coordinates near the float "
+                        "range); use ct_bvh_build_fast"));
   if (r.error & 1u)
     return cleanup(fail(ctx, CT_ERR_UNSUPPORTED,
                         "device BVH build: scene extent too large for the SAH cost (area x count >= 1e34); "
@@ -628,10 +639,16 @@ ct_status ct_bvh_build_device(ct_ctx* ctx, const ct_scene* scene, void* stream, 
   if ((s = dev_alloc(ctx, b->allocs, &nodes, (size_t)r.quad_nodes * sizeof(QNodeDev))) != CT_OK) return cleanup(s);
   if ((s = dev_alloc(ctx, b->allocs, &tris, (size_t)n * 3 * sizeof(float4))) != CT_OK) return cleanup(s);
   if ((s = dev_alloc(ctx, b->allocs, &prims, (size_t)n * 4)) != CT_OK) return cleanup(s);
-  e = gpu_bvh_emit(scene->dev, scratch, r, shift, quad, (QNodeDev*)nodes, (float4*)tris, (uint32_t*)prims, st);
+  e = fast ? gpu_fbvh_emit(scene->dev, scratch, r, shift, quad, (QNodeDev*)nodes, (float4*)tris, (uint32_t*)prims, st)
+           : gpu_bvh_emit(scene->dev, scratch, r, shift, quad, (QNodeDev*)nodes, (float4*)tris, (uint32_t*)prims, st);
   if (e != cudaSuccess) return cleanup(cuda_fail(ctx, e, "device BVH emit"));
   e = st ? cudaStreamSynchronize(st) : cudaDeviceSynchronize();
   if (e != cudaSuccess) return cleanup(cuda_fail(ctx, e, "device BVH build"));
+  if (fast) {
+    const uint32_t werr = gpu_fbvh_error(scratch, n, hc, st);
+    if (werr) return cleanup(fail(ctx, CT_ERR_CUDA, "device BVH emit: internal check failed (code " +
+                                                        std::to_string(werr) + ")"));
+  }
   const auto t2 = std::chrono::high_resolution_clock::now();
   b->device_built = true;
   b->device = ctx->device;
@@ -647,7 +664,7 @@ ct_status ct_bvh_build_device(ct_ctx* ctx, const ct_scene* scene, void* stream, 
   b->dev.stack_entries = (int32_t)std::min<uint32_t>(3 * r.depth + 1, 256);
   b->nt = n;
   ct_bvh_info& i = b->info;
-  i.binary_node_count = r.binary_nodes;
+  i.binary_node_count = fast ? 0u : r.binary_nodes;  // as ct_bvh_build_fast: a quad tree only
   i.quad_node_count = r.quad_nodes;
   i.prim_count = n;
   i.max_leaf_size = r.max_leaf;
@@ -661,6 +678,18 @@ ct_status ct_bvh_build_device(ct_ctx* ctx, const ct_scene* scene, void* stream, 
   i.device_bytes = bytes;
   *out = b;
   return cleanup(CT_OK);
+}
+
+}  // namespace
+
+extern "C" {
+
+ct_status ct_bvh_build_device(ct_ctx* ctx, const ct_scene* scene, void* stream, ct_bvh** out) {
+  return build_device_quad(ctx, scene, stream, out, false);
+}
+
+ct_status ct_bvh_build_fast_device(ct_ctx* ctx, const ct_scene* scene, void* stream, ct_bvh** out) {
+  return build_device_quad(ctx, scene, stream, out, true);
 }
 
 ct_status ct_bvh_build_wide(ct_ctx* ctx, const ct_scene* scene, void* stream, ct_bvh** out) {

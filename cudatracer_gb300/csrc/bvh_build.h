@@ -40,6 +40,9 @@ void collapse_quad(HostBVH& out);
 // leaves of at most four triangles. Fills out.quad and out.prims; out.bin stays
 // empty.
 void build_fast_quad(const float* verts, const uint32_t* idx, uint32_t ntri, int nthreads, HostBVH& out);
+// The power-of-two scale of that build's surface-area costs, from the root box
+// (shared with the device build, bvh_gpu_fast.cu).
+float fast_area_scale(const float mn[3], const float mx[3]);
 // Structural validation of an imported tree; returns "" when valid.
 std::string validate_quad(const std::vector<QuadNode>& q, uint32_t prim_count);
 std::string validate_binary(const std::vector<BinNode>& b, uint32_t prim_count);

@@ -28,7 +28,10 @@
 // The primitive order is the binary tree's leaf order (each subtree covers one
 // contiguous range), so every leaf slot is a contiguous range. The result does
 // not depend on the thread count: children are always numbered after their
-// parent and the collapse walks the tree by structure, not by number.
+// parent and the collapse walks the tree by structure, not by number. Every
+// step is a fixed sequence of IEEE operations and every partition is stable,
+// so the device build (bvh_gpu_fast.cu) reproduces the nodes and the primitive
+// order byte for byte.
 #include <stdint.h>
 #include <string.h>
 
@@ -97,9 +100,14 @@ struct FCtx {
   float scale;  // area scale (farea)
 };
 
+// Bin of a centroid: floor((c - lo) * scale) clamped to [0, kBins - 1], defined
+// for every float (NaN bins to 0, +inf to the last bin) so that every machine,
+// and the device build, bins alike.
 inline int bin_of(float c, float lo, float scale) {
-  const int i = (int)((c - lo) * scale);
-  return std::min(kBins - 1, std::max(0, i));
+  const float f = (c - lo) * scale;
+  if (!(f >= 1.0f)) return 0;
+  if (f >= (float)(kBins - 1)) return kBins - 1;
+  return (int)f;
 }
 
 void bin_range(const FCtx& C, const float lo[3], const float scale[3], uint32_t b, uint32_t e, FBins& out) {
@@ -188,7 +196,9 @@ Cut binned_split(const FCtx& C, uint32_t first, uint32_t count) {
   Cut c;
   if (bax >= 0) {
     uint32_t* b = C.prims + first;
-    uint32_t* m = std::partition(b, b + count, [&](uint32_t p) {
+    // stable: the order inside each half (and with it the all-in-one-bin
+    // halving below and the leaf order) is a function of the input order only
+    uint32_t* m = std::stable_partition(b, b + count, [&](uint32_t p) {
       return bin_of(C.cent[3 * (size_t)p + bax], lo[bax], scale[bax]) < bsp;
     });
     c.mid = (uint32_t)(m - b);
@@ -389,6 +399,17 @@ void collapse(const std::vector<FNode>& nodes, const std::vector<Cost>& d, float
 
 }  // namespace
 
+// 2^-e with the largest root extent in [2^(e-1), 2^e): scaled extents below 1
+float fast_area_scale(const float mn[3], const float mx[3]) {
+  const float ext = std::max(mx[0] - mn[0], std::max(mx[1] - mn[1], mx[2] - mn[2]));
+  if (ext > 0.0f && std::isfinite(ext)) {
+    int e = 0;
+    std::frexp(ext, &e);
+    return std::ldexp(1.0f, -e);
+  }
+  return 1.0f;
+}
+
 void build_fast_quad(const float* verts, const uint32_t* idx, uint32_t ntri, int nthreads, HostBVH& out) {
   const auto t0 = std::chrono::high_resolution_clock::now();
   if (nthreads <= 0) nthreads = (int)std::max(1u, std::thread::hardware_concurrency());
@@ -414,6 +435,7 @@ void build_fast_quad(const float* verts, const uint32_t* idx, uint32_t ntri, int
         float mn = std::min(p0[k], std::min(p1[k], p2[k])), mx = std::max(p0[k], std::max(p1[k], p2[k]));
         const float pad = kPad * std::max(floor_mag, std::max(std::fabs(mn), std::fabs(mx)));
         mn -= pad, mx += pad;
+        mn += 0.0f, mx += 0.0f;  // -0 becomes +0: min/max unions then do not depend on the order
         t.mn[k] = mn, t.mx[k] = mx;
         cent[3 * (size_t)i + k] = 0.5f * (mn + mx);
       }
@@ -440,16 +462,7 @@ void build_fast_quad(const float* verts, const uint32_t* idx, uint32_t ntri, int
   nodes[0] = FNode{root, 0, ntri, -1, -1};
   std::atomic<uint32_t> next{1};
   std::atomic<int> busy{0};
-  // 2^-e with the largest root extent in [2^(e-1), 2^e): scaled extents below 1
-  float scale = 1.0f;
-  {
-    const float ext = std::max(root.mx[0] - root.mn[0], std::max(root.mx[1] - root.mn[1], root.mx[2] - root.mn[2]));
-    if (ext > 0.0f && std::isfinite(ext)) {
-      int e = 0;
-      std::frexp(ext, &e);
-      scale = std::ldexp(1.0f, -e);
-    }
-  }
+  const float scale = fast_area_scale(root.mn, root.mx);
   const FCtx C{pb.data(), cent.data(), out.prims.data(), nodes.data(), &next, &busy, nthreads, scale};
   build_node(C, 0, 0);
   const auto t1 = std::chrono::high_resolution_clock::now();

@@ -824,6 +824,16 @@ cudaError_t gpu_bvh_build(const DevScene& sc, void* scratch, uint32_t* host_coun
   return cudaSuccess;
 }
 
+cudaError_t launch_quad_to_dev(const QuadNode* quad, uint32_t nq, uint32_t leaf_shift, QNodeDev* nodes, cudaStream_t s) {
+  if (nq) k_qdev<<<blocks(nq, 256), 256, 0, s>>>(quad, nq, leaf_shift, nodes);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_leaf_tris(const DevScene& sc, const uint32_t* prims, uint32_t n, float4* tris, cudaStream_t s) {
+  if (n) k_tris<<<blocks(n, 256), 256, 0, s>>>(sc.verts, sc.idx, prims, n, tris);
+  return cudaGetLastError();
+}
+
 cudaError_t gpu_bvh_emit(const DevScene& sc, void* scratch, const GpuBvhResult& r, uint32_t leaf_shift, void* quad_out,
                          QNodeDev* nodes, float4* tris, uint32_t* prims_out, cudaStream_t s) {
   const uint32_t n = sc.tri_count;

@@ -225,6 +225,25 @@ cudaError_t gpu_bvh_build(const DevScene& sc, void* scratch, uint32_t* host_coun
 cudaError_t gpu_bvh_emit(const DevScene& sc, void* scratch, const GpuBvhResult& r, uint32_t leaf_shift, void* quad,
                          QNodeDev* nodes, float4* tris, uint32_t* prims, cudaStream_t s);
 
+struct QuadNode;  // bvh_build.h
+// QuadNode -> traversal node conversion, and the leaf-ordered triangle records
+// (3 x float4 per primitive: v0 + id, e1, e2), for trees built on the device.
+cudaError_t launch_quad_to_dev(const QuadNode* quad, uint32_t nq, uint32_t leaf_shift, QNodeDev* nodes, cudaStream_t s);
+cudaError_t launch_leaf_tris(const DevScene& sc, const uint32_t* prims, uint32_t n, float4* tris, cudaStream_t s);
+
+// Device build of ct_bvh_build_fast's tree (bvh_gpu_fast.cu), byte-equal to the
+// host build: gpu_fbvh_build fills `scratch` (gpu_fbvh_scratch_bytes) and
+// returns the sizes (r.error: 1 a padded box is not finite, 2 capacity, 4
+// stack, 8 partition mismatch, 16 collapse); gpu_fbvh_emit writes the quad
+// nodes, traversal nodes, triangles and primitive order. host_counters: 16
+// words of pinned host memory; the build synchronises with `s` once per level.
+size_t gpu_fbvh_scratch_bytes(uint32_t n);
+cudaError_t gpu_fbvh_build(const DevScene& sc, void* scratch, uint32_t* host_counters, cudaStream_t s, GpuBvhResult& r);
+cudaError_t gpu_fbvh_emit(const DevScene& sc, void* scratch, const GpuBvhResult& r, uint32_t leaf_shift, void* quad,
+                          QNodeDev* nodes, float4* tris, uint32_t* prims, cudaStream_t s);
+// error word of the last emit (reads the counters back; synchronises with `s`)
+uint32_t gpu_fbvh_error(void* scratch, uint32_t n, uint32_t* host_counters, cudaStream_t s);
+
 // Collapse of a wide-rule binary build (gpu_bvh_build with wide = 1) into
 // 8-wide quantised nodes. `scratch2` holds gpu_wbvh_scratch_bytes(binary_nodes);
 // nodes end up in scratch2 (read back their count in *wide_nodes, then copy

@@ -238,6 +238,14 @@ ct_status ct_bvh_build_device(ct_ctx* ctx, const ct_scene* scene, void* stream, 
  * threads (<= 0: every hardware thread); the tree does not depend on the
  * thread count. Exports the QUAD layout only. */
 ct_status ct_bvh_build_fast(ct_ctx* ctx, const ct_scene* scene, int32_t nthreads, ct_bvh** out);
+/* Device build of ct_bvh_build_fast's tree: the same quad nodes and primitive
+ * order, byte for byte, built on the GPU (no reference counterpart; for
+ * batches and served renders, whose scenes would otherwise wait on the host
+ * build). Runs on `stream` (a cudaStream_t, NULL = legacy) and returns when
+ * the tree is ready; reads one counter back per tree level. Fails with
+ * CT_ERR_UNSUPPORTED when a padded triangle box is not finite (coordinates
+ * within about 1e-5 of the float range). Exports the QUAD layout only. */
+ct_status ct_bvh_build_fast_device(ct_ctx* ctx, const ct_scene* scene, void* stream, ct_bvh** out);
 /* 8-wide BVH with 8-bit quantised child bounds (no reference counterpart: the
  * precision extension of the ray-query path). 80-byte nodes {quantisation
  * origin p, three exponents, inner-child mask, first inner child, first
