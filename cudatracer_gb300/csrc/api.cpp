@@ -718,18 +718,23 @@ ct_status ct_bvh_build_wide(ct_ctx* ctx, const ct_scene* scene, void* stream, ct
     }
     return r;
   };
-  if ((s = dev_alloc(ctx, scratch_allocs, &scratch, gpu_bvh_scratch_bytes(n))) != CT_OK) return cleanup(s);
+  // the binary tree of ct_bvh_build_fast's rules over exact triangle bounds, and
+  // the cost table of the 8-wide collapse
+  if ((s = dev_alloc(ctx, scratch_allocs, &scratch, gpu_fbvh_scratch_bytes(n, 1))) != CT_OK) return cleanup(s);
   cudaError_t e = cudaMallocHost((void**)&hc, 64);
   if (e != cudaSuccess) return cleanup(cuda_fail(ctx, e, "cudaMallocHost"));
   GpuBvhResult r;
-  e = gpu_bvh_build(scene->dev, scratch, hc, st, r, 1);
+  e = gpu_fbvh_build(scene->dev, scratch, hc, st, r, 1);
   if (e != cudaSuccess) return cleanup(cuda_fail(ctx, e, "device BVH build"));
   if (r.error & 1u)
     return cleanup(fail(ctx, CT_ERR_UNSUPPORTED,
-                        "wide BVH build: a node of more than 2,048 primitives has no separating plane "
-                        "(coincident centroids) or the scene's extent makes the SAH cost overflow"));
+                        "wide BVH build: a triangle box is not finite (coordinates near the float range)"));
   if (r.error) return cleanup(fail(ctx, CT_ERR_CUDA, "wide BVH build: internal check failed (code " +
                                                          std::to_string(r.error) + ")"));
+  const void* barena = nullptr;
+  const uint32_t* bprims = nullptr;
+  const WideCost* wcost = nullptr;
+  gpu_fbvh_binary(scratch, n, 1, &barena, &bprims, &wcost);
   const auto t1 = std::chrono::high_resolution_clock::now();
   void* tris = nullptr;
   void* stats = nullptr;
@@ -739,7 +744,8 @@ ct_status ct_bvh_build_wide(ct_ctx* ctx, const ct_scene* scene, void* stream, ct
   if ((s = dev_alloc(ctx, scratch_allocs, &scratch2, gpu_wbvh_scratch_bytes(r.binary_nodes))) != CT_OK)
     return cleanup(s);
   uint32_t nw = 0, depth = 0, werr = 0;
-  e = gpu_wbvh_collapse(scene->dev, scratch, scratch2, r.binary_nodes, (float4*)tris, hc, st, &nw, &depth, &werr);
+  e = gpu_wbvh_collapse(scene->dev, barena, bprims, wcost, scratch2, r.binary_nodes, (float4*)tris, hc, st, &nw, &depth,
+                        &werr);
   if (e != cudaSuccess) return cleanup(cuda_fail(ctx, e, "wide BVH collapse"));
   if (werr) return cleanup(fail(ctx, CT_ERR_UNSUPPORTED, "wide BVH collapse failed (code " + std::to_string(werr) +
                                                               "): a leaf needs more than 8 slots or a box did not quantise"));

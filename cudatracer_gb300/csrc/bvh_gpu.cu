@@ -248,15 +248,14 @@ __global__ void k_init(uint32_t* counters) {
 
 __global__ void __launch_bounds__(256) k_prep(const float4* __restrict__ v, const uint4* __restrict__ idx, uint32_t n,
                                               float4* __restrict__ lo, float4* __restrict__ hi,
-                                              uint32_t* __restrict__ prims, uint32_t* counters, int wide) {
+                                              uint32_t* __restrict__ prims, uint32_t* counters) {
   const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
   uint32_t kmn[3] = {fkey(1e34f), fkey(1e34f), fkey(1e34f)}, kmx[3] = {fkey(-1e34f), fkey(-1e34f), fkey(-1e34f)};
   if (i < n) {
     const uint4 t = idx[i];
     const float4 a = v[t.x], b = v[t.y], c = v[t.z];
-    // triangle::getBounds (src/Core/Triangle.cuh:59-65): min - 0.001, max + 0.01; the
-    // wide tree bounds the triangles exactly
-    const float plo = wide ? 0.0f : 0.001f, phi = wide ? 0.0f : 0.01f;
+    // triangle::getBounds (src/Core/Triangle.cuh:59-65): min - 0.001, max + 0.01
+    const float plo = 0.001f, phi = 0.01f;
     const float mn[3] = {__fsub_rn(gmin(a.x, gmin(b.x, c.x)), plo), __fsub_rn(gmin(a.y, gmin(b.y, c.y)), plo),
                          __fsub_rn(gmin(a.z, gmin(b.z, c.z)), plo)};
     const float mx[3] = {__fadd_rn(gmax(a.x, gmax(b.x, c.x)), phi), __fadd_rn(gmax(a.y, gmax(b.y, c.y)), phi),
@@ -356,7 +355,7 @@ __device__ __forceinline__ void classify(int32_t id, uint32_t count, int32_t dep
 
 __global__ void __launch_bounds__(256) k_split(BNode* arena, const int32_t* __restrict__ large, uint32_t nl,
                                                const uint32_t* __restrict__ gbins, Split* split, int32_t* next_large,
-                                               int32_t* small, uint32_t* counters, uint32_t cap, int wide) {
+                                               int32_t* small, uint32_t* counters, uint32_t cap) {
   const uint32_t s = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
   const int lane = threadIdx.x & 31;
   if (s >= nl) return;  // whole warp
@@ -366,13 +365,12 @@ __global__ void __launch_bounds__(256) k_split(BNode* arena, const int32_t* __re
   const int best = choose_split(gbins + (size_t)s * kBinWords, lane, c);
   const float parent_cost = __fmul_rn(area3(nd.mn, nd.mx), __uint2float_rn((uint32_t)nd.count));
   if (best == 32) {
-    // no candidate below 1e34: a leaf unless the parent's cost is not below it
-    // either (the wide tree must split every node above 3 primitives)
-    if ((wide || !(parent_cost < 1e34f)) && lane == 0) atomicOr(&counters[kError], kErrDegenerate);
+    // no candidate below 1e34: a leaf unless the parent's cost is not below it either
+    if (!(parent_cost < 1e34f) && lane == 0) atomicOr(&counters[kError], kErrDegenerate);
     return;
   }
   bcast_cand(c, best);
-  if (!wide && parent_cost < c.cost) return;
+  if (parent_cost < c.cost) return;
   if (lane != 0) return;
   const int a = best / kPlanes, i = best % kPlanes + 1;
   const uint32_t cid = atomicAdd(&counters[kArenaCount], 2u);
@@ -490,35 +488,11 @@ __global__ void __launch_bounds__(256) k_part_copy(const Chunk* __restrict__ chu
   for (uint32_t k = ch.begin + threadIdx.x; k < ch.end; k += blockDim.x) prims[k] = tmp[k];
 }
 
-// Halve [first, first + count) in its current order; child boxes by warp reductions.
-__device__ __forceinline__ void median_split(const float4* lo, const float4* hi, const uint32_t* prims,
-                                             uint32_t first, uint32_t count, int lane, Cand& c) {
-  c.lc = count / 2;
-  c.rc = count - c.lc;
-  for (int side = 0; side < 2; side++) {
-    const uint32_t b = side ? c.lc : 0u, e = side ? count : c.lc;
-    uint32_t kmn[3] = {fkey(1e34f), fkey(1e34f), fkey(1e34f)}, kmx[3] = {fkey(-1e34f), fkey(-1e34f), fkey(-1e34f)};
-    for (uint32_t k = b + lane; k < e; k += 32) {
-      const uint32_t p = prims[first + k];
-      const float4 l = lo[p], h = hi[p];
-      kmn[0] = min(kmn[0], fkey(l.x)), kmn[1] = min(kmn[1], fkey(l.y)), kmn[2] = min(kmn[2], fkey(l.z));
-      kmx[0] = max(kmx[0], fkey(h.x)), kmx[1] = max(kmx[1], fkey(h.y)), kmx[2] = max(kmx[2], fkey(h.z));
-    }
-    for (int k = 0; k < 3; k++) {
-      const float mn = unkey(__reduce_min_sync(0xffffffffu, kmn[k]));
-      const float mx = unkey(__reduce_max_sync(0xffffffffu, kmx[k]));
-      if (side) c.rmn[k] = mn, c.rmx[k] = mx;
-      else c.lmn[k] = mn, c.lmx[k] = mx;
-    }
-  }
-  c.cost = 0.0f;
-}
-
 // ---------------------------------------------------------------- small subtrees, one warp each
 __global__ void __launch_bounds__(kSmallWarps * 32) k_small(BNode* arena, const int32_t* __restrict__ small,
                                                             const uint32_t* counters_ro, const float4* __restrict__ lo,
                                                             const float4* __restrict__ hi, uint32_t* prims,
-                                                            uint32_t* counters, uint32_t cap, int wide) {
+                                                            uint32_t* counters, uint32_t cap) {
   __shared__ uint32_t sbins[kSmallWarps][kBinWords];
   __shared__ float splanes[kSmallWarps][3 * kPlanes];
   __shared__ int32_t sstack[kSmallWarps][kSmallStack];
@@ -551,25 +525,21 @@ __global__ void __launch_bounds__(kSmallWarps * 32) k_small(BNode* arena, const 
       Cand c;
       const int best = choose_split(bins, lane, c);
       const float parent_cost = __fmul_rn(area3(nd.mn, nd.mx), __uint2float_rn(count));
-      if (best == 32 && wide) {
-        // every centroid in one interval on all axes: halve the range as it lies
-        median_split(lo, hi, prims, first, count, lane, c);
-      } else if (best == 32) {
+      if (best == 32) {
         if (!(parent_cost < 1e34f) && lane == 0) atomicOr(&counters[kError], kErrDegenerate);
         continue;
-      } else {
-        bcast_cand(c, best);
-        if (!wide && parent_cost < c.cost) continue;
       }
-      const int a = best == 32 ? 0 : best / kPlanes;
-      const float coord = best == 32 ? 0.0f : planes[best];
-      // stable partition through shared memory (the halving keeps the order)
+      bcast_cand(c, best);
+      if (parent_cost < c.cost) continue;
+      const int a = best / kPlanes;
+      const float coord = planes[best];
+      // stable partition through shared memory
       uint32_t nl = 0, nr = 0;
       for (uint32_t k0 = 0; k0 < count; k0 += 32) {
         const uint32_t k = k0 + lane;
         const bool in = k < count;
         const uint32_t p = in ? prims[first + k] : 0u;
-        const bool left = in && (best == 32 ? k < c.lc : goes_left(lo, hi, p, a, coord));
+        const bool left = in && goes_left(lo, hi, p, a, coord);
         const uint32_t bl = __ballot_sync(0xffffffffu, left), br = __ballot_sync(0xffffffffu, in && !left);
         if (left) tmp[nl + __popc(bl & lt)] = p;
         else if (in) tmp[kWarpMax + nr + __popc(br & lt)] = p;
@@ -742,7 +712,7 @@ unsigned blocks(uint64_t n, unsigned per) { return (unsigned)((n + per - 1) / pe
 size_t gpu_bvh_scratch_bytes(uint32_t n) { return Layout(n).total; }
 
 cudaError_t gpu_bvh_build(const DevScene& sc, void* scratch, uint32_t* host_counters, cudaStream_t s,
-                          GpuBvhResult& r, int wide) {
+                          GpuBvhResult& r) {
   const uint32_t n = sc.tri_count;
   const Layout L(n);
   uint32_t* counters = at<uint32_t>(scratch, L.counters);
@@ -762,7 +732,7 @@ cudaError_t gpu_bvh_build(const DevScene& sc, void* scratch, uint32_t* host_coun
   uint32_t* qidx = at<uint32_t>(scratch, L.qidx);
 
   k_init<<<1, 32, 0, s>>>(counters);
-  k_prep<<<blocks(n, 256), 256, 0, s>>>(sc.verts, sc.idx, n, lo, hi, prims, counters, wide);
+  k_prep<<<blocks(n, 256), 256, 0, s>>>(sc.verts, sc.idx, n, lo, hi, prims, counters);
   k_root<<<1, 1, 0, s>>>(arena, large[0], small, n, counters);
   GB_TRY(cudaGetLastError());
   GB_TRY(cudaMemcpyAsync(host_counters, counters, 4 * kCounterWords, cudaMemcpyDeviceToHost, s));
@@ -777,7 +747,7 @@ cudaError_t gpu_bvh_build(const DevScene& sc, void* scratch, uint32_t* host_coun
     const unsigned nchunk = (unsigned)std::min<uint64_t>((uint64_t)n / kChunk + nl + 1, L.max_chunks);
     k_bin<<<nchunk, 256, 0, s>>>(arena, large[cur], chunks, counters, lo, hi, prims, bins);
     k_split<<<blocks((uint64_t)nl * 32, 256), 256, 0, s>>>(arena, large[cur], nl, bins, split, large[cur ^ 1], small,
-                                                          counters, L.cap, wide);
+                                                          counters, L.cap);
     k_part_count<<<nchunk, 256, 0, s>>>(chunks, split, counters, lo, hi, prims, chunk_left);
     k_part_offsets<<<blocks((uint64_t)nl * 32, 256), 256, 0, s>>>(arena, large[cur], nl, split, chunk_left, chunk_loff,
                                                                  counters);
@@ -795,7 +765,7 @@ cudaError_t gpu_bvh_build(const DevScene& sc, void* scratch, uint32_t* host_coun
   if (nsmall > 0 && !host_counters[kError]) {
     const int sms = sm_count();
     const unsigned g = (unsigned)std::min<uint64_t>(blocks(nsmall, kSmallWarps), (uint64_t)sms * 8);
-    k_small<<<g, kSmallWarps * 32, 0, s>>>(arena, small, counters, lo, hi, prims, counters, L.cap, wide);
+    k_small<<<g, kSmallWarps * 32, 0, s>>>(arena, small, counters, lo, hi, prims, counters, L.cap);
     GB_TRY(cudaGetLastError());
   }
   GB_TRY(cudaMemsetAsync(arrive, 0, 4 * (size_t)L.cap, s));
@@ -907,50 +877,67 @@ __device__ __forceinline__ bool quantise(float p, float s, float lo, float hi, u
   return __fmaf_rn(s, (float)ql, p) <= lo && __fmaf_rn(s, (float)qh, p) >= hi;
 }
 
+__device__ __forceinline__ uint32_t wsplit(const WideCost& c, int i) { return (c.split >> (3 * (i - 2))) & 7u; }
+
 __global__ void __launch_bounds__(128) k_wcollapse(const BNode* __restrict__ arena, const uint32_t* __restrict__ bprims,
-                                                   const float4* __restrict__ v, const uint4* __restrict__ idx,
-                                                   const WEntry* __restrict__ in, uint32_t n_in, WEntry* out,
-                                                   uint32_t* counters, WNode8* wn, float4* wtris, uint32_t cap,
-                                                   uint32_t n_prims) {
+                                                   const WideCost* __restrict__ cost, const float4* __restrict__ v,
+                                                   const uint4* __restrict__ idx, const WEntry* __restrict__ in,
+                                                   uint32_t n_in, WEntry* out, uint32_t* counters, WNode8* wn,
+                                                   float4* wtris, uint32_t cap, uint32_t n_prims) {
   const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= n_in) return;
   const WEntry en = in[i];
   const BNode b = arena[en.bin];
   // frontier of binary nodes under this wide node, in left-to-right order;
-  // open the inner entry of largest surface area while the slots last
+  // leafy[k]: entry k becomes leaf slots (its primitive range, three per slot)
   int32_t F[8];
+  bool leafy[8];
   int nf = 0;
-  if (b.left < 0) {
-    F[nf++] = (int32_t)en.bin;
-  } else {
-    F[nf++] = b.left;
-    F[nf++] = b.left + 1;
-  }
-  auto usage = [&](int32_t x) {
+  auto usage = [&](int32_t x, bool lf) {
     const BNode& c = arena[x];
-    return c.left >= 0 ? 1u : leaf_slots(c.count);
+    return lf ? leaf_slots(c.count) : 1u;
   };
-  uint32_t used = 0;
-  for (int k = 0; k < nf; k++) used += usage(F[k]);
-  while (true) {
-    int bi = -1;
-    float ba = -1.0f;
-    for (int k = 0; k < nf; k++) {
-      const BNode& c = arena[F[k]];
-      if (c.left < 0) continue;
-      const float a = area3(c.mn, c.mx);
-      if (a > ba) ba = a, bi = k;
+  if (b.left < 0) {
+    F[nf] = (int32_t)en.bin, leafy[nf++] = true;
+  } else {
+    // the slots of least cost (the optimal n-wide collapse of Ylitie, Karras and
+    // Laine, HPG 2017): k of 8 to the left child, then each side as its table says
+    const int32_t L = b.left, R = L + 1;
+    float best = 3e38f;
+    int bk = 1;
+    for (int k = 1; k < 8; k++) {
+      const float c = __fadd_rn(cost[L].c[k - 1], cost[R].c[8 - k - 1]);
+      if (c < best) best = c, bk = k;
     }
-    if (bi < 0) break;
-    const int32_t l = arena[F[bi]].left;
-    const uint32_t nu = used - 1 + usage(l) + usage(l + 1);
-    if (nu > 8) break;
-    for (int k = nf; k > bi + 1; k--) F[k] = F[k - 1];
-    F[bi] = l;
-    F[bi + 1] = l + 1;
-    nf++;
-    used = nu;
+    int32_t stn[16];
+    int sti[16];
+    int sp = 0;
+    stn[sp] = R, sti[sp++] = 8 - bk;
+    stn[sp] = L, sti[sp++] = bk;
+    while (sp > 0) {
+      const int32_t x = stn[--sp];
+      int ix = sti[sp];
+      const BNode& c = arena[x];
+      while (ix > 1 && (c.left < 0 || wsplit(cost[x], ix) == 0)) ix--;
+      if (ix == 1) {
+        if (nf >= 8) {
+          atomicOr(&counters[kWideError], kWErrSlots);
+          return;
+        }
+        F[nf] = x, leafy[nf++] = c.left < 0 || cost[x].leaf1 != 0;
+        continue;
+      }
+      const int k = (int)wsplit(cost[x], ix);
+      if (sp + 2 > 16) {
+        atomicOr(&counters[kWideError], kWErrSlots);
+        return;
+      }
+      stn[sp] = c.left + 1, sti[sp++] = ix - k;
+      stn[sp] = c.left, sti[sp++] = k;
+    }
   }
+  uint32_t used = 0;
+  for (int k = 0; k < nf; k++) used += usage(F[k], leafy[k]);
   if (used > 8) {
     atomicOr(&counters[kWideError], kWErrSlots);
     return;
@@ -958,7 +945,7 @@ __global__ void __launch_bounds__(128) k_wcollapse(const BNode* __restrict__ are
   uint32_t n_int = 0, n_tri = 0;
   for (int k = 0; k < nf; k++) {
     const BNode& c = arena[F[k]];
-    if (c.left >= 0) n_int++;
+    if (!leafy[k]) n_int++;
     else n_tri += (uint32_t)c.count;
   }
   const uint32_t child_base = n_int ? atomicAdd(&counters[kWideCount], n_int) : 0u;
@@ -985,7 +972,7 @@ __global__ void __launch_bounds__(128) k_wcollapse(const BNode* __restrict__ are
   uint32_t rank = 0, off = 0;
   for (int k = 0; k < nf; k++) {
     const BNode& c = arena[F[k]];
-    if (c.left >= 0) {
+    if (!leafy[k]) {
       for (int a = 0; a < 3; a++) ok &= quantise(p[a], sc[a], c.mn[a], c.mx[a], w.qlo[a][slot], w.qhi[a][slot]);
       w.meta[slot] = (uint8_t)(0x80u | rank);
       w.imask |= (uint8_t)(1u << slot);
@@ -1022,14 +1009,13 @@ __global__ void __launch_bounds__(128) k_wcollapse(const BNode* __restrict__ are
 
 size_t gpu_wbvh_scratch_bytes(uint32_t binary_nodes) { return WLayout(binary_nodes).total; }
 
-cudaError_t gpu_wbvh_collapse(const DevScene& sc, void* scratch, void* scratch2, uint32_t binary_nodes, float4* tris,
-                              uint32_t* host_counters, cudaStream_t s, uint32_t* wide_nodes, uint32_t* depth,
-                              uint32_t* error) {
+cudaError_t gpu_wbvh_collapse(const DevScene& sc, const void* arena_v, const uint32_t* bprims, const WideCost* cost,
+                              void* scratch2, uint32_t binary_nodes, float4* tris, uint32_t* host_counters,
+                              cudaStream_t s, uint32_t* wide_nodes, uint32_t* depth, uint32_t* error) {
   const uint32_t n = sc.tri_count;
-  const Layout L(n);
   const WLayout W(binary_nodes);
-  const BNode* arena = at<BNode>(scratch, L.arena);
-  const uint32_t* bprims = at<uint32_t>(scratch, L.prims);
+  // both binary builders write this 48-byte node layout (BNode here, FNodeD in bvh_gpu_fast.cu)
+  const BNode* arena = static_cast<const BNode*>(arena_v);
   WNode8* wn = at<WNode8>(scratch2, W.nodes);
   WEntry* lists[2] = {at<WEntry>(scratch2, W.list0), at<WEntry>(scratch2, W.list1)};
   uint32_t* counters = at<uint32_t>(scratch2, W.counters);
@@ -1041,8 +1027,8 @@ cudaError_t gpu_wbvh_collapse(const DevScene& sc, void* scratch, void* scratch2,
   int cur = 0;
   while (n_in > 0) {
     GB_TRY(cudaMemsetAsync(counters + kWideNext, 0, 4, s));
-    k_wcollapse<<<blocks(n_in, 128), 128, 0, s>>>(arena, bprims, sc.verts, sc.idx, lists[cur], n_in, lists[cur ^ 1],
-                                                  counters, wn, tris, W.cap, n);
+    k_wcollapse<<<blocks(n_in, 128), 128, 0, s>>>(arena, bprims, cost, sc.verts, sc.idx, lists[cur], n_in,
+                                                  lists[cur ^ 1], counters, wn, tris, W.cap, n);
     GB_TRY(cudaGetLastError());
     GB_TRY(cudaMemcpyAsync(host_counters, counters, 4 * kWideCounterWords, cudaMemcpyDeviceToHost, s));
     GB_TRY(cudaStreamSynchronize(s));

@@ -117,7 +117,7 @@ struct Layout {
   size_t lo, hi, cent, prims, tmp, arena, cost, arrive, large0, large1, small, chunks, chunk_left, chunk_loff, split,
       bins, cbk, qlist, qrec, scan, sums, counters, total;
   uint32_t cap, qcap, max_large, max_chunks, max_small, max_sums;
-  explicit Layout(uint32_t n) {
+  explicit Layout(uint32_t n, int wide = 0) {
     cap = 2 * n + 2;
     qcap = n + 2;
     max_large = n / (kWarpMax + 1) + 2;
@@ -136,7 +136,7 @@ struct Layout {
     prims = take(4 * (size_t)n);
     tmp = take(4 * (size_t)n);
     arena = take(sizeof(FNodeD) * (size_t)cap);
-    cost = take(sizeof(FCostD) * (size_t)cap);
+    cost = take((wide ? sizeof(WideCost) : sizeof(FCostD)) * (size_t)cap);
     arrive = take(4 * (size_t)cap);
     large0 = take(4 * (size_t)max_large);
     large1 = take(4 * (size_t)max_large);
@@ -358,10 +358,11 @@ __global__ void __launch_bounds__(256) k_fmag(const float4* __restrict__ v, cons
   if ((threadIdx.x & 31) == 0) atomicMax(&counters[kMag], r);
 }
 
+// rel_pad: kPad for the traversal-speed quad tree, 0 (exact bounds) for the wide tree
 __global__ void __launch_bounds__(256) k_fprep(const float4* __restrict__ v, const uint4* __restrict__ idx, uint32_t n,
                                                float4* __restrict__ lo, float4* __restrict__ hi,
                                                float4* __restrict__ cent, uint32_t* __restrict__ prims,
-                                               uint32_t* counters) {
+                                               uint32_t* counters, float rel_pad) {
   const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
   uint32_t kmn[3] = {fkey(1e34f), fkey(1e34f), fkey(1e34f)}, kmx[3] = {fkey(-1e34f), fkey(-1e34f), fkey(-1e34f)};
   if (i < n) {
@@ -373,7 +374,7 @@ __global__ void __launch_bounds__(256) k_fprep(const float4* __restrict__ v, con
     for (int k = 0; k < 3; k++) {
       const float pa = comp(a, k), pb = comp(b, k), pc = comp(c, k);
       float lo_k = gmin(pa, gmin(pb, pc)), hi_k = gmax(pa, gmax(pb, pc));
-      const float pad = __fmul_rn(kPad, gmax(floor_mag, gmax(fabsf(lo_k), fabsf(hi_k))));
+      const float pad = __fmul_rn(rel_pad, gmax(floor_mag, gmax(fabsf(lo_k), fabsf(hi_k))));
       lo_k = __fadd_rn(__fsub_rn(lo_k, pad), 0.0f);  // -0 becomes +0
       hi_k = __fadd_rn(__fadd_rn(hi_k, pad), 0.0f);
       mn[k] = lo_k, mx[k] = hi_k;
@@ -912,6 +913,78 @@ __global__ void __launch_bounds__(256) k_fcost(const FNodeD* __restrict__ arena,
   }
 }
 
+// ---------------------------------------------------------------- 8-wide cost table
+// Relative costs of the wide tree's traversal per unit of surface area: a wide
+// node (one 80-byte fetch and eight slot tests) and one triangle of a leaf slot.
+constexpr float kWideNodeCost = 1.0f;
+constexpr float kWideTriCost = 1.0f;
+
+__device__ __forceinline__ void wide_cost(const FNodeD& n, const WideCost* cost, float s, WideCost& e) {
+  const float A = farea(n.mn, n.mx, s);
+  const uint32_t count = (uint32_t)n.count;
+  const float inf = 3e38f;
+  e.split = 0;
+  e.pad[0] = e.pad[1] = 0;
+  if (n.left < 0) {
+    // a binary leaf takes ceil(count / 3) slots of three triangles
+    const uint32_t need = (count + 2u) / 3u;
+    const float leaf = __fmul_rn(A, __fmul_rn(kWideTriCost, __uint2float_rn(count)));
+    for (int i = 1; i <= 8; i++) e.c[i - 1] = (uint32_t)i >= need ? leaf : inf;
+    e.leaf1 = 1;
+    return;
+  }
+  float L[8], R[8];
+  for (int k = 0; k < 8; k++) L[k] = __ldcg(&cost[n.left].c[k]), R[k] = __ldcg(&cost[n.left + 1].c[k]);
+  float dist[9];
+  uint32_t dk[9];
+  for (int j = 0; j <= 8; j++) dist[j] = inf, dk[j] = 0;
+  for (int j = 2; j <= 8; j++)
+    for (int k = 1; k < j; k++) {
+      const float v = __fadd_rn(L[k - 1], R[j - k - 1]);
+      if (v < dist[j]) dist[j] = v, dk[j] = (uint32_t)k;
+    }
+  const float leaf = count <= 3u ? __fmul_rn(A, __fmul_rn(kWideTriCost, __uint2float_rn(count))) : inf;
+  const float inner = __fadd_rn(__fmul_rn(A, kWideNodeCost), dist[8]);
+  e.leaf1 = (count <= 3u && leaf <= inner) ? 1u : 0u;
+  e.c[0] = e.leaf1 ? leaf : inner;
+  for (int i = 2; i <= 8; i++) {
+    if (dist[i] < e.c[i - 2]) {
+      e.c[i - 1] = dist[i];
+      e.split |= dk[i] << (3 * (i - 2));
+    } else {
+      e.c[i - 1] = e.c[i - 2];
+    }
+  }
+}
+
+__device__ __forceinline__ void store_wide_cost(WideCost* dst, const WideCost& e) {
+  for (int k = 0; k < 8; k++) __stcg(&dst->c[k], e.c[k]);
+  __stcg(&dst->split, e.split);
+  __stcg(&dst->leaf1, e.leaf1);
+}
+
+__global__ void __launch_bounds__(256) k_fcost8(const FNodeD* __restrict__ arena, WideCost* cost, uint32_t* arrive,
+                                                const uint32_t* counters, uint32_t cap, float s) {
+  const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= min(counters[kArenaCount], cap)) return;
+  if (arena[i].left >= 0) return;
+  WideCost e;
+  wide_cost(arena[i], cost, s, e);
+  store_wide_cost(&cost[i], e);
+  int32_t cur = (int32_t)i;
+  while (true) {
+    const int32_t p = arena[cur].parent;
+    if (p < 0) break;
+    __threadfence();
+    if (atomicAdd(&arrive[p], 1u) == 0) return;  // the sibling's subtree is not finished yet
+    __threadfence();
+    const FNodeD np = arena[p];
+    wide_cost(np, cost, s, e);
+    store_wide_cost(&cost[p], e);
+    cur = p;
+  }
+}
+
 // ---------------------------------------------------------------- collapse
 __device__ __forceinline__ uint32_t split_of(uint32_t meta, int i) { return (meta >> (8 * (i - 1))) & 0xffu; }
 
@@ -1142,11 +1215,19 @@ cudaError_t read_counters(uint32_t* host, const uint32_t* dev, cudaStream_t s) {
 
 }  // namespace
 
-size_t gpu_fbvh_scratch_bytes(uint32_t n) { return Layout(n).total; }
+size_t gpu_fbvh_scratch_bytes(uint32_t n, int wide) { return Layout(n, wide).total; }
 
-cudaError_t gpu_fbvh_build(const DevScene& sc, void* scratch, uint32_t* hc, cudaStream_t s, GpuBvhResult& r) {
+void gpu_fbvh_binary(void* scratch, uint32_t n, int wide, const void** arena, const uint32_t** prims,
+                     const WideCost** cost) {
+  const Layout Lo(n, wide);
+  *arena = at<FNodeD>(scratch, Lo.arena);
+  *prims = at<uint32_t>(scratch, Lo.prims);
+  *cost = wide ? at<WideCost>(scratch, Lo.cost) : nullptr;
+}
+
+cudaError_t gpu_fbvh_build(const DevScene& sc, void* scratch, uint32_t* hc, cudaStream_t s, GpuBvhResult& r, int wide) {
   const uint32_t n = sc.tri_count;
-  const Layout Lo(n);
+  const Layout Lo(n, wide);
   uint32_t* counters = at<uint32_t>(scratch, Lo.counters);
   float4* lo = at<float4>(scratch, Lo.lo);
   float4* hi = at<float4>(scratch, Lo.hi);
@@ -1172,7 +1253,7 @@ cudaError_t gpu_fbvh_build(const DevScene& sc, void* scratch, uint32_t* hc, cuda
 
   k_finit<<<1, 32, 0, s>>>(counters);
   k_fmag<<<blocks(n, 256), 256, 0, s>>>(sc.verts, sc.idx, n, counters);
-  k_fprep<<<blocks(n, 256), 256, 0, s>>>(sc.verts, sc.idx, n, lo, hi, cent, prims, counters);
+  k_fprep<<<blocks(n, 256), 256, 0, s>>>(sc.verts, sc.idx, n, lo, hi, cent, prims, counters, wide ? 0.0f : kPad);
   k_froot<<<1, 1, 0, s>>>(arena, large[0], small, n, counters);
   FB_TRY(cudaGetLastError());
   FB_TRY(read_counters(hc, counters, s));
@@ -1244,6 +1325,13 @@ cudaError_t gpu_fbvh_build(const DevScene& sc, void* scratch, uint32_t* hc, cuda
     return cudaSuccess;
   }
   FB_TRY(cudaMemsetAsync(arrive, 0, 4 * (size_t)nb, s));
+  if (wide) {
+    k_fcost8<<<blocks(nb, 256), 256, 0, s>>>(arena, at<WideCost>(scratch, Lo.cost), arrive, counters, Lo.cap, ascale);
+    FB_TRY(cudaGetLastError());
+    FB_TRY(read_counters(hc, counters, s));
+    r.error = hc[kError];
+    return cudaSuccess;
+  }
   k_fcost<<<blocks(nb, 256), 256, 0, s>>>(arena, cost, arrive, counters, Lo.cap, ascale);
   // quad levels from the root (binary node 0)
   FB_TRY(cudaMemsetAsync(qlist, 0, 4, s));
@@ -1299,7 +1387,7 @@ cudaError_t gpu_fbvh_emit(const DevScene& sc, void* scratch, const GpuBvhResult&
 }
 
 uint32_t gpu_fbvh_error(void* scratch, uint32_t n, uint32_t* hc, cudaStream_t s) {
-  const Layout Lo(n);
+  const Layout Lo(n);  // quad mode (the wide mode reports its errors from gpu_fbvh_build)
   if (read_counters(hc, at<uint32_t>(scratch, Lo.counters), s) != cudaSuccess) return 0xffffffffu;
   return hc[kError];
 }

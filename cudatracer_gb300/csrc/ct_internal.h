@@ -218,10 +218,7 @@ struct GpuBvhResult {
   uint32_t levels = 0, small_roots = 0;
 };
 size_t gpu_bvh_scratch_bytes(uint32_t n);
-// wide = 1: the rules of the 8-wide quantised tree (exact triangle bounds, every
-// node above 3 primitives split, halving where no plane separates centroids).
-cudaError_t gpu_bvh_build(const DevScene& sc, void* scratch, uint32_t* host_counters, cudaStream_t s, GpuBvhResult& r,
-                          int wide = 0);
+cudaError_t gpu_bvh_build(const DevScene& sc, void* scratch, uint32_t* host_counters, cudaStream_t s, GpuBvhResult& r);
 cudaError_t gpu_bvh_emit(const DevScene& sc, void* scratch, const GpuBvhResult& r, uint32_t leaf_shift, void* quad,
                          QNodeDev* nodes, float4* tris, uint32_t* prims, cudaStream_t s);
 
@@ -231,27 +228,49 @@ struct QuadNode;  // bvh_build.h
 cudaError_t launch_quad_to_dev(const QuadNode* quad, uint32_t nq, uint32_t leaf_shift, QNodeDev* nodes, cudaStream_t s);
 cudaError_t launch_leaf_tris(const DevScene& sc, const uint32_t* prims, uint32_t n, float4* tris, cudaStream_t s);
 
+// Cost table of the 8-wide collapse (gpu_fbvh_build with wide = 1): C(n, i),
+// i = 1..8, the surface-area cost of binary subtree n spread over i slots of
+// its wide parent; split: 3 bits per i = 2..8 (bits 3(i-2)..), the slots given
+// to the left child (0: as with i - 1 slots); leaf1: with one slot the subtree
+// is one leaf slot.
+struct __align__(16) WideCost {
+  float c[8];
+  uint32_t split;
+  uint32_t leaf1;
+  uint32_t pad[2];
+};
+static_assert(sizeof(WideCost) == 48, "WideCost");
+
 // Device build of ct_bvh_build_fast's tree (bvh_gpu_fast.cu), byte-equal to the
 // host build: gpu_fbvh_build fills `scratch` (gpu_fbvh_scratch_bytes) and
 // returns the sizes (r.error: 1 a padded box is not finite, 2 capacity, 4
 // stack, 8 partition mismatch, 16 collapse); gpu_fbvh_emit writes the quad
 // nodes, traversal nodes, triangles and primitive order. host_counters: 16
 // words of pinned host memory; the build synchronises with `s` once per level.
-size_t gpu_fbvh_scratch_bytes(uint32_t n);
-cudaError_t gpu_fbvh_build(const DevScene& sc, void* scratch, uint32_t* host_counters, cudaStream_t s, GpuBvhResult& r);
+// wide = 1: the binary tree of the same rules over exact triangle bounds, then
+// the 8-wide cost table instead of the quad collapse (for gpu_wbvh_collapse;
+// gpu_fbvh_binary gives the arena, primitive order and table).
+size_t gpu_fbvh_scratch_bytes(uint32_t n, int wide = 0);
+cudaError_t gpu_fbvh_build(const DevScene& sc, void* scratch, uint32_t* host_counters, cudaStream_t s, GpuBvhResult& r,
+                           int wide = 0);
+void gpu_fbvh_binary(void* scratch, uint32_t n, int wide, const void** arena, const uint32_t** prims,
+                     const WideCost** cost);
 cudaError_t gpu_fbvh_emit(const DevScene& sc, void* scratch, const GpuBvhResult& r, uint32_t leaf_shift, void* quad,
                           QNodeDev* nodes, float4* tris, uint32_t* prims, cudaStream_t s);
 // error word of the last emit (reads the counters back; synchronises with `s`)
 uint32_t gpu_fbvh_error(void* scratch, uint32_t n, uint32_t* host_counters, cudaStream_t s);
 
-// Collapse of a wide-rule binary build (gpu_bvh_build with wide = 1) into
-// 8-wide quantised nodes. `scratch2` holds gpu_wbvh_scratch_bytes(binary_nodes);
+// Collapse of a binary build into 8-wide quantised nodes. `scratch2` holds gpu_wbvh_scratch_bytes(binary_nodes);
 // nodes end up in scratch2 (read back their count in *wide_nodes, then copy
 // them out with gpu_wbvh_copy_nodes); triangles go straight to `tris` (n x 48 B).
 size_t gpu_wbvh_scratch_bytes(uint32_t binary_nodes);
-cudaError_t gpu_wbvh_collapse(const DevScene& sc, void* scratch, void* scratch2, uint32_t binary_nodes, float4* tris,
-                              uint32_t* host_counters, cudaStream_t s, uint32_t* wide_nodes, uint32_t* depth,
-                              uint32_t* error);
+// arena / prims / cost: the binary tree (48-byte nodes {mn[3], first, mx[3],
+// count, left, parent, depth, -}), primitive order and cost table of
+// gpu_fbvh_build with wide = 1 (gpu_fbvh_binary); each wide node takes the
+// slots of least surface-area cost from the table.
+cudaError_t gpu_wbvh_collapse(const DevScene& sc, const void* arena, const uint32_t* prims, const WideCost* cost,
+                              void* scratch2, uint32_t binary_nodes, float4* tris, uint32_t* host_counters,
+                              cudaStream_t s, uint32_t* wide_nodes, uint32_t* depth, uint32_t* error);
 cudaError_t gpu_wbvh_copy_nodes(void* scratch2, uint32_t binary_nodes, WNode8* out, uint32_t count, cudaStream_t s);
 
 // Wide-tree queries: FP32 watertight tests; hits within the FP32 error bound

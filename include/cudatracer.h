@@ -253,8 +253,10 @@ ct_status ct_bvh_build_fast_device(ct_ctx* ctx, const ct_scene* scene, void* str
  * outward, triangles are tested watertight in FP32 and the hits FP32 cannot
  * settle (near an edge, near another hit's t) are re-tested in FP64, so
  * ct_trace_closest/ct_trace_any on this tree give the FP64 closest hit (equal
- * t: lower primitive id) and `tri_eps` is ignored. Built on the device from
- * exact triangle bounds (every node above 3 triangles split). Frames
+ * t: lower primitive id) and `tri_eps` is ignored. Built on the device: the
+ * binary tree of ct_bvh_build_fast's rules over exact triangle bounds,
+ * collapsed to eight slots per node by least surface-area cost (leaf slots of
+ * one to three triangles). Frames
  * (ct_render_accumulate, ct_batch) may trace it too: there the triangle test
  * is the reference's Moller-Trumbore with tri_eps, so the hits are the quad
  * tree's up to the winner of an exact t tie. Export with CT_BVH_WIDE8_Q8
