@@ -76,7 +76,9 @@ PATCHES = {
 # Camera-free device code see triangle::getBounds as host-only (its __m128 box
 # type is host code), and replace the grid sizes n / 128 and n + n % 128 by
 # ceil(n / 128): as written, the last n % 128 rays of a pass are dropped, and a
-# bounce pass can read up to 127 rays past the end of its ray buffer.
+# bounce pass can read up to 127 rays past the end of its ray buffer; and the
+# traversal stacks are enlarged from 32 to 64 entries (results are unchanged
+# wherever 32 sufficed).
 GPU_PATCHES = {
     "CUDA/Kernel.cuh": [
         ("#include <GL/glew.h>\n", "", 1),
@@ -103,6 +105,11 @@ GPU_PATCHES = {
     ],
     "BVH/BVHNode.cuh": PATCHES["BVH/BVHNode.cuh"],
     "BVH/BVHNode.cu": PATCHES["BVH/BVHNode.cu"],
+    # the traversal stacks hold 32 entries with no overflow check; a quad tree of
+    # depth d needs up to 3d + 1 (43 for the 3.1 M-triangle terrain's depth 14)
+    "BVH/MBVHNode.cuh": [
+        ("\t\tMBVHTraversal todo[32];\n", "\t\tMBVHTraversal todo[64];\n", 3),
+    ],
 }
 GPU_DIR = os.path.join(REF_OUT, "gpu")
 GPU_LIB = os.path.join(REF_OUT, "libctref_gpu.so")
