@@ -63,9 +63,11 @@ def parse_args():
     ap.add_argument("--height", type=int, default=1080)
     ap.add_argument("--skip-extras", action="store_true",
                     help="only the timed frames: no e2e pass, roofline model, CPU baseline or sphere query")
-    ap.add_argument("--case", choices=["soup"], default=None,
+    ap.add_argument("--case", choices=["soup", "sphere"], default=None,
                     help="profiling case instead of the benchmark: 'soup' builds the quad and the wide BVH of "
-                         "a seeded soup and traces incoherent rays twice through each (prints timings)")
+                         "a seeded soup and traces incoherent rays twice through each (prints timings); 'sphere' "
+                         "runs the closest-hit query on the 81,920-triangle sphere (3 + 10 launches per tree, "
+                         "the reference's tree first) and prints its JSON")
     ap.add_argument("--soup-tris", type=int, default=4_000_000)
     ap.add_argument("--soup-rays", type=int, default=2_000_000)
     ap.add_argument("--skip-serving", action="store_true",
@@ -174,12 +176,12 @@ def measured_peaks():
         return 6800.0, "fallback"
 
 
-def profiled_traffic(key: str = "dram_bytes_per_extension_ray"):
-    """Bytes per extension ray of the extend kernel (DRAM, or with
+def profiled_traffic(key: str = "dram_bytes_per_extension_ray", summary: str = "extend_terrain_1080p.md"):
+    """A figure from a committed ncu summary in profiles/: by default bytes per
+    extension ray of the extend kernel (DRAM, or with
     key="l2_bytes_per_extension_ray" L2; keys prefixed "reference_tree_" for
-    frames on the reference's tree), from the committed ncu summary
-    (profiles/extend_terrain_1080p.md), or None."""
-    path = os.path.join(ROOT, "profiles", "extend_terrain_1080p.md")
+    frames on the reference's tree), or None."""
+    path = os.path.join(ROOT, "profiles", summary)
     try:
         txt = open(path).read()
     except OSError:
@@ -294,12 +296,43 @@ def sphere_closest_hit(ctx):
     mrays = rate(bvh)
     fb = sc.build_bvh_fast_device()
     mrays_fast = rate(fb)
+
+    # the query's roofline: its working set (3.2 MB of nodes, 4.3 MB of triangles)
+    # stays in L2 while the 4.2 M rays of 40 B stream from HBM, so L2 bounds it;
+    # the algorithmic bytes (ray in and out + node visits x 128 + triangle tests
+    # x 52, counted by the oracle along the reference's traversal order, which
+    # the query kernel follows) are set against measured HBM, and the L2
+    # throughput as a share of the chip's L2 peak comes from the committed ncu
+    # capture of this kernel (profiles/query_sphere_81920.md)
+    import oracle
+
+    oracle.build_oracle()
+
+    def model(tree):
+        q, pr = tree.export()
+        oracle.work_read(reset=True)
+        oracle.trace_closest(q, pr, s.vertices, s.indices, o, d, nthreads=os.cpu_count() or 1)
+        w = oracle.work_read(reset=True)
+        vn, vt = w["ext_nodes"] / max(1, w["ext_rays"]), w["ext_tris"] / max(1, w["ext_rays"])
+        return {"mean_node_visits": vn, "mean_tri_tests": vt, "bytes_per_ray": 40 + 128 * vn + 52 * vt}
+
+    pk = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    hbm = json.load(open(pk)).get("hbm_gbs", 6800.0) if os.path.exists(pk) else 6800.0
+    roof = {}
+    for name, tree, rate_ in (("reference_tree", bvh, mrays), ("fast_tree", fb, mrays_fast)):
+        m = model(tree)
+        ach = rate_ * 1e6 * m["bytes_per_ray"] / 1e9
+        roof[name] = {**m, "achieved": ach, "unit": "GB/s", "hbm_frac": ach / hbm,
+                      "l2_pct_of_peak_ncu": profiled_traffic(name + "_l2_pct_of_peak", "query_sphere_81920.md"),
+                      "l2_gbs_ncu": profiled_traffic(name + "_l2_gbs", "query_sphere_81920.md")}
     fb.close()
     sc.close()
     bvh.close()
     return {"mrays_per_s": mrays, "fast_tree_mrays_per_s": mrays_fast, "rays": int(O.shape[0]),
             "workload": "81,920-tri sphere, 256x256 pinhole rays x64, ct_trace_closest (reference's tree; "
-                        "fast_tree_mrays_per_s: ct_bvh_build_fast's)"}
+                        "fast_tree_mrays_per_s: ct_bvh_build_fast's)",
+            "roofline": {"bound": "l2", "hbm_peak": hbm, "peak_source": "HBM: MEASURED_PEAKS.json; L2: ncu "
+                         "lts__throughput (share of the chip's L2 peak) in profiles/query_sphere_81920.md", **roof}}
 
 
 def precision_soup(ctx, ntri: int = 10_000_000, nray: int = 16_000_000, sample_every: int = 8) -> dict:
@@ -1040,6 +1073,12 @@ def main():
     args = parse_args()
     if args.case == "soup":
         soup_case(args)
+        return
+    if args.case == "sphere":
+        from cudatracer_gb300 import _build, api
+
+        _build.build()
+        print(json.dumps(sphere_closest_hit(api.Context(0))), flush=True)
         return
     world, rank, local = dist_setup(args)
     if args.impl == "reference":

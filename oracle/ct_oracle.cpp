@@ -922,14 +922,16 @@ void or_trace_closest(const void* qnodes, const uint32_t* prims, const float* ve
                       int nthreads) {
   Geo g{verts, idx, prims, (const QNode*)qnodes, nullptr, eps};
   parallel_range(n, nthreads, [&](int b, int e) {
+    Work w;
     for (int i = b; i < e; i++) {
       float t = kMaxDistance;
       int hi = -1, deep = 0;
-      trace_closest(g, load3(org, i), load3(dir, i), &t, &hi, &deep);
+      trace_closest(g, load3(org, i), load3(dir, i), &t, &hi, &deep, &w);
       hit[i] = hi;
       tout[i] = t;
       if (deep_out) deep_out[i] = deep;
     }
+    g_work[0] += w.rays, g_work[1] += w.nodes, g_work[2] += w.tris;  // counted as extension rays
   });
 }
 
