@@ -152,6 +152,12 @@ struct ct_bvh {
 // Msamples/s; with the current ones, 64-thread blocks: 6 slots 973, 8 slots
 // 991, 10 slots 997, 12 slots 995).
 constexpr int kFrameSlots = 10;
+// Exact-math frames overlap in up to kExactSlots of those slots, each frame
+// logging its per-pixel contributions (DevQueues::log: 2 x max_depth entries of
+// 16 bytes per pixel) for an in-order replay; the logs of a job may take up to
+// kExactLogBytes, beyond which exact frames run one after another.
+constexpr int kExactSlots = 4;
+constexpr size_t kExactLogBytes = (size_t)4 << 30;
 
 struct ct_render {
   int32_t w = 0, h = 0;
@@ -165,6 +171,13 @@ struct ct_render {
     cudaEvent_t done_ev = nullptr;  // recorded after the slot's frame finished
   } slots[kFrameSlots];
   int next_slot = 0;
+  // overlapped exact-math frames: one contribution log per exact slot
+  float4* logs[kExactSlots] = {};
+  int log_entries = 0;  // entries per pixel the logs hold (2 x max_depth)
+  int exact_slots = 0;  // slots with a log
+  int next_exact = 0;
+  uint32_t log_tag = 0;  // tag of the last exact frame issued into a slot
+  Allocs log_allocs;
   // stage profiling: event pairs per stage, recycled through a pool
   bool profile = false;
   std::vector<std::pair<cudaEvent_t, cudaEvent_t>> marks[4];
@@ -1107,6 +1120,7 @@ ct_status ct_render_destroy(ct_ctx* ctx, ct_render* r) {
       cudaEventDestroy(sl.done_ev);
     }
   }
+  free_all(ctx, r->log_allocs);
   free_all(ctx, r->allocs);
   delete r;
   return CT_OK;
@@ -1123,6 +1137,44 @@ static ct_status ensure_slots(ct_ctx* ctx, ct_render* r) {
     CT_CUDA(ctx, cudaEventCreateWithFlags(&sl.free_ev, cudaEventDisableTiming));
     CT_CUDA(ctx, cudaEventCreateWithFlags(&sl.done_ev, cudaEventDisableTiming));
   }
+  return CT_OK;
+}
+
+// Contribution logs for overlapped exact frames of up to max_depth passes;
+// false (exact frames then run in sequence) when they would exceed
+// kExactLogBytes. Growing them waits for the slots that use the old ones.
+static ct_status ensure_logs(ct_ctx* ctx, ct_render* r, int max_depth, bool* ok) {
+  const int entries = 2 * max_depth;
+  const size_t n = (size_t)r->w * r->h;
+  const size_t per_slot = (size_t)entries * n * sizeof(float4);
+  const int slots = (int)std::min<size_t>(kExactSlots, kExactLogBytes / std::max<size_t>(per_slot, 1));
+  *ok = slots >= 2;
+  if (!*ok || (r->log_entries >= entries && r->exact_slots > 0)) return CT_OK;
+  for (int k = 0; k < kExactSlots; k++)
+    if (r->slots[k].stream) CT_CUDA(ctx, cudaStreamSynchronize(r->slots[k].stream));
+  CT_CUDA(ctx, cudaDeviceSynchronize());  // folds on callers' streams may still read the old logs
+  free_all(ctx, r->log_allocs);
+  for (auto& l : r->logs) l = nullptr;
+  r->log_entries = 0, r->exact_slots = 0, r->next_exact = 0;
+  // within the context's budget and what the device has left; else in sequence
+  if (ctx->budget && ctx->bytes.load() + (size_t)slots * per_slot > ctx->budget) {
+    *ok = false;
+    return CT_OK;
+  }
+  for (int k = 0; k < slots; k++) {
+    if (cudaMalloc((void**)&r->logs[k], per_slot) != cudaSuccess) {
+      cudaGetLastError();
+      r->logs[k] = nullptr;
+      free_all(ctx, r->log_allocs);
+      for (auto& l : r->logs) l = nullptr;
+      *ok = false;
+      return CT_OK;
+    }
+    ctx->bytes += per_slot;
+    r->log_allocs.list.push_back({r->logs[k], per_slot});
+    CT_CUDA(ctx, cudaMemset(r->logs[k], 0, per_slot));  // tag 0 is never issued
+  }
+  r->log_entries = entries, r->exact_slots = slots;
   return CT_OK;
 }
 
@@ -1144,12 +1196,15 @@ static ct_status emit_frame(ct_ctx* ctx, ct_render* r, const DevQueues& q, const
       CT_CUDA(ctx, staged(r, 1, st, [&] { return launch_extend_wide(bvh->wdev, qx, cur, p->tri_eps, st); }));
     else
       CT_CUDA(ctx, staged(r, 1, st, [&] { return launch_extend(bvh->dev, qx, cur, p->tri_eps, fast, st); }));
-    CT_CUDA(ctx, staged(r, 2, st, [&] { return launch_shade(scene->dev, q, f, cur, path_length, exact_shade, st); }));
+    DevQueues qs = q, qc = q;  // log entries of this pass (used when q.log is set)
+    qs.log_entry = 2u * (uint32_t)pass;
+    qc.log_entry = 2u * (uint32_t)pass + 1u;
+    CT_CUDA(ctx, staged(r, 2, st, [&] { return launch_shade(scene->dev, qs, f, cur, path_length, exact_shade, st); }));
     if (p->shadow) {
       if (bvh->wide)
-        CT_CUDA(ctx, staged(r, 3, st, [&] { return launch_connect_wide(bvh->wdev, q, p->tri_eps, st); }));
+        CT_CUDA(ctx, staged(r, 3, st, [&] { return launch_connect_wide(bvh->wdev, qc, p->tri_eps, st); }));
       else
-        CT_CUDA(ctx, staged(r, 3, st, [&] { return launch_connect(bvh->dev, q, p->tri_eps, fast, st); }));
+        CT_CUDA(ctx, staged(r, 3, st, [&] { return launch_connect(bvh->dev, qc, p->tri_eps, fast, st); }));
     }
   }
   return CT_OK;
@@ -1182,8 +1237,34 @@ ct_status ct_render_accumulate(ct_ctx* ctx, const ct_scene* scene, const ct_bvh*
   if (s != CT_OK) return s;
   cudaStream_t st = (cudaStream_t)stream;
   const FrameConst f = frame_const(cam, p);
-  // exact math accumulates strictly in sequence; profiling times kernels alone
-  if (p->exact_math == CT_MATH_EXACT || r->profile) return emit_frame(ctx, r, r->q, scene, bvh, f, p, st);
+  // profiling times kernels alone: frames in sequence
+  if (r->profile) return emit_frame(ctx, r, r->q, scene, bvh, f, p, st);
+  if (p->exact_math == CT_MATH_EXACT) {
+    // Exact frames overlap too, but keep the sequential accumulation bit for
+    // bit: a frame in a slot logs each pixel's contributions (shade, connect;
+    // pass by pass) instead of adding them, and the log is replayed into the
+    // job's buffer on the caller's stream in frame order, with the same
+    // additions in the same order as a frame accumulated in place. Compat
+    // shading on quad trees only; FULL shading and wide trees run in sequence.
+    bool ok = p->shading_mode == CT_SHADE_COMPAT && !bvh->wide;
+    if (ok && (s = ensure_slots(ctx, r)) != CT_OK) return s;
+    if (ok && (s = ensure_logs(ctx, r, p->max_depth, &ok)) != CT_OK) return s;
+    if (!ok) return emit_frame(ctx, r, r->q, scene, bvh, f, p, st);
+    const int k = r->next_exact;
+    r->next_exact = (k + 1) % r->exact_slots;
+    ct_render::Slot& sl = r->slots[k];
+    if (++r->log_tag == 0) r->log_tag = 1;
+    DevQueues ql = sl.q;
+    ql.log = r->logs[k];
+    ql.log_tag = r->log_tag;
+    CT_CUDA(ctx, cudaStreamWaitEvent(sl.stream, sl.free_ev, 0));
+    if ((s = emit_frame(ctx, r, ql, scene, bvh, f, p, sl.stream)) != CT_OK) return s;
+    CT_CUDA(ctx, cudaEventRecord(sl.done_ev, sl.stream));
+    CT_CUDA(ctx, cudaStreamWaitEvent(st, sl.done_ev, 0));
+    CT_CUDA(ctx, launch_fold_log(r->q.accum, r->logs[k], 2 * p->max_depth, r->w * r->h, r->w * r->h, r->log_tag, st));
+    CT_CUDA(ctx, cudaEventRecord(sl.free_ev, st));
+    return CT_OK;
+  }
   // Fast-math frames overlap: the frame renders into one of kFrameSlots
   // private slots (queues + accumulation) on the slot's own stream, so its
   // first passes can run while earlier frames' last bounces are still

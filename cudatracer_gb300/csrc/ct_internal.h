@@ -120,6 +120,16 @@ struct DevQueues {
                      // result, only which rays share a warp
   int32_t* perm_buf; // capacity entries, written by launch_ray_sort
   int32_t capacity;
+  // Exact-math frames rendered in a slot (overlapped with other frames): instead
+  // of adding to accum, each pixel's contribution of this launch is stored as
+  // entry log_entry of log ([entry][pixel], capacity pixels per entry: shade of
+  // pass p writes entry 2p, connect entry 2p + 1), w = log_tag (uint bits); the
+  // fold replays the entries in order into the job's buffer, so every pixel
+  // sees the same additions in the same order as a frame accumulated in place.
+  // nullptr: add to accum.
+  float4* log;
+  uint32_t log_entry;
+  uint32_t log_tag;
   // queue selection without dynamic indexing into the (by-value) parameter struct
   __host__ __device__ float4* org_q(int i) const { return i ? org[1] : org[0]; }
   __host__ __device__ float4* dir_q(int i) const { return i ? dir[1] : dir[0]; }
@@ -204,7 +214,6 @@ cudaError_t launch_raygen(const DevQueues& q, const FrameConst& f, int exact, cu
 cudaError_t launch_shade(const DevScene& sc, const DevQueues& q, const FrameConst& f, int queue, int path_length,
                          int exact, cudaStream_t s);
 cudaError_t launch_present(const float4* accum, float4* out, int n, float samples, cudaStream_t s);
-// accum[i] += frame[i]; frame[i] = 0 (folds an overlapped frame's private buffer)
 // Device SAH build (bvh_gpu.cu). gpu_bvh_build runs the binary build and the
 // collapse bookkeeping in `scratch` (gpu_bvh_scratch_bytes) and returns the
 // sizes; gpu_bvh_emit then writes the reference-layout quad nodes (QuadNode,
@@ -311,7 +320,13 @@ constexpr int kSortWindow = 2048;
 cudaError_t launch_ray_sort(const DevQueues& q, int queue, int key, cudaStream_t s);
 cudaError_t launch_batch_connect_wide(const DevBatch& b, const DevQueues& q, cudaStream_t s);
 
+// accum[i] += frame[i]; frame[i] = 0 (folds an overlapped frame's private buffer)
 cudaError_t launch_fold(float4* accum, float4* frame, int n, cudaStream_t s);
+// accum[i] += each entry k < entries of log[k * stride + i] whose w is `tag`
+// (uint bits), in k order: rgb and w + 1 as separate round-to-nearest additions
+// (replays an overlapped exact-math frame's contributions, DevQueues::log)
+cudaError_t launch_fold_log(float4* accum, const float4* log, int entries, int stride, int n, uint32_t tag,
+                            cudaStream_t s);
 
 // allocation-free frame (noalloc.cu): queues in a static device array
 uint32_t noalloc_max_pixels();

@@ -124,6 +124,16 @@ __device__ __forceinline__ void accum_add(float4* accum, int pix, V3 c) {
   accum[pix] = a;
 }
 
+// A compat-shading contribution: added to the job's buffer, or, for an exact
+// frame in a slot, stored in this launch's log entry (DevQueues::log).
+__device__ __forceinline__ void add_contribution(const DevQueues& q, float4* acc, int pix, int pix_base, V3 c) {
+  if (q.log) {
+    q.log[(size_t)q.log_entry * q.capacity + pix] = make_float4(c.x, c.y, c.z, __uint_as_float(q.log_tag));
+    return;
+  }
+  accum_add(acc ? acc : q.accum, acc ? pix - pix_base : pix, c);
+}
+
 // Heron's formula, triangle::getArea (src/Core/Triangle.cuh:89-95)
 __device__ __forceinline__ float tri_area(V3 p0, V3 p1, V3 p2) {
   const float a = length(p0 - p1), b = length(p1 - p2), c = length(p2 - p0);
@@ -175,7 +185,7 @@ __device__ __forceinline__ void shade_compat(const DevScene& sc, const DevQueues
       const float u = 1.0f + (xatan2(dir.x, -dir.z) * kOneOverPi) * 0.5f;
       const float v = 1.0f - xacos(dir.y) * kOneOverPi;
       const float4 tc = tex_color(sc, sc.sky_tex, u, v, f.tex_filter);
-      accum_add(acc ? acc : q.accum, acc ? pix - pix_base : pix, (T / last_pdf) * v3(tc));
+      add_contribution(q, acc, pix, pix_base, (T / last_pdf) * v3(tc));
     }
     return;
   }
@@ -208,7 +218,7 @@ __device__ __forceinline__ void shade_compat(const DevScene& sc, const DevQueues
       const float lightPDF = ((t * t) / (DdotNL * tri_area(p0, p1, p2))) * (float)sc.light_count;
       c = (T * v3(alb)) * (1.0f / (last_pdf + lightPDF));
     }
-    accum_add(acc ? acc : q.accum, acc ? pix - pix_base : pix, vmax0(c));
+    add_contribution(q, acc, pix, pix_base, vmax0(c));
     return;
   }
   org = org + dir * t;  // getHitpoint

@@ -45,7 +45,30 @@ __global__ void k_fold(float4* __restrict__ accum, float4* __restrict__ frame, i
     frame[i] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
   }
 }
+__global__ void k_fold_log(float4* __restrict__ accum, const float4* __restrict__ log, int entries, int stride, int n,
+                           uint32_t tag) {
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+    float4 a = accum[i];
+    for (int k = 0; k < entries; k++) {
+      const float4 e = __ldg(log + (size_t)k * stride + i);
+      if (__float_as_uint(e.w) != tag) continue;
+      a.x = __fadd_rn(a.x, e.x);
+      a.y = __fadd_rn(a.y, e.y);
+      a.z = __fadd_rn(a.z, e.z);
+      a.w = __fadd_rn(a.w, 1.0f);
+    }
+    accum[i] = a;
+  }
+}
 }  // namespace
+
+cudaError_t launch_fold_log(float4* accum, const float4* log, int entries, int stride, int n, uint32_t tag,
+                            cudaStream_t s) {
+  if (n <= 0) return cudaSuccess;
+  const int grid = (n + 255) / 256 < 8 * sm_count() ? (n + 255) / 256 : 8 * sm_count();
+  k_fold_log<<<grid, 256, 0, s>>>(accum, log, entries, stride, n, tag);
+  return cudaGetLastError();
+}
 
 cudaError_t launch_fold(float4* accum, float4* frame, int n, cudaStream_t s) {
   if (n <= 0) return cudaSuccess;

@@ -140,6 +140,10 @@ __global__ void __launch_bounds__(kBlock) k_connect(DevBVH b, DevQueues q, float
     if (r.hit < 0) {
       const float4 c = __ldg(q.scol + i);
       const int pix = __float_as_int(o.w);
+      if (q.log) {  // an exact frame in a slot: this launch's log entry (DevQueues::log)
+        q.log[(size_t)q.log_entry * q.capacity + pix] = make_float4(c.x, c.y, c.z, __uint_as_float(q.log_tag));
+        continue;
+      }
       float4 a = q.accum[pix];
       a.x = __fadd_rn(a.x, c.x);
       a.y = __fadd_rn(a.y, c.y);

@@ -129,8 +129,16 @@ enum { CT_SHADE_COMPAT = 0, CT_SHADE_FULL = 1 };
  *                       contraction; sin/cos/atan2/acos as fixed sequences of
  *                       correctly rounded binary32 operations) and the
  *                       reference's traversal arithmetic and child order:
- *                       accumulation bit-identical to the oracle; frames run
- *                       one after another.
+ *                       accumulation bit-identical to the oracle. Frames with
+ *                       compat shading on quad trees overlap in up to four
+ *                       slots of the render job: each logs its per-pixel
+ *                       contributions (2 x max_depth entries of 16 bytes per
+ *                       pixel and slot, up to 4 GiB per job) and the log is
+ *                       replayed into the accumulation in frame order, pass
+ *                       by pass, so every pixel receives the same additions
+ *                       in the same order as frames run one after another
+ *                       (as they do with FULL shading, wide trees, while
+ *                       profiling, or when the logs do not fit).
  *   CT_MATH_EXACT_SHADE ray generation and shading as CT_MATH_EXACT, traversal
  *                       as CT_MATH_FAST. The traversal returns the same closest
  *                       hit (t bit-equal; only the winner of an exact t tie can

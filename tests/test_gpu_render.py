@@ -190,6 +190,38 @@ def test_overlapped_fast_frames_are_deterministic(gpu_ctx, small):
     assert a[:, 3].sum() > 0
 
 
+def test_overlapped_exact_frames_equal_frames_in_sequence(gpu_ctx, small):
+    """CT_MATH_EXACT frames overlap in slots and log their per-pixel
+    contributions, which are replayed into the job's buffer in frame order; the
+    accumulation equals the same frames run one after another (profiling runs
+    them so) byte for byte, also when a deeper frame makes the logs grow."""
+    import torch
+
+    from cudatracer_gb300 import api
+
+    W, H = 96, 64
+    cam = small["cam"]
+    camera = api.Camera(W, H, cam["fov"], cam["position"], cam["forward"], cam["up"])
+    outs = []
+    for in_sequence in (False, True):
+        job = api.RenderJob(gpu_ctx, W, H)
+        if in_sequence:
+            job.profile(True)
+        p = api.Params(W, H, camera=camera, max_depth=4, exact_math=True)
+        p.reset(job)
+        for _ in range(6):
+            api.launch_kernels(job, small["sc"], small["bvh"], p)
+        p.max_depth = 9
+        for _ in range(5):
+            api.launch_kernels(job, small["sc"], small["bvh"], p)
+        torch.cuda.synchronize()
+        gpu_ctx.check()
+        outs.append(job.accum_tensor().cpu().numpy().copy())
+        job.close()
+    assert np.array_equal(outs[0].view(np.int32), outs[1].view(np.int32))
+    assert outs[0][:, 3].sum() > 0
+
+
 def test_stats_and_validation(gpu_ctx, small):
     from cudatracer_gb300 import _lib, api
 
