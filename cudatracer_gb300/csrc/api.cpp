@@ -155,8 +155,10 @@ constexpr int kFrameSlots = 10;
 // Exact-math frames overlap in up to kExactSlots of those slots, each frame
 // logging its per-pixel contributions (DevQueues::log: 2 x max_depth entries of
 // 16 bytes per pixel) for an in-order replay; the logs of a job may take up to
-// kExactLogBytes, beyond which exact frames run one after another.
-constexpr int kExactSlots = 4;
+// kExactLogBytes, beyond which exact frames run one after another (1080p,
+// depth 8, 531 MB of log per slot: 2 slots 631, 4 slots 768, 6 slots 800, 8
+// slots 805 Msamples/s).
+constexpr int kExactSlots = 6;
 constexpr size_t kExactLogBytes = (size_t)4 << 30;
 
 struct ct_render {

@@ -130,7 +130,7 @@ enum { CT_SHADE_COMPAT = 0, CT_SHADE_FULL = 1 };
  *                       correctly rounded binary32 operations) and the
  *                       reference's traversal arithmetic and child order:
  *                       accumulation bit-identical to the oracle. Frames with
- *                       compat shading on quad trees overlap in up to four
+ *                       compat shading on quad trees overlap in up to six
  *                       slots of the render job: each logs its per-pixel
  *                       contributions (2 x max_depth entries of 16 bytes per
  *                       pixel and slot, up to 4 GiB per job) and the log is
