@@ -427,8 +427,13 @@ __global__ void __launch_bounds__(128, 8) k_trace_wide(const DevWBVH b, const fl
           load_node(b.nodes, ent, nd);
           slab_setup(nd, r.ox, r.oy, r.oz, r.ix, r.iy, r.iz, S);
           // the nearest hit slot is visited next without a stack round trip; the
-          // others are pushed (a slot displaced as nearest is pushed when replaced)
-          float tcur = __int_as_float(0x7f800000);
+          // others are pushed (a slot displaced as nearest is pushed when replaced).
+          // Closest hit also keeps the second nearest in a register and pushes it
+          // last, so it is the next entry popped (closer hits found sooner cull
+          // more; any hit stops at its first hit, where the order only costs)
+          float tcur = __int_as_float(0x7f800000), tsec = __int_as_float(0x7f800000);
+          uint32_t sec = 0;
+          bool have_sec = false;
 #pragma unroll
           for (int i = 0; i < 8; i++) {
             const uint32_t m = meta_at(nd, i);
@@ -447,11 +452,27 @@ __global__ void __launch_bounds__(128, 8) k_trace_wide(const DevWBVH b, const fl
                 continue;
               }
             }
+            if (!ANY) {
+              if (!have_sec) {
+                sec = pe, tsec = pt, have_sec = true;
+                continue;
+              }
+              if (pt < tsec) {
+                const uint32_t e2 = sec;
+                const float t2 = tsec;
+                sec = pe, tsec = pt;
+                pe = e2, pt = t2;
+              }
+            }
             if (sp >= kWStack) {
               overflow = true;  // settled by the full FP64 traversal
               continue;
             }
             st_node[sp] = pe, st_t[sp] = pt, sp++;
+          }
+          if (!ANY && have_sec) {
+            if (sp >= kWStack) overflow = true;
+            else st_node[sp] = sec, st_t[sp] = tsec, sp++;
           }
         }
         finished = (!have_cur && sp == 0) || overflow || (ANY && occluded);
