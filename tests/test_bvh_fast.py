@@ -270,3 +270,26 @@ def test_fast_padding_keeps_grazing_hits(lib, small_terrain, which):
     # the check has teeth: exact (unpadded) triangle boxes lose some of these rays
     lo, hi = P.min(axis=1).astype(np.float32), P.max(axis=1).astype(np.float32)
     assert (~_fma_slab_hits(lo, hi, o, d)).sum() > 0
+
+
+def test_fast_tree_is_order_deterministic(lib):
+    """What lets the device build reproduce the host tree byte for byte: no box
+    coordinate is a negative zero (min/max unions then do not depend on the
+    order in which boxes meet), and the tree is a function of the input alone:
+    the same bytes for every thread count, also for coincident triangles (ranges
+    halved as they lie) and for a scene at the origin (no padding)."""
+    rng = np.random.default_rng(3)
+    z = np.zeros((60, 3), np.float32)
+    z[::2, 0] = -0.0
+    z[1::3, 1] = -0.0
+    v1 = np.array([[0, 0, 0], [1, 0, 0], [0, 1, 0]], np.float32)
+    soup = rng.normal(size=(3000, 3)).astype(np.float32)
+    soup[::5] *= -0.0
+    for v, ix in ((z, np.arange(60, dtype=np.uint32).reshape(-1, 3)),
+                  (v1, np.tile(np.array([[0, 1, 2]], np.uint32), (300, 1))),
+                  (soup, np.arange(3000, dtype=np.uint32).reshape(-1, 3))):
+        trees = [_fast(v, ix, t) for t in (1, 3, 8)]
+        for t in trees[1:]:
+            assert np.array_equal(t["quad"], trees[0]["quad"]) and np.array_equal(t["prims"], trees[0]["prims"])
+        bounds = trees[0]["quad"][:, :24].view(np.uint32)
+        assert not (bounds == 0x80000000).any(), "a negative zero in a node box"
